@@ -1,0 +1,647 @@
+// cg_capi.cu -- host side of the C ABI declared in include/chromo_gb300.h.
+//
+// Owns the device buffers of a cg_sim, converts host FP64 / int64 arrays to
+// the resident layout (V4 positions in FP32 or FP64, packed int8 binder
+// states, int64 fixed-point grid), sizes the per-warp shared-memory region
+// and launches the kernels of cg_mc.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cg_kernels.h"
+
+using cg::KArgs;
+using cg::RepDev;
+template <typename T> using V4 = cg::V4<T>;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CUDA_TRY(x)                                                                 \
+  do {                                                                              \
+    cudaError_t e_ = (x);                                                           \
+    if (e_ != cudaSuccess)                                                          \
+      return fail(CG_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));    \
+  } while (0)
+
+size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+int next_log2(long long x) {
+  int l = 0;
+  while ((1LL << l) < x) l++;
+  return l;
+}
+
+}  // namespace
+
+struct cg_sim {
+  int R = 0, nb = 0, ncol = 0, fp64 = 0, wpb = 1, n_sm = 0, nonuniform = 0;
+  std::vector<long long> n_beads, bead_off, n_vox, vox_off, picked_off;
+  std::vector<int> dims;
+  long long total_beads = 0, total_vox = 0, total_picked = 0;
+  long long max_segment = 0, max_tangent = 0, max_beads = 0;
+  int n_ctl = 5;
+  long long kernels = 0;
+  // device buffers
+  RepDev* reps = nullptr;
+  cg_move_ctl* ctl = nullptr;
+  unsigned long long* tally = nullptr;
+  void *r4 = nullptr, *t34 = nullptr, *t24 = nullptr;
+  unsigned *states = nullptr, *marks = nullptr;
+  double* bonds = nullptr;
+  long long* grid = nullptr;
+  double* access_vol = nullptr;
+  int *g_keys = nullptr, *g_used = nullptr;
+  long long* g_vals = nullptr;
+  int g_logH = 0;
+  void* g_stage = nullptr;
+  int* g_idx = nullptr;
+  long long g_stage_cap = 0;
+  unsigned* picked = nullptr;
+  long long* d_picked_off = nullptr;
+  double* eout = nullptr;
+  long long* aout = nullptr;
+  int* rep_of_rung = nullptr;
+  unsigned long long *swaps = nullptr, *swap_attempts = nullptr, *xround = nullptr;
+  // shared-memory layout
+  int logH = 0, warp_smem = 0, off_keys = 0, off_used = 0, off_vals = 0, off_stage = 0, off_idx = 0;
+  long long stage_cap = 0;
+  // captured batched graph
+  cudaGraphExec_t graph = nullptr;
+  long long graph_rounds = -1, graph_steps = -1;
+  int graph_rungs = -1;
+  unsigned long long graph_seed = 0;
+  cudaStream_t graph_stream = nullptr;
+
+  size_t pos_bytes() const { return fp64 ? sizeof(V4<double>) : sizeof(V4<float>); }
+  size_t scal_bytes() const { return fp64 ? 8 : 4; }
+
+  KArgs args() const {
+    KArgs a{};
+    a.reps = reps; a.ctl = ctl; a.n_ctl = n_ctl; a.n_reps = R; a.tally = tally;
+    a.r4 = r4; a.t34 = t34; a.t24 = t24; a.states = states; a.marks = marks; a.bonds = bonds;
+    a.grid = grid; a.access_vol = access_vol; a.ncol = ncol;
+    a.g_keys = g_keys; a.g_used = g_used; a.g_vals = g_vals; a.g_logH = g_logH;
+    a.g_stage = g_stage; a.g_idx = g_idx; a.g_stage_cap = g_stage_cap;
+    a.picked = picked; a.picked_off = d_picked_off;
+    a.wpb = wpb; a.logH = logH; a.stage_cap = stage_cap; a.warp_smem = warp_smem;
+    a.off_keys = off_keys; a.off_used = off_used; a.off_vals = off_vals; a.off_stage = off_stage;
+    a.off_idx = off_idx;
+    a.rep_of_rung = rep_of_rung; a.swaps = swaps; a.swap_attempts = swap_attempts;
+    a.xround = xround;
+    return a;
+  }
+
+  // Shared-memory layout for hash capacity 2^lh and staging capacity sc.
+  int layout(int lh, long long sc) {
+    size_t H = size_t(1) << lh;
+    size_t o = align16(sizeof(cg::WarpShared));
+    off_keys = (int)o; o += 4 * H;
+    off_used = (int)o; o += 4 * H;
+    o = align16(o);
+    off_vals = (int)o; o += 8 * H * ncol;
+    off_stage = (int)o; o += sc * 9 * scal_bytes();
+    o = align16(o);
+    off_idx = (int)o; o += 4 * sc;
+    o = align16(o);
+    logH = lh; stage_cap = sc; warp_smem = (int)o;
+    return warp_smem;
+  }
+};
+
+template <typename P>
+static void pack_pos(const double* src, long long n, std::vector<unsigned char>& out) {
+  out.resize(sizeof(V4<P>) * n);
+  V4<P>* o = reinterpret_cast<V4<P>*>(out.data());
+  for (long long i = 0; i < n; i++) o[i] = V4<P>{(P)src[3 * i], (P)src[3 * i + 1], (P)src[3 * i + 2], (P)0};
+}
+template <typename P>
+static void unpack_pos(const std::vector<unsigned char>& in, long long n, double* dst) {
+  const V4<P>* o = reinterpret_cast<const V4<P>*>(in.data());
+  for (long long i = 0; i < n; i++) {
+    dst[3 * i] = (double)o[i].x; dst[3 * i + 1] = (double)o[i].y; dst[3 * i + 2] = (double)o[i].z;
+  }
+}
+
+extern "C" {
+
+const char* cg_last_error(void) { return g_err.c_str(); }
+
+void cg_destroy(cg_sim* s) {
+  if (!s) return;
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
+                  s->grid, s->access_vol, s->g_keys, s->g_used, s->g_vals, s->g_stage, s->g_idx,
+                  s->picked, s->d_picked_off, s->eout, s->aout, s->rep_of_rung, s->swaps,
+                  s->swap_attempts, s->xround};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete s;
+}
+
+static int choose_shape(cg_sim* s, int wpb_req) {
+  // Replicas are independent warps; pack enough of them per SM that all are
+  // resident at once, and give each the largest hash that then fits.
+  const int smem_per_sm = 227 * 1024;
+  long long warps_per_sm = (s->R + s->n_sm - 1) / std::max(1, s->n_sm);
+  if (warps_per_sm < 1) warps_per_sm = 1;
+  int wpb = wpb_req > 0 ? wpb_req : 1;
+  if (wpb > 4) wpb = 4;
+  long long per_warp = smem_per_sm / std::max<long long>(warps_per_sm, wpb) - 1024;
+  if (per_warp * wpb > 200 * 1024) per_warp = 200 * 1024 / wpb;
+  const long long sc = 192;
+  int lh = 12;
+  while (lh > 6 && s->layout(lh, sc) > per_warp) lh--;
+  s->layout(lh, sc);
+  s->wpb = wpb;
+  cudaError_t e = cg_set_mc_smem(s->fp64 != 0, s->warp_smem * wpb);
+  if (e != cudaSuccess) return fail(CG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+  return CG_OK;
+}
+
+int cg_create(const cg_config* cfg, cg_sim** out) {
+  if (!cfg || !out) return fail(CG_ERR_ARG, "null argument");
+  if (cfg->n_replicas < 1) return fail(CG_ERR_ARG, "n_replicas must be >= 1");
+  if (cfg->n_binders < 1 || cfg->n_binders > CG_MAX_BINDERS)
+    return fail(CG_ERR_ARG, "n_binders must be in 1..3");
+  cg_sim* s = new cg_sim();
+  s->R = cfg->n_replicas;
+  s->nb = cfg->n_binders;
+  s->ncol = cfg->n_binders + 1 <= 2 ? 2 : 4;
+  s->fp64 = cfg->pos_fp64 ? 1 : 0;
+  s->nonuniform = cfg->nonuniform_access ? 1 : 0;
+  s->max_segment = std::max<long long>(cfg->max_segment, 2);
+  s->max_tangent = std::max<long long>(cfg->max_tangent, 1);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&s->n_sm, cudaDevAttrMultiProcessorCount, dev);
+  for (int r = 0; r < s->R; r++) {
+    long long n = cfg->n_beads[r];
+    if (n < 2) { cg_destroy(s); return fail(CG_ERR_ARG, "every chain needs at least 2 beads"); }
+    int nx = cfg->grid_dims[3 * r], ny = cfg->grid_dims[3 * r + 1], nz = cfg->grid_dims[3 * r + 2];
+    if (nx < 1 || ny < 1 || nz < 1) { cg_destroy(s); return fail(CG_ERR_ARG, "grid dims must be >= 1"); }
+    if ((long long)nx * ny * nz > (1LL << 30)) { cg_destroy(s); return fail(CG_ERR_ARG, "grid too large"); }
+    s->n_beads.push_back(n);
+    s->bead_off.push_back(s->total_beads);
+    s->total_beads += n;
+    s->dims.insert(s->dims.end(), {nx, ny, nz});
+    s->n_vox.push_back((long long)nx * ny * nz);
+    s->vox_off.push_back(s->total_vox);
+    s->total_vox += (long long)nx * ny * nz;
+    s->picked_off.push_back(s->total_picked);
+    s->total_picked += (n + 31) / 32;
+    s->max_beads = std::max(s->max_beads, n);
+  }
+  s->g_logH = next_log2(32 * s->max_segment);
+  s->g_stage_cap = std::max(s->max_segment, s->max_tangent);
+  const long long Hg = 1LL << s->g_logH;
+  auto M = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes == 0 ? 16 : bytes); };
+  cudaError_t e = cudaSuccess;
+#define ALLOC(ptr, bytes) if (e == cudaSuccess) e = M((void**)&(ptr), (bytes))
+  ALLOC(s->reps, sizeof(RepDev) * s->R);
+  ALLOC(s->ctl, sizeof(cg_move_ctl) * 5 * s->R);
+  ALLOC(s->tally, sizeof(unsigned long long) * 30 * s->R);
+  ALLOC(s->r4, s->pos_bytes() * s->total_beads);
+  ALLOC(s->t34, s->pos_bytes() * s->total_beads);
+  ALLOC(s->t24, s->pos_bytes() * s->total_beads);
+  ALLOC(s->states, 4 * s->total_beads);
+  ALLOC(s->marks, 4 * s->total_beads);
+  ALLOC(s->bonds, 6 * 8 * s->total_beads);
+  ALLOC(s->grid, 8 * s->ncol * s->total_vox);
+  if (s->nonuniform) ALLOC(s->access_vol, 8 * s->total_vox);
+  ALLOC(s->g_keys, 4 * Hg * s->R);
+  ALLOC(s->g_used, 4 * Hg * s->R);
+  ALLOC(s->g_vals, 8 * Hg * s->ncol * s->R);
+  ALLOC(s->g_stage, s->scal_bytes() * 9 * s->g_stage_cap * s->R);
+  ALLOC(s->g_idx, 4 * s->g_stage_cap * s->R);
+  ALLOC(s->picked, 4 * s->total_picked);
+  ALLOC(s->d_picked_off, 8 * s->R);
+  ALLOC(s->eout, 8 * 5 * s->R);
+  ALLOC(s->aout, 8 * 4);
+  ALLOC(s->rep_of_rung, 4 * s->R);
+  ALLOC(s->swaps, 8 * s->R);
+  ALLOC(s->swap_attempts, 8 * s->R);
+  ALLOC(s->xround, 8);
+#undef ALLOC
+  if (e != cudaSuccess) {
+    cg_destroy(s);
+    return fail(CG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  cudaMemset(s->reps, 0, sizeof(RepDev) * s->R);
+  cudaMemset(s->ctl, 0, sizeof(cg_move_ctl) * 5 * s->R);
+  cudaMemset(s->tally, 0, 8 * 30 * s->R);
+  cudaMemset(s->r4, 0, s->pos_bytes() * s->total_beads);
+  cudaMemset(s->t34, 0, s->pos_bytes() * s->total_beads);
+  cudaMemset(s->t24, 0, s->pos_bytes() * s->total_beads);
+  cudaMemset(s->states, 0, 4 * s->total_beads);
+  cudaMemset(s->marks, 0, 4 * s->total_beads);
+  cudaMemset(s->bonds, 0, 48 * s->total_beads);
+  cudaMemset(s->grid, 0, 8 * s->ncol * s->total_vox);
+  cudaMemset(s->g_keys, 0xFF, 4 * Hg * s->R);
+  cudaMemset(s->g_vals, 0, 8 * Hg * s->ncol * s->R);
+  cudaMemset(s->picked, 0, 4 * s->total_picked);
+  cudaMemset(s->swaps, 0, 8 * s->R);
+  cudaMemset(s->swap_attempts, 0, 8 * s->R);
+  cudaMemset(s->xround, 0, 8);
+  cudaMemcpy(s->d_picked_off, s->picked_off.data(), 8 * s->R, cudaMemcpyHostToDevice);
+  std::vector<int> ror(s->R);
+  for (int r = 0; r < s->R; r++) ror[r] = r;
+  cudaMemcpy(s->rep_of_rung, ror.data(), 4 * s->R, cudaMemcpyHostToDevice);
+  std::vector<RepDev> rd(s->R);
+  for (int r = 0; r < s->R; r++) {
+    RepDev& d = rd[r];
+    memset(&d, 0, sizeof(d));
+    d.bead_off = s->bead_off[r];
+    d.n_beads = s->n_beads[r];
+    d.vox_off = s->vox_off[r];
+    d.n_vox = s->n_vox[r];
+    d.nx = s->dims[3 * r]; d.ny = s->dims[3 * r + 1]; d.nz = s->dims[3 * r + 2];
+    d.nb = s->nb;
+    d.wx = d.wy = d.wz = 1.0;
+    d.dx = d.dy = d.dz = 1.0;
+    d.vol_bin = 1.0;
+    d.max_binders = -1;
+    d.vf_limit = 0.5;
+    d.mu_adjust = 1.0;
+  }
+  cudaMemcpy(s->reps, rd.data(), sizeof(RepDev) * s->R, cudaMemcpyHostToDevice);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) { cg_destroy(s); return fail(CG_ERR_CUDA, cudaGetErrorString(e)); }
+  int rc = choose_shape(s, cfg->warps_per_block);
+  if (rc) { cg_destroy(s); return rc; }
+  *out = s;
+  return CG_OK;
+}
+
+static int check_rep(cg_sim* s, int rep) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (rep < 0 || rep >= s->R) return fail(CG_ERR_ARG, "replica index out of range");
+  return CG_OK;
+}
+
+static int get_rep(cg_sim* s, int rep, RepDev* d) {
+  CUDA_TRY(cudaMemcpy(d, s->reps + rep, sizeof(RepDev), cudaMemcpyDeviceToHost));
+  return CG_OK;
+}
+static int put_rep(cg_sim* s, int rep, const RepDev* d) {
+  CUDA_TRY(cudaMemcpy(s->reps + rep, d, sizeof(RepDev), cudaMemcpyHostToDevice));
+  return CG_OK;
+}
+
+int cg_set_chain(cg_sim* s, int rep, const double* r, const double* t3, const double* t2,
+                 const int64_t* states, const int64_t* marks, const double* bonds) {
+  if (int rc = check_rep(s, rep)) return rc;
+  const long long n = s->n_beads[rep], off = s->bead_off[rep];
+  std::vector<unsigned char> buf;
+  const double* src[3] = {r, t3, t2};
+  void* dst[3] = {s->r4, s->t34, s->t24};
+  for (int k = 0; k < 3; k++) {
+    if (!src[k]) continue;
+    for (long long i = 0; i < 3 * n; i++)
+      if (!std::isfinite(src[k][i])) return fail(CG_ERR_NONFINITE, "non-finite position or tangent");
+    if (s->fp64) pack_pos<double>(src[k], n, buf);
+    else pack_pos<float>(src[k], n, buf);
+    CUDA_TRY(cudaMemcpy((char*)dst[k] + s->pos_bytes() * off, buf.data(), buf.size(), cudaMemcpyHostToDevice));
+  }
+  std::vector<unsigned> pk(n);
+  const int64_t* sm[2] = {states, marks};
+  unsigned* dsm[2] = {s->states, s->marks};
+  for (int k = 0; k < 2; k++) {
+    if (!sm[k]) continue;
+    for (long long i = 0; i < n; i++) {
+      unsigned w = 0;
+      for (int b = 0; b < s->nb; b++) {
+        int64_t v = sm[k][i * s->nb + b];
+        if (v < 0 || v > CG_MAX_MARK)
+          return fail(CG_ERR_ARG, k == 0 ? "binding states must be in 0..3" : "chemical_mods must be in 0..3");
+        w |= (unsigned)v << (8 * b);
+      }
+      pk[i] = w;
+    }
+    CUDA_TRY(cudaMemcpy(dsm[k] + off, pk.data(), 4 * n, cudaMemcpyHostToDevice));
+  }
+  if (bonds) {
+    std::vector<double> bb(6 * n, 0.0);
+    for (long long i = 0; i + 1 < n; i++)
+      for (int j = 0; j < 5; j++) bb[6 * i + j] = bonds[5 * i + j];
+    CUDA_TRY(cudaMemcpy(s->bonds + 6 * off, bb.data(), 8 * 6 * n, cudaMemcpyHostToDevice));
+  }
+  return CG_OK;
+}
+
+int cg_get_chain(cg_sim* s, int rep, double* r, double* t3, double* t2, int64_t* states) {
+  if (int rc = check_rep(s, rep)) return rc;
+  const long long n = s->n_beads[rep], off = s->bead_off[rep];
+  std::vector<unsigned char> buf(s->pos_bytes() * n);
+  double* dst[3] = {r, t3, t2};
+  void* src[3] = {s->r4, s->t34, s->t24};
+  for (int k = 0; k < 3; k++) {
+    if (!dst[k]) continue;
+    CUDA_TRY(cudaMemcpy(buf.data(), (char*)src[k] + s->pos_bytes() * off, buf.size(), cudaMemcpyDeviceToHost));
+    if (s->fp64) unpack_pos<double>(buf, n, dst[k]);
+    else unpack_pos<float>(buf, n, dst[k]);
+  }
+  if (states) {
+    std::vector<unsigned> pk(n);
+    CUDA_TRY(cudaMemcpy(pk.data(), s->states + off, 4 * n, cudaMemcpyDeviceToHost));
+    for (long long i = 0; i < n; i++)
+      for (int b = 0; b < s->nb; b++) states[i * s->nb + b] = (pk[i] >> (8 * b)) & 0xFF;
+  }
+  return CG_OK;
+}
+
+int cg_set_field(cg_sim* s, int rep, const cg_field_params* f, const double* access_vol) {
+  if (int rc = check_rep(s, rep)) return rc;
+  if (!f) return fail(CG_ERR_ARG, "null field");
+  if (f->field_kind < 0 || f->field_kind > 2) return fail(CG_ERR_ARG, "field_kind must be 0, 1 or 2");
+  if (f->confine_kind < 0 || f->confine_kind > 2) return fail(CG_ERR_ARG, "confine_kind must be 0, 1 or 2");
+  if (f->field_kind == 2) {
+    if (f->nx != s->dims[3 * rep] || f->ny != s->dims[3 * rep + 1] || f->nz != s->dims[3 * rep + 2])
+      return fail(CG_ERR_ARG, "field grid differs from the grid given at creation");
+    if (f->n_binders != s->nb) return fail(CG_ERR_ARG, "field binder count differs from the polymer's");
+    if (!(f->x_width > 0 && f->y_width > 0 && f->z_width > 0)) return fail(CG_ERR_ARG, "box widths must be > 0");
+  }
+  if (access_vol && !s->nonuniform)
+    return fail(CG_ERR_ARG, "per-voxel accessible volumes need nonuniform_access at creation");
+  RepDev d;
+  if (int rc = get_rep(s, rep, &d)) return rc;
+  d.field_kind = f->field_kind;
+  d.confine_kind = f->confine_kind;
+  d.confine_length = f->confine_length;
+  if (f->field_kind == 2) {
+    d.wx = f->x_width; d.wy = f->y_width; d.wz = f->z_width;
+    d.dx = f->x_width / f->nx; d.dy = f->y_width / f->ny; d.dz = f->z_width / f->nz;
+    d.vol_bin = f->x_width * f->y_width * f->z_width / (double)(d.n_vox);
+  }
+  d.chi = f->chi; d.vf_limit = f->vf_limit; d.bead_vol = f->bead_vol;
+  for (int b = 0; b < CG_MAX_BINDERS; b++) { d.pref[b] = f->pref[b]; d.intra[b] = f->intra[b]; }
+  for (int b = 0; b < CG_MAX_BINDERS * CG_MAX_BINDERS; b++) d.xpref[b] = f->xpref[b];
+  d.has_access = access_vol ? 1 : 0;
+  if (access_vol)
+    CUDA_TRY(cudaMemcpy(s->access_vol + s->vox_off[rep], access_vol, 8 * s->n_vox[rep], cudaMemcpyHostToDevice));
+  return put_rep(s, rep, &d);
+}
+
+int cg_set_binding(cg_sim* s, int rep, const cg_binding_params* b) {
+  if (int rc = check_rep(s, rep)) return rc;
+  if (!b || b->n_binders != s->nb) return fail(CG_ERR_ARG, "binding parameters do not match n_binders");
+  for (int i = 0; i < s->nb; i++)
+    if (b->sites[i] < 0 || b->sites[i] > CG_MAX_MARK) return fail(CG_ERR_ARG, "sites_per_bead must be in 0..3");
+  RepDev d;
+  if (int rc = get_rep(s, rep, &d)) return rc;
+  d.max_binders = b->max_binders;
+  for (int i = 0; i < CG_MAX_BINDERS; i++) { d.sites[i] = b->sites[i]; d.mu[i] = b->mu[i]; }
+  d.mu_adjust = b->mu_adjust_factor;
+  for (int i = 0; i < CG_MAX_BINDERS * (CG_MAX_MARK + 1) * (CG_MAX_MARK + 1); i++) d.bind_f[i] = b->bind_f[i];
+  return put_rep(s, rep, &d);
+}
+
+int cg_set_controllers(cg_sim* s, int rep, const cg_move_ctl* c, int n_ctl) {
+  if (int rc = check_rep(s, rep)) return rc;
+  if (!c || n_ctl < 1 || n_ctl > 5) return fail(CG_ERR_ARG, "between 1 and 5 controllers");
+  for (int i = 0; i < n_ctl; i++) {
+    if (c[i].move_kind < 0 || c[i].move_kind > 4) return fail(CG_ERR_ARG, "unknown move kind");
+    double top = c[i].ctrl_kind == 1 ? std::max<double>((double)c[i].amp_bead, c[i].bead_hi) : (double)c[i].amp_bead;
+    if (c[i].move_kind == CG_TANGENT_ROTATION) {
+      if (top > (double)s->max_tangent)
+        return fail(CG_ERR_ARG, "tangent_rotation bead amplitude exceeds max_tangent given at creation");
+      if (c[i].move_on && c[i].amp_bead < 1) return fail(CG_ERR_ARG, "tangent_rotation needs amp_bead >= 1");
+    } else if (top + 1 > (double)s->max_segment) {
+      return fail(CG_ERR_ARG, "bead amplitude exceeds max_segment given at creation");
+    }
+  }
+  if (rep == 0) s->n_ctl = n_ctl;
+  else if (n_ctl != s->n_ctl) return fail(CG_ERR_ARG, "every replica needs the same number of controllers");
+  CUDA_TRY(cudaMemcpy(s->ctl + 5LL * rep, c, sizeof(cg_move_ctl) * n_ctl, cudaMemcpyHostToDevice));
+  return CG_OK;
+}
+
+int cg_get_controllers(cg_sim* s, int rep, cg_move_ctl* c, int n_ctl) {
+  if (int rc = check_rep(s, rep)) return rc;
+  if (!c || n_ctl < 1 || n_ctl > 5) return fail(CG_ERR_ARG, "between 1 and 5 controllers");
+  CUDA_TRY(cudaMemcpy(c, s->ctl + 5LL * rep, sizeof(cg_move_ctl) * n_ctl, cudaMemcpyDeviceToHost));
+  return CG_OK;
+}
+
+int cg_deposit(cg_sim* s, int rep) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (rep >= s->R) return fail(CG_ERR_ARG, "replica index out of range");
+  KArgs a = s->args();
+  if (rep < 0) {
+    CUDA_TRY(cudaMemset(s->grid, 0, 8 * s->ncol * s->total_vox));
+    cg_launch_deposit(a, s->fp64, -1, s->R, s->max_beads, 0);
+  } else {
+    CUDA_TRY(cudaMemset(s->grid + s->ncol * s->vox_off[rep], 0, 8 * s->ncol * s->n_vox[rep]));
+    cg_launch_deposit(a, s->fp64, rep, 1, s->n_beads[rep], 0);
+  }
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaDeviceSynchronize());
+  return CG_OK;
+}
+
+int cg_get_density(cg_sim* s, int rep, int64_t* grid) {
+  if (int rc = check_rep(s, rep)) return rc;
+  const long long G = s->n_vox[rep];
+  std::vector<long long> buf(G * s->ncol);
+  CUDA_TRY(cudaMemcpy(buf.data(), s->grid + s->ncol * s->vox_off[rep], 8 * G * s->ncol, cudaMemcpyDeviceToHost));
+  for (long long v = 0; v < G; v++)
+    for (int c = 0; c <= s->nb; c++) grid[v * (s->nb + 1) + c] = buf[v * s->ncol + c];
+  return CG_OK;
+}
+
+static int device_errors(cg_sim* s) {
+  std::vector<RepDev> rd(s->R);
+  CUDA_TRY(cudaMemcpy(rd.data(), s->reps, sizeof(RepDev) * s->R, cudaMemcpyDeviceToHost));
+  unsigned any = 0;
+  int first = -1;
+  for (int r = 0; r < s->R; r++)
+    if (rd[r].err) { any |= rd[r].err; if (first < 0) first = r; }
+  if (!any) return CG_OK;
+  // leave the replicas and the global scratch clean for the caller
+  for (int r = 0; r < s->R; r++) rd[r].err = 0;
+  cudaMemcpy(s->reps, rd.data(), sizeof(RepDev) * s->R, cudaMemcpyHostToDevice);
+  const long long Hg = 1LL << s->g_logH;
+  cudaMemset(s->g_keys, 0xFF, 4 * Hg * s->R);
+  cudaMemset(s->g_vals, 0, 8 * Hg * s->ncol * s->R);
+  cudaMemset(s->picked, 0, 4 * s->total_picked);
+  char msg[160];
+  snprintf(msg, sizeof msg, "device error bits 0x%x (first at replica %d)", any, first);
+  if (any & cg::E_WINDOW) return fail(CG_ERR_WINDOW, std::string(msg) + ": bead selection window must be less than polymer length");
+  if (any & cg::E_STREAM) return fail(CG_ERR_STREAM, std::string(msg) + ": supplied random stream exhausted");
+  if (any & cg::E_NONFINITE) return fail(CG_ERR_NONFINITE, std::string(msg) + ": non-finite position");
+  return fail(CG_ERR_SPIN, std::string(msg) + ": iteration cap reached");
+}
+
+int cg_run(cg_sim* s, int64_t n_steps, uint64_t seed, void* stream) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (n_steps < 0) return fail(CG_ERR_ARG, "n_steps must be >= 0");
+  if (n_steps == 0) return CG_OK;
+  KArgs a = s->args();
+  a.n_steps = n_steps;
+  a.seed = seed;
+  cg_launch_mc(a, s->fp64, false, (cudaStream_t)stream);
+  s->kernels++;
+  CUDA_TRY(cudaGetLastError());
+  return CG_OK;
+}
+
+int cg_sync(cg_sim* s, void* stream) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return device_errors(s);
+}
+
+int cg_run_audit(cg_sim* s, int rep, int64_t n_steps, const uint32_t* draws, int64_t n_draws,
+                 const int8_t* bstates, int64_t n_bstates, cg_move_record* records,
+                 int64_t max_records, int64_t* n_records, int64_t* draws_used, int64_t* bstates_used) {
+  if (int rc = check_rep(s, rep)) return rc;
+  if (n_steps < 0 || n_draws < 0 || n_bstates < 0 || max_records < 0) return fail(CG_ERR_ARG, "negative size");
+  for (int64_t i = 0; i < n_draws; i++)
+    if (draws[i] > 2147483647u) return fail(CG_ERR_ARG, "draws must be in [0, 2^31-1]");
+  for (int64_t i = 0; i < n_bstates; i++)
+    if (bstates[i] < 0 || bstates[i] > CG_MAX_MARK) return fail(CG_ERR_ARG, "binding-state draws must be in 0..3");
+  unsigned* d_draws = nullptr;
+  signed char* d_bs = nullptr;
+  cg_move_record* d_rec = nullptr;
+  cudaError_t e = cudaMalloc(&d_draws, 4 * std::max<int64_t>(n_draws, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&d_bs, std::max<int64_t>(n_bstates, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&d_rec, sizeof(cg_move_record) * std::max<int64_t>(max_records, 1));
+  if (e == cudaSuccess && n_draws) e = cudaMemcpy(d_draws, draws, 4 * n_draws, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n_bstates) e = cudaMemcpy(d_bs, bstates, n_bstates, cudaMemcpyHostToDevice);
+  int rc = CG_OK;
+  if (e == cudaSuccess) {
+    KArgs a = s->args();
+    a.n_steps = n_steps;
+    a.audit_rep = rep;
+    a.a_draws = d_draws; a.a_n_draws = n_draws;
+    a.a_bstates = d_bs; a.a_n_bstates = n_bstates;
+    a.a_recs = d_rec; a.a_max_recs = max_records;
+    a.a_out = s->aout;
+    cg_launch_mc(a, s->fp64, true, 0);
+    s->kernels++;
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  }
+  long long out[3] = {0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(out, s->aout, sizeof out, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && records && max_records)
+    e = cudaMemcpy(records, d_rec, sizeof(cg_move_record) * std::min<long long>(out[0], max_records),
+                   cudaMemcpyDeviceToHost);
+  cudaFree(d_draws); cudaFree(d_bs); cudaFree(d_rec);
+  if (e != cudaSuccess) return fail(CG_ERR_CUDA, cudaGetErrorString(e));
+  if (n_records) *n_records = out[0];
+  if (draws_used) *draws_used = out[1];
+  if (bstates_used) *bstates_used = out[2];
+  rc = device_errors(s);
+  return rc;
+}
+
+int cg_energy(cg_sim* s, int rep, double* out) {
+  if (int rc = check_rep(s, rep)) return rc;
+  KArgs a = s->args();
+  cg_launch_energy(a, s->fp64, s->eout, 0);
+  CUDA_TRY(cudaGetLastError());
+  double buf[5];
+  CUDA_TRY(cudaMemcpy(buf, s->eout + 5 * rep, sizeof buf, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 4; i++) out[i] = buf[i];
+  return CG_OK;
+}
+
+int cg_reset_running_energy(cg_sim* s) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  std::vector<RepDev> rd(s->R);
+  CUDA_TRY(cudaMemcpy(rd.data(), s->reps, sizeof(RepDev) * s->R, cudaMemcpyDeviceToHost));
+  for (auto& d : rd) d.run_dE = 0;
+  CUDA_TRY(cudaMemcpy(s->reps, rd.data(), sizeof(RepDev) * s->R, cudaMemcpyHostToDevice));
+  return CG_OK;
+}
+
+int cg_get_tally(cg_sim* s, int rep, uint64_t* out) {
+  if (int rc = check_rep(s, rep)) return rc;
+  CUDA_TRY(cudaMemcpy(out, s->tally + 30LL * rep, 30 * 8, cudaMemcpyDeviceToHost));
+  return CG_OK;
+}
+
+int cg_reset_tally(cg_sim* s) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  CUDA_TRY(cudaMemset(s->tally, 0, 8 * 30 * s->R));
+  return CG_OK;
+}
+
+static int enqueue_exchange(cg_sim* s, int n_rungs, long long round, uint64_t seed, cudaStream_t st) {
+  KArgs a = s->args();
+  cg_launch_energy(a, s->fp64, s->eout, st);
+  cg_launch_exchange(a, s->eout, n_rungs, round, seed, st);
+  return CG_OK;
+}
+
+int cg_exchange(cg_sim* s, int n_rungs, int64_t round, uint64_t seed, void* stream) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (n_rungs < 2 || s->R % n_rungs) return fail(CG_ERR_ARG, "n_rungs must be >= 2 and divide n_replicas");
+  enqueue_exchange(s, n_rungs, round, seed, (cudaStream_t)stream);
+  CUDA_TRY(cudaGetLastError());
+  return CG_OK;
+}
+
+int cg_get_chi(cg_sim* s, double* chi) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  std::vector<RepDev> rd(s->R);
+  CUDA_TRY(cudaMemcpy(rd.data(), s->reps, sizeof(RepDev) * s->R, cudaMemcpyDeviceToHost));
+  for (int r = 0; r < s->R; r++) chi[r] = rd[r].chi;
+  return CG_OK;
+}
+
+int cg_run_batched(cg_sim* s, int64_t n_rounds, int64_t n_steps, int32_t n_rungs, uint64_t seed,
+                   void* stream) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (n_rounds < 1 || n_steps < 1) return fail(CG_ERR_ARG, "n_rounds and n_steps must be >= 1");
+  if (n_rungs && (n_rungs < 2 || s->R % n_rungs)) return fail(CG_ERR_ARG, "n_rungs must be 0 or divide n_replicas");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!(s->graph && s->graph_rounds == n_rounds && s->graph_steps == n_steps && s->graph_rungs == n_rungs &&
+        s->graph_seed == seed && s->graph_stream == st)) {
+    if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+    cudaStream_t cap;
+    CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t gr;
+    CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    for (long long k = 0; k < n_rounds; k++) {
+      KArgs a = s->args();
+      a.n_steps = n_steps;
+      a.seed = seed;
+      cg_launch_mc(a, s->fp64, false, cap);
+      if (n_rungs) enqueue_exchange(s, n_rungs, -1, seed, cap);
+    }
+    cudaError_t e = cudaStreamEndCapture(cap, &gr);
+    cudaStreamDestroy(cap);
+    if (e != cudaSuccess) return fail(CG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) return fail(CG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    s->graph_rounds = n_rounds; s->graph_steps = n_steps; s->graph_rungs = n_rungs;
+    s->graph_seed = seed; s->graph_stream = st;
+  }
+  CUDA_TRY(cudaGraphLaunch(s->graph, st));
+  s->kernels += n_rounds;
+  return CG_OK;
+}
+
+int cg_get_launch_info(cg_sim* s, int32_t* wpb, int32_t* hash_slots, int64_t* kernels) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (wpb) *wpb = s->wpb;
+  if (hash_slots) *hash_slots = 1 << s->logH;
+  if (kernels) *kernels = s->kernels;
+  return CG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,323 @@
+// cg_device.cuh -- device-side building blocks of the GB300 MC inner loop.
+//
+// Everything here runs inside one warp per replica.  Scalars of a move
+// (random draws, bead bounds, the rotation matrix, dE totals, the decision)
+// are computed redundantly and identically by all 32 lanes, so the warp never
+// diverges on them; per-bead and per-voxel work is spread over the lanes.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/chromo_gb300.h"
+
+namespace cg {
+
+constexpr double kFxScale = 1099511627776.0;          // 2^40 fixed-point units per unit weight
+constexpr double kFxInv = 1.0 / 1099511627776.0;
+constexpr double kEHugePoly = 1e25;                     // chromo/polymers.pyx:35
+constexpr double kEHugeField = 1e99;                    // chromo/fields.pyx:32
+constexpr double kRandMax = 2147483647.0;               // glibc RAND_MAX
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kMaxIter = 4096;                          // cap on resampling loops
+
+// device-side error bits (mapped to cg_status on the host)
+enum : unsigned { E_WINDOW = 1u, E_STREAM = 2u, E_NONFINITE = 4u, E_SPIN = 8u };
+
+template <typename T> struct alignas(4 * sizeof(T)) V4 { T x, y, z, w; };
+
+// Per-replica parameters (device global; copied into shared memory per warp).
+struct RepDev {
+  long long bead_off, n_beads, vox_off, n_vox;
+  int nx, ny, nz, nb;
+  double wx, wy, wz, dx, dy, dz, vol_bin;
+  int field_kind, confine_kind, max_binders, has_access;
+  double confine_length, chi, vf_limit, bead_vol;
+  double pref[CG_MAX_BINDERS], intra[CG_MAX_BINDERS], xpref[CG_MAX_BINDERS * CG_MAX_BINDERS];
+  int sites[CG_MAX_BINDERS], pad0;
+  double mu[CG_MAX_BINDERS], mu_adjust;
+  double bind_f[CG_MAX_BINDERS * (CG_MAX_MARK + 1) * (CG_MAX_MARK + 1)];
+  unsigned long long draw_pos, bstate_pos;
+  double run_dE;
+  unsigned err, pad1;
+};
+
+// ---------------------------------------------------------------- RNG
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter-based.
+__device__ __forceinline__ uint4 philox(uint4 c, uint2 k) {
+#pragma unroll
+  for (int i = 0; i < 10; i++) {
+    unsigned hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    unsigned hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += 0x9E3779B9u;
+    k.y += 0xBB67AE85u;
+  }
+  return c;
+}
+
+__device__ __forceinline__ unsigned comp4(uint4 v, unsigned i) {
+  return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+
+// Stream of 31-bit draws (the role of libc rand()) and of binding states (the
+// role of np.random.randint(0, sites + 1)).  Both are indexed: draw j of the
+// replica's stream is a pure function of j, so lanes can read ahead.
+template <bool AUDIT> struct Rng;
+
+template <> struct Rng<false> {
+  uint2 key, keyb;
+  unsigned long long pos, bpos;
+  unsigned long long cctr;
+  uint4 cache;
+  bool fail;
+  __device__ void init(unsigned long long seed, int rep, unsigned long long p, unsigned long long bp) {
+    key = make_uint2((unsigned)seed ^ (unsigned)rep * 0x85EBCA6Bu, (unsigned)(seed >> 32));
+    keyb = make_uint2(key.x ^ 0x68E31DA4u, key.y ^ 0xB5297A4Du);
+    pos = p; bpos = bp; cctr = ~0ull; fail = false;
+  }
+  __device__ __forceinline__ unsigned at(unsigned long long j, bool& ok) const {
+    ok = true;
+    uint4 o = philox(make_uint4((unsigned)(j >> 2), (unsigned)(j >> 34), 0x2545F491u, 0u), key);
+    return comp4(o, (unsigned)(j & 3)) >> 1;
+  }
+  __device__ __forceinline__ unsigned next() {
+    unsigned long long j = pos++, c = j >> 2;
+    if (c != cctr) {
+      cache = philox(make_uint4((unsigned)c, (unsigned)(c >> 32), 0x2545F491u, 0u), key);
+      cctr = c;
+    }
+    return comp4(cache, (unsigned)(j & 3)) >> 1;
+  }
+  __device__ __forceinline__ int state_at(unsigned long long j, int nt, bool& ok) const {
+    ok = true;
+    uint4 o = philox(make_uint4((unsigned)(j >> 2), (unsigned)(j >> 34), 0x7F4A7C15u, 0u), keyb);
+    return (int)__umulhi(comp4(o, (unsigned)(j & 3)), (unsigned)(nt + 1));
+  }
+};
+
+template <> struct Rng<true> {
+  const unsigned* draws;
+  long long n;
+  const signed char* bs;
+  long long nbs;
+  unsigned long long pos, bpos;
+  bool fail;
+  __device__ __forceinline__ unsigned at(unsigned long long j, bool& ok) const {
+    ok = j < (unsigned long long)n;
+    return ok ? draws[j] : 0u;
+  }
+  __device__ __forceinline__ unsigned next() {
+    bool ok;
+    unsigned v = at(pos++, ok);
+    if (!ok) fail = true;
+    return v;
+  }
+  __device__ __forceinline__ int state_at(unsigned long long j, int nt, bool& ok) const {
+    ok = j < (unsigned long long)nbs;
+    return ok ? (int)bs[j] : 0;
+  }
+};
+
+__device__ __forceinline__ double unif(unsigned x) { return (double)x / kRandMax; }
+
+// ---------------------------------------------------------------- bead selection
+// chromo/util/bead_selection.pyx:19-192
+
+template <class R>
+__device__ long long capped_exponential(R& g, long long window, long long cap, unsigned& err) {
+  long long r = (long long)(-log10(unif(g.next()) + 0.00001) * (double)window * 0.45 + 1.0001);
+  int it = 0;
+  while (r > cap) {
+    if (g.fail) return cap;  // stream exhausted: reported by the caller
+    if (++it > kMaxIter) { err |= E_SPIN; return cap; }
+    r = (long long)(-log10(unif(g.next()) + 0.00001) * (double)window * 0.45 + 1.0001);
+  }
+  return r;
+}
+
+template <class R>
+__device__ long long from_left(R& g, long long window, long long n, unsigned& err) {
+  if (window > n) { err |= E_WINDOW; return 0; }
+  return capped_exponential(g, window, window, err);
+}
+
+template <class R>
+__device__ long long from_point(R& g, long long window, long long n, long long ind0, unsigned& err) {
+  if (window > n) { err |= E_WINDOW; return 0; }
+  if (window < 1) return ind0;
+  long long side = (long long)g.next() % 2;
+  if (side == 0) {
+    long long ws = window < ind0 ? window : ind0;
+    if (ws < 1) ws = 1;
+    long long ub = ind0 > 1 ? ind0 : 1;
+    return ub - from_left(g, ws, ub, err);
+  }
+  long long rem = n - ind0;
+  long long ws = window < rem ? window : rem;
+  if (ws < 1) ws = 1;
+  long long ub = rem > 1 ? rem : 1;
+  return from_left(g, ws, ub, err) + ind0;
+}
+
+__device__ __forceinline__ void check_bead_bounds(long long b0, long long b1, long long n,
+                                                  long long& i0, long long& i1) {
+  if (b0 > n) b0 = n;
+  if (b0 < 0) b0 = 0;
+  if (b1 > n) { i0 = b0; i1 = n; }
+  else if (b1 < 0) { i0 = 0; i1 = b0 + 1; }
+  else if (b0 == b1) { i0 = b0; i1 = b0 + 1; }
+  else { i0 = b0 < b1 ? b0 : b1; i1 = b0 > b1 ? b0 : b1; }
+}
+
+// ---------------------------------------------------------------- geometry
+// chromo/util/linalg.pyx:23-199
+
+template <class R>
+__device__ __forceinline__ void sphere(R& g, double v[3]) {
+  double phi = unif(g.next()) * (2.0 * 3.141592653589793);
+  double theta = acos(unif(g.next()) * 2 - 1);
+  double sp, cp, st, ct;
+  sincos(phi, &sp, &cp);
+  sincos(theta, &st, &ct);
+  v[0] = cp * st;
+  v[1] = sp * st;
+  v[2] = ct;
+}
+
+// Rotation by `ang` about unit axis a through point p: x' = M[:, :3] x + M[:, 3].
+__device__ __forceinline__ void axis_rotation(const double a[3], const double p[3], double ang,
+                                              double M[3][4]) {
+  double s, c;
+  sincos(ang, &s, &c);
+  double oc = 1 - c, a0 = a[0] * a[0], a1 = a[1] * a[1], a2 = a[2] * a[2];
+  M[0][0] = a0 + (a1 + a2) * c;
+  M[0][1] = a[0] * a[1] * oc - a[2] * s;
+  M[0][2] = a[0] * a[2] * oc + a[1] * s;
+  M[1][0] = a[0] * a[1] * oc + a[2] * s;
+  M[1][1] = a1 + (a0 + a2) * c;
+  M[1][2] = a[1] * a[2] * oc - a[0] * s;
+  M[2][0] = a[0] * a[2] * oc - a[1] * s;
+  M[2][1] = a[1] * a[2] * oc + a[0] * s;
+  M[2][2] = a2 + (a0 + a1) * c;
+  M[0][3] = (p[1] * a[2] - p[2] * a[1]) * s;
+  M[1][3] = (p[2] * a[0] - p[0] * a[2]) * s;
+  M[2][3] = (p[0] * a[1] - p[1] * a[0]) * s;
+  M[0][3] += (p[0] * (1 - a0) - a[0] * (p[1] * a[1] + p[2] * a[2])) * oc;
+  M[1][3] += (p[1] * (1 - a1) - a[1] * (p[0] * a[0] + p[2] * a[2])) * oc;
+  M[2][3] += (p[2] * (1 - a2) - a[2] * (p[0] * a[0] + p[1] * a[1])) * oc;
+}
+
+template <typename Pos>
+__device__ __forceinline__ void ld3(const V4<Pos>* a, long long i, double v[3]) {
+  V4<Pos> q = a[i];
+  v[0] = (double)q.x; v[1] = (double)q.y; v[2] = (double)q.z;
+}
+
+template <typename Pos>
+__device__ __forceinline__ double rnd_pos(double x) { return (double)(Pos)x; }
+
+// ---------------------------------------------------------------- SSWLC energy
+// chromo/polymers.pyx:1148-1346
+
+struct Bond { double eb, g, ep, epp, eta; };
+
+__device__ __forceinline__ Bond load_bond(const double* bonds, long long i) {
+  const double* b = bonds + 6 * i;
+  return Bond{b[0], b[1], b[2], b[3], b[4]};
+}
+
+__device__ __forceinline__ double e_pair(const Bond& b, const double bend[3], double par,
+                                         const double dp[3]) {
+  double x = par - b.g;
+  return 0.5 * b.eb * (bend[0] * bend[0] + bend[1] * bend[1] + bend[2] * bend[2])
+       + 0.5 * b.ep * (x * x)
+       + 0.5 * b.epp * (dp[0] * dp[0] + dp[1] * dp[1] + dp[2] * dp[2]);
+}
+
+// bond (0 -> 1) with bead 1 moved: bead_pair_dE_poly_forward
+__device__ __forceinline__ double pair_dE_fwd(const Bond& b, const double r0[3], const double r1[3],
+                                              const double tr1[3], const double t30[3],
+                                              const double t31[3], const double tt31[3]) {
+  double drt[3], dr[3], dpt[3], dp[3], bt[3], bc[3];
+  for (int i = 0; i < 3; i++) { drt[i] = tr1[i] - r0[i]; dr[i] = r1[i] - r0[i]; }
+  double pt = t30[0] * drt[0] + t30[1] * drt[1] + t30[2] * drt[2];
+  double pc = t30[0] * dr[0] + t30[1] * dr[1] + t30[2] * dr[2];
+  for (int i = 0; i < 3; i++) {
+    dpt[i] = drt[i] - t30[i] * pt;
+    dp[i] = dr[i] - t30[i] * pc;
+    bt[i] = tt31[i] - t30[i] - dpt[i] * b.eta;
+    bc[i] = t31[i] - t30[i] - dp[i] * b.eta;
+  }
+  return e_pair(b, bt, pt, dpt) - e_pair(b, bc, pc, dp);
+}
+
+// bond (0 -> 1) with bead 0 moved: bead_pair_dE_poly_reverse
+__device__ __forceinline__ double pair_dE_rev(const Bond& b, const double r0[3], const double tr0[3],
+                                              const double r1[3], const double t30[3],
+                                              const double tt30[3], const double t31[3]) {
+  double drt[3], dr[3], dpt[3], dp[3], bt[3], bc[3];
+  for (int i = 0; i < 3; i++) { drt[i] = r1[i] - tr0[i]; dr[i] = r1[i] - r0[i]; }
+  double pt = tt30[0] * drt[0] + tt30[1] * drt[1] + tt30[2] * drt[2];
+  double pc = t30[0] * dr[0] + t30[1] * dr[1] + t30[2] * dr[2];
+  for (int i = 0; i < 3; i++) {
+    dpt[i] = drt[i] - tt30[i] * pt;
+    dp[i] = dr[i] - t30[i] * pc;
+    bt[i] = t31[i] - tt30[i] - dpt[i] * b.eta;
+    bc[i] = t31[i] - t30[i] - dp[i] * b.eta;
+  }
+  return e_pair(b, bt, pt, dpt) - e_pair(b, bc, pc, dp);
+}
+
+// ---------------------------------------------------------------- density field
+// chromo/fields.pyx:1430-1673: eight trilinear weights and periodic voxel indices.
+
+__device__ __forceinline__ double pymod(double a, double b) {
+  double m = fmod(a, b);
+  if (m != 0 && ((m < 0) != (b < 0))) m += b;
+  return m;
+}
+
+__device__ __forceinline__ void voxel_weights(const RepDev& rd, const double pos[3], double w[8],
+                                              int v[8]) {
+  const double width[3] = {rd.wx, rd.wy, rd.wz};
+  const int n[3] = {rd.nx, rd.ny, rd.nz};
+  double wl[3];
+  int lo[3], hi[3];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    double d = width[j] / (double)n[j];
+    double x = pymod(pos[j] + 0.5 * width[j], width[j]) - 0.5 * d;
+    long long ind = (long long)floor(x / d);
+    int li = ind == -1 ? n[j] - 1 : (int)ind;
+    lo[j] = li < 0 ? 0 : (li >= n[j] ? n[j] - 1 : li);  // in range for finite x; guards the rest
+    hi[j] = lo[j] + 1 == n[j] ? 0 : lo[j] + 1;
+    wl[j] = 1 - (x / d - (double)ind);
+  }
+#pragma unroll
+  for (int l = 0; l < 8; l++) {
+    int bx = l & 1, by = (l >> 1) & 1, bz = (l >> 2) & 1;
+    double fx = bx ? (1 - wl[0]) : wl[0];
+    double fy = by ? (1 - wl[1]) : wl[1];
+    double fz = bz ? (1 - wl[2]) : wl[2];
+    w[l] = fx * fy * fz;
+    v[l] = (bx ? hi[0] : lo[0]) + rd.nx * ((by ? hi[1] : lo[1]) + rd.ny * (bz ? hi[2] : lo[2]));
+  }
+}
+
+__device__ __forceinline__ long long q40(double w) { return __double2ll_rn(w * kFxScale); }
+
+// ---------------------------------------------------------------- warp helpers
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+}  // namespace cg

@@ -1,0 +1,72 @@
+// cg_kernels.h -- arguments shared by the host C ABI and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "cg_device.cuh"
+
+namespace cg {
+
+// Per-warp header at the start of the warp's shared-memory region.
+struct WarpShared {
+  RepDev rd;
+  cg_move_ctl ctl[5];
+  unsigned long long tally[30];
+  int nused;
+  int pad[3];
+};
+
+struct KArgs {
+  RepDev* reps;
+  cg_move_ctl* ctl;
+  int n_ctl, n_reps;
+  unsigned long long* tally;  // [n_reps * 30]
+  void* r4;                   // V4<Pos> per bead (all replicas concatenated)
+  void* t34;
+  void* t24;
+  unsigned* states;           // packed int8 binding states per bead
+  unsigned* marks;            // packed int8 chemical_mods per bead
+  const double* bonds;        // 6 doubles per bead (bond i -> i+1)
+  long long* grid;            // ncol int64 per voxel
+  const double* access_vol;   // per voxel, or null
+  int ncol;
+  // per-replica global scratch for moves too large for shared memory
+  int* g_keys;
+  int* g_used;
+  long long* g_vals;
+  int g_logH;
+  void* g_stage;
+  int* g_idx;
+  long long g_stage_cap;
+  unsigned* picked;           // tangent-rotation bitmaps
+  const long long* picked_off;
+  // launch shape and shared-memory layout (bytes within one warp's region)
+  long long n_steps;
+  int wpb, logH;
+  long long stage_cap;
+  int warp_smem, off_keys, off_used, off_vals, off_stage, off_idx;
+  unsigned long long seed;
+  // audit mode
+  int audit_rep;
+  const unsigned* a_draws;
+  long long a_n_draws;
+  const signed char* a_bstates;
+  long long a_n_bstates;
+  cg_move_record* a_recs;
+  long long a_max_recs;
+  long long* a_out;
+  // replica exchange
+  int* rep_of_rung;
+  unsigned long long* swaps;
+  unsigned long long* swap_attempts;
+  unsigned long long* xround;  // exchange rounds performed (graph replays)
+};
+
+}  // namespace cg
+
+void cg_launch_mc(const cg::KArgs& a, bool fp64, bool audit, cudaStream_t s);
+cudaError_t cg_set_mc_smem(bool fp64, int bytes);
+void cg_launch_deposit(const cg::KArgs& a, bool fp64, int rep, int n_reps_launch, long long max_beads,
+                       cudaStream_t s);
+void cg_launch_energy(const cg::KArgs& a, bool fp64, double* out, cudaStream_t s);
+void cg_launch_exchange(const cg::KArgs& a, const double* eout, int n_rungs, long long round,
+                        unsigned long long seed, cudaStream_t s);

@@ -1,0 +1,829 @@
+// cg_mc.cu -- the MC inner loop of chromo on GB300 (sm_103a), one warp per replica.
+//
+// One launch runs `n_steps` MC steps (chromo/mc/mc_sim.pyx:88-103) on every
+// replica.  Warp w of the grid owns replica w: it keeps the replica's
+// parameters and move controllers in shared memory, proposes each move
+// (chromo/mc/move_funcs.pyx), evaluates the SSWLC elastic dE of the two
+// boundary bonds or of each rotated bead (chromo/polymers.pyx:1024-1346), the
+// binding dE from a precomputed single-site free-energy table
+// (:1383-1538), re-deposits the moved beads into the voxel grid by trilinear
+// weights and evaluates the chi / binder field dE over only the touched
+// voxels (chromo/fields.pyx:1149-1875), applies the Metropolis test
+// (chromo/mc/mc_sim.pyx:163-182) and commits.
+//
+// Touched voxels are deduplicated in a per-warp open-addressing hash in
+// shared memory whose values are int64 fixed-point density deltas (2^-40 of a
+// unit trilinear weight); the grid itself is int64 fixed point, so a deposit
+// is exactly undone by the opposite deposit and the grid never depends on the
+// order of updates.
+#include <cuda_runtime.h>
+
+#include "cg_device.cuh"
+#include "cg_kernels.h"
+
+namespace cg {
+
+
+// ---------------------------------------------------------------- hash insert
+__device__ __forceinline__ int hash_slot(int* keys, int* used, int* nused, int logH, int key,
+                                         unsigned& err) {
+  unsigned mask = (1u << logH) - 1u;
+  unsigned h = ((unsigned)key * 0x9E3779B1u) >> (32 - logH);
+  for (int it = 0; it <= (int)mask; it++) {
+    int prev = atomicCAS(&keys[h], -1, key);
+    if (prev == -1) {
+      int idx = atomicAdd(nused, 1);
+      used[idx] = (int)h;
+      return (int)h;
+    }
+    if (prev == key) return (int)h;
+    h = (h + 1) & mask;
+  }
+  err |= E_SPIN;
+  return -1;
+}
+
+__device__ __forceinline__ void add_delta(long long* vals, int ncol, int slot, int col, long long d) {
+  if (d != 0) atomicAdd((unsigned long long*)&vals[(long long)slot * ncol + col], (unsigned long long)d);
+}
+
+// Deposit +/- one bead's eight trilinear weights with binder states `st`
+// (packed int8) into the hash.
+__device__ __forceinline__ void deposit_bead(const RepDev& rd, int ncol, int* keys, int* used,
+                                             int* nused, long long* vals, int logH,
+                                             const double w[8], const int v[8], unsigned st,
+                                             bool negate, unsigned& err) {
+#pragma unroll
+  for (int l = 0; l < 8; l++) {
+    long long q = q40(w[l]);
+    if (negate) q = -q;
+    int slot = hash_slot(keys, used, nused, logH, v[l], err);
+    if (slot < 0) return;
+    add_delta(vals, ncol, slot, 0, q);
+    for (int b = 0; b < rd.nb; b++) add_delta(vals, ncol, slot, 1 + b, q * (long long)((st >> (8 * b)) & 0xFF));
+  }
+}
+
+// Field dE over the touched voxels (fixed-point grid); also stores the
+// post-move grid values into the hash values for the commit.
+__device__ double field_dE_voxels(const RepDev& rd, const KArgs& a, int ncol, const int* keys,
+                                  const int* used, long long* vals, int nused, int lane,
+                                  long long& n_vox) {
+  double part = 0;
+  const long long* grid = a.grid + rd.vox_off * ncol;
+  for (int i = lane; i < nused; i += 32) {
+    int slot = used[i];
+    int v = keys[slot];
+    long long* d = vals + (long long)slot * ncol;
+    const long long* gv = grid + (long long)v * ncol;
+    long long g0 = gv[0], d0 = d[0];
+    double V = rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin;
+    double c = 0, rho[CG_MAX_BINDERS], dd[CG_MAX_BINDERS];
+    for (int b = 0; b < rd.nb; b++) {
+      long long gb = gv[1 + b], db = d[1 + b];
+      rho[b] = ((double)gb * kFxInv) / V;
+      dd[b] = ((double)db * kFxInv) / V;
+      c += rd.pref[b] * (dd[b] * (2 * rho[b] + dd[b]));
+      d[1 + b] = gb + db;
+    }
+    for (int b = 0; b < rd.nb; b++)
+      for (int e = 0; e < rd.nb; e++)
+        c += rd.xpref[b * CG_MAX_BINDERS + e] * (rho[b] * dd[e] + dd[b] * rho[e] + dd[b] * dd[e]);
+    double vf0 = ((double)g0 * kFxInv) / V * rd.bead_vol;
+    double vf1 = ((double)(g0 + d0) * kFxInv) / V * rd.bead_vol;
+    double k = rd.chi * (V / rd.bead_vol);
+    if (vf1 > rd.vf_limit || vf0 > rd.vf_limit) {
+      c += (vf1 > rd.vf_limit ? kEHugeField * vf1 : k * vf1 * vf1)
+         - (vf0 > rd.vf_limit ? kEHugeField * vf0 : k * vf0 * vf0);
+    } else {
+      c += k * ((vf1 - vf0) * (vf1 + vf0));
+    }
+    d[0] = g0 + d0;
+    part += c;
+  }
+  n_vox = nused;
+  return warp_sum(part);
+}
+
+__device__ __forceinline__ void commit_grid(const RepDev& rd, const KArgs& a, int ncol, int* keys,
+                                            const int* used, long long* vals, int nused, int lane,
+                                            bool accept) {
+  long long* grid = a.grid + rd.vox_off * ncol;
+  for (int i = lane; i < nused; i += 32) {
+    int slot = used[i];
+    if (accept) {
+      int v = keys[slot];
+      for (int c = 0; c < ncol; c++) grid[(long long)v * ncol + c] = vals[(long long)slot * ncol + c];
+    }
+    keys[slot] = -1;
+    for (int c = 0; c < ncol; c++) vals[(long long)slot * ncol + c] = 0;
+  }
+}
+
+// confinement count of one position (chromo/fields.pyx:121-202)
+__device__ __forceinline__ int out_of_bounds(const RepDev& rd, const double p[3], bool trial) {
+  if (rd.confine_kind == 1)
+    return sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]) > rd.confine_length ? 1 : 0;
+  if (rd.confine_kind == 2 && trial) {
+    int o = 0;
+    for (int j = 0; j < 3; j++) o += fabs(p[j]) > rd.confine_length / 2 ? 1 : 0;
+    return o;
+  }
+  return 0;
+}
+
+__device__ __forceinline__ double bind_f(const RepDev& rd, int b, int nm, int s) {
+  return rd.bind_f[(b * (CG_MAX_MARK + 1) + nm) * (CG_MAX_MARK + 1) + s];
+}
+
+// ---------------------------------------------------------------- the kernel
+
+template <typename Pos, bool AUDIT>
+__global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rep = AUDIT ? a.audit_rep : blockIdx.x * a.wpb + warp;
+  if (!AUDIT && rep >= a.n_reps) return;
+  if (AUDIT && (blockIdx.x != 0 || warp != 0)) return;
+  unsigned char* base = smem + (size_t)warp * a.warp_smem;
+  WarpShared& ws = *reinterpret_cast<WarpShared*>(base);
+  int* s_keys = reinterpret_cast<int*>(base + a.off_keys);
+  int* s_used = reinterpret_cast<int*>(base + a.off_used);
+  long long* s_vals = reinterpret_cast<long long*>(base + a.off_vals);
+  Pos* s_stage = reinterpret_cast<Pos*>(base + a.off_stage);
+  int* s_idx = reinterpret_cast<int*>(base + a.off_idx);
+  const int ncol = a.ncol;
+
+  {  // load replica parameters and controllers into shared memory
+    const unsigned* src = reinterpret_cast<const unsigned*>(a.reps + rep);
+    unsigned* dst = reinterpret_cast<unsigned*>(&ws.rd);
+    for (int i = lane; i < (int)(sizeof(RepDev) / 4); i += 32) dst[i] = src[i];
+    const unsigned* cs = reinterpret_cast<const unsigned*>(a.ctl + (long long)rep * 5);
+    unsigned* cd = reinterpret_cast<unsigned*>(ws.ctl);
+    for (int i = lane; i < (int)(5 * sizeof(cg_move_ctl) / 4); i += 32) cd[i] = cs[i];
+    for (int i = lane; i < (1 << a.logH); i += 32) s_keys[i] = -1;
+    for (int i = lane; i < (1 << a.logH) * ncol; i += 32) s_vals[i] = 0;
+    if (lane < 30) ws.tally[lane] = 0;
+    if (lane == 0) ws.nused = 0;
+  }
+  __syncwarp();
+  const RepDev& rd = ws.rd;
+  const long long N = rd.n_beads;
+  const V4<Pos>* r4 = reinterpret_cast<const V4<Pos>*>(a.r4) + rd.bead_off;
+  const V4<Pos>* t34 = reinterpret_cast<const V4<Pos>*>(a.t34) + rd.bead_off;
+  const V4<Pos>* t24 = reinterpret_cast<const V4<Pos>*>(a.t24) + rd.bead_off;
+  V4<Pos>* r4w = reinterpret_cast<V4<Pos>*>(a.r4) + rd.bead_off;
+  V4<Pos>* t34w = reinterpret_cast<V4<Pos>*>(a.t34) + rd.bead_off;
+  V4<Pos>* t24w = reinterpret_cast<V4<Pos>*>(a.t24) + rd.bead_off;
+  unsigned* st = a.states + rd.bead_off;
+  const unsigned* mk = a.marks + rd.bead_off;
+  const double* bonds = a.bonds + rd.bead_off * 6;
+  // per-replica global scratch (used when a move is too large for shared memory)
+  int* g_keys = a.g_keys + (long long)rep * (1 << a.g_logH);
+  int* g_used = a.g_used + (long long)rep * (1 << a.g_logH);
+  long long* g_vals = a.g_vals + (long long)rep * (1 << a.g_logH) * ncol;
+  Pos* g_stage = reinterpret_cast<Pos*>(a.g_stage) + (long long)rep * a.g_stage_cap * 9;
+  int* g_idx = a.g_idx + (long long)rep * a.g_stage_cap;
+  unsigned* picked = a.picked + a.picked_off[rep];
+
+  Rng<AUDIT> g;
+  if constexpr (AUDIT) {
+    g.draws = a.a_draws; g.n = a.a_n_draws; g.bs = a.a_bstates; g.nbs = a.a_n_bstates;
+    g.pos = 0; g.bpos = 0; g.fail = false;
+  } else {
+    g.init(a.seed, rep, rd.draw_pos, rd.bstate_pos);
+  }
+  unsigned err = rd.err;
+  double run_dE = rd.run_dE;
+  long long nrec = 0;
+  unsigned long long* tally = ws.tally;
+
+  for (long long step = 0; step < a.n_steps && !err; step++) {
+    for (int ci = 0; ci < a.n_ctl && !err; ci++) {
+      cg_move_ctl& c = ws.ctl[ci];
+      const int kind = (int)c.move_kind;
+      if (c.move_on == 1) {
+        for (long long jj = 0; jj < c.num_per_cycle && !err; jj++) {
+          // ------------------------------------------------ one mc_step
+          const unsigned long long draw0 = g.pos;
+          const bool check_field = rd.field_kind != 0 && kind != CG_TANGENT_ROTATION;
+          const bool density = rd.field_kind == 2;
+          if (lane == 0) c.num_attempt += 1;  // moves.pyx:151
+          long long ind0 = 0, indf = 0, m = 0;
+          int bsel = -1;
+          double dEp = 0, dEf = 0;
+          long long nvox = 0;
+          bool empty = false;
+          int* keys = s_keys; int* used = s_used; long long* vals = s_vals; int logH = a.logH;
+          Pos* stage = s_stage;
+          int* idx = s_idx;
+          if (kind <= CG_SLIDE) {
+            // ---------------- segment moves: crank_shaft / end_pivot / slide
+            double M[3][4];
+            if (kind == CG_CRANK_SHAFT) {  // move_funcs.pyx:39-101, 157-280
+              double ang = c.amp_move * (unif(g.next()) - 0.5);
+              long long b0 = (int)(unif(g.next()) * (double)N);
+              long long b1 = from_point(g, c.amp_bead, N, b0, err);
+              if (b1 < 1) b1 = 1;
+              check_bead_bounds(b0, b1, N, ind0, indf);
+              double pa[3], pb[3], dir[3], p[3];
+              long long ia, ib;
+              if (ind0 == indf - 1 && ind0 == 0) { ia = indf; ib = ind0; }
+              else if (ind0 == indf - 1 && ind0 == N - 1) { ia = ind0; ib = ind0 - 1; }
+              else if (ind0 == 0 && indf == N) { ia = indf - 1; ib = ind0; }
+              else if (ind0 == 0) { ia = indf; ib = ind0; }
+              else if (indf == N) { ia = indf - 1; ib = ind0 - 1; }
+              else { ia = indf; ib = ind0 - 1; }
+              if (err) break;
+              ld3(r4, ia, pa); ld3(r4, ib, pb);
+              for (int i = 0; i < 3; i++) dir[i] = pa[i] - pb[i];
+              double mag = sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+              if (mag < 1E-5) sphere(g, dir);
+              else { double sc = 1.0 / mag; for (int i = 0; i < 3; i++) dir[i] = dir[i] * sc; }
+              long long ip;
+              if (ind0 == 0 && indf != N) ip = indf;
+              else if (ind0 != 0 && indf == N) ip = ind0 - 1;
+              else if (ind0 == 0 && indf == N) ip = ind0;
+              else ip = ind0 - 1;
+              ld3(r4, ip, p);
+              axis_rotation(dir, p, ang, M);
+            } else if (kind == CG_END_PIVOT) {  // move_funcs.pyx:285-398
+              double ang = c.amp_move * (unif(g.next()) - 0.5);
+              long long lhs = (long long)g.next() % 2;
+              if (lhs == 1) { ind0 = 0; indf = from_left(g, c.amp_bead, N, err) + 1; }
+              else { ind0 = N - from_left(g, c.amp_bead, N, err); indf = N; }
+              double axis[3], p[3];
+              sphere(g, axis);
+              long long ip;
+              if (ind0 == 0 && indf != N) ip = indf;
+              else if (ind0 != 0 && indf == N) ip = ind0 - 1;
+              else if (ind0 == 0 && indf == N && lhs == 1) ip = indf - 1;
+              else ip = ind0;
+              if (err) break;
+              ld3(r4, ip, p);
+              axis_rotation(axis, p, ang, M);
+            } else {  // slide, move_funcs.pyx:403-465
+              double amp = c.amp_move * unif(g.next()), d[3];
+              sphere(g, d);
+              for (int i = 0; i < 3; i++) { M[i][3] = d[i] * amp; }
+              long long b0 = (long long)g.next() % N;
+              long long b1 = from_point(g, c.amp_bead, N, b0, err);
+              check_bead_bounds(b0, b1, N, ind0, indf);
+            }
+            if (err) break;
+            m = indf - ind0;
+            if (m == 0) {
+              empty = true;
+            } else {
+              if (m > a.stage_cap) { stage = g_stage; }
+              const bool smem_hash = 16 * m * 2 <= (1LL << a.logH);
+              if (!smem_hash) { keys = g_keys; used = g_used; vals = g_vals; logH = a.g_logH; }
+              double part = 0;
+              int oob = 0;
+              for (long long k = lane; k < m; k += 32) {
+                const long long i = ind0 + k;
+                V4<Pos> R = r4[i], T3 = t34[i], T2 = t24[i];
+                double r[3] = {(double)R.x, (double)R.y, (double)R.z};
+                double t3[3] = {(double)T3.x, (double)T3.y, (double)T3.z};
+                double t2[3] = {(double)T2.x, (double)T2.y, (double)T2.z};
+                double tr[3], tt3[3], tt2[3];
+                if (kind == CG_SLIDE) {
+                  for (int j = 0; j < 3; j++) { tr[j] = rnd_pos<Pos>(r[j] + M[j][3]); tt3[j] = t3[j]; tt2[j] = t2[j]; }
+                } else {
+                  for (int j = 0; j < 3; j++) {
+                    double er = 0, e3 = 0, e2 = 0;
+                    for (int q = 0; q < 3; q++) { er += M[j][q] * r[q]; e3 += M[j][q] * t3[q]; e2 += M[j][q] * t2[q]; }
+                    tr[j] = rnd_pos<Pos>(er + M[j][3]);
+                    tt3[j] = rnd_pos<Pos>(e3);
+                    tt2[j] = rnd_pos<Pos>(e2);
+                  }
+                }
+                const bool fin = isfinite(tr[0]) && isfinite(tr[1]) && isfinite(tr[2]);
+                if (!fin) err |= E_NONFINITE;
+                Pos* sg = stage + k * 9;
+                for (int j = 0; j < 3; j++) { sg[j] = (Pos)tr[j]; sg[3 + j] = (Pos)tt3[j]; sg[6 + j] = (Pos)tt2[j]; }
+                if (k == 0 && ind0 != 0) {  // continuous_dE_poly forward bond, polymers.pyx:1121-1131
+                  double r0[3], t30[3];
+                  ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
+                  part += pair_dE_fwd(load_bond(bonds, i - 1), r0, r, tr, t30, t3, tt3);
+                }
+                if (k == m - 1 && indf != N) {  // reverse bond, polymers.pyx:1132-1142
+                  double r1[3], t31[3];
+                  ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
+                  part += pair_dE_rev(load_bond(bonds, i), r, tr, r1, t3, tt3, t31);
+                }
+                if (check_field && rd.confine_kind) {
+                  oob += out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
+                }
+                if (density && fin) {
+                  double w0[8], w1[8];
+                  int v0[8], v1[8];
+                  voxel_weights(rd, r, w0, v0);
+                  voxel_weights(rd, tr, w1, v1);
+                  unsigned s = st[i];
+                  deposit_bead(rd, ncol, keys, used, &ws.nused, vals, logH, w0, v0, s, true, err);
+                  deposit_bead(rd, ncol, keys, used, &ws.nused, vals, logH, w1, v1, s, false, err);
+                }
+              }
+              err = __reduce_or_sync(kFull, err);
+              dEp = warp_sum(part);
+              if (check_field) {
+                int oo = __reduce_add_sync(kFull, (unsigned)oob);
+                double conf = 0;
+                conf += (double)(oo >> 16) * kEHugeField;
+                conf -= (double)(oo & 0xFFFF) * kEHugeField;
+                dEf = conf;
+              }
+              __syncwarp();
+              if (density) {
+                int nu = ws.nused;
+                dEf += field_dE_voxels(rd, a, ncol, keys, used, vals, nu, lane, nvox);
+              }
+            }
+          } else if (kind == CG_TANGENT_ROTATION) {
+            // ---------------- tangent_rotation, move_funcs.pyx:470-582
+            double ang = c.amp_move * (unif(g.next()) - 0.5);
+            long long n = (long long)g.next() % c.amp_bead + 1;
+            if (n > N) { err |= E_WINDOW; break; }
+            m = n;
+            if (m > a.stage_cap) { stage = g_stage; idx = g_idx; }
+            // distinct random beads, drawn in order with redraws (get_inds)
+            long long got = 0;
+            int it = 0;
+            while (got < n) {
+              if (++it > kMaxIter) { err |= E_SPIN; break; }
+              bool ok;
+              unsigned x = g.at(g.pos + lane, ok);
+              long long cand = ok ? (long long)x % N : -1 - lane;
+              unsigned grp = __match_any_sync(kFull, cand);
+              bool first = (grp & ((1u << lane) - 1u)) == 0;
+              bool fresh = ok && first && !((picked[cand >> 5] >> (cand & 31)) & 1u);
+              unsigned bal = __ballot_sync(kFull, fresh);
+              unsigned okb = __ballot_sync(kFull, ok);
+              long long need = n - got;
+              int cnt = __popc(bal);
+              int rank = __popc(bal & ((1u << lane) - 1u));
+              if (fresh && rank < need) {
+                idx[got + rank] = (int)cand;
+                atomicOr(&picked[cand >> 5], 1u << (cand & 31));
+              }
+              long long consumed;
+              if (cnt >= need) {
+                unsigned b = bal;
+                for (long long q = 1; q < need; q++) b &= b - 1;
+                consumed = __ffs(b);  // lane of the last needed candidate + 1
+                got = n;
+              } else {
+                consumed = 32;
+                got += cnt;
+              }
+              if ((okb & (consumed >= 32 ? kFull : ((1u << consumed) - 1u))) !=
+                  (consumed >= 32 ? kFull : ((1u << consumed) - 1u))) {
+                g.fail = true; err |= E_STREAM;
+              }
+              g.pos += consumed;
+              __syncwarp();
+            }
+            if (err) break;
+            const unsigned long long axis_base = g.pos;
+            double part = 0;
+            for (long long k = lane; k < m; k += 32) {
+              const long long i = idx[k];
+              bool ok1, ok2;
+              double phi = unif(g.at(axis_base + 2 * k, ok1)) * (2.0 * 3.141592653589793);
+              double theta = acos(unif(g.at(axis_base + 2 * k + 1, ok2)) * 2 - 1);
+              if (!(ok1 && ok2)) err |= E_STREAM;
+              double sp, cp, sth, cth;
+              sincos(phi, &sp, &cp);
+              sincos(theta, &sth, &cth);
+              const double axis[3] = {cp * sth, sp * sth, cth};
+              const double origin[3] = {0, 0, 0};
+              double M[3][4];
+              axis_rotation(axis, origin, ang, M);
+              double r[3], t3[3], t2[3], tt3[3], tt2[3];
+              ld3(r4, i, r); ld3(t34, i, t3); ld3(t24, i, t2);
+              for (int j = 0; j < 3; j++) {
+                double e3 = 0, e2 = 0;
+                for (int q = 0; q < 3; q++) { e3 += M[j][q] * t3[q]; e2 += M[j][q] * t2[q]; }
+                tt3[j] = rnd_pos<Pos>(e3);
+                tt2[j] = rnd_pos<Pos>(e2);
+              }
+              Pos* sg = stage + k * 9;
+              for (int j = 0; j < 3; j++) { sg[3 + j] = (Pos)tt3[j]; sg[6 + j] = (Pos)tt2[j]; }
+              double de = 0;
+              if (i != 0) {
+                double r0[3], t30[3];
+                ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
+                de += pair_dE_fwd(load_bond(bonds, i - 1), r0, r, r, t30, t3, tt3);
+              }
+              if (i + 1 != N) {
+                double r1[3], t31[3];
+                ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
+                de += pair_dE_rev(load_bond(bonds, i), r, r, r1, t3, tt3, t31);
+              }
+              part += de;
+            }
+            g.pos = axis_base + 2 * (unsigned long long)m;
+            err = __reduce_or_sync(kFull, err);
+            dEp = warp_sum(part);
+            ind0 = idx[0]; indf = ind0 + 1;
+          } else {
+            // ---------------- change_binding_state, move_funcs.pyx:717-820
+            bsel = (int)((long long)g.next() % rd.nb);
+            long long b0 = (long long)g.next() % N;
+            long long b1 = from_point(g, c.amp_bead, N, b0, err);
+            if (err) break;
+            check_bead_bounds(b0, b1, N, ind0, indf);
+            m = indf - ind0;
+            const int nt = rd.sites[bsel];
+            if (m > a.stage_cap) idx = g_idx;
+            const bool smem_hash = 8 * m * 2 <= (1LL << a.logH);
+            if (!smem_hash) { keys = g_keys; used = g_used; vals = g_vals; logH = a.g_logH; }
+            double part = 0;
+            int dbl = 0;  // doubly-bound trial minus current, chosen binder (fields.pyx:1877-1937)
+            for (long long k = lane; k < m; k += 32) {
+              const long long i = ind0 + k;
+              bool ok;
+              int s_new = g.state_at(g.bpos + k, nt, ok);
+              if (!ok) err |= E_STREAM;
+              unsigned sw = st[i], mw = mk[i];
+              int s_old = (int)((sw >> (8 * bsel)) & 0xFF);
+              // bead_binding_dE, polymers.pyx:1408-1538
+              double de = 0;
+              if (rd.max_binders != -1) {
+                int tot_t = 0, tot_c = 0;
+                for (int h = 0; h < rd.nb; h++) {
+                  int sh = (int)((sw >> (8 * h)) & 0xFF);
+                  tot_c += sh;
+                  tot_t += h == bsel ? s_new : sh;
+                }
+                if (tot_t > rd.max_binders) de += kEHugePoly * (double)(tot_t - rd.max_binders);
+                if (tot_c > rd.max_binders) de -= kEHugePoly * (double)(tot_c - rd.max_binders);
+              }
+              for (int b = 0; b < rd.nb; b++) {
+                int sc = (int)((sw >> (8 * b)) & 0xFF);
+                int stt = b == bsel ? s_new : sc;
+                int nm = (int)((mw >> (8 * b)) & 0xFF);
+                de += bind_f(rd, b, nm, stt);
+                de -= bind_f(rd, b, nm, sc);
+                if (rd.mu[b] > 0) {
+                  double me = rd.mu[b] * (-rd.mu_adjust + 2);
+                  de -= (double)stt * me;
+                  de += (double)sc * me;
+                } else {
+                  de -= (double)stt * rd.mu[b] * rd.mu_adjust;
+                  de += (double)sc * rd.mu[b] * rd.mu_adjust;
+                }
+              }
+              part += de;
+              dbl += (s_new == 2 ? 1 : 0) - (s_old == 2 ? 1 : 0);
+              idx[k] = s_new;
+              if (density && s_new != s_old) {
+                double p[3], w[8];
+                int v[8];
+                ld3(r4, i, p);
+                voxel_weights(rd, p, w, v);
+#pragma unroll
+                for (int l = 0; l < 8; l++) {
+                  int slot = hash_slot(keys, used, &ws.nused, logH, v[l], err);
+                  if (slot < 0) break;
+                  add_delta(vals, ncol, slot, 1 + bsel, q40(w[l]) * (long long)(s_new - s_old));
+                }
+              }
+            }
+            g.bpos += (unsigned long long)m;
+            err = __reduce_or_sync(kFull, err);
+            dEp = warp_sum(part);
+            int ddb = __reduce_add_sync(kFull, (unsigned)dbl);
+            if (check_field && rd.field_kind == 1 && rd.confine_kind == 2) {
+              // NullField evaluates the (cubical) confinement on binding moves too
+              int oob = 0;
+              for (long long k = lane; k < m; k += 32) {
+                double p[3];
+                ld3(r4, ind0 + k, p);
+                oob += out_of_bounds(rd, p, true);
+              }
+              dEf = (double)__reduce_add_sync(kFull, (unsigned)oob) * kEHugeField;
+            }
+            __syncwarp();
+            if (density) {
+              int nu = ws.nused;
+              dEf += field_dE_voxels(rd, a, ncol, keys, used, vals, nu, lane, nvox);
+              dEf += rd.intra[bsel] * (double)ddb;
+            }
+          }
+          if (AUDIT && g.fail) err |= E_STREAM;
+          if (err) break;
+          // ------------------------------------------------ Metropolis + commit
+          int accepted = -1;
+          if (!empty) {
+            double dE = 0;
+            dE += dEp;
+            dE += dEf;
+            double ex = exp(-dE);
+            bool acc = unif(g.next()) < ex;
+            if (AUDIT && g.fail) { err |= E_STREAM; break; }
+            accepted = acc ? 1 : 0;
+            if (acc) {
+              if (kind <= CG_SLIDE) {
+                for (long long k = lane; k < m; k += 32) {
+                  const Pos* sg = stage + k * 9;
+                  const long long i = ind0 + k;
+                  r4w[i] = V4<Pos>{sg[0], sg[1], sg[2], (Pos)0};
+                  if (kind != CG_SLIDE) {
+                    t34w[i] = V4<Pos>{sg[3], sg[4], sg[5], (Pos)0};
+                    t24w[i] = V4<Pos>{sg[6], sg[7], sg[8], (Pos)0};
+                  }
+                }
+              } else if (kind == CG_TANGENT_ROTATION) {
+                for (long long k = lane; k < m; k += 32) {
+                  const Pos* sg = stage + k * 9;
+                  const long long i = idx[k];
+                  t34w[i] = V4<Pos>{sg[3], sg[4], sg[5], (Pos)0};
+                  t24w[i] = V4<Pos>{sg[6], sg[7], sg[8], (Pos)0};
+                }
+              } else {
+                for (long long k = lane; k < m; k += 32) {
+                  const long long i = ind0 + k;
+                  unsigned sw = st[i];
+                  sw = (sw & ~(0xFFu << (8 * bsel))) | ((unsigned)idx[k] << (8 * bsel));
+                  st[i] = sw;
+                }
+              }
+              if (lane == 0) { c.num_success += 1; run_dE += dE; }
+            }
+            if (density && check_field) commit_grid(rd, a, ncol, keys, used, vals, ws.nused, lane, acc);
+            if (kind == CG_TANGENT_ROTATION) {
+              for (long long k = lane; k < m; k += 32) {
+                int i = idx[k];
+                atomicAnd(&picked[i >> 5], ~(1u << (i & 31)));
+              }
+            }
+            if (lane == 0) {
+              c.acc_rate = c.alpha * (acc ? 1.0 : 0.0) + (1 - c.alpha) * c.acc_rate;
+              tally[kind * 6 + 1] += acc ? 1 : 0;
+              tally[kind * 6 + 4] += acc ? (unsigned long long)m : 0;
+              tally[kind * 6 + 5] += acc ? (unsigned long long)nvox : 0;
+            }
+          }
+          if (lane == 0) {
+            tally[kind * 6 + 0] += 1;
+            tally[kind * 6 + 2] += (unsigned long long)m;
+            tally[kind * 6 + 3] += (unsigned long long)nvox;
+          }
+          __syncwarp();
+          if (lane == 0) ws.nused = 0;
+          if (AUDIT && lane == 0 && nrec < a.a_max_recs) {
+            cg_move_record rec;
+            rec.kind = kind; rec.n_inds = (int)m; rec.ind0 = (int)ind0; rec.indf = (int)indf;
+            rec.dE_poly = empty ? 0.0 : dEp; rec.dE_field = empty ? 0.0 : dEf;
+            rec.accepted = accepted; rec.n_draws = (int)(g.pos - draw0);
+            a.a_recs[nrec] = rec;
+          }
+          nrec++;
+          __syncwarp();
+        }
+      }
+      // SimpleControl.update_amplitudes, mc_controller.py:126-189
+      if (lane == 0 && c.ctrl_kind == 1) {
+        double acc = c.acc_rate;
+        if (acc < 0.5) {
+          double prop = c.amp_move * 0.95;
+          if (prop > c.move_lo) c.amp_move = prop;
+          else {
+            c.amp_move = c.move_hi;
+            double nb = (double)(c.amp_bead - 1);
+            c.amp_bead = (long long)(c.bead_lo > nb ? c.bead_lo : nb);
+          }
+        } else if (acc > 0.5) {
+          double prop = c.amp_move / 0.95;
+          if (prop < c.move_hi) c.amp_move = prop;
+          else {
+            c.amp_move = c.move_lo;
+            double nb = (double)(c.amp_bead + 1);
+            c.amp_bead = (long long)(c.bead_hi < nb ? c.bead_hi : nb);
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  // ------------------------------------------------ write back
+  __syncwarp();
+  {
+    unsigned* cd = reinterpret_cast<unsigned*>(a.ctl + (long long)rep * 5);
+    const unsigned* cs = reinterpret_cast<const unsigned*>(ws.ctl);
+    for (int i = lane; i < (int)(5 * sizeof(cg_move_ctl) / 4); i += 32) cd[i] = cs[i];
+  }
+  if (lane == 0) {
+    RepDev* out = a.reps + rep;
+    out->draw_pos = AUDIT ? rd.draw_pos : g.pos;
+    out->bstate_pos = AUDIT ? rd.bstate_pos : g.bpos;
+    out->run_dE = run_dE;
+    out->err = err;
+    if (AUDIT) {
+      a.a_out[0] = nrec;
+      a.a_out[1] = (long long)g.pos;
+      a.a_out[2] = (long long)g.bpos;
+    }
+    unsigned long long* t = a.tally + (long long)rep * 30;
+    for (int i = 0; i < 30; i++) t[i] += tally[i];
+  }
+}
+
+// ---------------------------------------------------------------- re-deposit
+// update_all_densities_for_all_polymers (chromo/fields.pyx:2041-2106): every
+// bead adds its eight fixed-point weights; int64 atomics make the result
+// independent of the order of the adds.
+template <typename Pos>
+__global__ void deposit_kernel(KArgs a, int rep_only) {
+  const int rep = rep_only >= 0 ? rep_only : blockIdx.y;
+  const RepDev& rd = a.reps[rep];
+  if (rd.field_kind != 2) return;
+  const V4<Pos>* r4 = reinterpret_cast<const V4<Pos>*>(a.r4) + rd.bead_off;
+  long long* grid = a.grid + rd.vox_off * a.ncol;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < rd.n_beads;
+       i += (long long)gridDim.x * blockDim.x) {
+    double p[3], w[8];
+    int v[8];
+    ld3(r4, i, p);
+    voxel_weights(rd, p, w, v);
+    unsigned s = a.states[rd.bead_off + i];
+    for (int l = 0; l < 8; l++) {
+      long long q = q40(w[l]);
+      atomicAdd((unsigned long long*)&grid[(long long)v[l] * a.ncol], (unsigned long long)q);
+      for (int b = 0; b < rd.nb; b++) {
+        long long qb = q * (long long)((s >> (8 * b)) & 0xFF);
+        if (qb) atomicAdd((unsigned long long*)&grid[(long long)v[l] * a.ncol + 1 + b], (unsigned long long)qb);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- FP64 energies
+// one block per replica; deterministic block tree reduction.
+__device__ double block_sum(double v, double* sh) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0;
+  if (threadIdx.x < 32) {
+    t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+    t = warp_sum(t);
+  }
+  return t;  // valid in warp 0
+}
+
+template <typename Pos>
+__global__ void energy_kernel(KArgs a, double* out) {
+  __shared__ double sh[32];
+  const int rep = blockIdx.x;
+  const RepDev& rd = a.reps[rep];
+  const V4<Pos>* r4 = reinterpret_cast<const V4<Pos>*>(a.r4) + rd.bead_off;
+  const V4<Pos>* t34 = reinterpret_cast<const V4<Pos>*>(a.t34) + rd.bead_off;
+  const double* bonds = a.bonds + rd.bead_off * 6;
+  const unsigned* st = a.states + rd.bead_off;
+  const unsigned* mk = a.marks + rd.bead_off;
+  double el = 0, bi = 0, fe = 0, sx = 0;
+  long long dbl[CG_MAX_BINDERS] = {0, 0, 0};
+  for (long long i = threadIdx.x; i < rd.n_beads; i += blockDim.x) {
+    if (i > 0) {  // SSWLC.compute_E, polymers.pyx:1348-1381
+      double r0[3], r1[3], a0[3], a1[3], dr[3], dp[3], bend[3];
+      ld3(r4, i - 1, r0); ld3(r4, i, r1); ld3(t34, i - 1, a0); ld3(t34, i, a1);
+      Bond b = load_bond(bonds, i - 1);
+      for (int j = 0; j < 3; j++) dr[j] = r1[j] - r0[j];
+      double par = a0[0] * dr[0] + a0[1] * dr[1] + a0[2] * dr[2];
+      for (int j = 0; j < 3; j++) dp[j] = dr[j] - a0[j] * par;
+      for (int j = 0; j < 3; j++) bend[j] = a1[j] + (-a0[j] - b.eta * dp[j]);
+      el += e_pair(b, bend, par, dp);
+    }
+    unsigned sw = st[i], mw = mk[i];
+    int tot = 0;
+    for (int b = 0; b < rd.nb; b++) {
+      int s = (int)((sw >> (8 * b)) & 0xFF), nm = (int)((mw >> (8 * b)) & 0xFF);
+      double me = rd.mu[b] > 0 ? rd.mu[b] * (-rd.mu_adjust + 2) : rd.mu[b] * rd.mu_adjust;
+      bi += bind_f(rd, b, nm, s) - (double)s * me;
+      tot += s;
+      dbl[b] += s == 2;
+    }
+    if (rd.max_binders != -1 && tot > rd.max_binders) bi += kEHugePoly * (double)(tot - rd.max_binders);
+  }
+  if (rd.field_kind == 2) {
+    const long long* grid = a.grid + rd.vox_off * a.ncol;
+    for (long long v = threadIdx.x; v < rd.n_vox; v += blockDim.x) {
+      double V = rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin;
+      double rho[CG_MAX_BINDERS];
+      for (int b = 0; b < rd.nb; b++) rho[b] = ((double)grid[v * a.ncol + 1 + b] * kFxInv) / V;
+      for (int b = 0; b < rd.nb; b++) fe += rd.pref[b] * rho[b] * rho[b];
+      for (int b = 0; b < rd.nb; b++)
+        for (int e = 0; e < rd.nb; e++) fe += rd.xpref[b * CG_MAX_BINDERS + e] * rho[b] * rho[e];
+      double vf = ((double)grid[v * a.ncol] * kFxInv) / V * rd.bead_vol;
+      double sv = (V / rd.bead_vol) * vf * vf;
+      sx += sv;
+      fe += vf > rd.vf_limit ? kEHugeField * vf : rd.chi * sv;
+    }
+  }
+  double t_el = block_sum(el, sh);
+  double t_bi = block_sum(bi, sh);
+  double t_fe = block_sum(fe, sh);
+  double t_sx = block_sum(sx, sh);
+  double t_db[CG_MAX_BINDERS];
+  for (int b = 0; b < CG_MAX_BINDERS; b++) t_db[b] = block_sum((double)dbl[b], sh);
+  if (threadIdx.x == 0) {
+    double intra = 0;
+    for (int b = 0; b < rd.nb; b++) intra += rd.intra[b] * t_db[b];
+    out[rep * 5 + 0] = t_el;
+    out[rep * 5 + 1] = t_bi;
+    out[rep * 5 + 2] = rd.field_kind == 2 ? t_fe + intra : 0.0;
+    out[rep * 5 + 3] = rd.run_dE;
+    out[rep * 5 + 4] = t_sx;
+  }
+}
+
+// ---------------------------------------------------------------- replica exchange
+// Swap chi between neighbouring rungs of each ladder (n_rungs consecutive
+// rung slots per ladder).  eout[5 r + 4] holds S_r = sum over voxels of
+// (V/Vb) vf^2, the chi-free part of replica r's field energy, so that
+// E_r = chi_r S_r + (chi-independent terms).  One block; round < 0 takes the
+// round number from a device counter and advances it (graph replays).
+__global__ void exchange_kernel(KArgs a, const double* eout, int n_rungs, long long round_in,
+                                unsigned long long seed) {
+  __shared__ long long round_sh;
+  if (threadIdx.x == 0) round_sh = round_in >= 0 ? round_in : (long long)a.xround[0];
+  __syncthreads();
+  const long long round = round_sh;
+  const int parity = (int)(round & 1);
+  const int ladders = a.n_reps / n_rungs;
+  const int per = n_rungs / 2;
+  for (int t = threadIdx.x; t < ladders * per; t += blockDim.x) {
+    const int ladder = t / per, pair = t % per;
+    if (2 * pair + 1 + parity >= n_rungs) continue;
+    const int ra = ladder * n_rungs + 2 * pair + parity, rb = ra + 1;
+    const int ia = a.rep_of_rung[ra], ib = a.rep_of_rung[rb];
+    const double ca = a.reps[ia].chi, cb = a.reps[ib].chi;
+    const double x = (ca - cb) * (eout[5 * ia + 4] - eout[5 * ib + 4]);
+    uint4 o = philox(make_uint4((unsigned)round, (unsigned)(round >> 32), (unsigned)ra, 0x3C6EF372u),
+                     make_uint2((unsigned)seed ^ 0xA4093822u, (unsigned)(seed >> 32)));
+    const double u = (double)(o.x >> 1) / kRandMax;
+    if (u < exp(x)) {
+      a.reps[ia].chi = cb;
+      a.reps[ib].chi = ca;
+      a.rep_of_rung[ra] = ib;
+      a.rep_of_rung[rb] = ia;
+      a.swaps[ra] += 1;
+    }
+    a.swap_attempts[ra] += 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && round_in < 0) a.xround[0] += 1;
+}
+
+// ---------------------------------------------------------------- launchers
+
+template <typename Pos>
+static void launch_mc_t(const KArgs& a, bool audit, int blocks, cudaStream_t s) {
+  const size_t shm = (size_t)a.warp_smem * (audit ? 1 : a.wpb);
+  const int threads = audit ? 32 : 32 * a.wpb;
+  if (audit) mc_kernel<Pos, true><<<1, threads, shm, s>>>(a);
+  else mc_kernel<Pos, false><<<blocks, threads, shm, s>>>(a);
+}
+
+template <typename Pos>
+static cudaError_t set_smem_t(int bytes) {
+  cudaError_t e = cudaFuncSetAttribute(mc_kernel<Pos, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(mc_kernel<Pos, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+}  // namespace cg
+
+void cg_launch_mc(const cg::KArgs& a, bool fp64, bool audit, cudaStream_t s) {
+  const int blocks = (a.n_reps + a.wpb - 1) / a.wpb;
+  if (fp64) cg::launch_mc_t<double>(a, audit, blocks, s);
+  else cg::launch_mc_t<float>(a, audit, blocks, s);
+}
+
+cudaError_t cg_set_mc_smem(bool fp64, int bytes) {
+  return fp64 ? cg::set_smem_t<double>(bytes) : cg::set_smem_t<float>(bytes);
+}
+
+void cg_launch_deposit(const cg::KArgs& a, bool fp64, int rep, int n_reps_launch, long long max_beads,
+                       cudaStream_t s) {
+  dim3 grid((unsigned)((max_beads + 255) / 256 < 1024 ? (max_beads + 255) / 256 : 1024),
+            rep >= 0 ? 1 : (unsigned)n_reps_launch);
+  if (grid.x == 0) grid.x = 1;
+  if (fp64) cg::deposit_kernel<double><<<grid, 256, 0, s>>>(a, rep);
+  else cg::deposit_kernel<float><<<grid, 256, 0, s>>>(a, rep);
+}
+
+void cg_launch_energy(const cg::KArgs& a, bool fp64, double* out, cudaStream_t s) {
+  if (fp64) cg::energy_kernel<double><<<a.n_reps, 256, 0, s>>>(a, out);
+  else cg::energy_kernel<float><<<a.n_reps, 256, 0, s>>>(a, out);
+}
+
+void cg_launch_exchange(const cg::KArgs& a, const double* eout, int n_rungs, long long round,
+                        unsigned long long seed, cudaStream_t s) {
+  cg::exchange_kernel<<<1, 256, 0, s>>>(a, eout, n_rungs, round, seed);
+}

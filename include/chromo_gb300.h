@@ -1,0 +1,200 @@
+/*
+ * chromo_gb300.h -- C ABI of the GB300 Monte Carlo inner loop for chromo.
+ *
+ * One handle (cg_sim) holds R replicas resident in GPU memory.  A replica is
+ * one polymer (SSWLC / Chromatin chain) in its own UniformDensityField (or a
+ * NullField, or no field), with its five move controllers.  Everything is
+ * plain pointers and sizes; host buffers are copied inside each call.
+ *
+ * Each entry point names the reference interface it replaces (paths inside
+ * the chromo repository).  Return value: 0 on success, a negative cg_status
+ * otherwise; cg_last_error() gives the message of the last failure on the
+ * calling thread.
+ */
+#ifndef CHROMO_GB300_H
+#define CHROMO_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CG_MAX_BINDERS 3
+#define CG_MAX_MARK 3  /* marks (chemical_mods) and sites per bead in 0..3 */
+
+typedef struct cg_sim cg_sim;
+
+typedef enum {
+    CG_OK = 0,
+    CG_ERR_ARG = -1,          /* invalid argument (ValueError / TypeError in the reference) */
+    CG_ERR_CUDA = -2,         /* CUDA runtime failure */
+    CG_ERR_WINDOW = -3,       /* bead window larger than the chain (ValueError raised by
+                                 chromo/util/bead_selection.pyx:86-89,138-141) */
+    CG_ERR_STREAM = -4,       /* a supplied random stream ran out (audit mode) */
+    CG_ERR_NONFINITE = -5,    /* NaN / Inf position produced by a move */
+    CG_ERR_SPIN = -6,         /* an iteration cap was hit (bead-selection resampling,
+                                 tangent-index redraws, hash probing) */
+    CG_ERR_NOMEM = -7
+} cg_status;
+
+/* Move kinds, in the order of chromo/mc/mc_controller.py:255-258. */
+enum { CG_CRANK_SHAFT = 0, CG_END_PIVOT = 1, CG_SLIDE = 2, CG_TANGENT_ROTATION = 3,
+       CG_CHANGE_BINDING_STATE = 4 };
+
+/* State of one MC move and its controller: MCAdapter (chromo/mc/moves.pxd:14-25),
+ * SimpleControl / NoControl (chromo/mc/mc_controller.py:74-189) and the EWMA
+ * AcceptanceTracker (chromo/util/mc_stat.py:190-208). */
+typedef struct {
+    int64_t move_kind;     /* CG_* above */
+    int64_t ctrl_kind;     /* 0: NoControl, 1: SimpleControl */
+    int64_t num_per_cycle;
+    int64_t move_on;
+    double amp_move;
+    int64_t amp_bead;
+    double bead_lo, bead_hi, move_lo, move_hi;  /* controller bounds */
+    double acc_rate;       /* EWMA acceptance rate */
+    double alpha;          /* 2 / (moves_in_average + 1) */
+    int64_t num_attempt, num_success;
+} cg_move_ctl;
+
+/* One attempted move in audit mode. accepted = -1 marks an empty move
+ * (no beads selected), which returns before the energy evaluation
+ * (chromo/mc/mc_sim.pyx:148-151). */
+typedef struct {
+    int32_t kind, n_inds, ind0, indf;
+    double dE_poly, dE_field;
+    int32_t accepted, n_draws;
+} cg_move_record;
+
+/* UniformDensityField / NullField description (chromo/fields.pyx:453-535,
+ * 687-712; prefactors precomputed as there). */
+typedef struct {
+    int32_t field_kind;    /* 0: polymer in no field, 1: NullField, 2: UniformDensityField */
+    int32_t confine_kind;  /* 0: none (periodic box), 1: "Spherical", 2: "Cubical" */
+    double confine_length;
+    int32_t nx, ny, nz, n_binders;
+    double x_width, y_width, z_width;
+    double chi, vf_limit, bead_vol;
+    double pref[CG_MAX_BINDERS];    /* field_energy_prefactor */
+    double intra[CG_MAX_BINDERS];   /* interaction_energy_intranucleosome */
+    double xpref[CG_MAX_BINDERS * CG_MAX_BINDERS]; /* cross_talk_field_energy_prefactor[b][c] */
+} cg_field_params;
+
+/* Binding energetics of the polymer's beads (chromo/polymers.pyx:1408-1538). */
+typedef struct {
+    int32_t n_binders, max_binders;   /* max_binders = -1: no cap */
+    int32_t sites[CG_MAX_BINDERS];    /* sites_per_bead */
+    int32_t pad;
+    double mu[CG_MAX_BINDERS];        /* chemical_potential */
+    double mu_adjust_factor;
+    /* bind_f[(b*(CG_MAX_MARK+1) + n_marked)*(CG_MAX_MARK+1) + n_bound] =
+       -ln(single-site binding partition function) */
+    double bind_f[CG_MAX_BINDERS * (CG_MAX_MARK + 1) * (CG_MAX_MARK + 1)];
+} cg_binding_params;
+
+typedef struct {
+    int32_t n_replicas;
+    int32_t pos_fp64;          /* 1: positions stored in FP64, 0: in FP32 */
+    int32_t n_binders;         /* 1..CG_MAX_BINDERS (same for every replica) */
+    int32_t warps_per_block;   /* 0: chosen by the library */
+    const int64_t *n_beads;    /* [n_replicas] */
+    const int32_t *grid_dims;  /* [n_replicas * 3] voxels in x, y, z (1,1,1 without a field) */
+    int64_t max_segment;       /* largest bead amplitude of a segment move + 1 */
+    int64_t max_tangent;       /* largest bead amplitude of tangent_rotation */
+    int32_t nonuniform_access; /* 1: per-voxel accessible volumes are uploaded */
+    int32_t pad;
+} cg_config;
+
+/* Allocate device state for R replicas.  Replaces constructing the reference's
+ * PolymerBase / UniformDensityField objects (chromo/polymers.pyx:164-258,
+ * chromo/fields.pyx:453-535) for the GPU. */
+int cg_create(const cg_config *cfg, cg_sim **out);
+void cg_destroy(cg_sim *sim);
+const char *cg_last_error(void);
+
+/* Upload one chain: r, t3, t2 [N*3], states and chemical_mods [N*n_binders],
+ * bond parameters [(N-1)*5] = eps_bend, gamma, eps_par, eps_perp, eta per bond
+ * (SSWLC._find_parameters, chromo/polymers.pyx:1545-1601). */
+int cg_set_chain(cg_sim *sim, int32_t rep, const double *r, const double *t3, const double *t2,
+                 const int64_t *states, const int64_t *marks, const double *bonds);
+int cg_get_chain(cg_sim *sim, int32_t rep, double *r, double *t3, double *t2, int64_t *states);
+
+/* Field of one replica; access_vol [G] or NULL when every voxel is fully
+ * accessible (get_accessible_volumes, chromo/fields.pyx:714-768). */
+int cg_set_field(cg_sim *sim, int32_t rep, const cg_field_params *field, const double *access_vol);
+int cg_set_binding(cg_sim *sim, int32_t rep, const cg_binding_params *bind);
+
+/* Controllers of one replica, in the order they are cycled. */
+int cg_set_controllers(cg_sim *sim, int32_t rep, const cg_move_ctl *ctl, int32_t n_ctl);
+int cg_get_controllers(cg_sim *sim, int32_t rep, cg_move_ctl *ctl, int32_t n_ctl);
+
+/* Re-deposit every bead into the density grid of one replica (rep = -1: all).
+ * Replaces update_all_densities_for_all_polymers (chromo/fields.pyx:2041-2106).
+ * The grid is int64 fixed point in units of 2^-40 of trilinear weight, so the
+ * result does not depend on the order of the deposits. */
+int cg_deposit(cg_sim *sim, int32_t rep);
+/* Density grid of one replica as int64 fixed point [G * (n_binders+1)]. */
+int cg_get_density(cg_sim *sim, int32_t rep, int64_t *grid);
+
+/* Run mc_sim on every replica (chromo/mc/mc_sim.pyx:26-103): n_steps steps,
+ * each cycling the controllers, each controller attempting num_per_cycle moves
+ * (mc_step, chromo/mc/mc_sim.pyx:106-182) and then updating its amplitudes.
+ * Random numbers come from counter-based Philox4x32-10 streams keyed by
+ * (seed, replica).  stream: a cudaStream_t or NULL for the default stream.
+ * Returns after the kernel has been enqueued; cg_sync() waits and reports
+ * device-side errors. */
+int cg_run(cg_sim *sim, int64_t n_steps, uint64_t seed, void *stream);
+int cg_sync(cg_sim *sim, void *stream);
+
+/* Audit mode for one replica: the same kernel, but every random number is
+ * taken from the supplied arrays -- draws[] in [0, 2^31-1] where the reference
+ * calls libc rand(), bstates[] where it calls np.random.randint for a new
+ * binding state (chromo/mc/move_funcs.pyx:805-820) -- and every attempted move
+ * is recorded.  Synchronous. */
+int cg_run_audit(cg_sim *sim, int32_t rep, int64_t n_steps,
+                 const uint32_t *draws, int64_t n_draws,
+                 const int8_t *bstates, int64_t n_bstates,
+                 cg_move_record *records, int64_t max_records, int64_t *n_records,
+                 int64_t *draws_used, int64_t *bstates_used);
+
+/* FP64 energies of one replica, recomputed from the resident state:
+ * out[0] elastic (SSWLC.compute_E, chromo/polymers.pyx:1348-1381),
+ * out[1] binding free energy (sum of the single-site terms whose differences
+ *        are binding_dE, chromo/polymers.pyx:1383-1538),
+ * out[2] field energy in the form whose differences are the per-move field dE
+ *        (chromo/fields.pyx:1675-1875),
+ * out[3] running sum of accepted dE since the last cg_reset_running_energy. */
+int cg_energy(cg_sim *sim, int32_t rep, double *out);
+int cg_reset_running_energy(cg_sim *sim);
+
+/* Per-replica, per-move tallies [5 * 6]: attempts, accepts, beads moved,
+ * voxels touched, beads moved in accepted moves, voxels touched in accepted
+ * moves.  Used for the algorithmic-bytes roofline. */
+int cg_get_tally(cg_sim *sim, int32_t rep, uint64_t *out);
+int cg_reset_tally(cg_sim *sim);
+
+/* Replica exchange across a chi ladder (no counterpart in the reference,
+ * which has a single chain per run): replicas are grouped in ladders of
+ * n_rungs consecutive replicas; in round `round` the rungs (2i+p, 2i+1+p),
+ * p = round % 2, propose to swap chi with probability
+ * min(1, exp((chi_a - chi_b) * (S_a - S_b))), S the chi-free part of the
+ * field energy.  chi_of_rep is read and written [n_replicas]. */
+int cg_exchange(cg_sim *sim, int32_t n_rungs, int64_t round, uint64_t seed, void *stream);
+int cg_get_chi(cg_sim *sim, double *chi);
+
+/* Batched run: n_rounds x (n_steps MC steps on every replica, then one
+ * exchange round), captured once in a CUDA graph and replayed.  n_rungs = 0
+ * disables exchange. */
+int cg_run_batched(cg_sim *sim, int64_t n_rounds, int64_t n_steps, int32_t n_rungs,
+                   uint64_t seed, void *stream);
+
+/* Kernel launch shape currently in use, and the number of MC kernels the
+ * library launched since creation. */
+int cg_get_launch_info(cg_sim *sim, int32_t *warps_per_block, int32_t *hash_slots,
+                       int64_t *kernels_launched);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CHROMO_GB300_H */

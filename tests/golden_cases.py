@@ -40,3 +40,38 @@ def oracle_ctls(g):
                             num_per_cycle=int(npc), simple=bool(simple),
                             bead_bounds=(blo, bhi), move_bounds=(mlo, mhi)))
     return out
+
+
+def gpu_sim(g, pos_fp64, state="0"):
+    """A one-replica ``chromo_gb300._native.Sim`` holding a golden case."""
+    from chromo_gb300 import _native as nat
+    from chromo_gb300.device import binding_params, bonds_array, field_params, move_ctl
+    n, nb = g["states0"].shape
+    uniform = int(g["field_kind"]) == 2
+    ctl0 = g["ctl0"]
+    max_seg = int(max(max(row[1], row[5]) for k, row in enumerate(ctl0) if k != 3)) + 2
+    max_tan = int(max(ctl0[3][1], ctl0[3][5]))
+    sim = nat.Sim([n], [list(g["nxyz"])], nb, pos_fp64=pos_fp64, max_segment=max_seg,
+                  max_tangent=max_tan)
+    sim.set_chain(0, r=g["r" + state], t3=g["t3" + state], t2=g["t2" + state],
+                  states=g["states" + state], marks=g["marks"],
+                  bonds=bonds_array(g["eps_bend"], g["gamma"], g["eps_par"], g["eps_perp"], g["eta"]))
+    sim.set_field(0, field_params(
+        field_kind=int(g["field_kind"]), confine_kind=int(g["confine_kind"]),
+        confine_length=float(g["confine_length"]), nxyz=g["nxyz"], widths=g["widths"],
+        n_binders=nb, chi=float(g["chi"]), vf_limit=float(g["vf_limit"]),
+        bead_vol=4.0 / 3.0 * np.pi * float(g["bead_rad"]) ** 3, pref=g["pref"], intra=g["intra"],
+        xpref=g["xpref"]))
+    sim.set_binding(0, binding_params(sites=g["sites"], e_mod=g["e_mod"], e_nomod=g["e_nomod"],
+                                      mu=g["mu"], mu_adjust_factor=float(g["mu_adjust_factor"]),
+                                      max_binders=int(g["max_binders"])))
+    ctls = []
+    for k, row in enumerate(ctl0):
+        amp_move, amp_bead, npc, simple, blo, bhi, mlo, mhi = row
+        ctls.append(move_ctl(MOVE_NAMES[k], amp_move=amp_move, amp_bead=int(amp_bead),
+                             num_per_cycle=int(npc), simple=bool(simple), bead_bounds=(blo, bhi),
+                             move_bounds=(mlo, mhi)))
+    sim.set_controllers(0, ctls)
+    if uniform:
+        sim.deposit(0)
+    return sim

@@ -1,0 +1,320 @@
+#!/usr/bin/env python3
+"""Attempted MC moves/s of chromo's inner loop on GB300 (batched vs plain GPU).
+
+One "step" is one replica-exchange round of the batched workload: every
+replica (256 chains, 2,000-20,000 beads, own 40^3 grid, two binders) runs 62
+MC steps of all five moves (~1e4 attempted moves per replica), then chi is
+exchanged along 16-rung ladders.  The round is a captured CUDA graph replayed
+K times.  ``value`` is whole-job attempted moves/s with the state resident in
+HBM; ``e2e`` is the same through the C ABI with host buffers (state uploaded
+from pinned memory and the snapshot read back every step); ``plain`` is one
+10,000-bead chain on the same kernel (one warp); ``roofline`` reports the MC
+kernel's algorithmic bytes per launch over its CUDA-event duration against
+the measured HBM peak; ``cpu_baseline`` is the reference's own CPU code on
+this host's cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "attempted MC moves/s on 1 GB300 (batched vs plain GPU) at dE err ≤1e-5 vs FP64"
+WORKLOAD_DESC = ("batched replicas: 256 chains, lengths log-uniform in [2000, 20000] beads (seeded), "
+                 "each in its own periodic 1600 nm box with a 40^3 grid of 40 nm voxels; FP32 "
+                 "positions, int64 fixed-point density, FP64 dE; two binders (eps_AA=-4, eps_BB=-3, "
+                 "eps_AB=+1, mu ~ U[-1,0]); all five moves with SimpleControl; chi ladder of 16 rungs "
+                 "in [0.5, 2.0], exchange every 62 MC steps (~1e4 moves per replica)")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "large", "diff"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-budget", type=float, default=2.0)
+    return ap.parse_args()
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        import statistics
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import refbench
+    from chromo_gb300.workloads import make_workload
+    w = make_workload(args.workload)
+    per_step = 1.0
+    res = refbench.run(args.workload, budget=per_step * (args.steps + args.warmup),
+                       n_procs=os.cpu_count())
+    out = {
+        "impl": "reference", "metric": METRIC, "value": res["value"], "unit": "moves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD_DESC if args.workload == "batched" else args.workload,
+                   "replicas": int(w.replicas)},
+        "cpu_baseline": {"value": res["value"], "unit": "moves/s", "cores": res["cores"],
+                         "kind": res["kind"], "sample": res["sample"]},
+        "e2e": {"value": res["value"], "unit": "moves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    if res.get("fallback_reason"):
+        out["cpu_baseline"]["note"] = "reference unavailable (" + res["fallback_reason"] + "); C port timed"
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_init(args)
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    # CPU baseline first (spawned workers, before this process touches the GPU)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import refbench
+        cpu = refbench.run(args.workload, budget=args.cpu_budget, n_procs=os.cpu_count())
+    import numpy as np
+    import torch
+    from chromo_gb300.build import build
+    build()
+    import chromo_gb300._native as nat
+    from chromo_gb300 import workloads as wl
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    w = wl.make_workload(args.workload, seed_offset=rank)
+    chains = wl.make_chains(w)
+    sim = wl.build_sim(w, chains)
+    steps_round = w.steps_per_round
+    moves_round = w.replicas * steps_round * w.moves_per_step
+    # ---- warm-up rounds (graph capture happens on the first)
+    for _ in range(max(args.warmup, 3)):
+        sim.run_batched(1, steps_round, w.n_rungs, 11 + rank, sh)
+    sim.sync(sh)
+    sim.reset_tally()
+    # ---- timed rounds
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sim.run_batched(1, steps_round, w.n_rungs, 11 + rank, sh)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    sim.sync(sh)
+    barrier(world)
+    ms = ev0.elapsed_time(ev1)
+    ms_max = allreduce_max(ms, world)
+    tal = np.stack([sim.tally(r) for r in range(w.replicas)])
+    attempts = float(tal[:, :, 0].sum())
+    total_attempts = allreduce_sum(attempts, world)
+    value = total_attempts / (ms_max / 1000.0)
+    # ---- roofline: MC kernel alone, CUDA events per launch
+    sim.reset_tally()
+    n_launch = 5
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(n_launch + 1)]
+    evs[0].record(stream)
+    for i in range(n_launch):
+        sim.run(steps_round, 101 + i, sh)
+        evs[i + 1].record(stream)
+    torch.cuda.synchronize()
+    sim.sync(sh)
+    launch_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(n_launch)]
+    avg_launch_s = sum(launch_ms) / n_launch / 1000.0
+    tal2 = np.stack([sim.tally(r) for r in range(w.replicas)])
+    bytes_per_launch = wl.algorithmic_bytes(tal2, w.n_binders) / n_launch
+    peak, peak_kind = load_peaks()
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    traffic = None
+    tj = ROOT / "profiles" / "mc_kernel_traffic.json"
+    if tj.exists():
+        d = json.loads(tj.read_text())
+        traffic = d.get("dram_bytes_per_move", 0) * float(tal2[:, :, 0].sum()) / n_launch
+    # ---- e2e through the C ABI with host buffers
+    h2d = d2h = 0
+    pos_b = 16
+    e2e_steps = max(2, min(args.steps, 5))
+    t_e2e = 0.0
+    for k in range(e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for rep in range(w.replicas):
+            c = chains[rep]
+            sim.set_chain(rep, r=c.r, t3=c.t3, t2=c.t2, states=c.states)
+        sim.run_batched(1, steps_round, w.n_rungs, 11 + rank, sh)
+        snap = [sim.get_chain(rep) for rep in range(w.replicas)]
+        sim.sync(sh)
+        dt = time.perf_counter() - t0
+        if k > 0:
+            t_e2e += dt
+    nbeads = int(w.lengths.sum())
+    h2d = nbeads * (3 * pos_b + 4)
+    d2h = nbeads * (3 * pos_b + 4)
+    e2e_value = allreduce_sum(moves_round * e2e_steps, world) / allreduce_max(t_e2e, world)
+    # ---- plain single chain (one warp) on the same kernel
+    wp = wl.make_workload("plain", seed_offset=rank)
+    psim = wl.build_sim(wp)
+    psim.run(20, 5, sh)
+    psim.sync(sh)
+    psim.reset_tally()
+    pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pe0.record(stream)
+    psim.run(300, 6, sh)
+    pe1.record(stream)
+    torch.cuda.synchronize()
+    psim.sync(sh)
+    p_att = float(psim.tally(0)[:, 0].sum())
+    plain_value = p_att / (pe0.elapsed_time(pe1) / 1000.0)
+    launches = args.steps * (3 if w.n_rungs else 1)
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "moves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Gaussian-walk chains, Markov mark tracks)",
+            "config": {"workload": WORKLOAD_DESC, "replicas": int(w.replicas),
+                       "beads_total": nbeads, "mc_steps_per_step": steps_round,
+                       "attempted_moves_per_step": int(attempts / args.steps),
+                       "l2": "inputs larger than L2 (grids 256 x 1.5 MB + chains > 129 MB)",
+                       "graph": "one exchange round captured in a CUDA graph, replayed per step"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "mc_kernel<float,false>", "peak_source": peak_kind,
+                         "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
+                         "moves_per_launch": float(tal2[:, :, 0].sum()) / n_launch},
+            "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h,
+                    "path": "C ABI: cg_set_chain x R (host FP64 -> pinned -> HBM), cg_run_batched, "
+                            "cg_get_chain x R"},
+            "plain": {"value": plain_value, "unit": "moves/s",
+                      "workload": "one 10,000-bead chain, 60^3 grid, one binder, 300 MC steps",
+                      "batched_over_plain": value / plain_value},
+            "gpu_launches": launches,
+            "clocks": clocks.summary(),
+        }
+        if cpu is not None:
+            out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

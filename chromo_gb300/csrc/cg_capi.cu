@@ -83,6 +83,20 @@ struct cg_sim {
   int graph_rungs = -1;
   unsigned long long graph_seed = 0;
   cudaStream_t graph_stream = nullptr;
+  // pinned host staging for chain uploads / downloads
+  void* pinned = nullptr;
+  size_t pinned_bytes = 0;
+
+  unsigned char* staging(size_t bytes) {
+    if (bytes > pinned_bytes) {
+      if (pinned) cudaFreeHost(pinned);
+      pinned = nullptr;
+      pinned_bytes = 0;
+      if (cudaHostAlloc(&pinned, bytes, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+      pinned_bytes = bytes;
+    }
+    return static_cast<unsigned char*>(pinned);
+  }
 
   size_t pos_bytes() const { return fp64 ? sizeof(V4<double>) : sizeof(V4<float>); }
   size_t scal_bytes() const { return fp64 ? 8 : 4; }
@@ -121,14 +135,13 @@ struct cg_sim {
 };
 
 template <typename P>
-static void pack_pos(const double* src, long long n, std::vector<unsigned char>& out) {
-  out.resize(sizeof(V4<P>) * n);
-  V4<P>* o = reinterpret_cast<V4<P>*>(out.data());
+static void pack_pos(const double* src, long long n, unsigned char* out) {
+  V4<P>* o = reinterpret_cast<V4<P>*>(out);
   for (long long i = 0; i < n; i++) o[i] = V4<P>{(P)src[3 * i], (P)src[3 * i + 1], (P)src[3 * i + 2], (P)0};
 }
 template <typename P>
-static void unpack_pos(const std::vector<unsigned char>& in, long long n, double* dst) {
-  const V4<P>* o = reinterpret_cast<const V4<P>*>(in.data());
+static void unpack_pos(const unsigned char* in, long long n, double* dst) {
+  const V4<P>* o = reinterpret_cast<const V4<P>*>(in);
   for (long long i = 0; i < n; i++) {
     dst[3 * i] = (double)o[i].x; dst[3 * i + 1] = (double)o[i].y; dst[3 * i + 2] = (double)o[i].z;
   }
@@ -141,6 +154,7 @@ const char* cg_last_error(void) { return g_err.c_str(); }
 void cg_destroy(cg_sim* s) {
   if (!s) return;
   if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->pinned) cudaFreeHost(s->pinned);
   void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
                   s->grid, s->access_vol, s->g_keys, s->g_used, s->g_vals, s->g_stage, s->g_idx,
                   s->picked, s->d_picked_off, s->eout, s->aout, s->rep_of_rung, s->swaps,
@@ -303,18 +317,20 @@ int cg_set_chain(cg_sim* s, int rep, const double* r, const double* t3, const do
                  const int64_t* states, const int64_t* marks, const double* bonds) {
   if (int rc = check_rep(s, rep)) return rc;
   const long long n = s->n_beads[rep], off = s->bead_off[rep];
-  std::vector<unsigned char> buf;
   const double* src[3] = {r, t3, t2};
   void* dst[3] = {s->r4, s->t34, s->t24};
+  unsigned char* buf = s->staging(s->pos_bytes() * n * 3 + 4 * n);
+  if (!buf) return fail(CG_ERR_NOMEM, "pinned staging allocation failed");
   for (int k = 0; k < 3; k++) {
     if (!src[k]) continue;
     for (long long i = 0; i < 3 * n; i++)
       if (!std::isfinite(src[k][i])) return fail(CG_ERR_NONFINITE, "non-finite position or tangent");
-    if (s->fp64) pack_pos<double>(src[k], n, buf);
-    else pack_pos<float>(src[k], n, buf);
-    CUDA_TRY(cudaMemcpy((char*)dst[k] + s->pos_bytes() * off, buf.data(), buf.size(), cudaMemcpyHostToDevice));
+    unsigned char* b = buf + s->pos_bytes() * n * k;
+    if (s->fp64) pack_pos<double>(src[k], n, b);
+    else pack_pos<float>(src[k], n, b);
+    CUDA_TRY(cudaMemcpy((char*)dst[k] + s->pos_bytes() * off, b, s->pos_bytes() * n, cudaMemcpyHostToDevice));
   }
-  std::vector<unsigned> pk(n);
+  unsigned* pk = reinterpret_cast<unsigned*>(buf + s->pos_bytes() * n * 3);
   const int64_t* sm[2] = {states, marks};
   unsigned* dsm[2] = {s->states, s->marks};
   for (int k = 0; k < 2; k++) {
@@ -329,7 +345,7 @@ int cg_set_chain(cg_sim* s, int rep, const double* r, const double* t3, const do
       }
       pk[i] = w;
     }
-    CUDA_TRY(cudaMemcpy(dsm[k] + off, pk.data(), 4 * n, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dsm[k] + off, pk, 4 * n, cudaMemcpyHostToDevice));
   }
   if (bonds) {
     std::vector<double> bb(6 * n, 0.0);
@@ -343,18 +359,19 @@ int cg_set_chain(cg_sim* s, int rep, const double* r, const double* t3, const do
 int cg_get_chain(cg_sim* s, int rep, double* r, double* t3, double* t2, int64_t* states) {
   if (int rc = check_rep(s, rep)) return rc;
   const long long n = s->n_beads[rep], off = s->bead_off[rep];
-  std::vector<unsigned char> buf(s->pos_bytes() * n);
+  unsigned char* buf = s->staging(s->pos_bytes() * n * 3 + 4 * n);
+  if (!buf) return fail(CG_ERR_NOMEM, "pinned staging allocation failed");
   double* dst[3] = {r, t3, t2};
   void* src[3] = {s->r4, s->t34, s->t24};
   for (int k = 0; k < 3; k++) {
     if (!dst[k]) continue;
-    CUDA_TRY(cudaMemcpy(buf.data(), (char*)src[k] + s->pos_bytes() * off, buf.size(), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(buf, (char*)src[k] + s->pos_bytes() * off, s->pos_bytes() * n, cudaMemcpyDeviceToHost));
     if (s->fp64) unpack_pos<double>(buf, n, dst[k]);
     else unpack_pos<float>(buf, n, dst[k]);
   }
   if (states) {
-    std::vector<unsigned> pk(n);
-    CUDA_TRY(cudaMemcpy(pk.data(), s->states + off, 4 * n, cudaMemcpyDeviceToHost));
+    unsigned* pk = reinterpret_cast<unsigned*>(buf + s->pos_bytes() * n * 3);
+    CUDA_TRY(cudaMemcpy(pk, s->states + off, 4 * n, cudaMemcpyDeviceToHost));
     for (long long i = 0; i < n; i++)
       for (int b = 0; b < s->nb; b++) states[i * s->nb + b] = (pk[i] >> (8 * b)) & 0xFF;
   }

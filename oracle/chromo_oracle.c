@@ -128,16 +128,19 @@ typedef struct {
 
 /* ---------------- random stream ---------------------------------------- */
 
+/* draws == NULL: take libc rand() itself, as the reference does (timing runs) */
 static int64_t rnd(or_rng *g)
 {
+    if (!g->a) { g->pos++; return (int64_t)rand(); }
     if (g->pos >= g->n) { g->err = OR_ERR_DRAWS; return 0; }
     return (int64_t)g->a[g->pos++];
 }
 
 static double rndu(or_rng *g) { return (double)rnd(g) / OR_RAND_MAX; }
 
-static int64_t rnd_state(or_rng *g)
+static int64_t rnd_state(or_rng *g, int64_t n_tails)
 {
+    if (!g->b) { g->bpos++; return (int64_t)(rand() % (int)(n_tails + 1)); }
     if (g->bpos >= g->nb_) { g->err = OR_ERR_BSTATES; return 0; }
     return g->b[g->bpos++];
 }
@@ -962,7 +965,7 @@ static int64_t mc_step(or_system *s, or_ctl *c, or_rng *g, or_record *rec)
         n = indf - ind0;
         for (int64_t k = 0; k < n; k++) {
             s->inds[k] = ind0 + k;
-            s->new_states[k] = rnd_state(g);
+            s->new_states[k] = rnd_state(g, s->sites[bsel]);
             for (int j = 0; j < 3; j++) s->trial[9 * k + j] = (double)s->r[3 * (ind0 + k) + j];
         }
         if (g->err) return g->err;

@@ -130,11 +130,12 @@ class OracleSystem:
                  pos="f64", fixed_density=0):
         self.pos = pos
         fdt = np.float64 if pos == "f64" else np.float32
-        self.r = np.ascontiguousarray(r, dtype=fdt)
-        self.t3 = np.ascontiguousarray(t3, dtype=fdt)
-        self.t2 = np.ascontiguousarray(t2, dtype=fdt)
-        self.states = np.ascontiguousarray(states, dtype=np.int64)
-        self.marks = np.ascontiguousarray(marks, dtype=np.int64)
+        # private copies: the oracle mutates its state in place
+        self.r = np.array(r, dtype=fdt, order="C", copy=True)
+        self.t3 = np.array(t3, dtype=fdt, order="C", copy=True)
+        self.t2 = np.array(t2, dtype=fdt, order="C", copy=True)
+        self.states = np.array(states, dtype=np.int64, order="C", copy=True)
+        self.marks = np.array(marks, dtype=np.int64, order="C", copy=True)
         N, nb = self.states.shape
         self.params = [np.ascontiguousarray(x, dtype=np.float64)
                        for x in (eps_bend, gamma, eps_par, eps_perp, eta)]
@@ -204,16 +205,17 @@ class OracleSystem:
     def mc_sim(self, ctls, n_steps, draws, bstates, max_records=None):
         """Run ``mc_sim`` (chromo/mc/mc_sim.pyx:26-103); returns the per-move records."""
         arr = (Ctl * len(ctls))(*ctls)
-        draws = np.ascontiguousarray(draws, dtype=np.uint32)
-        bstates = np.ascontiguousarray(bstates, dtype=np.int64)
+        internal = draws is None
+        draws = np.zeros(1, np.uint32) if internal else np.ascontiguousarray(draws, dtype=np.uint32)
+        bstates = np.zeros(1, np.int64) if internal else np.ascontiguousarray(bstates, dtype=np.int64)
         if max_records is None:
             max_records = n_steps * sum(int(c.num_per_cycle) for c in ctls if c.move_on)
         recs = np.zeros(max_records, dtype=RECORD_DTYPE)
         dp, bp = _I(self.draw_pos), _I(self.bstate_pos)
         n = self._L.or_mc_sim(C.byref(self._s), arr, len(ctls), n_steps,
-                              draws.ctypes.data, len(draws), C.byref(dp),
-                              bstates.ctypes.data, len(bstates), C.byref(bp),
-                              recs.ctypes.data, max_records)
+                              None if internal else draws.ctypes.data, len(draws), C.byref(dp),
+                              None if internal else bstates.ctypes.data, len(bstates), C.byref(bp),
+                              recs.ctypes.data if max_records else None, max_records)
         self.draw_pos, self.bstate_pos = dp.value, bp.value
         for i, c in enumerate(ctls):
             C.memmove(C.byref(c), C.byref(arr[i]), C.sizeof(Ctl))

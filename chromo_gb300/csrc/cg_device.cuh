@@ -119,19 +119,55 @@ template <> struct Rng<true> {
   }
 };
 
-__device__ __forceinline__ double unif(unsigned x) { return (double)x / kRandMax; }
+// x / (2^31 - 1) correctly rounded, as the reference's rand() / RAND_MAX, with
+// one FMA instead of a double division: with a = x 2^-31 (exact),
+// fma(a, 2^-31 + 2^-62, a) equals the quotient for every x in [0, 2^31 - 1]
+// (checked exhaustively on the host).
+__device__ __forceinline__ double unif(unsigned x) {
+  double a = (double)x * 0x1p-31;
+  return __fma_rn(a, 0x1.00000002p-31, a);
+}
+__device__ __forceinline__ float unif32(unsigned x) { return (float)unif(x); }
+
+// floor(-log10(u + 1e-5) * window * 0.45 + 1.0001) (bead_selection.pyx:56-65)
+// evaluated in FP32 when the result is unambiguous, else in FP64, so the
+// integer equals the reference's FP64 value.
+__device__ __forceinline__ long long sel_floor(unsigned x, long long window) {
+  float y = -log10f(unif32(x) + 0.00001f) * (float)window * 0.45f + 1.0001f;
+  float fl = floorf(y);
+  float margin = 1e-3f + 1e-6f * y;
+  if (y - fl > margin && fl + 1.0f - y > margin) return (long long)fl;
+  return (long long)(-log10(unif(x) + 0.00001) * (double)window * 0.45 + 1.0001);
+}
+
+// The Metropolis test u < exp(t) (mc_sim.pyx:164-171) with u = unif(x):
+// decided in FP32 away from the boundary, in FP64 near it; same outcome as
+// the FP64 comparison.
+__device__ __forceinline__ bool metropolis(unsigned x, double t) {
+  double u = unif(x);
+  if (t != t) return false;
+  if (t > 80.0) return true;
+  if (t >= -80.0) {
+    double e = (double)expf((float)t);
+    if (u < e * (1.0 - 1e-4)) return true;
+    if (u > e * (1.0 + 1e-4)) return false;
+  } else if (u > 0.0) {
+    return false;
+  }
+  return u < exp(t);
+}
 
 // ---------------------------------------------------------------- bead selection
 // chromo/util/bead_selection.pyx:19-192
 
 template <class R>
 __device__ long long capped_exponential(R& g, long long window, long long cap, unsigned& err) {
-  long long r = (long long)(-log10(unif(g.next()) + 0.00001) * (double)window * 0.45 + 1.0001);
+  long long r = sel_floor(g.next(), window);
   int it = 0;
   while (r > cap) {
     if (g.fail) return cap;  // stream exhausted: reported by the caller
     if (++it > kMaxIter) { err |= E_SPIN; return cap; }
-    r = (long long)(-log10(unif(g.next()) + 0.00001) * (double)window * 0.45 + 1.0001);
+    r = sel_floor(g.next(), window);
   }
   return r;
 }
@@ -173,24 +209,43 @@ __device__ __forceinline__ void check_bead_bounds(long long b0, long long b1, lo
 // ---------------------------------------------------------------- geometry
 // chromo/util/linalg.pyx:23-199
 
-template <class R>
-__device__ __forceinline__ void sphere(R& g, double v[3]) {
-  double phi = unif(g.next()) * (2.0 * 3.141592653589793);
-  double theta = acos(unif(g.next()) * 2 - 1);
-  double sp, cp, st, ct;
-  sincos(phi, &sp, &cp);
-  sincos(theta, &st, &ct);
+__device__ __forceinline__ void rsincos(double x, double* sn, double* cs) { sincos(x, sn, cs); }
+__device__ __forceinline__ void rsincos(float x, float* sn, float* cs) { sincosf(x, sn, cs); }
+__device__ __forceinline__ double racos(double x) { return acos(x); }
+__device__ __forceinline__ float racos(float x) { return acosf(x); }
+__device__ __forceinline__ double rsqrt_(double x) { return sqrt(x); }
+__device__ __forceinline__ float rsqrt_(float x) { return sqrtf(x); }
+
+template <typename Real> __device__ __forceinline__ Real uni(unsigned x);
+template <> __device__ __forceinline__ double uni<double>(unsigned x) { return unif(x); }
+template <> __device__ __forceinline__ float uni<float>(unsigned x) { return unif32(x); }
+
+// uniform_sample_unit_sphere from two draws (phi, theta)
+template <typename Real>
+__device__ __forceinline__ void sphere_from(unsigned xphi, unsigned xtheta, Real v[3]) {
+  Real phi = uni<Real>(xphi) * (Real)(2.0 * 3.141592653589793);
+  Real theta = racos(uni<Real>(xtheta) * 2 - 1);
+  Real sp, cp, st, ct;
+  rsincos(phi, &sp, &cp);
+  rsincos(theta, &st, &ct);
   v[0] = cp * st;
   v[1] = sp * st;
   v[2] = ct;
 }
 
-// Rotation by `ang` about unit axis a through point p: x' = M[:, :3] x + M[:, 3].
-__device__ __forceinline__ void axis_rotation(const double a[3], const double p[3], double ang,
-                                              double M[3][4]) {
-  double s, c;
-  sincos(ang, &s, &c);
-  double oc = 1 - c, a0 = a[0] * a[0], a1 = a[1] * a[1], a2 = a[2] * a[2];
+template <typename Real, class R>
+__device__ __forceinline__ void sphere(R& g, Real v[3]) {
+  unsigned a = g.next();
+  unsigned b = g.next();
+  sphere_from<Real>(a, b, v);
+}
+
+// Rotation by `ang` (sine s, cosine c) about unit axis a through point p:
+// x' = M[:, :3] x + M[:, 3].
+template <typename Real>
+__device__ __forceinline__ void axis_rotation_sc(const Real a[3], const Real p[3], Real s, Real c,
+                                                 Real M[3][4]) {
+  Real oc = 1 - c, a0 = a[0] * a[0], a1 = a[1] * a[1], a2 = a[2] * a[2];
   M[0][0] = a0 + (a1 + a2) * c;
   M[0][1] = a[0] * a[1] * oc - a[2] * s;
   M[0][2] = a[0] * a[2] * oc + a[1] * s;
@@ -208,10 +263,17 @@ __device__ __forceinline__ void axis_rotation(const double a[3], const double p[
   M[2][3] += (p[2] * (1 - a2) - a[2] * (p[0] * a[0] + p[1] * a[1])) * oc;
 }
 
-template <typename Pos>
-__device__ __forceinline__ void ld3(const V4<Pos>* a, long long i, double v[3]) {
+template <typename Real>
+__device__ __forceinline__ void axis_rotation(const Real a[3], const Real p[3], Real ang, Real M[3][4]) {
+  Real s, c;
+  rsincos(ang, &s, &c);
+  axis_rotation_sc(a, p, s, c, M);
+}
+
+template <typename Pos, typename Real>
+__device__ __forceinline__ void ld3(const V4<Pos>* a, long long i, Real v[3]) {
   V4<Pos> q = a[i];
-  v[0] = (double)q.x; v[1] = (double)q.y; v[2] = (double)q.z;
+  v[0] = (Real)q.x; v[1] = (Real)q.y; v[2] = (Real)q.z;
 }
 
 template <typename Pos>
@@ -220,66 +282,98 @@ __device__ __forceinline__ double rnd_pos(double x) { return (double)(Pos)x; }
 // ---------------------------------------------------------------- SSWLC energy
 // chromo/polymers.pyx:1148-1346
 
-struct Bond { double eb, g, ep, epp, eta; };
+template <typename Real> struct Bond { Real eb, g, ep, epp, eta; };
 
-__device__ __forceinline__ Bond load_bond(const double* bonds, long long i) {
+template <typename Real>
+__device__ __forceinline__ Bond<Real> load_bond(const double* bonds, long long i) {
   const double* b = bonds + 6 * i;
-  return Bond{b[0], b[1], b[2], b[3], b[4]};
+  return Bond<Real>{(Real)b[0], (Real)b[1], (Real)b[2], (Real)b[3], (Real)b[4]};
 }
 
-__device__ __forceinline__ double e_pair(const Bond& b, const double bend[3], double par,
-                                         const double dp[3]) {
-  double x = par - b.g;
-  return 0.5 * b.eb * (bend[0] * bend[0] + bend[1] * bend[1] + bend[2] * bend[2])
-       + 0.5 * b.ep * (x * x)
-       + 0.5 * b.epp * (dp[0] * dp[0] + dp[1] * dp[1] + dp[2] * dp[2]);
+template <typename Real>
+__device__ __forceinline__ Real e_pair(const Bond<Real>& b, const Real bend[3], Real par, const Real dp[3]) {
+  Real x = par - b.g;
+  return (Real)0.5 * b.eb * (bend[0] * bend[0] + bend[1] * bend[1] + bend[2] * bend[2])
+       + (Real)0.5 * b.ep * (x * x)
+       + (Real)0.5 * b.epp * (dp[0] * dp[0] + dp[1] * dp[1] + dp[2] * dp[2]);
 }
 
-// bond (0 -> 1) with bead 1 moved: bead_pair_dE_poly_forward
-__device__ __forceinline__ double pair_dE_fwd(const Bond& b, const double r0[3], const double r1[3],
-                                              const double tr1[3], const double t30[3],
-                                              const double t31[3], const double tt31[3]) {
-  double drt[3], dr[3], dpt[3], dp[3], bt[3], bc[3];
+// bond (0 -> 1) with bead 1 moved: bead_pair_dE_poly_forward (FP64 difference)
+template <typename Real>
+__device__ __forceinline__ double pair_dE_fwd(const Bond<Real>& b, const Real r0[3], const Real r1[3],
+                                              const Real tr1[3], const Real t30[3],
+                                              const Real t31[3], const Real tt31[3]) {
+  Real drt[3], dr[3], dpt[3], dp[3], bt[3], bc[3];
   for (int i = 0; i < 3; i++) { drt[i] = tr1[i] - r0[i]; dr[i] = r1[i] - r0[i]; }
-  double pt = t30[0] * drt[0] + t30[1] * drt[1] + t30[2] * drt[2];
-  double pc = t30[0] * dr[0] + t30[1] * dr[1] + t30[2] * dr[2];
+  Real pt = t30[0] * drt[0] + t30[1] * drt[1] + t30[2] * drt[2];
+  Real pc = t30[0] * dr[0] + t30[1] * dr[1] + t30[2] * dr[2];
   for (int i = 0; i < 3; i++) {
     dpt[i] = drt[i] - t30[i] * pt;
     dp[i] = dr[i] - t30[i] * pc;
     bt[i] = tt31[i] - t30[i] - dpt[i] * b.eta;
     bc[i] = t31[i] - t30[i] - dp[i] * b.eta;
   }
-  return e_pair(b, bt, pt, dpt) - e_pair(b, bc, pc, dp);
+  return (double)e_pair(b, bt, pt, dpt) - (double)e_pair(b, bc, pc, dp);
 }
 
-// bond (0 -> 1) with bead 0 moved: bead_pair_dE_poly_reverse
-__device__ __forceinline__ double pair_dE_rev(const Bond& b, const double r0[3], const double tr0[3],
-                                              const double r1[3], const double t30[3],
-                                              const double tt30[3], const double t31[3]) {
-  double drt[3], dr[3], dpt[3], dp[3], bt[3], bc[3];
+// bond (0 -> 1) with bead 0 moved: bead_pair_dE_poly_reverse (FP64 difference)
+template <typename Real>
+__device__ __forceinline__ double pair_dE_rev(const Bond<Real>& b, const Real r0[3], const Real tr0[3],
+                                              const Real r1[3], const Real t30[3],
+                                              const Real tt30[3], const Real t31[3]) {
+  Real drt[3], dr[3], dpt[3], dp[3], bt[3], bc[3];
   for (int i = 0; i < 3; i++) { drt[i] = r1[i] - tr0[i]; dr[i] = r1[i] - r0[i]; }
-  double pt = tt30[0] * drt[0] + tt30[1] * drt[1] + tt30[2] * drt[2];
-  double pc = t30[0] * dr[0] + t30[1] * dr[1] + t30[2] * dr[2];
+  Real pt = tt30[0] * drt[0] + tt30[1] * drt[1] + tt30[2] * drt[2];
+  Real pc = t30[0] * dr[0] + t30[1] * dr[1] + t30[2] * dr[2];
   for (int i = 0; i < 3; i++) {
     dpt[i] = drt[i] - tt30[i] * pt;
     dp[i] = dr[i] - t30[i] * pc;
     bt[i] = t31[i] - tt30[i] - dpt[i] * b.eta;
     bc[i] = t31[i] - t30[i] - dp[i] * b.eta;
   }
-  return e_pair(b, bt, pt, dpt) - e_pair(b, bc, pc, dp);
+  return (double)e_pair(b, bt, pt, dpt) - (double)e_pair(b, bc, pc, dp);
 }
 
 // ---------------------------------------------------------------- density field
 // chromo/fields.pyx:1430-1673: eight trilinear weights and periodic voxel indices.
 
 __device__ __forceinline__ double pymod(double a, double b) {
+  if (a >= 0 && a < b) return a;  // fmod(a, b) == a exactly here
   double m = fmod(a, b);
   if (m != 0 && ((m < 0) != (b < 0))) m += b;
   return m;
 }
+__device__ __forceinline__ float pymodf(float a, float b) {
+  if (a >= 0 && a < b) return a;
+  float m = fmodf(a, b);
+  if (m != 0 && ((m < 0) != (b < 0))) m += b;
+  return m;
+}
 
-__device__ __forceinline__ void voxel_weights(const RepDev& rd, const double pos[3], double w[8],
-                                              int v[8]) {
+// FP32 copies of the grid geometry, derived once per launch
+struct GridF {
+  float w[3], half_w[3], half_d[3], inv_d[3];
+  int n[3], nx, nxy;
+};
+
+__device__ __forceinline__ void make_gridf(const RepDev& rd, GridF& gf) {
+  const double W[3] = {rd.wx, rd.wy, rd.wz};
+  const int n[3] = {rd.nx, rd.ny, rd.nz};
+  for (int j = 0; j < 3; j++) {
+    double d = W[j] / (double)n[j];
+    gf.w[j] = (float)W[j];
+    gf.half_w[j] = (float)(0.5 * W[j]);
+    gf.half_d[j] = (float)(0.5 * d);
+    gf.inv_d[j] = (float)(1.0 / d);
+    gf.n[j] = n[j];
+  }
+  gf.nx = rd.nx;
+  gf.nxy = rd.nx * rd.ny;
+}
+
+// Exact reference arithmetic (FP64 storage).
+__device__ __forceinline__ void voxel_weights(const RepDev& rd, const GridF&, const double pos[3],
+                                              double w[8], int v[8]) {
   const double width[3] = {rd.wx, rd.wy, rd.wz};
   const int n[3] = {rd.nx, rd.ny, rd.nz};
   double wl[3];
@@ -305,7 +399,35 @@ __device__ __forceinline__ void voxel_weights(const RepDev& rd, const double pos
   }
 }
 
+// FP32 arithmetic (FP32 storage): same construction, one reciprocal multiply.
+__device__ __forceinline__ void voxel_weights(const RepDev&, const GridF& gf, const float pos[3],
+                                              float w[8], int v[8]) {
+  float wl[3];
+  int lo[3], hi[3];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    float x = pymodf(pos[j] + gf.half_w[j], gf.w[j]) - gf.half_d[j];
+    float t = x * gf.inv_d[j];
+    float fl = floorf(t);
+    int ind = (int)fl;
+    int li = ind == -1 ? gf.n[j] - 1 : ind;
+    lo[j] = li < 0 ? 0 : (li >= gf.n[j] ? gf.n[j] - 1 : li);
+    hi[j] = lo[j] + 1 == gf.n[j] ? 0 : lo[j] + 1;
+    wl[j] = 1 - (t - fl);
+  }
+#pragma unroll
+  for (int l = 0; l < 8; l++) {
+    int bx = l & 1, by = (l >> 1) & 1, bz = (l >> 2) & 1;
+    float fx = bx ? (1 - wl[0]) : wl[0];
+    float fy = by ? (1 - wl[1]) : wl[1];
+    float fz = bz ? (1 - wl[2]) : wl[2];
+    w[l] = fx * fy * fz;
+    v[l] = (bx ? hi[0] : lo[0]) + gf.nx * (by ? hi[1] : lo[1]) + gf.nxy * (bz ? hi[2] : lo[2]);
+  }
+}
+
 __device__ __forceinline__ long long q40(double w) { return __double2ll_rn(w * kFxScale); }
+__device__ __forceinline__ long long q40(float w) { return __float2ll_rn(w * 1099511627776.0f); }
 
 // ---------------------------------------------------------------- warp helpers
 

@@ -11,6 +11,13 @@ struct WarpShared {
   RepDev rd;
   cg_move_ctl ctl[5];
   unsigned long long tally[30];
+  GridF gf;
+  // FP32 copies of the field constants (uniform accessible volume)
+  float f_pref[CG_MAX_BINDERS], f_xpref[CG_MAX_BINDERS * CG_MAX_BINDERS];
+  float f_scale;  // 2^-40 / vol_bin
+  float f_vb;     // bead volume
+  float f_k;      // chi * vol_bin / bead volume
+  float f_lim;    // vf_limit
   int nused;
   int pad[3];
 };

@@ -49,9 +49,10 @@ __device__ __forceinline__ void add_delta(long long* vals, int ncol, int slot, i
 
 // Deposit +/- one bead's eight trilinear weights with binder states `st`
 // (packed int8) into the hash.
+template <typename Real>
 __device__ __forceinline__ void deposit_bead(const RepDev& rd, int ncol, int* keys, int* used,
                                              int* nused, long long* vals, int logH,
-                                             const double w[8], const int v[8], unsigned st,
+                                             const Real w[8], const int v[8], unsigned st,
                                              bool negate, unsigned& err) {
 #pragma unroll
   for (int l = 0; l < 8; l++) {
@@ -64,11 +65,23 @@ __device__ __forceinline__ void deposit_bead(const RepDev& rd, int ncol, int* ke
   }
 }
 
-// Field dE over the touched voxels (fixed-point grid); also stores the
-// post-move grid values into the hash values for the commit.
-__device__ double field_dE_voxels(const RepDev& rd, const KArgs& a, int ncol, const int* keys,
+// chi term of one voxel in FP64 (fields.pyx:1792-1875 with the vf_limit branch)
+__device__ __forceinline__ double chi_term64(const RepDev& rd, double V, long long g0, long long d0) {
+  double vf0 = ((double)g0 * kFxInv) / V * rd.bead_vol;
+  double vf1 = ((double)(g0 + d0) * kFxInv) / V * rd.bead_vol;
+  double k = rd.chi * (V / rd.bead_vol);
+  if (vf1 > rd.vf_limit || vf0 > rd.vf_limit)
+    return (vf1 > rd.vf_limit ? kEHugeField * vf1 : k * vf1 * vf1)
+         - (vf0 > rd.vf_limit ? kEHugeField * vf0 : k * vf0 * vf0);
+  return k * ((vf1 - vf0) * (vf1 + vf0));
+}
+
+// Field dE over the touched voxels (fixed-point grid), FP64 arithmetic; also
+// stores the post-move grid values into the hash values for the commit.
+__device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int ncol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
-                                  long long& n_vox) {
+                                  long long& n_vox, double) {
+  const RepDev& rd = ws.rd;
   double part = 0;
   const long long* grid = a.grid + rd.vox_off * ncol;
   for (int i = lane; i < nused; i += 32) {
@@ -89,17 +102,54 @@ __device__ double field_dE_voxels(const RepDev& rd, const KArgs& a, int ncol, co
     for (int b = 0; b < rd.nb; b++)
       for (int e = 0; e < rd.nb; e++)
         c += rd.xpref[b * CG_MAX_BINDERS + e] * (rho[b] * dd[e] + dd[b] * rho[e] + dd[b] * dd[e]);
-    double vf0 = ((double)g0 * kFxInv) / V * rd.bead_vol;
-    double vf1 = ((double)(g0 + d0) * kFxInv) / V * rd.bead_vol;
-    double k = rd.chi * (V / rd.bead_vol);
-    if (vf1 > rd.vf_limit || vf0 > rd.vf_limit) {
-      c += (vf1 > rd.vf_limit ? kEHugeField * vf1 : k * vf1 * vf1)
-         - (vf0 > rd.vf_limit ? kEHugeField * vf0 : k * vf0 * vf0);
-    } else {
-      c += k * ((vf1 - vf0) * (vf1 + vf0));
-    }
+    c += chi_term64(rd, V, g0, d0);
     d[0] = g0 + d0;
     part += c;
+  }
+  n_vox = nused;
+  return warp_sum(part);
+}
+
+// FP32 arithmetic per voxel, FP64 accumulation; voxels at or near the volume
+// fraction limit take the FP64 branch so the 1e99 penalty is decided as in FP64.
+__device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int ncol, const int* keys,
+                                  const int* used, long long* vals, int nused, int lane,
+                                  long long& n_vox, float) {
+  const RepDev& rd = ws.rd;
+  double part = 0;
+  const long long* grid = a.grid + rd.vox_off * ncol;
+  for (int i = lane; i < nused; i += 32) {
+    int slot = used[i];
+    int v = keys[slot];
+    long long* d = vals + (long long)slot * ncol;
+    const long long* gv = grid + (long long)v * ncol;
+    long long g0 = gv[0], d0 = d[0];
+    float sc = ws.f_scale, k = ws.f_k;
+    double V = rd.vol_bin;
+    if (rd.has_access) {
+      V = a.access_vol[rd.vox_off + v];
+      sc = (float)(kFxInv / V);
+      k = (float)(rd.chi * (V / rd.bead_vol));
+    }
+    float c = 0, rho[CG_MAX_BINDERS], dd[CG_MAX_BINDERS];
+    for (int b = 0; b < rd.nb; b++) {
+      long long gb = gv[1 + b], db = d[1 + b];
+      rho[b] = (float)gb * sc;
+      dd[b] = (float)db * sc;
+      c += ws.f_pref[b] * (dd[b] * (2.0f * rho[b] + dd[b]));
+      d[1 + b] = gb + db;
+    }
+    for (int b = 0; b < rd.nb; b++)
+      for (int e = 0; e < rd.nb; e++)
+        c += ws.f_xpref[b * CG_MAX_BINDERS + e] * (rho[b] * dd[e] + dd[b] * rho[e] + dd[b] * dd[e]);
+    float vf0 = (float)g0 * sc * ws.f_vb;
+    float dvf = (float)d0 * sc * ws.f_vb;
+    if (vf0 > ws.f_lim - 1e-3f || vf0 + dvf > ws.f_lim - 1e-3f) {
+      part += (double)c + chi_term64(rd, V, g0, d0);
+    } else {
+      part += (double)(c + k * (dvf * (2.0f * vf0 + dvf)));
+    }
+    d[0] = g0 + d0;
   }
   n_vox = nused;
   return warp_sum(part);
@@ -121,7 +171,9 @@ __device__ __forceinline__ void commit_grid(const RepDev& rd, const KArgs& a, in
 }
 
 // confinement count of one position (chromo/fields.pyx:121-202)
-__device__ __forceinline__ int out_of_bounds(const RepDev& rd, const double p[3], bool trial) {
+template <typename Real>
+__device__ __forceinline__ int out_of_bounds(const RepDev& rd, const Real q[3], bool trial) {
+  const double p[3] = {(double)q[0], (double)q[1], (double)q[2]};
   if (rd.confine_kind == 1)
     return sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]) > rd.confine_length ? 1 : 0;
   if (rd.confine_kind == 2 && trial) {
@@ -139,7 +191,7 @@ __device__ __forceinline__ double bind_f(const RepDev& rd, int b, int nm, int s)
 // ---------------------------------------------------------------- the kernel
 
 template <typename Pos, bool AUDIT>
-__global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
+__global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rep = AUDIT ? a.audit_rep : blockIdx.x * a.wpb + warp;
@@ -167,7 +219,19 @@ __global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
     if (lane == 0) ws.nused = 0;
   }
   __syncwarp();
+  if (lane == 0) {
+    make_gridf(ws.rd, ws.gf);
+    for (int b = 0; b < CG_MAX_BINDERS; b++) ws.f_pref[b] = (float)ws.rd.pref[b];
+    for (int b = 0; b < CG_MAX_BINDERS * CG_MAX_BINDERS; b++) ws.f_xpref[b] = (float)ws.rd.xpref[b];
+    ws.f_scale = (float)(kFxInv / ws.rd.vol_bin);
+    ws.f_vb = (float)ws.rd.bead_vol;
+    ws.f_k = (float)(ws.rd.chi * (ws.rd.vol_bin / ws.rd.bead_vol));
+    ws.f_lim = (float)ws.rd.vf_limit;
+  }
+  __syncwarp();
+  using Real = Pos;
   const RepDev& rd = ws.rd;
+  const GridF& gf = ws.gf;
   const long long N = rd.n_beads;
   const V4<Pos>* r4 = reinterpret_cast<const V4<Pos>*>(a.r4) + rd.bead_off;
   const V4<Pos>* t34 = reinterpret_cast<const V4<Pos>*>(a.t34) + rd.bead_off;
@@ -219,14 +283,14 @@ __global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
           int* idx = s_idx;
           if (kind <= CG_SLIDE) {
             // ---------------- segment moves: crank_shaft / end_pivot / slide
-            double M[3][4];
+            Real M[3][4];
             if (kind == CG_CRANK_SHAFT) {  // move_funcs.pyx:39-101, 157-280
-              double ang = c.amp_move * (unif(g.next()) - 0.5);
+              Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
               long long b0 = (int)(unif(g.next()) * (double)N);
               long long b1 = from_point(g, c.amp_bead, N, b0, err);
               if (b1 < 1) b1 = 1;
               check_bead_bounds(b0, b1, N, ind0, indf);
-              double pa[3], pb[3], dir[3], p[3];
+              Real pa[3], pb[3], dir[3], p[3];
               long long ia, ib;
               if (ind0 == indf - 1 && ind0 == 0) { ia = indf; ib = ind0; }
               else if (ind0 == indf - 1 && ind0 == N - 1) { ia = ind0; ib = ind0 - 1; }
@@ -237,9 +301,9 @@ __global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
               if (err) break;
               ld3(r4, ia, pa); ld3(r4, ib, pb);
               for (int i = 0; i < 3; i++) dir[i] = pa[i] - pb[i];
-              double mag = sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
-              if (mag < 1E-5) sphere(g, dir);
-              else { double sc = 1.0 / mag; for (int i = 0; i < 3; i++) dir[i] = dir[i] * sc; }
+              Real mag = rsqrt_(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+              if (mag < (Real)1E-5) sphere<Real>(g, dir);
+              else { Real sc = (Real)1.0 / mag; for (int i = 0; i < 3; i++) dir[i] = dir[i] * sc; }
               long long ip;
               if (ind0 == 0 && indf != N) ip = indf;
               else if (ind0 != 0 && indf == N) ip = ind0 - 1;
@@ -248,12 +312,12 @@ __global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
               ld3(r4, ip, p);
               axis_rotation(dir, p, ang, M);
             } else if (kind == CG_END_PIVOT) {  // move_funcs.pyx:285-398
-              double ang = c.amp_move * (unif(g.next()) - 0.5);
+              Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
               long long lhs = (long long)g.next() % 2;
               if (lhs == 1) { ind0 = 0; indf = from_left(g, c.amp_bead, N, err) + 1; }
               else { ind0 = N - from_left(g, c.amp_bead, N, err); indf = N; }
-              double axis[3], p[3];
-              sphere(g, axis);
+              Real axis[3], p[3];
+              sphere<Real>(g, axis);
               long long ip;
               if (ind0 == 0 && indf != N) ip = indf;
               else if (ind0 != 0 && indf == N) ip = ind0 - 1;
@@ -263,8 +327,8 @@ __global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
               ld3(r4, ip, p);
               axis_rotation(axis, p, ang, M);
             } else {  // slide, move_funcs.pyx:403-465
-              double amp = c.amp_move * unif(g.next()), d[3];
-              sphere(g, d);
+              Real amp = (Real)c.amp_move * uni<Real>(g.next()), d[3];
+              sphere<Real>(g, d);
               for (int i = 0; i < 3; i++) { M[i][3] = d[i] * amp; }
               long long b0 = (long long)g.next() % N;
               long long b1 = from_point(g, c.amp_bead, N, b0, err);
@@ -283,19 +347,19 @@ __global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
               for (long long k = lane; k < m; k += 32) {
                 const long long i = ind0 + k;
                 V4<Pos> R = r4[i], T3 = t34[i], T2 = t24[i];
-                double r[3] = {(double)R.x, (double)R.y, (double)R.z};
-                double t3[3] = {(double)T3.x, (double)T3.y, (double)T3.z};
-                double t2[3] = {(double)T2.x, (double)T2.y, (double)T2.z};
-                double tr[3], tt3[3], tt2[3];
+                Real r[3] = {R.x, R.y, R.z};
+                Real t3[3] = {T3.x, T3.y, T3.z};
+                Real t2[3] = {T2.x, T2.y, T2.z};
+                Real tr[3], tt3[3], tt2[3];
                 if (kind == CG_SLIDE) {
-                  for (int j = 0; j < 3; j++) { tr[j] = rnd_pos<Pos>(r[j] + M[j][3]); tt3[j] = t3[j]; tt2[j] = t2[j]; }
+                  for (int j = 0; j < 3; j++) { tr[j] = r[j] + M[j][3]; tt3[j] = t3[j]; tt2[j] = t2[j]; }
                 } else {
                   for (int j = 0; j < 3; j++) {
-                    double er = 0, e3 = 0, e2 = 0;
+                    Real er = 0, e3 = 0, e2 = 0;
                     for (int q = 0; q < 3; q++) { er += M[j][q] * r[q]; e3 += M[j][q] * t3[q]; e2 += M[j][q] * t2[q]; }
-                    tr[j] = rnd_pos<Pos>(er + M[j][3]);
-                    tt3[j] = rnd_pos<Pos>(e3);
-                    tt2[j] = rnd_pos<Pos>(e2);
+                    tr[j] = er + M[j][3];
+                    tt3[j] = e3;
+                    tt2[j] = e2;
                   }
                 }
                 const bool fin = isfinite(tr[0]) && isfinite(tr[1]) && isfinite(tr[2]);
@@ -303,23 +367,23 @@ __global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
                 Pos* sg = stage + k * 9;
                 for (int j = 0; j < 3; j++) { sg[j] = (Pos)tr[j]; sg[3 + j] = (Pos)tt3[j]; sg[6 + j] = (Pos)tt2[j]; }
                 if (k == 0 && ind0 != 0) {  // continuous_dE_poly forward bond, polymers.pyx:1121-1131
-                  double r0[3], t30[3];
+                  Real r0[3], t30[3];
                   ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
-                  part += pair_dE_fwd(load_bond(bonds, i - 1), r0, r, tr, t30, t3, tt3);
+                  part += pair_dE_fwd(load_bond<Real>(bonds, i - 1), r0, r, tr, t30, t3, tt3);
                 }
                 if (k == m - 1 && indf != N) {  // reverse bond, polymers.pyx:1132-1142
-                  double r1[3], t31[3];
+                  Real r1[3], t31[3];
                   ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
-                  part += pair_dE_rev(load_bond(bonds, i), r, tr, r1, t3, tt3, t31);
+                  part += pair_dE_rev(load_bond<Real>(bonds, i), r, tr, r1, t3, tt3, t31);
                 }
                 if (check_field && rd.confine_kind) {
                   oob += out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
                 }
                 if (density && fin) {
-                  double w0[8], w1[8];
+                  Real w0[8], w1[8];
                   int v0[8], v1[8];
-                  voxel_weights(rd, r, w0, v0);
-                  voxel_weights(rd, tr, w1, v1);
+                  voxel_weights(rd, gf, r, w0, v0);
+                  voxel_weights(rd, gf, tr, w1, v1);
                   unsigned s = st[i];
                   deposit_bead(rd, ncol, keys, used, &ws.nused, vals, logH, w0, v0, s, true, err);
                   deposit_bead(rd, ncol, keys, used, &ws.nused, vals, logH, w1, v1, s, false, err);
@@ -337,12 +401,12 @@ __global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
               __syncwarp();
               if (density) {
                 int nu = ws.nused;
-                dEf += field_dE_voxels(rd, a, ncol, keys, used, vals, nu, lane, nvox);
+                dEf += field_dE_voxels(ws, a, ncol, keys, used, vals, nu, lane, nvox, (Real)0);
               }
             }
           } else if (kind == CG_TANGENT_ROTATION) {
             // ---------------- tangent_rotation, move_funcs.pyx:470-582
-            double ang = c.amp_move * (unif(g.next()) - 0.5);
+            Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
             long long n = (long long)g.next() % c.amp_bead + 1;
             if (n > N) { err |= E_WINDOW; break; }
             m = n;
@@ -387,39 +451,38 @@ __global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
             if (err) break;
             const unsigned long long axis_base = g.pos;
             double part = 0;
+            Real sa, ca;
+            rsincos(ang, &sa, &ca);
             for (long long k = lane; k < m; k += 32) {
               const long long i = idx[k];
               bool ok1, ok2;
-              double phi = unif(g.at(axis_base + 2 * k, ok1)) * (2.0 * 3.141592653589793);
-              double theta = acos(unif(g.at(axis_base + 2 * k + 1, ok2)) * 2 - 1);
+              unsigned xa = g.at(axis_base + 2 * k, ok1), xb = g.at(axis_base + 2 * k + 1, ok2);
               if (!(ok1 && ok2)) err |= E_STREAM;
-              double sp, cp, sth, cth;
-              sincos(phi, &sp, &cp);
-              sincos(theta, &sth, &cth);
-              const double axis[3] = {cp * sth, sp * sth, cth};
-              const double origin[3] = {0, 0, 0};
-              double M[3][4];
-              axis_rotation(axis, origin, ang, M);
-              double r[3], t3[3], t2[3], tt3[3], tt2[3];
+              Real axis[3];
+              sphere_from<Real>(xa, xb, axis);
+              const Real origin[3] = {0, 0, 0};
+              Real M[3][4];
+              axis_rotation_sc(axis, origin, sa, ca, M);
+              Real r[3], t3[3], t2[3], tt3[3], tt2[3];
               ld3(r4, i, r); ld3(t34, i, t3); ld3(t24, i, t2);
               for (int j = 0; j < 3; j++) {
-                double e3 = 0, e2 = 0;
+                Real e3 = 0, e2 = 0;
                 for (int q = 0; q < 3; q++) { e3 += M[j][q] * t3[q]; e2 += M[j][q] * t2[q]; }
-                tt3[j] = rnd_pos<Pos>(e3);
-                tt2[j] = rnd_pos<Pos>(e2);
+                tt3[j] = e3;
+                tt2[j] = e2;
               }
               Pos* sg = stage + k * 9;
               for (int j = 0; j < 3; j++) { sg[3 + j] = (Pos)tt3[j]; sg[6 + j] = (Pos)tt2[j]; }
               double de = 0;
               if (i != 0) {
-                double r0[3], t30[3];
+                Real r0[3], t30[3];
                 ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
-                de += pair_dE_fwd(load_bond(bonds, i - 1), r0, r, r, t30, t3, tt3);
+                de += pair_dE_fwd(load_bond<Real>(bonds, i - 1), r0, r, r, t30, t3, tt3);
               }
               if (i + 1 != N) {
-                double r1[3], t31[3];
+                Real r1[3], t31[3];
                 ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
-                de += pair_dE_rev(load_bond(bonds, i), r, r, r1, t3, tt3, t31);
+                de += pair_dE_rev(load_bond<Real>(bonds, i), r, r, r1, t3, tt3, t31);
               }
               part += de;
             }
@@ -479,10 +542,10 @@ __global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
               dbl += (s_new == 2 ? 1 : 0) - (s_old == 2 ? 1 : 0);
               idx[k] = s_new;
               if (density && s_new != s_old) {
-                double p[3], w[8];
+                Real p[3], w[8];
                 int v[8];
                 ld3(r4, i, p);
-                voxel_weights(rd, p, w, v);
+                voxel_weights(rd, gf, p, w, v);
 #pragma unroll
                 for (int l = 0; l < 8; l++) {
                   int slot = hash_slot(keys, used, &ws.nused, logH, v[l], err);
@@ -508,7 +571,7 @@ __global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
             __syncwarp();
             if (density) {
               int nu = ws.nused;
-              dEf += field_dE_voxels(rd, a, ncol, keys, used, vals, nu, lane, nvox);
+              dEf += field_dE_voxels(ws, a, ncol, keys, used, vals, nu, lane, nvox, (Real)0);
               dEf += rd.intra[bsel] * (double)ddb;
             }
           }
@@ -520,8 +583,7 @@ __global__ void __launch_bounds__(128) mc_kernel(KArgs a) {
             double dE = 0;
             dE += dEp;
             dE += dEf;
-            double ex = exp(-dE);
-            bool acc = unif(g.next()) < ex;
+            bool acc = metropolis(g.next(), -dE);
             if (AUDIT && g.fail) { err |= E_STREAM; break; }
             accepted = acc ? 1 : 0;
             if (acc) {
@@ -642,12 +704,14 @@ __global__ void deposit_kernel(KArgs a, int rep_only) {
   if (rd.field_kind != 2) return;
   const V4<Pos>* r4 = reinterpret_cast<const V4<Pos>*>(a.r4) + rd.bead_off;
   long long* grid = a.grid + rd.vox_off * a.ncol;
+  GridF gf;
+  make_gridf(rd, gf);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < rd.n_beads;
        i += (long long)gridDim.x * blockDim.x) {
-    double p[3], w[8];
+    Pos p[3], w[8];
     int v[8];
     ld3(r4, i, p);
-    voxel_weights(rd, p, w, v);
+    voxel_weights(rd, gf, p, w, v);
     unsigned s = a.states[rd.bead_off + i];
     for (int l = 0; l < 8; l++) {
       long long q = q40(w[l]);
@@ -692,7 +756,7 @@ __global__ void energy_kernel(KArgs a, double* out) {
     if (i > 0) {  // SSWLC.compute_E, polymers.pyx:1348-1381
       double r0[3], r1[3], a0[3], a1[3], dr[3], dp[3], bend[3];
       ld3(r4, i - 1, r0); ld3(r4, i, r1); ld3(t34, i - 1, a0); ld3(t34, i, a1);
-      Bond b = load_bond(bonds, i - 1);
+      Bond<double> b = load_bond<double>(bonds, i - 1);
       for (int j = 0; j < 3; j++) dr[j] = r1[j] - r0[j];
       double par = a0[0] * dr[0] + a0[1] * dr[1] + a0[2] * dr[2];
       for (int j = 0; j < 3; j++) dp[j] = dr[j] - a0[j] * par;

@@ -44,7 +44,39 @@ def parse():
     ap.add_argument("--workload", default="batched", choices=["batched", "large", "diff"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-budget", type=float, default=2.0)
+    ap.add_argument("--profile", action="store_true",
+                    help="small case for ncu: 64 x 5000-bead replicas, 1 warm-up + 2 MC launches")
     return ap.parse_args()
+
+
+def profile_case(args):
+    """A bounded case for profilers: the 64-replica workload (5,000 beads each,
+    40^3 grids, ~130 MB of grids: larger than L2), one warm-up launch and two
+    launches of the MC kernel of 62 steps each."""
+    import numpy as np
+    import torch
+    from chromo_gb300.build import build
+    build()
+    from chromo_gb300 import workloads as wl
+    w = wl.make_workload("diff")
+    sim = wl.build_sim(w)
+    sh = torch.cuda.current_stream().cuda_stream
+    sim.run(w.steps_per_round, 1, sh)
+    sim.sync(sh)
+    sim.reset_tally()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(2):
+        sim.run(w.steps_per_round, 2 + i, sh)
+    e1.record()
+    torch.cuda.synchronize()
+    sim.sync(sh)
+    tal = np.stack([sim.tally(r) for r in range(w.replicas)])
+    moves = float(tal[:, :, 0].sum())
+    ms = e0.elapsed_time(e1)
+    print(json.dumps({"case": "profile", "replicas": int(w.replicas), "moves": moves, "ms": ms,
+                      "moves_per_s": moves / (ms / 1000.0),
+                      "algorithmic_bytes": wl.algorithmic_bytes(tal, w.n_binders)}), flush=True)
 
 
 def load_peaks():
@@ -179,6 +211,9 @@ def reference_arm(args, rank, world):
 
 def main():
     args = parse()
+    if args.profile:
+        profile_case(args)
+        return
     rank, world, local = dist_init(args)
     if args.impl == "reference":
         reference_arm(args, rank, world)

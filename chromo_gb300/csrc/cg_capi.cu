@@ -203,6 +203,7 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   for (int r = 0; r < s->R; r++) {
     long long n = cfg->n_beads[r];
     if (n < 2) { cg_destroy(s); return fail(CG_ERR_ARG, "every chain needs at least 2 beads"); }
+    if (n > 2000000000LL) { cg_destroy(s); return fail(CG_ERR_ARG, "chains are limited to 2e9 beads"); }
     int nx = cfg->grid_dims[3 * r], ny = cfg->grid_dims[3 * r + 1], nz = cfg->grid_dims[3 * r + 2];
     if (nx < 1 || ny < 1 || nz < 1) { cg_destroy(s); return fail(CG_ERR_ARG, "grid dims must be >= 1"); }
     if ((long long)nx * ny * nz > (1LL << 30)) { cg_destroy(s); return fail(CG_ERR_ARG, "grid too large"); }
@@ -434,6 +435,7 @@ int cg_set_controllers(cg_sim* s, int rep, const cg_move_ctl* c, int n_ctl) {
       if (top > (double)s->max_tangent)
         return fail(CG_ERR_ARG, "tangent_rotation bead amplitude exceeds max_tangent given at creation");
       if (c[i].move_on && c[i].amp_bead < 1) return fail(CG_ERR_ARG, "tangent_rotation needs amp_bead >= 1");
+      if (top > 2e9) return fail(CG_ERR_ARG, "bead amplitude too large");
     } else if (top + 1 > (double)s->max_segment) {
       return fail(CG_ERR_ARG, "bead amplitude exceeds max_segment given at creation");
     }

@@ -182,7 +182,7 @@ template <class R>
 __device__ long long from_point(R& g, long long window, long long n, long long ind0, unsigned& err) {
   if (window > n) { err |= E_WINDOW; return 0; }
   if (window < 1) return ind0;
-  long long side = (long long)g.next() % 2;
+  long long side = g.next() & 1u;
   if (side == 0) {
     long long ws = window < ind0 ? window : ind0;
     if (ws < 1) ws = 1;
@@ -332,6 +332,57 @@ __device__ __forceinline__ double pair_dE_rev(const Bond<Real>& b, const Real r0
     bc[i] = t31[i] - t30[i] - dp[i] * b.eta;
   }
   return (double)e_pair(b, bt, pt, dpt) - (double)e_pair(b, bc, pc, dp);
+}
+
+// FP32 evaluation of E_pair(trial) - E_pair(current) in difference form:
+// |b_t|^2 - |b_c|^2 = sum (b_t - b_c)(b_t + b_c) and likewise for the other
+// two terms, with the differences formed from the (small) input differences,
+// so the rounding error scales with dE rather than with E.
+// Forward bond (bead 1 moved; bead 0 and its tangent fixed).
+__device__ __forceinline__ double pair_dE_fwd(const Bond<float>& b, const float r0[3], const float r1[3],
+                                              const float tr1[3], const float t30[3],
+                                              const float t31[3], const float tt31[3]) {
+  float drt[3], dr[3], ddr[3];
+  for (int i = 0; i < 3; i++) { drt[i] = tr1[i] - r0[i]; dr[i] = r1[i] - r0[i]; ddr[i] = tr1[i] - r1[i]; }
+  float pt = t30[0] * drt[0] + t30[1] * drt[1] + t30[2] * drt[2];
+  float pc = t30[0] * dr[0] + t30[1] * dr[1] + t30[2] * dr[2];
+  float dpar = t30[0] * ddr[0] + t30[1] * ddr[1] + t30[2] * ddr[2];
+  float e_par = dpar * ((pt - b.g) + (pc - b.g));
+  float e_perp = 0, e_bend = 0;
+  for (int i = 0; i < 3; i++) {
+    float dpt = drt[i] - t30[i] * pt, dp = dr[i] - t30[i] * pc;
+    float ddp = ddr[i] - t30[i] * dpar;
+    float bt = tt31[i] - t30[i] - dpt * b.eta, bc = t31[i] - t30[i] - dp * b.eta;
+    float db = (tt31[i] - t31[i]) - ddp * b.eta;
+    e_perp += ddp * (dpt + dp);
+    e_bend += db * (bt + bc);
+  }
+  return 0.5 * ((double)(b.eb * e_bend) + (double)(b.ep * e_par) + (double)(b.epp * e_perp));
+}
+
+// Reverse bond (bead 0 moved; bead 1 fixed).
+__device__ __forceinline__ double pair_dE_rev(const Bond<float>& b, const float r0[3], const float tr0[3],
+                                              const float r1[3], const float t30[3],
+                                              const float tt30[3], const float t31[3]) {
+  float drt[3], dr[3], ddr[3], dt[3];
+  for (int i = 0; i < 3; i++) {
+    drt[i] = r1[i] - tr0[i]; dr[i] = r1[i] - r0[i]; ddr[i] = r0[i] - tr0[i]; dt[i] = tt30[i] - t30[i];
+  }
+  float pt = tt30[0] * drt[0] + tt30[1] * drt[1] + tt30[2] * drt[2];
+  float pc = t30[0] * dr[0] + t30[1] * dr[1] + t30[2] * dr[2];
+  float dpar = (tt30[0] * ddr[0] + tt30[1] * ddr[1] + tt30[2] * ddr[2])
+             + (dt[0] * dr[0] + dt[1] * dr[1] + dt[2] * dr[2]);
+  float e_par = dpar * ((pt - b.g) + (pc - b.g));
+  float e_perp = 0, e_bend = 0;
+  for (int i = 0; i < 3; i++) {
+    float dpt = drt[i] - tt30[i] * pt, dp = dr[i] - t30[i] * pc;
+    float ddp = ddr[i] - (dt[i] * pt + t30[i] * dpar);
+    float bt = t31[i] - tt30[i] - dpt * b.eta, bc = t31[i] - t30[i] - dp * b.eta;
+    float db = -dt[i] - ddp * b.eta;
+    e_perp += ddp * (dpt + dp);
+    e_bend += db * (bt + bc);
+  }
+  return 0.5 * ((double)(b.eb * e_bend) + (double)(b.ep * e_par) + (double)(b.epp * e_perp));
 }
 
 // ---------------------------------------------------------------- density field

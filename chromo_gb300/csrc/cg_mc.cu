@@ -283,14 +283,14 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
           int* idx = s_idx;
           if (kind <= CG_SLIDE) {
             // ---------------- segment moves: crank_shaft / end_pivot / slide
-            Real M[3][4];
+            double Md[3][4];
             if (kind == CG_CRANK_SHAFT) {  // move_funcs.pyx:39-101, 157-280
-              Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
+              double ang = c.amp_move * (unif(g.next()) - 0.5);
               long long b0 = (int)(unif(g.next()) * (double)N);
               long long b1 = from_point(g, c.amp_bead, N, b0, err);
               if (b1 < 1) b1 = 1;
               check_bead_bounds(b0, b1, N, ind0, indf);
-              Real pa[3], pb[3], dir[3], p[3];
+              double pa[3], pb[3], dir[3], p[3];
               long long ia, ib;
               if (ind0 == indf - 1 && ind0 == 0) { ia = indf; ib = ind0; }
               else if (ind0 == indf - 1 && ind0 == N - 1) { ia = ind0; ib = ind0 - 1; }
@@ -301,23 +301,23 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
               if (err) break;
               ld3(r4, ia, pa); ld3(r4, ib, pb);
               for (int i = 0; i < 3; i++) dir[i] = pa[i] - pb[i];
-              Real mag = rsqrt_(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
-              if (mag < (Real)1E-5) sphere<Real>(g, dir);
-              else { Real sc = (Real)1.0 / mag; for (int i = 0; i < 3; i++) dir[i] = dir[i] * sc; }
+              double mag = sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+              if (mag < 1E-5) sphere<double>(g, dir);
+              else { double sc = 1.0 / mag; for (int i = 0; i < 3; i++) dir[i] = dir[i] * sc; }
               long long ip;
               if (ind0 == 0 && indf != N) ip = indf;
               else if (ind0 != 0 && indf == N) ip = ind0 - 1;
               else if (ind0 == 0 && indf == N) ip = ind0;
               else ip = ind0 - 1;
               ld3(r4, ip, p);
-              axis_rotation(dir, p, ang, M);
+              axis_rotation(dir, p, ang, Md);
             } else if (kind == CG_END_PIVOT) {  // move_funcs.pyx:285-398
-              Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
-              long long lhs = (long long)g.next() % 2;
+              double ang = c.amp_move * (unif(g.next()) - 0.5);
+              long long lhs = g.next() & 1u;
               if (lhs == 1) { ind0 = 0; indf = from_left(g, c.amp_bead, N, err) + 1; }
               else { ind0 = N - from_left(g, c.amp_bead, N, err); indf = N; }
-              Real axis[3], p[3];
-              sphere<Real>(g, axis);
+              double axis[3], p[3];
+              sphere<double>(g, axis);
               long long ip;
               if (ind0 == 0 && indf != N) ip = indf;
               else if (ind0 != 0 && indf == N) ip = ind0 - 1;
@@ -325,16 +325,20 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
               else ip = ind0;
               if (err) break;
               ld3(r4, ip, p);
-              axis_rotation(axis, p, ang, M);
+              axis_rotation(axis, p, ang, Md);
             } else {  // slide, move_funcs.pyx:403-465
-              Real amp = (Real)c.amp_move * uni<Real>(g.next()), d[3];
-              sphere<Real>(g, d);
-              for (int i = 0; i < 3; i++) { M[i][3] = d[i] * amp; }
-              long long b0 = (long long)g.next() % N;
+              double amp = c.amp_move * unif(g.next()), d[3];
+              sphere<double>(g, d);
+              for (int i = 0; i < 3; i++) { Md[i][3] = d[i] * amp; }
+              long long b0 = g.next() % (unsigned)N;
               long long b1 = from_point(g, c.amp_bead, N, b0, err);
               check_bead_bounds(b0, b1, N, ind0, indf);
             }
             if (err) break;
+            // the matrix in the arithmetic of the storage type (exact for FP64)
+            Real M[3][4];
+            for (int i = 0; i < 3; i++)
+              for (int j = 0; j < 4; j++) M[i][j] = (Real)Md[i][j];
             m = indf - ind0;
             if (m == 0) {
               empty = true;
@@ -406,8 +410,8 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
             }
           } else if (kind == CG_TANGENT_ROTATION) {
             // ---------------- tangent_rotation, move_funcs.pyx:470-582
-            Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
-            long long n = (long long)g.next() % c.amp_bead + 1;
+            double ang = c.amp_move * (unif(g.next()) - 0.5);
+            long long n = (long long)(g.next() % (unsigned)c.amp_bead) + 1;
             if (n > N) { err |= E_WINDOW; break; }
             m = n;
             if (m > a.stage_cap) { stage = g_stage; idx = g_idx; }
@@ -418,7 +422,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
               if (++it > kMaxIter) { err |= E_SPIN; break; }
               bool ok;
               unsigned x = g.at(g.pos + lane, ok);
-              long long cand = ok ? (long long)x % N : -1 - lane;
+              long long cand = ok ? (long long)(x % (unsigned)N) : -1 - lane;
               unsigned grp = __match_any_sync(kFull, cand);
               bool first = (grp & ((1u << lane) - 1u)) == 0;
               bool fresh = ok && first && !((picked[cand >> 5] >> (cand & 31)) & 1u);
@@ -451,18 +455,21 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
             if (err) break;
             const unsigned long long axis_base = g.pos;
             double part = 0;
-            Real sa, ca;
+            double sa, ca;
             rsincos(ang, &sa, &ca);
             for (long long k = lane; k < m; k += 32) {
               const long long i = idx[k];
               bool ok1, ok2;
               unsigned xa = g.at(axis_base + 2 * k, ok1), xb = g.at(axis_base + 2 * k + 1, ok2);
               if (!(ok1 && ok2)) err |= E_STREAM;
-              Real axis[3];
-              sphere_from<Real>(xa, xb, axis);
-              const Real origin[3] = {0, 0, 0};
+              double axis[3];
+              sphere_from<double>(xa, xb, axis);
+              const double origin[3] = {0, 0, 0};
+              double Md[3][4];
+              axis_rotation_sc(axis, origin, sa, ca, Md);
               Real M[3][4];
-              axis_rotation_sc(axis, origin, sa, ca, M);
+              for (int ii = 0; ii < 3; ii++)
+                for (int jj2 = 0; jj2 < 4; jj2++) M[ii][jj2] = (Real)Md[ii][jj2];
               Real r[3], t3[3], t2[3], tt3[3], tt2[3];
               ld3(r4, i, r); ld3(t34, i, t3); ld3(t24, i, t2);
               for (int j = 0; j < 3; j++) {
@@ -492,8 +499,8 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
             ind0 = idx[0]; indf = ind0 + 1;
           } else {
             // ---------------- change_binding_state, move_funcs.pyx:717-820
-            bsel = (int)((long long)g.next() % rd.nb);
-            long long b0 = (long long)g.next() % N;
+            bsel = (int)(g.next() % (unsigned)rd.nb);
+            long long b0 = g.next() % (unsigned)N;
             long long b1 = from_point(g, c.amp_bead, N, b0, err);
             if (err) break;
             check_bead_bounds(b0, b1, N, ind0, indf);

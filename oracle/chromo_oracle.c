@@ -250,6 +250,14 @@ static inline void ld3(const OR_POS *a, int64_t i, double v[3])
 
 static inline double rnd_pos(double x) { return (double)(OR_POS)x; }
 
+/* FP32-storage emulation of the GPU (positions stored as float and a
+ * fixed-point grid): the GPU applies the FP64 move matrix rounded to FP32 with
+ * FP32 arithmetic and computes trilinear weights in FP32, so this mode does
+ * the same to keep the state bit-identical; every energy difference is still
+ * evaluated in FP64 here (the recomputation the GPU's dE is checked against). */
+#define OR_F32 (sizeof(OR_POS) == 4)
+static inline int emu32(const or_system *s) { return OR_F32 && s->fixed_density; }
+
 
 
 /* transform_r_t3_t2, move_funcs.pyx:121-154: trial = round_to_storage(M * x) */
@@ -257,6 +265,23 @@ static void transform_bead(const or_system *s, int64_t i, double M[3][4], double
 {
     double r[3], t3[3], t2[3];
     ld3(s->r, i, r); ld3(s->t3, i, t3); ld3(s->t2, i, t2);
+    if (emu32(s)) {
+        float Mf[3][4];
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 4; b++) Mf[a][b] = (float)M[a][b];
+        for (int j = 0; j < 3; j++) {
+            float er = 0, e3 = 0, e2 = 0;
+            for (int k = 0; k < 3; k++) {
+                er += Mf[j][k] * (float)r[k];
+                e3 += Mf[j][k] * (float)t3[k];
+                e2 += Mf[j][k] * (float)t2[k];
+            }
+            out[j] = (double)(er + Mf[j][3]);
+            out[3 + j] = (double)e3;
+            out[6 + j] = (double)e2;
+        }
+        return;
+    }
     for (int j = 0; j < 3; j++) {
         double er = 0, e3 = 0, e2 = 0;
         for (int k = 0; k < 3; k++) {
@@ -427,8 +452,48 @@ static inline double pymod(double a, double b)
 /* Eight trilinear weights and voxel super-indices of one position,
  * fields.pyx:1430-1458 (bin + lower weight), :1524-1598 (weights),
  * :1600-1673 (indices), :565-575 (periodic super-index table). */
+static float pymodf_(float a, float b)
+{
+    if (a >= 0 && a < b) return a;
+    float m = fmodf(a, b);
+    if (m != 0 && ((m < 0) != (b < 0))) m += b;
+    return m;
+}
+
+/* FP32 trilinear weights, the GPU's FP32-storage arithmetic */
+static void voxel_weights_f32(const or_system *s, const double pos[3], double w[8], int64_t v[8])
+{
+    const double width[3] = {s->x_width, s->y_width, s->z_width};
+    const int64_t n[3] = {s->nx, s->ny, s->nz};
+    float wl[3];
+    int64_t lo[3], hi[3];
+    for (int j = 0; j < 3; j++) {
+        double d = width[j] / (double)n[j];
+        float fw = (float)width[j], hw = (float)(0.5 * width[j]), hd = (float)(0.5 * d);
+        float inv = (float)(1.0 / d);
+        float x = pymodf_((float)pos[j] + hw, fw) - hd;
+        float t = x * inv;
+        float fl = floorf(t);
+        int ind = (int)fl;
+        int64_t li = ind == -1 ? n[j] - 1 : ind;
+        lo[j] = li < 0 ? 0 : (li >= n[j] ? n[j] - 1 : li);
+        hi[j] = (lo[j] + 1) % n[j];
+        wl[j] = 1 - (t - fl);
+    }
+    for (int l = 0; l < 8; l++) {
+        int bx = l & 1, by = (l >> 1) & 1, bz = (l >> 2) & 1;
+        float fx = bx ? (1 - wl[0]) : wl[0];
+        float fy = by ? (1 - wl[1]) : wl[1];
+        float fz = bz ? (1 - wl[2]) : wl[2];
+        w[l] = (double)(fx * fy * fz);
+        int64_t ix = bx ? hi[0] : lo[0], iy = by ? hi[1] : lo[1], iz = bz ? hi[2] : lo[2];
+        v[l] = ix + s->nx * iy + s->nx * s->ny * iz;
+    }
+}
+
 static void voxel_weights(const or_system *s, const double pos[3], double w[8], int64_t v[8])
 {
+    if (emu32(s)) { voxel_weights_f32(s, pos, w, v); return; }
     const double width[3] = {s->x_width, s->y_width, s->z_width};
     const int64_t n[3] = {s->nx, s->ny, s->nz};
     double wl[3];
@@ -915,7 +980,8 @@ static int64_t mc_step(or_system *s, or_ctl *c, or_rng *g, or_record *rec)
                 double r[3];
                 ld3(s->r, ind0 + k, r);
                 for (int j = 0; j < 3; j++) {
-                    s->trial[9 * k + j] = rnd_pos(r[j] + M[j][3]);
+                    s->trial[9 * k + j] = emu32(s) ? (double)((float)r[j] + (float)M[j][3])
+                                                   : rnd_pos(r[j] + M[j][3]);
                     s->trial[9 * k + 3 + j] = (double)s->t3[3 * (ind0 + k) + j];
                     s->trial[9 * k + 6 + j] = (double)s->t2[3 * (ind0 + k) + j];
                 }
@@ -944,10 +1010,20 @@ static int64_t mc_step(or_system *s, or_ctl *c, or_rng *g, or_record *rec)
             axis_rotation(axis, origin, ang, M, !s->fixed_density);
             ld3(s->t3, i, t3); ld3(s->t2, i, t2);
             for (int j = 0; j < 3; j++) {
-                double e3 = 0, e2 = 0;
-                for (int q = 0; q < 3; q++) { e3 += M[j][q] * t3[q]; e2 += M[j][q] * t2[q]; }
-                s->trial[9 * k + 3 + j] = rnd_pos(e3);
-                s->trial[9 * k + 6 + j] = rnd_pos(e2);
+                if (emu32(s)) {
+                    float e3 = 0, e2 = 0;
+                    for (int q = 0; q < 3; q++) {
+                        e3 += (float)M[j][q] * (float)t3[q];
+                        e2 += (float)M[j][q] * (float)t2[q];
+                    }
+                    s->trial[9 * k + 3 + j] = (double)e3;
+                    s->trial[9 * k + 6 + j] = (double)e2;
+                } else {
+                    double e3 = 0, e2 = 0;
+                    for (int q = 0; q < 3; q++) { e3 += M[j][q] * t3[q]; e2 += M[j][q] * t2[q]; }
+                    s->trial[9 * k + 3 + j] = rnd_pos(e3);
+                    s->trial[9 * k + 6 + j] = rnd_pos(e2);
+                }
                 s->trial[9 * k + j] = (double)s->r[3 * i + j];
             }
         }

@@ -52,10 +52,12 @@ def metropolis_u(recs, draws):
 
 @pytest.mark.parametrize("name", [c for c in CASES if c != "vf_limit"])
 def test_fp32_path_within_tolerance_of_fp64_oracle(name):
-    """FP32 storage and FP32 arithmetic: every move's dE is within
-    1e-5 * max(1, |dE|) of the oracle's FP64 evaluation of the same proposal,
-    bead selections are identical, and decisions are identical outside the
-    tie band |dE + ln u| <= 1e-5 * max(1, |dE|)."""
+    """FP32 storage and FP32 arithmetic: the oracle applies the same FP32 move
+    matrices and FP32 trilinear weights, so the two states stay bit-identical;
+    every move's dE (FP32 arithmetic on the GPU) is within 1e-5 * max(1, |dE|)
+    of the oracle's FP64 evaluation of the same proposal, bead selections are
+    identical, and decisions are identical outside the tie band
+    |dE + ln u| <= 1e-5 * max(1, |dE|)."""
     g = load(name)
     o = oracle_system(g, pos="f32", fixed_density=1)
     if int(g["field_kind"]) == 2:
@@ -81,11 +83,11 @@ def test_fp32_path_within_tolerance_of_fp64_oracle(name):
     if not len(flips):
         assert len(recs) == len(orecs) and du == o.draw_pos and bu == o.bstate_pos
         r, t3, t2, st = sim.get_chain(0)
-        np.testing.assert_allclose(r, o.r, rtol=0, atol=1e-2)
+        np.testing.assert_array_equal(r.astype(np.float32), o.r)
+        np.testing.assert_array_equal(t3.astype(np.float32), o.t3)
         np.testing.assert_array_equal(st, o.states)
         if int(g["field_kind"]) == 2:
-            gd, od = sim.density(0).astype(np.float64), o.density_fx.astype(np.float64)
-            assert np.abs(gd - od).max() <= 1e-5 * np.abs(od).max()
+            np.testing.assert_array_equal(sim.density(0), o.density_fx)
 
 
 def test_fp32_path_dE_accuracy_report():
@@ -108,7 +110,7 @@ def test_fp32_path_dE_accuracy_report():
         d = np.abs(_dE(recs)[:stop] - _dE(orecs)[:stop]) / np.maximum(1, np.abs(_dE(orecs)[:stop]))
         worst = max(worst, float(d[ok].max()))
     print(f"worst relative dE error of the FP32 path: {worst:.3e}")
-    assert worst < 1e-7
+    assert worst < 1e-6
 
 
 @pytest.mark.parametrize("name", ["one_binder", "two_binders", "big_amps"])

@@ -1,0 +1,100 @@
+"""Host-side parts of the drop-in API, checked against the reference's values
+(stored in the golden cases) and its documented behaviour."""
+import numpy as np
+import pytest
+
+import chromo_gb300.binders as cb
+from chromo_gb300.fields import NullField, UniformDensityField
+from chromo_gb300.mc import get_amplitude_bounds
+from chromo_gb300.mc.mc_controller import SimpleControl, all_moves
+from chromo_gb300.polymers import Chromatin
+from golden_cases import CASES, load
+
+
+def _poly_from_golden(g, state="0"):
+    names = [str(x) for x in g["binder_names"]]
+    for i, nm in enumerate(names):
+        b = cb.get_by_name(nm)
+        b.chemical_potential = float(g["mu"][i])
+        b.interaction_energy = float(g["interaction_energy"][i])
+        b.cross_talk_interaction_energy = {
+            str(o): float(g["cross"][i, j]) for j, o in enumerate(names)
+            if not np.isnan(g["cross"][i, j])}
+    p = Chromatin("p", g["r" + state], bead_length=g["bead_length"], t3=g["t3" + state],
+                  t2=g["t2" + state], states=g["states" + state], binder_names=np.array(names),
+                  chemical_mods=g["marks"], chemical_mod_names=np.array(names),
+                  max_binders=int(g["max_binders"]))
+    binders = cb.make_binder_collection([cb.get_by_name(n) for n in names])
+    return p, binders
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_sswlc_parameters_match_reference(name):
+    g = load(name)
+    p, _ = _poly_from_golden(g)
+    for k in ("eps_bend", "gamma", "eps_par", "eps_perp", "eta"):
+        np.testing.assert_array_equal(getattr(p, k), g[k])
+
+
+@pytest.mark.parametrize("name", [c for c in CASES if c != "null_spherical"])
+def test_field_prefactors_match_reference(name):
+    g = load(name)
+    p, binders = _poly_from_golden(g)
+    n = [int(x) for x in g["nxyz"]]
+    w = [float(x) for x in g["widths"]]
+    f = UniformDensityField([p], binders, w[0], n[0], w[1], n[1], w[2], n[2], chi=float(g["chi"]),
+                            vf_limit=float(g["vf_limit"]))
+    pref, intra, xpref = f.prefactor_arrays()
+    np.testing.assert_array_equal(pref, g["pref"])
+    np.testing.assert_array_equal(intra, g["intra"])
+    np.testing.assert_array_equal(xpref, g["xpref"])
+    assert f.vol_bin == pytest.approx(w[0] * w[1] * w[2] / (n[0] * n[1] * n[2]))
+
+
+def test_binder_presets_and_lookup():
+    assert cb.get_by_name("HP1") is cb.hp1
+    assert cb.get_by_name("PRC1") is cb.prc1
+    with pytest.raises(ValueError):
+        cb.get_by_name("nope")
+    t = cb.make_binder_collection(["HP1", cb.prc1])
+    assert len(t) == 2 and t.loc[1, "name"] == "PRC1"
+    assert t.iloc[0].interaction_volume == pytest.approx(4 / 3 * np.pi * 27)
+    assert t.to_dict(orient="records")[0]["sites_per_bead"] == 2
+
+
+def test_amplitude_bounds_and_controllers():
+    p = Chromatin.straight_line_in_x("p", np.full(999, 16.5), binder_names=np.array(["HP1"]))
+    bab, mab = get_amplitude_bounds([p])
+    assert bab.bounds["crank_shaft"] == (30, 150)
+    assert bab.bounds["end_pivot"] == (50, 150)
+    assert bab.bounds["tangent_rotation"] == (1, 1000)
+    assert mab.bounds["slide"] == pytest.approx((0.2 * 16.5, 0.3 * 16.5))
+    cs = all_moves("/tmp", bab.bounds, mab.bounds, SimpleControl)
+    assert [c.move.num_per_cycle for c in cs] == [30, 1, 60, 60, 10]
+    assert [c.move.name for c in cs] == ["crank_shaft", "end_pivot", "slide", "tangent_rotation",
+                                         "change_binding_state"]
+    assert cs[0].move.amp_bead == 30 and cs[0].move.amp_move == pytest.approx(0.1 * np.pi)
+
+
+def test_simple_control_rule_on_host():
+    p = Chromatin.straight_line_in_x("p", np.full(99, 16.5), binder_names=np.array(["HP1"]))
+    bab, mab = get_amplitude_bounds([p])
+    c = all_moves("/tmp", bab.bounds, mab.bounds, SimpleControl)[2]
+    c.move.acceptance_tracker.acceptance_rate = 0.9
+    a0 = c.move.amp_move
+    c.update_amplitudes()
+    assert c.move.amp_move == pytest.approx(a0 / 0.95)
+    c.move.acceptance_tracker.acceptance_rate = 0.1
+    c.move.amp_move = mab.bounds["slide"][0] * 1.01
+    c.update_amplitudes()
+    assert c.move.amp_bead == max(bab.bounds["slide"][0], 10 - 1)
+    assert c.move.amp_move == pytest.approx(mab.bounds["slide"][1])
+
+
+def test_null_field_membership():
+    p = Chromatin.straight_line_in_x("p", np.full(9, 16.5), binder_names=np.array(["HP1"]))
+    f = NullField([p], confine_type="Spherical", confine_length=100.0)
+    assert p in f
+    assert Chromatin.straight_line_in_x("q", np.full(9, 16.5), binder_names=np.array(["HP1"])) not in f
+    with pytest.raises(ValueError):
+        NullField([p], confine_type="Tetrahedral")

@@ -1,0 +1,175 @@
+// cg_move.cuh -- per-move building blocks shared by the MC kernels: the
+// per-warp voxel hash (int64 fixed-point density deltas), the field dE over
+// the touched voxels, commit of the touched voxels, confinement counts and
+// the binding free-energy lookup.
+#pragma once
+#include "cg_device.cuh"
+#include "cg_kernels.h"
+
+namespace cg {
+
+// ---------------------------------------------------------------- hash insert
+__device__ __forceinline__ int hash_slot(int* keys, int* used, int* nused, int logH, int key,
+                                         unsigned& err) {
+  unsigned mask = (1u << logH) - 1u;
+  unsigned h = ((unsigned)key * 0x9E3779B1u) >> (32 - logH);
+  for (int it = 0; it <= (int)mask; it++) {
+    int prev = atomicCAS(&keys[h], -1, key);
+    if (prev == -1) {
+      int idx = atomicAdd(nused, 1);
+      used[idx] = (int)h;
+      return (int)h;
+    }
+    if (prev == key) return (int)h;
+    h = (h + 1) & mask;
+  }
+  err |= E_SPIN;
+  return -1;
+}
+
+__device__ __forceinline__ void add_delta(long long* vals, int ncol, int slot, int col, long long d) {
+  if (d != 0) atomicAdd((unsigned long long*)&vals[(long long)slot * ncol + col], (unsigned long long)d);
+}
+
+// Deposit +/- one bead's eight trilinear weights with binder states `st`
+// (packed int8) into the hash.
+template <typename Real>
+__device__ __forceinline__ void deposit_bead(const RepDev& rd, int ncol, int* keys, int* used,
+                                             int* nused, long long* vals, int logH,
+                                             const Real w[8], const int v[8], unsigned st,
+                                             bool negate, unsigned& err) {
+#pragma unroll
+  for (int l = 0; l < 8; l++) {
+    long long q = q40(w[l]);
+    if (negate) q = -q;
+    int slot = hash_slot(keys, used, nused, logH, v[l], err);
+    if (slot < 0) return;
+    add_delta(vals, ncol, slot, 0, q);
+    for (int b = 0; b < rd.nb; b++) add_delta(vals, ncol, slot, 1 + b, q * (long long)((st >> (8 * b)) & 0xFF));
+  }
+}
+
+// chi term of one voxel in FP64 (fields.pyx:1792-1875 with the vf_limit branch)
+__device__ __forceinline__ double chi_term64(const RepDev& rd, double V, long long g0, long long d0) {
+  double vf0 = ((double)g0 * kFxInv) / V * rd.bead_vol;
+  double vf1 = ((double)(g0 + d0) * kFxInv) / V * rd.bead_vol;
+  double k = rd.chi * (V / rd.bead_vol);
+  if (vf1 > rd.vf_limit || vf0 > rd.vf_limit)
+    return (vf1 > rd.vf_limit ? kEHugeField * vf1 : k * vf1 * vf1)
+         - (vf0 > rd.vf_limit ? kEHugeField * vf0 : k * vf0 * vf0);
+  return k * ((vf1 - vf0) * (vf1 + vf0));
+}
+
+// Field dE over the touched voxels (fixed-point grid), FP64 arithmetic; also
+// stores the post-move grid values into the hash values for the commit.
+__device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int ncol, const int* keys,
+                                  const int* used, long long* vals, int nused, int lane,
+                                  long long& n_vox, double) {
+  const RepDev& rd = ws.rd;
+  double part = 0;
+  const long long* grid = a.grid + rd.vox_off * ncol;
+  for (int i = lane; i < nused; i += 32) {
+    int slot = used[i];
+    int v = keys[slot];
+    long long* d = vals + (long long)slot * ncol;
+    const long long* gv = grid + (long long)v * ncol;
+    long long g0 = gv[0], d0 = d[0];
+    double V = rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin;
+    double c = 0, rho[CG_MAX_BINDERS], dd[CG_MAX_BINDERS];
+    for (int b = 0; b < rd.nb; b++) {
+      long long gb = gv[1 + b], db = d[1 + b];
+      rho[b] = ((double)gb * kFxInv) / V;
+      dd[b] = ((double)db * kFxInv) / V;
+      c += rd.pref[b] * (dd[b] * (2 * rho[b] + dd[b]));
+      d[1 + b] = gb + db;
+    }
+    for (int b = 0; b < rd.nb; b++)
+      for (int e = 0; e < rd.nb; e++)
+        c += rd.xpref[b * CG_MAX_BINDERS + e] * (rho[b] * dd[e] + dd[b] * rho[e] + dd[b] * dd[e]);
+    c += chi_term64(rd, V, g0, d0);
+    d[0] = g0 + d0;
+    part += c;
+  }
+  n_vox = nused;
+  return warp_sum(part);
+}
+
+// FP32 arithmetic per voxel, FP64 accumulation; voxels at or near the volume
+// fraction limit take the FP64 branch so the 1e99 penalty is decided as in FP64.
+__device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int ncol, const int* keys,
+                                  const int* used, long long* vals, int nused, int lane,
+                                  long long& n_vox, float) {
+  const RepDev& rd = ws.rd;
+  double part = 0;
+  const long long* grid = a.grid + rd.vox_off * ncol;
+  for (int i = lane; i < nused; i += 32) {
+    int slot = used[i];
+    int v = keys[slot];
+    long long* d = vals + (long long)slot * ncol;
+    const long long* gv = grid + (long long)v * ncol;
+    long long g0 = gv[0], d0 = d[0];
+    float sc = ws.f_scale, k = ws.f_k;
+    double V = rd.vol_bin;
+    if (rd.has_access) {
+      V = a.access_vol[rd.vox_off + v];
+      sc = (float)(kFxInv / V);
+      k = (float)(rd.chi * (V / rd.bead_vol));
+    }
+    float c = 0, rho[CG_MAX_BINDERS], dd[CG_MAX_BINDERS];
+    for (int b = 0; b < rd.nb; b++) {
+      long long gb = gv[1 + b], db = d[1 + b];
+      rho[b] = (float)gb * sc;
+      dd[b] = (float)db * sc;
+      c += ws.f_pref[b] * (dd[b] * (2.0f * rho[b] + dd[b]));
+      d[1 + b] = gb + db;
+    }
+    for (int b = 0; b < rd.nb; b++)
+      for (int e = 0; e < rd.nb; e++)
+        c += ws.f_xpref[b * CG_MAX_BINDERS + e] * (rho[b] * dd[e] + dd[b] * rho[e] + dd[b] * dd[e]);
+    float vf0 = (float)g0 * sc * ws.f_vb;
+    float dvf = (float)d0 * sc * ws.f_vb;
+    if (vf0 > ws.f_lim - 1e-3f || vf0 + dvf > ws.f_lim - 1e-3f) {
+      part += (double)c + chi_term64(rd, V, g0, d0);
+    } else {
+      part += (double)(c + k * (dvf * (2.0f * vf0 + dvf)));
+    }
+    d[0] = g0 + d0;
+  }
+  n_vox = nused;
+  return warp_sum(part);
+}
+
+__device__ __forceinline__ void commit_grid(const RepDev& rd, const KArgs& a, int ncol, int* keys,
+                                            const int* used, long long* vals, int nused, int lane,
+                                            bool accept) {
+  long long* grid = a.grid + rd.vox_off * ncol;
+  for (int i = lane; i < nused; i += 32) {
+    int slot = used[i];
+    if (accept) {
+      int v = keys[slot];
+      for (int c = 0; c < ncol; c++) grid[(long long)v * ncol + c] = vals[(long long)slot * ncol + c];
+    }
+    keys[slot] = -1;
+    for (int c = 0; c < ncol; c++) vals[(long long)slot * ncol + c] = 0;
+  }
+}
+
+// confinement count of one position (chromo/fields.pyx:121-202)
+template <typename Real>
+__device__ __forceinline__ int out_of_bounds(const RepDev& rd, const Real q[3], bool trial) {
+  const double p[3] = {(double)q[0], (double)q[1], (double)q[2]};
+  if (rd.confine_kind == 1)
+    return sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]) > rd.confine_length ? 1 : 0;
+  if (rd.confine_kind == 2 && trial) {
+    int o = 0;
+    for (int j = 0; j < 3; j++) o += fabs(p[j]) > rd.confine_length / 2 ? 1 : 0;
+    return o;
+  }
+  return 0;
+}
+
+__device__ __forceinline__ double bind_f(const RepDev& rd, int b, int nm, int s) {
+  return rd.bind_f[(b * (CG_MAX_MARK + 1) + nm) * (CG_MAX_MARK + 1) + s];
+}
+
+}  // namespace cg

@@ -62,7 +62,7 @@ struct cg_sim {
   double* bonds = nullptr;
   long long* grid = nullptr;
   double* access_vol = nullptr;
-  int *g_keys = nullptr, *g_used = nullptr;
+  int *g_keys = nullptr, *g_used = nullptr, *g_bslot = nullptr;
   long long* g_vals = nullptr;
   int g_logH = 0;
   void* g_stage = nullptr;
@@ -75,8 +75,11 @@ struct cg_sim {
   int* rep_of_rung = nullptr;
   unsigned long long *swaps = nullptr, *swap_attempts = nullptr, *xround = nullptr;
   // shared-memory layout
-  int logH = 0, warp_smem = 0, off_keys = 0, off_used = 0, off_vals = 0, off_stage = 0, off_idx = 0;
+  int logH = 0, warp_smem = 0, off_keys = 0, off_used = 0, off_bslot = 0, off_vals = 0, off_stage = 0,
+      off_idx = 0;
+  int spec_w = 1, spec_logHB = 11, spec_off_bkeys = 0, spec_off_bmask = 0, spec_off_warps = 0;
   long long stage_cap = 0;
+  size_t spec_bytes = 0;
   // captured batched graph
   cudaGraphExec_t graph = nullptr;
   long long graph_rounds = -1, graph_steps = -1;
@@ -106,23 +109,27 @@ struct cg_sim {
     a.reps = reps; a.ctl = ctl; a.n_ctl = n_ctl; a.n_reps = R; a.tally = tally;
     a.r4 = r4; a.t34 = t34; a.t24 = t24; a.states = states; a.marks = marks; a.bonds = bonds;
     a.grid = grid; a.access_vol = access_vol; a.ncol = ncol;
-    a.g_keys = g_keys; a.g_used = g_used; a.g_vals = g_vals; a.g_logH = g_logH;
+    a.g_keys = g_keys; a.g_used = g_used; a.g_bslot = g_bslot; a.g_vals = g_vals; a.g_logH = g_logH;
     a.g_stage = g_stage; a.g_idx = g_idx; a.g_stage_cap = g_stage_cap;
     a.picked = picked; a.picked_off = d_picked_off;
     a.wpb = wpb; a.logH = logH; a.stage_cap = stage_cap; a.warp_smem = warp_smem;
     a.off_keys = off_keys; a.off_used = off_used; a.off_vals = off_vals; a.off_stage = off_stage;
-    a.off_idx = off_idx;
+    a.off_idx = off_idx; a.off_bslot = off_bslot;
+    a.spec_w = spec_w; a.spec_logHB = spec_logHB; a.spec_off_bkeys = spec_off_bkeys;
+    a.spec_off_bmask = spec_off_bmask; a.spec_off_warps = spec_off_warps;
     a.rep_of_rung = rep_of_rung; a.swaps = swaps; a.swap_attempts = swap_attempts;
     a.xround = xround;
     return a;
   }
 
-  // Shared-memory layout for hash capacity 2^lh and staging capacity sc.
+  // Per-warp region for hash capacity 2^lh and staging capacity sc (offsets
+  // within the region); returns the region size.
   int layout(int lh, long long sc) {
     size_t H = size_t(1) << lh;
-    size_t o = align16(sizeof(cg::WarpShared));
+    size_t o = 0;
     off_keys = (int)o; o += 4 * H;
     off_used = (int)o; o += 4 * H;
+    off_bslot = (int)o; o += 4 * H;
     o = align16(o);
     off_vals = (int)o; o += 8 * H * ncol;
     off_stage = (int)o; o += sc * 9 * scal_bytes();
@@ -131,6 +138,17 @@ struct cg_sim {
     o = align16(o);
     logH = lh; stage_cap = sc; warp_smem = (int)o;
     return warp_smem;
+  }
+  // CTA layout: header, block voxel table (2^lhb entries), W warp regions.
+  size_t cta_layout(int lhb, int W) {
+    size_t o = align16(sizeof(cg::SpecShared));
+    spec_off_bkeys = (int)o; o += 4 * (size_t(1) << lhb);
+    spec_off_bmask = (int)o; o += 4 * (size_t(1) << lhb);
+    o = align16(o);
+    spec_off_warps = (int)o;
+    spec_logHB = lhb;
+    spec_w = W;
+    return o + (size_t)W * warp_smem;
   }
 };
 
@@ -156,7 +174,7 @@ void cg_destroy(cg_sim* s) {
   if (s->graph) cudaGraphExecDestroy(s->graph);
   if (s->pinned) cudaFreeHost(s->pinned);
   void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
-                  s->grid, s->access_vol, s->g_keys, s->g_used, s->g_vals, s->g_stage, s->g_idx,
+                  s->grid, s->access_vol, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
                   s->picked, s->d_picked_off, s->eout, s->aout, s->rep_of_rung, s->swaps,
                   s->swap_attempts, s->xround};
   for (void* p : ptrs)
@@ -164,22 +182,29 @@ void cg_destroy(cg_sim* s) {
   delete s;
 }
 
-static int choose_shape(cg_sim* s, int wpb_req) {
-  // Replicas are independent warps; pack enough of them per SM that all are
-  // resident at once, and give each the largest hash that then fits.
-  const int smem_per_sm = 227 * 1024;
-  long long warps_per_sm = (s->R + s->n_sm - 1) / std::max(1, s->n_sm);
-  if (warps_per_sm < 1) warps_per_sm = 1;
-  int wpb = wpb_req > 0 ? wpb_req : 1;
-  if (wpb > 4) wpb = 4;
-  long long per_warp = smem_per_sm / std::max<long long>(warps_per_sm, wpb) - 1024;
-  if (per_warp * wpb > 200 * 1024) per_warp = 200 * 1024 / wpb;
-  const long long sc = 192;
+static int choose_shape(cg_sim* s, int w_req) {
+  // One CTA per replica with W warps (moves in flight).  Enough CTAs must be
+  // resident per SM for every replica to run at once; each warp region gets
+  // the largest voxel hash that then fits.
+  const size_t smem_per_sm = 227 * 1024;
+  long long ctas_per_sm = (s->R + s->n_sm - 1) / std::max(1, s->n_sm);
+  if (ctas_per_sm < 1) ctas_per_sm = 1;
+  int W = w_req > 0 ? w_req : (s->R <= s->n_sm ? 8 : 4);
+  if (W > cg::kMaxW) W = cg::kMaxW;
+  s->spec_w = W;
+  const size_t budget = std::min<size_t>(smem_per_sm / ctas_per_sm - 1024, 220 * 1024);
+  const int lhb = 11;
+  const long long sc = 96;
   int lh = 12;
-  while (lh > 6 && s->layout(lh, sc) > per_warp) lh--;
+  for (; lh > 6; lh--) {
+    s->layout(lh, sc);
+    if (s->cta_layout(lhb, W) <= budget) break;
+  }
   s->layout(lh, sc);
-  s->wpb = wpb;
-  cudaError_t e = cg_set_mc_smem(s->fp64 != 0, s->warp_smem * wpb);
+  s->spec_bytes = s->cta_layout(lhb, W);
+  s->wpb = 1;
+  cudaError_t e = cg_set_spec_smem(s->fp64 != 0, (int)s->spec_bytes);
+  if (e == cudaSuccess) e = cg_set_mc_smem(s->fp64 != 0, (int)(s->spec_off_warps + s->warp_smem));
   if (e != cudaSuccess) return fail(CG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
   return CG_OK;
 }
@@ -221,6 +246,17 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   s->g_logH = next_log2(32 * s->max_segment);
   s->g_stage_cap = std::max(s->max_segment, s->max_tangent);
   const long long Hg = 1LL << s->g_logH;
+  {
+    int W = cfg->warps_per_block > 0 ? cfg->warps_per_block : (s->R <= s->n_sm ? 8 : 4);
+    s->spec_w = W > cg::kMaxW ? cg::kMaxW : W;
+  }
+  const long long RW = (long long)s->R * s->spec_w;
+  // tangent-rotation bitmaps: one per (replica, warp)
+  s->total_picked = 0;
+  for (int r = 0; r < s->R; r++) {
+    s->picked_off[r] = s->total_picked;
+    s->total_picked += (long long)s->spec_w * ((s->n_beads[r] + 31) / 32);
+  }
   auto M = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes == 0 ? 16 : bytes); };
   cudaError_t e = cudaSuccess;
 #define ALLOC(ptr, bytes) if (e == cudaSuccess) e = M((void**)&(ptr), (bytes))
@@ -235,11 +271,12 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   ALLOC(s->bonds, 6 * 8 * s->total_beads);
   ALLOC(s->grid, 8 * s->ncol * s->total_vox);
   if (s->nonuniform) ALLOC(s->access_vol, 8 * s->total_vox);
-  ALLOC(s->g_keys, 4 * Hg * s->R);
-  ALLOC(s->g_used, 4 * Hg * s->R);
-  ALLOC(s->g_vals, 8 * Hg * s->ncol * s->R);
-  ALLOC(s->g_stage, s->scal_bytes() * 9 * s->g_stage_cap * s->R);
-  ALLOC(s->g_idx, 4 * s->g_stage_cap * s->R);
+  ALLOC(s->g_keys, 4 * Hg * RW);
+  ALLOC(s->g_used, 4 * Hg * RW);
+  ALLOC(s->g_bslot, 4 * Hg * RW);
+  ALLOC(s->g_vals, 8 * Hg * s->ncol * RW);
+  ALLOC(s->g_stage, s->scal_bytes() * 9 * s->g_stage_cap * RW);
+  ALLOC(s->g_idx, 4 * s->g_stage_cap * RW);
   ALLOC(s->picked, 4 * s->total_picked);
   ALLOC(s->d_picked_off, 8 * s->R);
   ALLOC(s->eout, 8 * 5 * s->R);
@@ -263,8 +300,9 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   cudaMemset(s->marks, 0, 4 * s->total_beads);
   cudaMemset(s->bonds, 0, 48 * s->total_beads);
   cudaMemset(s->grid, 0, 8 * s->ncol * s->total_vox);
-  cudaMemset(s->g_keys, 0xFF, 4 * Hg * s->R);
-  cudaMemset(s->g_vals, 0, 8 * Hg * s->ncol * s->R);
+  cudaMemset(s->g_keys, 0xFF, 4 * Hg * RW);
+  cudaMemset(s->g_bslot, 0xFF, 4 * Hg * RW);
+  cudaMemset(s->g_vals, 0, 8 * Hg * s->ncol * RW);
   cudaMemset(s->picked, 0, 4 * s->total_picked);
   cudaMemset(s->swaps, 0, 8 * s->R);
   cudaMemset(s->swap_attempts, 0, 8 * s->R);
@@ -491,8 +529,10 @@ static int device_errors(cg_sim* s) {
   for (int r = 0; r < s->R; r++) rd[r].err = 0;
   cudaMemcpy(s->reps, rd.data(), sizeof(RepDev) * s->R, cudaMemcpyHostToDevice);
   const long long Hg = 1LL << s->g_logH;
-  cudaMemset(s->g_keys, 0xFF, 4 * Hg * s->R);
-  cudaMemset(s->g_vals, 0, 8 * Hg * s->ncol * s->R);
+  const long long RW = (long long)s->R * s->spec_w;
+  cudaMemset(s->g_keys, 0xFF, 4 * Hg * RW);
+  cudaMemset(s->g_bslot, 0xFF, 4 * Hg * RW);
+  cudaMemset(s->g_vals, 0, 8 * Hg * s->ncol * RW);
   cudaMemset(s->picked, 0, 4 * s->total_picked);
   char msg[160];
   snprintf(msg, sizeof msg, "device error bits 0x%x (first at replica %d)", any, first);
@@ -509,7 +549,7 @@ int cg_run(cg_sim* s, int64_t n_steps, uint64_t seed, void* stream) {
   KArgs a = s->args();
   a.n_steps = n_steps;
   a.seed = seed;
-  cg_launch_mc(a, s->fp64, false, (cudaStream_t)stream);
+  cg_launch_spec(a, s->fp64, s->spec_bytes, (cudaStream_t)stream);
   s->kernels++;
   CUDA_TRY(cudaGetLastError());
   return CG_OK;
@@ -638,7 +678,7 @@ int cg_run_batched(cg_sim* s, int64_t n_rounds, int64_t n_steps, int32_t n_rungs
       KArgs a = s->args();
       a.n_steps = n_steps;
       a.seed = seed;
-      cg_launch_mc(a, s->fp64, false, cap);
+      cg_launch_spec(a, s->fp64, s->spec_bytes, cap);
       if (n_rungs) enqueue_exchange(s, n_rungs, -1, seed, cap);
     }
     cudaError_t e = cudaStreamEndCapture(cap, &gr);
@@ -657,7 +697,7 @@ int cg_run_batched(cg_sim* s, int64_t n_rounds, int64_t n_steps, int32_t n_rungs
 
 int cg_get_launch_info(cg_sim* s, int32_t* wpb, int32_t* hash_slots, int64_t* kernels) {
   if (!s) return fail(CG_ERR_ARG, "null sim");
-  if (wpb) *wpb = s->wpb;
+  if (wpb) *wpb = s->spec_w;
   if (hash_slots) *hash_slots = 1 << s->logH;
   if (kernels) *kernels = s->kernels;
   return CG_OK;

@@ -22,6 +22,29 @@ struct WarpShared {
   int pad[3];
 };
 
+constexpr int kMaxW = 8;
+
+// Outcome of one speculatively evaluated move.
+struct MovePlan {
+  int kind, m, ind0, indf;
+  int empty, err, regfail, dec;
+  unsigned cmask;
+  int nvox, gtab, gstage, bsel, pad;
+  double dE;
+};
+
+// Shared-memory header of one replica's CTA.
+struct SpecShared {
+  WarpShared ws;
+  MovePlan plan[kMaxW];
+  int nused[kMaxW];
+  unsigned long long t0;   // move counter (selects each move's random sub-stream)
+  double run_dE;
+  int cut, stop;
+  unsigned accmask;
+  int pad;
+};
+
 struct KArgs {
   RepDev* reps;
   cg_move_ctl* ctl;
@@ -39,6 +62,7 @@ struct KArgs {
   // per-replica global scratch for moves too large for shared memory
   int* g_keys;
   int* g_used;
+  int* g_bslot;
   long long* g_vals;
   int g_logH;
   void* g_stage;
@@ -50,7 +74,9 @@ struct KArgs {
   long long n_steps;
   int wpb, logH;
   long long stage_cap;
-  int warp_smem, off_keys, off_used, off_vals, off_stage, off_idx;
+  int warp_smem, off_keys, off_used, off_bslot, off_vals, off_stage, off_idx;
+  // multi-warp layout: header, block voxel table, then one region per warp
+  int spec_w, spec_logHB, spec_off_bkeys, spec_off_bmask, spec_off_warps;
   unsigned long long seed;
   // audit mode
   int audit_rep;
@@ -71,6 +97,8 @@ struct KArgs {
 }  // namespace cg
 
 void cg_launch_mc(const cg::KArgs& a, bool fp64, bool audit, cudaStream_t s);
+void cg_launch_spec(const cg::KArgs& a, bool fp64, size_t smem_bytes, cudaStream_t s);
+cudaError_t cg_set_spec_smem(bool fp64, int bytes);
 cudaError_t cg_set_mc_smem(bool fp64, int bytes);
 void cg_launch_deposit(const cg::KArgs& a, bool fp64, int rep, int n_reps_launch, long long max_beads,
                        cudaStream_t s);

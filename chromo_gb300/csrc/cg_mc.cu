@@ -34,8 +34,8 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
   const int rep = AUDIT ? a.audit_rep : blockIdx.x * a.wpb + warp;
   if (!AUDIT && rep >= a.n_reps) return;
   if (AUDIT && (blockIdx.x != 0 || warp != 0)) return;
-  unsigned char* base = smem + (size_t)warp * a.warp_smem;
-  WarpShared& ws = *reinterpret_cast<WarpShared*>(base);
+  unsigned char* base = smem + a.spec_off_warps + (size_t)warp * a.warp_smem;
+  WarpShared& ws = reinterpret_cast<SpecShared*>(smem)->ws;
   int* s_keys = reinterpret_cast<int*>(base + a.off_keys);
   int* s_used = reinterpret_cast<int*>(base + a.off_used);
   long long* s_vals = reinterpret_cast<long long*>(base + a.off_vals);
@@ -80,11 +80,12 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
   const unsigned* mk = a.marks + rd.bead_off;
   const double* bonds = a.bonds + rd.bead_off * 6;
   // per-replica global scratch (used when a move is too large for shared memory)
-  int* g_keys = a.g_keys + (long long)rep * (1 << a.g_logH);
-  int* g_used = a.g_used + (long long)rep * (1 << a.g_logH);
-  long long* g_vals = a.g_vals + (long long)rep * (1 << a.g_logH) * ncol;
-  Pos* g_stage = reinterpret_cast<Pos*>(a.g_stage) + (long long)rep * a.g_stage_cap * 9;
-  int* g_idx = a.g_idx + (long long)rep * a.g_stage_cap;
+  const long long gi = (long long)rep * a.spec_w;  // the replica's first warp region
+  int* g_keys = a.g_keys + gi * (1 << a.g_logH);
+  int* g_used = a.g_used + gi * (1 << a.g_logH);
+  long long* g_vals = a.g_vals + gi * (1 << a.g_logH) * ncol;
+  Pos* g_stage = reinterpret_cast<Pos*>(a.g_stage) + gi * a.g_stage_cap * 9;
+  int* g_idx = a.g_idx + gi * a.g_stage_cap;
   unsigned* picked = a.picked + a.picked_off[rep];
 
   Rng<AUDIT> g;
@@ -692,7 +693,7 @@ __global__ void exchange_kernel(KArgs a, const double* eout, int n_rungs, long l
 
 template <typename Pos>
 static void launch_mc_t(const KArgs& a, bool audit, int blocks, cudaStream_t s) {
-  const size_t shm = (size_t)a.warp_smem * (audit ? 1 : a.wpb);
+  const size_t shm = (size_t)a.spec_off_warps + (size_t)a.warp_smem * (audit ? 1 : a.wpb);
   const int threads = audit ? 32 : 32 * a.wpb;
   if (audit) mc_kernel<Pos, true><<<1, threads, shm, s>>>(a);
   else mc_kernel<Pos, false><<<blocks, threads, shm, s>>>(a);

@@ -62,7 +62,7 @@ __device__ __forceinline__ double chi_term64(const RepDev& rd, double V, long lo
 
 // Field dE over the touched voxels (fixed-point grid), FP64 arithmetic; also
 // stores the post-move grid values into the hash values for the commit.
-__device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int ncol, const int* keys,
+static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int ncol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
                                   long long& n_vox, double) {
   const RepDev& rd = ws.rd;
@@ -96,7 +96,7 @@ __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int ncol
 
 // FP32 arithmetic per voxel, FP64 accumulation; voxels at or near the volume
 // fraction limit take the FP64 branch so the 1e99 penalty is decided as in FP64.
-__device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int ncol, const int* keys,
+static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int ncol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
                                   long long& n_vox, float) {
   const RepDev& rd = ws.rd;

@@ -203,10 +203,11 @@ def mc_sim_audit(polymers, readerproteins, num_mc_steps, mc_move_controllers, fi
 
 def _energies_of(poly, field=None):
     """(elastic, binding, field-consistent, 0) energies of ``poly`` in FP64 on the GPU."""
+    # a one-off evaluation: positions stay in FP64, as on the host
     if field is None:
-        sim = _device(poly, NullField([]))
+        sim = _device(poly, NullField([]), precision="fp64")
     else:
-        sim = _device(poly, field)
+        sim = _device(poly, field, precision="fp64")
     try:
         return sim.energy(0)
     finally:

@@ -9,6 +9,7 @@
 #include <stdint.h>
 
 #include "../../include/chromo_gb300.h"
+#include "cg_math32.h"
 
 namespace cg {
 
@@ -209,16 +210,19 @@ __device__ __forceinline__ void check_bead_bounds(long long b0, long long b1, lo
 // ---------------------------------------------------------------- geometry
 // chromo/util/linalg.pyx:23-199
 
+// Proposal math.  FP64 storage: the CUDA FP64 functions, as the reference
+// uses libm.  FP32 storage: the deterministic binary32 functions of
+// cg_math32.h, which the host oracle compiles from the same source.
 __device__ __forceinline__ void rsincos(double x, double* sn, double* cs) { sincos(x, sn, cs); }
-__device__ __forceinline__ void rsincos(float x, float* sn, float* cs) { sincosf(x, sn, cs); }
+__device__ __forceinline__ void rsincos(float x, float* sn, float* cs) { cgm_sincosf(x, sn, cs); }
 __device__ __forceinline__ double racos(double x) { return acos(x); }
-__device__ __forceinline__ float racos(float x) { return acosf(x); }
+__device__ __forceinline__ float racos(float x) { return cgm_acosf(x); }
 __device__ __forceinline__ double rsqrt_(double x) { return sqrt(x); }
 __device__ __forceinline__ float rsqrt_(float x) { return sqrtf(x); }
 
 template <typename Real> __device__ __forceinline__ Real uni(unsigned x);
 template <> __device__ __forceinline__ double uni<double>(unsigned x) { return unif(x); }
-template <> __device__ __forceinline__ float uni<float>(unsigned x) { return unif32(x); }
+template <> __device__ __forceinline__ float uni<float>(unsigned x) { return cgm_unif24(x); }
 
 // uniform_sample_unit_sphere from two draws (phi, theta)
 template <typename Real>

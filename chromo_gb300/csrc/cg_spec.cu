@@ -120,9 +120,9 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
   int* nused = &sh.nused[w];
 
   if (kind <= CG_SLIDE) {
-    double Md[3][4];
+    Real Md[3][4];
     if (kind == CG_CRANK_SHAFT) {
-      double ang = c.amp_move * (unif(g.next()) - 0.5);
+      Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
       long long b0 = (int)(unif(g.next()) * (double)N);
       long long b1 = from_point(g, c.amp_bead, N, b0, err);
       if (b1 < 1) b1 = 1;
@@ -135,12 +135,12 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
       else if (indf == N) { ia = indf - 1; ib = ind0 - 1; }
       else { ia = indf; ib = ind0 - 1; }
       if (!err) {
-        double pa[3], pb[3], dir[3], p[3];
+        Real pa[3], pb[3], dir[3], p[3];
         ld3(r4, ia, pa); ld3(r4, ib, pb);
         for (int i = 0; i < 3; i++) dir[i] = pa[i] - pb[i];
-        double mag = sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
-        if (mag < 1E-5) sphere<double>(g, dir);
-        else { double sc = 1.0 / mag; for (int i = 0; i < 3; i++) dir[i] = dir[i] * sc; }
+        Real mag = rsqrt_(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+        if (mag < (Real)1E-5) sphere<Real>(g, dir);
+        else { Real sc = (Real)1 / mag; for (int i = 0; i < 3; i++) dir[i] = dir[i] * sc; }
         long long ip;
         if (ind0 == 0 && indf != N) ip = indf;
         else if (ind0 != 0 && indf == N) ip = ind0 - 1;
@@ -150,12 +150,12 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
         axis_rotation(dir, p, ang, Md);
       }
     } else if (kind == CG_END_PIVOT) {
-      double ang = c.amp_move * (unif(g.next()) - 0.5);
+      Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
       long long lhs = g.next() & 1u;
       if (lhs == 1) { ind0 = 0; indf = from_left(g, c.amp_bead, N, err) + 1; }
       else { ind0 = N - from_left(g, c.amp_bead, N, err); indf = N; }
-      double axis[3], p[3];
-      sphere<double>(g, axis);
+      Real axis[3], p[3];
+      sphere<Real>(g, axis);
       long long ip;
       if (ind0 == 0 && indf != N) ip = indf;
       else if (ind0 != 0 && indf == N) ip = ind0 - 1;
@@ -166,10 +166,10 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
         axis_rotation(axis, p, ang, Md);
       }
     } else {
-      double amp = c.amp_move * unif(g.next()), d[3];
-      sphere<double>(g, d);
+      Real amp = (Real)c.amp_move * uni<Real>(g.next()), d[3];
+      sphere<Real>(g, d);
       for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) Md[i][j] = i == j ? 1.0 : 0.0;
+        for (int j = 0; j < 3; j++) Md[i][j] = i == j ? (Real)1 : (Real)0;
       for (int i = 0; i < 3; i++) Md[i][3] = d[i] * amp;
       long long b0 = g.next() % (unsigned)N;
       long long b1 = from_point(g, c.amp_bead, N, b0, err);
@@ -238,7 +238,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
       if (density) dEf += field_dE_voxels(ws, a, ncol, S.keys, S.used, S.vals, *nused, lane, nvox, (Real)0);
     }
   } else if (kind == CG_TANGENT_ROTATION) {
-    double ang = c.amp_move * (unif(g.next()) - 0.5);
+    Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
     long long n = (long long)(g.next() % (unsigned)c.amp_bead) + 1;
     if (n > N) err |= E_WINDOW;
     m = err ? 0 : n;
@@ -279,16 +279,16 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
       const unsigned long long axis_base = g.pos;
       Pos* stage = reinterpret_cast<Pos*>(S.stage);
       double part = 0;
-      double sa, ca;
+      Real sa, ca;
       rsincos(ang, &sa, &ca);
       for (long long k = lane; k < m; k += 32) {
         const long long i = idx[k];
         bool ok1, ok2;
         unsigned xa = g.at(axis_base + 2 * k, ok1), xb = g.at(axis_base + 2 * k + 1, ok2);
-        double axis[3];
-        sphere_from<double>(xa, xb, axis);
-        const double origin[3] = {0, 0, 0};
-        double Md[3][4];
+        Real axis[3];
+        sphere_from<Real>(xa, xb, axis);
+        const Real origin[3] = {0, 0, 0};
+        Real Md[3][4];
         axis_rotation_sc(axis, origin, sa, ca, Md);
         Real M[3][4];
         for (int ii = 0; ii < 3; ii++)

@@ -41,6 +41,10 @@
  */
 #include <math.h>
 #include <stdint.h>
+
+/* Deterministic binary32 sin / cos / acos shared with the GPU's FP32-storage
+ * path (same source, so the emulation below is bit-identical to it). */
+#include "../chromo_gb300/csrc/cg_math32.h"
 #include <stdlib.h>
 #include <string.h>
 
@@ -239,6 +243,46 @@ static void axis_rotation(const double a[3], const double p[3], double ang, doub
     M[0][3] += (p[0] * (1 - a0) - a[0] * (p[1] * a[1] + p[2] * a[2])) * oc;
     M[1][3] += (p[1] * (1 - a1) - a[1] * (p[0] * a[0] + p[2] * a[2])) * oc;
     M[2][3] += (p[2] * (1 - a2) - a[2] * (p[0] * a[0] + p[1] * a[1])) * oc;
+}
+
+/* FP32-storage proposal math, as on the GPU */
+static void sphere_f32(or_rng *g, double v[3])
+{
+    unsigned xa = (unsigned)rnd(g), xb = (unsigned)rnd(g);
+    float phi = cgm_unif24(xa) * 6.2831855f;
+    float theta = cgm_acosf(cgm_unif24(xb) * 2.0f - 1.0f);
+    float sp, cp, st, ct;
+    cgm_sincosf(phi, &sp, &cp);
+    cgm_sincosf(theta, &st, &ct);
+    v[0] = (double)(cp * st);
+    v[1] = (double)(sp * st);
+    v[2] = (double)ct;
+}
+
+/* axis rotation in binary32 with the GPU's operation order; the result is
+ * returned widened (exactly) to double */
+static void axis_rotation_f32(const double ad[3], const double pd[3], float s, float c, double M[3][4])
+{
+    float a[3] = {(float)ad[0], (float)ad[1], (float)ad[2]};
+    float p[3] = {(float)pd[0], (float)pd[1], (float)pd[2]};
+    float oc = 1 - c, a0 = a[0] * a[0], a1 = a[1] * a[1], a2 = a[2] * a[2], m[3][4];
+    m[0][0] = a0 + (a1 + a2) * c;
+    m[0][1] = a[0] * a[1] * oc - a[2] * s;
+    m[0][2] = a[0] * a[2] * oc + a[1] * s;
+    m[1][0] = a[0] * a[1] * oc + a[2] * s;
+    m[1][1] = a1 + (a0 + a2) * c;
+    m[1][2] = a[1] * a[2] * oc - a[0] * s;
+    m[2][0] = a[0] * a[2] * oc - a[1] * s;
+    m[2][1] = a[1] * a[2] * oc + a[0] * s;
+    m[2][2] = a2 + (a0 + a1) * c;
+    m[0][3] = (p[1] * a[2] - p[2] * a[1]) * s;
+    m[1][3] = (p[2] * a[0] - p[0] * a[2]) * s;
+    m[2][3] = (p[0] * a[1] - p[1] * a[0]) * s;
+    m[0][3] += (p[0] * (1 - a0) - a[0] * (p[1] * a[1] + p[2] * a[2])) * oc;
+    m[1][3] += (p[1] * (1 - a1) - a[1] * (p[0] * a[0] + p[2] * a[2])) * oc;
+    m[2][3] += (p[2] * (1 - a2) - a[2] * (p[0] * a[0] + p[1] * a[1])) * oc;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 4; j++) M[i][j] = (double)m[i][j];
 }
 
 /* ---------------- helpers ------------------------------------------------ */
@@ -898,6 +942,14 @@ static void rot_axis_crank(const or_system *s, or_rng *g, int64_t ind0, int64_t 
     else if (ind0 == 0) { ld3(s->r, indf, a); ld3(s->r, ind0, b); }
     else if (indf == N) { ld3(s->r, indf - 1, a); ld3(s->r, ind0 - 1, b); }
     else { ld3(s->r, indf, a); ld3(s->r, ind0 - 1, b); }
+    if (emu32(s)) {
+        float d[3] = {(float)a[0] - (float)b[0], (float)a[1] - (float)b[1], (float)a[2] - (float)b[2]};
+        float mag = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        if (mag < 1E-5f) { sphere_f32(g, dir); return; }
+        float sc = 1.0f / mag;
+        for (int i = 0; i < 3; i++) dir[i] = (double)(d[i] * sc);
+        return;
+    }
     for (int i = 0; i < 3; i++) dir[i] = a[i] - b[i];
     int rp = !s->fixed_density;
     double mag = sqrt(sq(dir[0], rp) + sq(dir[1], rp) + sq(dir[2], rp));
@@ -942,7 +994,9 @@ static int64_t mc_step(or_system *s, or_ctl *c, or_rng *g, or_record *rec)
     if (kind == MV_CRANK || kind == MV_END_PIVOT || kind == MV_SLIDE) {
         double M[3][4];
         if (kind == MV_CRANK) {                 /* move_funcs.pyx:39-101 */
-            double ang = c->amp_move * (rndu(g) - 0.5);
+            int64_t xang = rnd(g);
+            double ang = c->amp_move * ((double)xang / OR_RAND_MAX - 0.5);
+            float angf = (float)c->amp_move * (cgm_unif24((unsigned)xang) - 0.5f);
             int64_t b0 = (int32_t)(rndu(g) * (double)N);
             int64_t b1 = from_point(g, c->amp_bead, N, b0);
             if (b1 < 1) b1 = 1;
@@ -950,20 +1004,38 @@ static int64_t mc_step(or_system *s, or_ctl *c, or_rng *g, or_record *rec)
             double dir[3], p[3];
             rot_axis_crank(s, g, ind0, indf, dir);
             crank_fulcrum(s, ind0, indf, p);
-            axis_rotation(dir, p, ang, M, !s->fixed_density);
+            if (emu32(s)) {
+                float sn, cs;
+                cgm_sincosf(angf, &sn, &cs);
+                axis_rotation_f32(dir, p, sn, cs, M);
+            } else axis_rotation(dir, p, ang, M, !s->fixed_density);
         } else if (kind == MV_END_PIVOT) {      /* move_funcs.pyx:285-346 */
-            double ang = c->amp_move * (rndu(g) - 0.5);
+            int64_t xang = rnd(g);
+            double ang = c->amp_move * ((double)xang / OR_RAND_MAX - 0.5);
+            float angf = (float)c->amp_move * (cgm_unif24((unsigned)xang) - 0.5f);
             int64_t lhs = rnd(g) % 2;
             if (lhs == 1) { ind0 = 0; indf = from_left(g, c->amp_bead, N) + 1; }
             else { ind0 = from_right(g, c->amp_bead, N); indf = N; }
             double axis[3], p[3];
-            sphere(g, axis);
+            if (emu32(s)) sphere_f32(g, axis);
+            else sphere(g, axis);
             end_pivot_fulcrum(s, ind0, indf, lhs, p);
-            axis_rotation(axis, p, ang, M, !s->fixed_density);
+            if (emu32(s)) {
+                float sn, cs;
+                cgm_sincosf(angf, &sn, &cs);
+                axis_rotation_f32(axis, p, sn, cs, M);
+            } else axis_rotation(axis, p, ang, M, !s->fixed_density);
         } else {                                /* move_funcs.pyx:403-465 */
-            double amp = c->amp_move * rndu(g), d[3];
-            sphere(g, d);
-            for (int i = 0; i < 3; i++) d[i] = d[i] * amp;
+            int64_t xamp = rnd(g);
+            double amp = c->amp_move * ((double)xamp / OR_RAND_MAX), d[3];
+            if (emu32(s)) {
+                float ampf = (float)c->amp_move * cgm_unif24((unsigned)xamp);
+                sphere_f32(g, d);
+                for (int i = 0; i < 3; i++) d[i] = (double)((float)d[i] * ampf);
+            } else {
+                sphere(g, d);
+                for (int i = 0; i < 3; i++) d[i] = d[i] * amp;
+            }
             memset(M, 0, sizeof(M));
             M[0][0] = M[1][1] = M[2][2] = 1;
             M[0][3] = d[0]; M[1][3] = d[1]; M[2][3] = d[2];
@@ -991,7 +1063,11 @@ static int64_t mc_step(or_system *s, or_ctl *c, or_rng *g, or_record *rec)
         dEp = continuous_dE(s, ind0, indf, s->trial, s->trial + 9 * (n - 1));
         if (check_field) dEf = field_dE(s, n, 0, -1);
     } else if (kind == MV_TANGENT) {            /* move_funcs.pyx:470-582 */
-        double ang = c->amp_move * (rndu(g) - 0.5);
+        int64_t xang = rnd(g);
+        double ang = c->amp_move * ((double)xang / OR_RAND_MAX - 0.5);
+        float angf = (float)c->amp_move * (cgm_unif24((unsigned)xang) - 0.5f);
+        float sang, cang;
+        cgm_sincosf(angf, &sang, &cang);
         n = rnd(g) % c->amp_bead + 1;
         if (n > N) { g->err = OR_ERR_WINDOW; return g->err; }
         for (int64_t k = 0; k < n && !g->err; k++) {
@@ -1006,8 +1082,13 @@ static int64_t mc_step(or_system *s, or_ctl *c, or_rng *g, or_record *rec)
         for (int64_t k = 0; k < n; k++) {      /* rotate_select_beads, :517-549 */
             double axis[3], M[3][4], t3[3], t2[3];
             int64_t i = s->inds[k];
-            sphere(g, axis);
-            axis_rotation(axis, origin, ang, M, !s->fixed_density);
+            if (emu32(s)) {
+                sphere_f32(g, axis);
+                axis_rotation_f32(axis, origin, sang, cang, M);
+            } else {
+                sphere(g, axis);
+                axis_rotation(axis, origin, ang, M, !s->fixed_density);
+            }
             ld3(s->t3, i, t3); ld3(s->t2, i, t2);
             for (int j = 0; j < 3; j++) {
                 if (emu32(s)) {

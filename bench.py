@@ -8,7 +8,7 @@ exchanged along 16-rung ladders.  The round is a captured CUDA graph replayed
 K times.  ``value`` is whole-job attempted moves/s with the state resident in
 HBM; ``e2e`` is the same through the C ABI with host buffers (state uploaded
 from pinned memory and the snapshot read back every step); ``plain`` is one
-10,000-bead chain on the same kernel (one warp); ``roofline`` reports the MC
+10,000-bead chain on the same kernel (one CTA); ``roofline`` reports the MC
 kernel's algorithmic bytes per launch over its CUDA-event duration against
 the measured HBM peak; ``cpu_baseline`` is the reference's own CPU code on
 this host's cores.
@@ -45,14 +45,15 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-budget", type=float, default=2.0)
     ap.add_argument("--profile", action="store_true",
-                    help="small case for ncu: 64 x 5000-bead replicas, 1 warm-up + 2 MC launches")
+                    help="case for ncu: 256 x 5000-bead replicas, 1 warm-up + 2 MC launches")
     return ap.parse_args()
 
 
 def profile_case(args):
-    """A bounded case for profilers: the 64-replica workload (5,000 beads each,
-    40^3 grids, ~130 MB of grids: larger than L2), one warm-up launch and two
-    launches of the MC kernel of 62 steps each."""
+    """A bounded case for profilers: 256 replicas of 5,000 beads each (the
+    batched workload's CTA shape), 40^3 grids of 3 int64 columns (393 MB of
+    grids: larger than L2, under 1 GB on the device), one warm-up launch and
+    two launches of the MC kernel of 62 steps each."""
     import numpy as np
     import torch
     from chromo_gb300.build import build
@@ -196,7 +197,7 @@ def reference_arm(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": res["value"], "unit": "moves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD_DESC if args.workload == "batched" else args.workload,
                    "replicas": int(w.replicas)},
         "cpu_baseline": {"value": res["value"], "unit": "moves/s", "cores": res["cores"],
@@ -302,7 +303,7 @@ def main():
     h2d = nbeads * (3 * pos_b + 4)
     d2h = nbeads * (3 * pos_b + 4)
     e2e_value = allreduce_sum(moves_round * e2e_steps, world) / allreduce_max(t_e2e, world)
-    # ---- plain single chain (one warp) on the same kernel
+    # ---- plain single chain (one CTA) on the same kernel
     wp = wl.make_workload("plain", seed_offset=rank)
     psim = wl.build_sim(wp)
     psim.run(20, 5, sh)
@@ -321,7 +322,7 @@ def main():
         out = {
             "metric": METRIC, "value": value, "unit": "moves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Gaussian-walk chains, Markov mark tracks)",
             "config": {"workload": WORKLOAD_DESC, "replicas": int(w.replicas),
                        "beads_total": nbeads, "mc_steps_per_step": steps_round,
@@ -330,7 +331,7 @@ def main():
                        "graph": "one exchange round captured in a CUDA graph, replayed per step"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "mc_kernel<float,false>", "peak_source": peak_kind,
+                         "kernel": "spec_kernel<float>", "peak_source": peak_kind,
                          "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
                          "moves_per_launch": float(tal2[:, :, 0].sum()) / n_launch},
             "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d,

@@ -97,8 +97,8 @@ def make_workload(name: str, seed_offset: int = 0) -> Workload:
         chi = np.tile(np.linspace(0.5, 2.0, rungs), R // rungs)
         return Workload("batched", lengths, 40, 2, mu, chi, [-4.0, -3.0], [{"PRC1": 1.0}, {}],
                         50, rungs, BASE_SEED + 2 + seed_offset)
-    if name == "diff":
-        R = 64
+    if name == "diff":  # fixed-length chains for profiling; the same CTA shape as "batched"
+        R = 256
         mu = rng.uniform(-1.0, 0.0, size=(R, 2))
         chi = np.tile(np.linspace(0.5, 2.0, 16), R // 16)
         return Workload("diff", np.full(R, 5000), 40, 2, mu, chi, [-4.0, -3.0],

@@ -1,7 +1,7 @@
 """Compile the CUDA library in place (sm_103a only).
 
 ``python -m chromo_gb300.build`` writes ``chromo_gb300/_lib/libchromo_gb300.so``.
-The two translation units are compiled in parallel and linked with nvcc.
+The translation units are compiled in parallel and linked with nvcc.
 Device code is built with ``-fmad=false`` so that every floating-point
 operation is individually rounded, as in the CPU restatement used to check it.
 """
@@ -15,7 +15,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_lib"
 LIB = OUT / "libchromo_gb300.so"
-SOURCES = ["cg_mc.cu", "cg_spec.cu", "cg_capi.cu"]
+SOURCES = ["cg_mc.cu", "cg_spec.cu", "cg_capi.cu", "cg_static.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
          f"-I{PKG.parent / 'include'}"]

@@ -704,3 +704,5 @@ int cg_get_launch_info(cg_sim* s, int32_t* wpb, int32_t* hash_slots, int64_t* ke
 }
 
 }  // extern "C"
+
+int cg::record_error(int code, const std::string& msg) { return fail(code, msg); }

@@ -2,9 +2,14 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "cg_device.cuh"
 
 namespace cg {
+
+// Records msg as the calling thread's cg_last_error() and returns code.
+int record_error(int code, const std::string& msg);
 
 // Per-warp header at the start of the warp's shared-memory region.
 struct WarpShared {

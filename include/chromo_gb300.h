@@ -194,6 +194,31 @@ int cg_run_batched(cg_sim *sim, int64_t n_rounds, int64_t n_steps, int32_t n_run
 int cg_get_launch_info(cg_sim *sim, int32_t *warps_per_block, int32_t *hash_slots,
                        int64_t *kernels_launched);
 
+/* Field energy of one chain, allocating nothing (no counterpart in the
+ * reference).  Deposits the chain into a fixed-point density grid and writes
+ * out[0] = the field energy in the form cg_energy reports in its out[2]
+ * (chromo/fields.pyx:1939-2316, :1675-1875, re-deposit of :2041-2106) and
+ * out[1] = the chi-free sum S = sum_v (V / V_bead) vf^2.  For callers that
+ * must not allocate device memory (a server whose device memory belongs to its
+ * own pool; code in which a cudaMalloc would stall work in flight).
+ *
+ * All array arguments are DEVICE pointers: r [n_beads x 3] FP64, states
+ * [n_beads x n_binders] int64 in 0..3, access_vol [nx*ny*nz] FP64 or NULL for
+ * the uniform voxel volume, out [2] FP64.  field->field_kind must be 2.  The
+ * work is enqueued on `stream` (a cudaStream_t, NULL for the default stream);
+ * read out after synchronising it.
+ *
+ * The grid lives in a static device array of 1,048,576 int64 cells (8 MiB):
+ * nx*ny*nz*(n_binders+1) above that is rejected with CG_ERR_ARG.  Each call
+ * zeroes the cells it uses on `stream` first, so nothing needs to start at
+ * zero.  The first call on each device looks up the array's address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  There is
+ * one array per device: calls that overlap in time on one device (different
+ * streams or host threads) race on it; calls on one stream are ordered. */
+int cg_field_energy_static(const cg_field_params *field, int64_t n_beads, const double *r,
+                           const int64_t *states, const double *access_vol, double *out,
+                           void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -277,11 +277,15 @@ def main():
     bytes_per_launch = wl.algorithmic_bytes(tal2, w.n_binders) / n_launch
     peak, peak_kind = load_peaks()
     achieved = bytes_per_launch / avg_launch_s / 1e9
+    # DRAM bytes per attempted move from the committed ncu capture of the
+    # same kernel (256 x 5,000-bead case), scaled by the moves of one launch
     traffic = None
-    tj = ROOT / "profiles" / "mc_kernel_traffic.json"
-    if tj.exists():
-        d = json.loads(tj.read_text())
-        traffic = d.get("dram_bytes_per_move", 0) * float(tal2[:, :, 0].sum()) / n_launch
+    prof = ROOT / "profiles" / "spec_kernel_256x5000.md"
+    if prof.exists():
+        import re
+        hit = re.search(r"DRAM bytes per attempted move \| ([0-9.]+)", prof.read_text())
+        if hit:
+            traffic = float(hit.group(1)) * float(tal2[:, :, 0].sum()) / n_launch
     # ---- e2e through the C ABI with host buffers
     h2d = d2h = 0
     pos_b = 16

@@ -82,7 +82,7 @@ EXPORTS = [
     "cg_set_binding", "cg_set_controllers", "cg_get_controllers", "cg_deposit", "cg_get_density",
     "cg_run", "cg_sync", "cg_run_audit", "cg_energy", "cg_reset_running_energy", "cg_get_tally",
     "cg_reset_tally", "cg_exchange", "cg_get_chi", "cg_run_batched", "cg_get_launch_info",
-    "cg_field_energy_static",
+    "cg_field_energy_static", "cg_energies",
 ]
 
 
@@ -123,6 +123,7 @@ def lib():
             "cg_run_batched": ([P, I64, I64, I32, C.c_uint64, P], C.c_int),
             "cg_get_launch_info": ([P, P, P, P], C.c_int),
             "cg_field_energy_static": ([C.POINTER(FieldParams), I64, P, P, P, P, P], C.c_int),
+            "cg_energies": ([P, P, P], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -244,6 +245,12 @@ class Sim:
     def energy(self, rep):
         out = np.zeros(4)
         check(lib().cg_energy(self.h, rep, _ptr(out)))
+        return out
+
+    def energies(self, stream=None):
+        """[R, 5]: elastic, binding, field, running sum of accepted dE, chi-free S."""
+        out = np.zeros((self.R, 5))
+        check(lib().cg_energies(self.h, _ptr(out), stream))
         return out
 
     def reset_running_energy(self):

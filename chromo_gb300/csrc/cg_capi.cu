@@ -182,6 +182,15 @@ void cg_destroy(cg_sim* s) {
   delete s;
 }
 
+// Moves in flight per replica: the largest W <= kMaxW for which every
+// replica's CTA is resident at once (ceil(R / SMs) CTAs per SM, W warps each,
+// within the register file).
+static int default_warps(const cg_sim* s) {
+  const long long ctas = (s->R + s->n_sm - 1) / std::max(1, s->n_sm);
+  const long long W = cg_spec_warps_per_sm(s->fp64 != 0) / std::max(1LL, ctas);
+  return (int)std::min<long long>(cg::kMaxW, std::max<long long>(1, W));
+}
+
 static int choose_shape(cg_sim* s, int w_req) {
   // One CTA per replica with W warps (moves in flight).  Enough CTAs must be
   // resident per SM for every replica to run at once; each warp region gets
@@ -189,7 +198,7 @@ static int choose_shape(cg_sim* s, int w_req) {
   const size_t smem_per_sm = 227 * 1024;
   long long ctas_per_sm = (s->R + s->n_sm - 1) / std::max(1, s->n_sm);
   if (ctas_per_sm < 1) ctas_per_sm = 1;
-  int W = w_req > 0 ? w_req : (s->R <= s->n_sm ? 8 : 4);
+  int W = w_req > 0 ? w_req : default_warps(s);
   if (W > cg::kMaxW) W = cg::kMaxW;
   s->spec_w = W;
   const size_t budget = std::min<size_t>(smem_per_sm / ctas_per_sm - 1024, 220 * 1024);
@@ -247,7 +256,7 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   s->g_stage_cap = std::max(s->max_segment, s->max_tangent);
   const long long Hg = 1LL << s->g_logH;
   {
-    int W = cfg->warps_per_block > 0 ? cfg->warps_per_block : (s->R <= s->n_sm ? 8 : 4);
+    int W = cfg->warps_per_block > 0 ? cfg->warps_per_block : default_warps(s);
     s->spec_w = W > cg::kMaxW ? cg::kMaxW : W;
   }
   const long long RW = (long long)s->R * s->spec_w;
@@ -617,6 +626,17 @@ int cg_energy(cg_sim* s, int rep, double* out) {
   return CG_OK;
 }
 
+int cg_energies(cg_sim* s, double* out, void* stream) {
+  if (!s || !out) return fail(CG_ERR_ARG, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  KArgs a = s->args();
+  cg_launch_energy(a, s->fp64, s->eout, st);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(out, s->eout, sizeof(double) * 5 * s->R, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return CG_OK;
+}
+
 int cg_reset_running_energy(cg_sim* s) {
   if (!s) return fail(CG_ERR_ARG, "null sim");
   std::vector<RepDev> rd(s->R);
@@ -640,7 +660,7 @@ int cg_reset_tally(cg_sim* s) {
 
 static int enqueue_exchange(cg_sim* s, int n_rungs, long long round, uint64_t seed, cudaStream_t st) {
   KArgs a = s->args();
-  cg_launch_energy(a, s->fp64, s->eout, st);
+  cg_launch_chi_sum(a, s->eout, st);
   cg_launch_exchange(a, s->eout, n_rungs, round, seed, st);
   return CG_OK;
 }

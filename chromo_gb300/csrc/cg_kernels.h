@@ -108,5 +108,8 @@ cudaError_t cg_set_mc_smem(bool fp64, int bytes);
 void cg_launch_deposit(const cg::KArgs& a, bool fp64, int rep, int n_reps_launch, long long max_beads,
                        cudaStream_t s);
 void cg_launch_energy(const cg::KArgs& a, bool fp64, double* out, cudaStream_t s);
+void cg_launch_chi_sum(const cg::KArgs& a, double* out, cudaStream_t s);
+// warps of the MC kernel that fit one SM's register file
+int cg_spec_warps_per_sm(bool fp64);
 void cg_launch_exchange(const cg::KArgs& a, const double* eout, int n_rungs, long long round,
                         unsigned long long seed, cudaStream_t s);

@@ -651,6 +651,26 @@ __global__ void energy_kernel(KArgs a, double* out) {
   }
 }
 
+// The chi-free sums S_r alone (the input of the exchange): the same per-thread
+// order and block reduction as energy_kernel's out[5 r + 4], so the values are
+// identical, without the elastic, binding and binder-density terms.
+__global__ void chi_sum_kernel(KArgs a, double* out) {
+  __shared__ double sh[32];
+  const int rep = blockIdx.x;
+  const RepDev& rd = a.reps[rep];
+  double sx = 0;
+  if (rd.field_kind == 2) {
+    const long long* grid = a.grid + rd.vox_off * a.ncol;
+    for (long long v = threadIdx.x; v < rd.n_vox; v += blockDim.x) {
+      double V = rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin;
+      double vf = ((double)grid[v * a.ncol] * kFxInv) / V * rd.bead_vol;
+      sx += (V / rd.bead_vol) * vf * vf;
+    }
+  }
+  const double t = block_sum(sx, sh);
+  if (threadIdx.x == 0) out[rep * 5 + 4] = t;
+}
+
 // ---------------------------------------------------------------- replica exchange
 // Swap chi between neighbouring rungs of each ladder (n_rungs consecutive
 // rung slots per ladder).  eout[5 r + 4] holds S_r = sum over voxels of
@@ -730,6 +750,10 @@ void cg_launch_deposit(const cg::KArgs& a, bool fp64, int rep, int n_reps_launch
 void cg_launch_energy(const cg::KArgs& a, bool fp64, double* out, cudaStream_t s) {
   if (fp64) cg::energy_kernel<double><<<a.n_reps, 256, 0, s>>>(a, out);
   else cg::energy_kernel<float><<<a.n_reps, 256, 0, s>>>(a, out);
+}
+
+void cg_launch_chi_sum(const cg::KArgs& a, double* out, cudaStream_t s) {
+  cg::chi_sum_kernel<<<a.n_reps, 256, 0, s>>>(a, out);
 }
 
 void cg_launch_exchange(const cg::KArgs& a, const double* eout, int n_rungs, long long round,

@@ -719,6 +719,15 @@ void cg_launch_spec(const cg::KArgs& a, bool fp64, size_t smem_bytes, cudaStream
   else cg::spec_kernel<float><<<a.n_reps, threads, smem_bytes, s>>>(a);
 }
 
+int cg_spec_warps_per_sm(bool fp64) {
+  cudaFuncAttributes at;
+  cudaError_t e = fp64 ? cudaFuncGetAttributes(&at, cg::spec_kernel<double>)
+                       : cudaFuncGetAttributes(&at, cg::spec_kernel<float>);
+  if (e != cudaSuccess || at.numRegs <= 0) return cg::kMaxW;
+  const int per_warp = (at.numRegs * 32 + 255) / 256 * 256;  // allocation unit: 256 registers
+  return 65536 / per_warp;
+}
+
 cudaError_t cg_set_spec_smem(bool fp64, int bytes) {
   return fp64 ? cg::spec_smem_t<double>(bytes) : cg::spec_smem_t<float>(bytes);
 }

@@ -168,6 +168,13 @@ int cg_run_audit(cg_sim *sim, int32_t rep, int64_t n_steps,
 int cg_energy(cg_sim *sim, int32_t rep, double *out);
 int cg_reset_running_energy(cg_sim *sim);
 
+/* cg_energy for every replica at once: out [n_replicas x 5] = elastic,
+ * binding, field (as cg_energy), running sum of accepted dE, and the chi-free
+ * part S = sum_v (V / V_bead) vf^2 of the field energy (field = chi * S +
+ * terms that do not depend on chi).  Work is enqueued on `stream`; the call
+ * returns once out is filled. */
+int cg_energies(cg_sim *sim, double *out, void *stream);
+
 /* Per-replica, per-move tallies [5 * 6]: attempts, accepts, beads moved,
  * voxels touched, beads moved in accepted moves, voxels touched in accepted
  * moves.  Used for the algorithmic-bytes roofline. */

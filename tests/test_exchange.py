@@ -1,0 +1,142 @@
+"""Replica exchange along chi ladders (new here: the reference runs one chain
+per simulation).
+
+The device's swap decisions are checked against a host restatement of the
+rule: rungs (2i + p, 2i + 1 + p) of each ladder, p = round % 2, swap their chi
+iff u < exp((chi_a - chi_b) (S_a - S_b)), with S_r = sum_v (V / V_bead) vf^2
+from replica r's fixed-point grid and u = (x >> 1) / (2^31 - 1), x the first
+word of Philox4x32-10 at counter (round, rung, 0x3C6EF372) under the seed's
+key.  The host Philox is pinned to the published known-answer vectors."""
+import numpy as np
+import pytest
+
+M0, M1 = 0xD2511F53, 0xCD9E8D57
+W0, W1 = 0x9E3779B9, 0xBB67AE85
+MASK = 0xFFFFFFFF
+
+
+def philox4x32_10(ctr, key):
+    """Philox4x32 with 10 rounds (Salmon et al., SC'11)."""
+    c = [int(x) & MASK for x in ctr]
+    k = [int(x) & MASK for x in key]
+    for _ in range(10):
+        p0, p1 = M0 * c[0], M1 * c[2]
+        c = [(p1 >> 32) ^ c[1] ^ k[0], p1 & MASK, (p0 >> 32) ^ c[3] ^ k[1], p0 & MASK]
+        k = [(k[0] + W0) & MASK, (k[1] + W1) & MASK]
+    return c
+
+
+def test_philox_known_answers():
+    """Known-answer vectors published with the Random123 library."""
+    assert philox4x32_10([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert philox4x32_10([MASK] * 4, [MASK] * 2) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+    assert philox4x32_10([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344],
+                         [0xA4093822, 0x299F31D0]) == [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def exchange_uniform(seed, round_, rung):
+    o = philox4x32_10([round_ & MASK, (round_ >> 32) & MASK, rung, 0x3C6EF372],
+                      [(seed & MASK) ^ 0xA4093822, (seed >> 32) & MASK])
+    return (o[0] >> 1) / 2147483647.0
+
+
+def chi_free_sum(grid, vol_bin, bead_vol):
+    vf = (grid[:, 0].astype(np.float64) * 2.0 ** -40) / vol_bin * bead_vol
+    return float(np.sum((vol_bin / bead_vol) * vf * vf))
+
+
+def expected_exchange(chi, S, rep_of_rung, n_rungs, round_, seed, tie=1e-9):
+    """One exchange round on the host; returns (chi, rep_of_rung, n_swaps, ties)."""
+    chi, ror = chi.copy(), rep_of_rung.copy()
+    parity = round_ & 1
+    swaps = ties = 0
+    for ladder in range(len(chi) // n_rungs):
+        for pair in range(n_rungs // 2):
+            if 2 * pair + 1 + parity >= n_rungs:
+                continue
+            ra = ladder * n_rungs + 2 * pair + parity
+            ia, ib = ror[ra], ror[ra + 1]
+            x = (chi[ia] - chi[ib]) * (S[ia] - S[ib])
+            u = exchange_uniform(seed, round_, ra)
+            ties += abs(u - np.exp(x)) < tie
+            if u < np.exp(x):
+                chi[ia], chi[ib] = chi[ib], chi[ia]
+                ror[ra], ror[ra + 1] = ib, ia
+                swaps += 1
+    return chi, ror, swaps, ties
+
+
+def _small_ladder_sim(chi=None):
+    from chromo_gb300 import workloads as wl
+    R = 8
+    rng = np.random.default_rng(5)
+    w = wl.Workload("exchange", np.full(R, 400), 10, 2, rng.uniform(-1, 0, size=(R, 2)),
+                    np.zeros(R) if chi is None else chi, [-4.0, -3.0], [{"PRC1": 1.0}, {}], 50, 4,
+                    wl.BASE_SEED + 11)
+    return w, wl.build_sim(w)
+
+
+def _chi_sums(sim, w):
+    from chromo_gb300 import workloads as wl
+    vol_bin = wl.VOXEL ** 3
+    bead_vol = 4.0 / 3.0 * np.pi * wl.BEAD_RAD ** 3
+    return np.array([chi_free_sum(sim.density(r), vol_bin, bead_vol) for r in range(w.replicas)])
+
+
+@pytest.mark.gpu
+def test_exchange_rounds_match_host_rule():
+    pytest.importorskip("torch")
+    w, sim = _small_ladder_sim()
+    S0 = _chi_sums(sim, w)
+    sim.close()
+    # a ladder spacing that makes |(chi_a - chi_b)(S_a - S_b)| of order one
+    spread = max(float(np.std(S0)), 1e-12)
+    chi = np.tile(np.arange(4) / spread, 2)
+    w, sim = _small_ladder_sim(chi)
+    try:
+        seed = 0x1234_5678_9ABC
+        ror = np.arange(w.replicas)
+        cur = sim.chi()
+        np.testing.assert_array_equal(cur, chi)
+        total = 0
+        for rnd in range(8):
+            sim.run(2, 100 + rnd)
+            S = _chi_sums(sim, w)
+            want, ror, swaps, ties = expected_exchange(cur, S, ror, 4, rnd, seed)
+            sim.exchange(4, rnd, seed)
+            got = sim.chi()
+            if not ties:
+                np.testing.assert_array_equal(got, want)
+            cur = got
+            total += swaps
+        assert 0 < total < 8 * 6, "the rule should both accept and reject some swaps here"
+    finally:
+        sim.close()
+
+
+@pytest.mark.gpu
+def test_batched_rounds_exchange_after_mc():
+    """cg_run_batched: MC then exchange per round, the round number taken from a
+    device counter starting at 0; the chi-free sums are those of the grids
+    left by the MC kernel."""
+    pytest.importorskip("torch")
+    w, sim = _small_ladder_sim()
+    S0 = _chi_sums(sim, w)
+    sim.close()
+    chi = np.tile(np.arange(4) / max(float(np.std(S0)), 1e-12), 2)
+    w, sim = _small_ladder_sim(chi)
+    try:
+        seed = 77
+        ror = np.arange(w.replicas)
+        cur = sim.chi()
+        for rnd in range(4):
+            sim.run_batched(1, 2, 4, seed)
+            sim.sync()
+            S = _chi_sums(sim, w)
+            want, ror, _, ties = expected_exchange(cur, S, ror, 4, rnd, seed)
+            got = sim.chi()
+            if not ties:
+                np.testing.assert_array_equal(got, want)
+            cur = got
+    finally:
+        sim.close()

@@ -21,6 +21,8 @@ def lib(tmp_path_factory):
     so = d / "m32.so"
     subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-ffp-contract=off", "-o", str(so), str(src), "-lm"])
     L = ctypes.CDLL(str(so))
+    L.sc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    L.ac.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
     return L
 
 

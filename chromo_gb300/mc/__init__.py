@@ -2,8 +2,8 @@
 
 ``mc_sim`` runs on the GPU; ``get_amplitude_bounds`` and ``polymer_in_field``
 mirror the reference's host-side orchestration (snapshots are kept in memory
-or written as .npz files; the reference's CSV snapshot format is not
-reproduced).
+and, with an output directory, written in the reference's polymer CSV
+format).
 """
 from pathlib import Path
 from typing import Dict, List, Optional, Tuple
@@ -39,7 +39,8 @@ def polymer_in_field(polymers, binders, field, num_save_mc, num_saves, bead_amp_
                      random_seed: Optional[int] = 0, mu_schedule=None, output_dir=None, **kwargs):
     """Run ``num_saves`` rounds of ``num_save_mc`` MC steps, keeping a snapshot of
     every polymer after each round (chromo/mc/__init__.py:36-161).  With an
-    ``output_dir`` the snapshots are written as ``<name>-<i>.npz``."""
+    ``output_dir`` each snapshot is also written as ``<name>-<i>.csv`` in the
+    reference's polymer CSV format (``PolymerBase.to_csv``)."""
     np.random.seed(random_seed)
     if mc_move_controllers is None:
         mc_move_controllers = all_moves(str(output_dir or "."), bead_amp_bounds.bounds,
@@ -54,6 +55,6 @@ def polymer_in_field(polymers, binders, field, num_save_mc, num_saves, bead_amp_
                 for p in polymers]
         snapshots.append(snap)
         if output_dir is not None:
-            for p, s in zip(polymers, snap):
-                np.savez(Path(output_dir) / f"{p.name}-{mc_count}.npz", **s)
+            for p in polymers:
+                p.to_csv(str(Path(output_dir) / f"{p.name}-{mc_count}.csv"))
     return snapshots

@@ -121,6 +121,36 @@ class PolymerBase(TransformedObject):
     def __str__(self):
         return f"Polymer<{self.name}, nbeads={self.num_beads}, nbinder={self.num_binders}>"
 
+    # ---- snapshots in the reference's CSV format (chromo/polymers.pyx:575-758) ----
+    def to_csv(self, path=None):
+        """Write the snapshot CSV to ``path``; with ``path=None`` return its text."""
+        from .util.poly_csv import to_csv_text
+        text = to_csv_text(self)
+        if path is None:
+            return text
+        with open(path, "w", newline="") as fh:
+            fh.write(text)
+        return None
+
+    def to_file(self, path):
+        """Synonym of ``to_csv``."""
+        return self.to_csv(path)
+
+    @classmethod
+    def from_csv(cls, csv_file):
+        return cls.from_file(csv_file)
+
+    @classmethod
+    def from_file(cls, path, name=None, **kwargs):
+        """Construct the polymer stored by ``to_csv`` (a path or a text buffer);
+        ``name`` defaults to the file's stem."""
+        from .util.poly_csv import polymer_kwargs
+        if name is None and isinstance(path, str):
+            name = path.split("/")[-1].split(".")[0]
+        kw = polymer_kwargs(path, name)
+        kw.update(kwargs)
+        return cls(**kw)
+
 
 class SSWLC(PolymerBase):
     """Stretchable, shearable wormlike chain (chromo/polymers.pyx:911-1601)."""

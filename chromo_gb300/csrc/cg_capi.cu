@@ -108,7 +108,7 @@ struct cg_sim {
     KArgs a{};
     a.reps = reps; a.ctl = ctl; a.n_ctl = n_ctl; a.n_reps = R; a.tally = tally;
     a.r4 = r4; a.t34 = t34; a.t24 = t24; a.states = states; a.marks = marks; a.bonds = bonds;
-    a.grid = grid; a.access_vol = access_vol; a.ncol = ncol;
+    a.grid = grid; a.access_vol = access_vol; a.ncol = ncol; a.hcol = nb + 1;
     a.g_keys = g_keys; a.g_used = g_used; a.g_bslot = g_bslot; a.g_vals = g_vals; a.g_logH = g_logH;
     a.g_stage = g_stage; a.g_idx = g_idx; a.g_stage_cap = g_stage_cap;
     a.picked = picked; a.picked_off = d_picked_off;
@@ -131,7 +131,7 @@ struct cg_sim {
     off_used = (int)o; o += 4 * H;
     off_bslot = (int)o; o += 4 * H;
     o = align16(o);
-    off_vals = (int)o; o += 8 * H * ncol;
+    off_vals = (int)o; o += 8 * H * (nb + 1);
     off_stage = (int)o; o += sc * 9 * scal_bytes();
     o = align16(o);
     off_idx = (int)o; o += 4 * sc;
@@ -202,8 +202,8 @@ static int choose_shape(cg_sim* s, int w_req) {
   if (W > cg::kMaxW) W = cg::kMaxW;
   s->spec_w = W;
   const size_t budget = std::min<size_t>(smem_per_sm / ctas_per_sm - 1024, 220 * 1024);
-  const int lhb = 11;
-  const long long sc = 96;
+  const int lhb = 10;
+  const long long sc = 48;
   int lh = 12;
   for (; lh > 6; lh--) {
     s->layout(lh, sc);
@@ -283,7 +283,7 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   ALLOC(s->g_keys, 4 * Hg * RW);
   ALLOC(s->g_used, 4 * Hg * RW);
   ALLOC(s->g_bslot, 4 * Hg * RW);
-  ALLOC(s->g_vals, 8 * Hg * s->ncol * RW);
+  ALLOC(s->g_vals, 8 * Hg * (s->nb + 1) * RW);
   ALLOC(s->g_stage, s->scal_bytes() * 9 * s->g_stage_cap * RW);
   ALLOC(s->g_idx, 4 * s->g_stage_cap * RW);
   ALLOC(s->picked, 4 * s->total_picked);
@@ -311,7 +311,7 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   cudaMemset(s->grid, 0, 8 * s->ncol * s->total_vox);
   cudaMemset(s->g_keys, 0xFF, 4 * Hg * RW);
   cudaMemset(s->g_bslot, 0xFF, 4 * Hg * RW);
-  cudaMemset(s->g_vals, 0, 8 * Hg * s->ncol * RW);
+  cudaMemset(s->g_vals, 0, 8 * Hg * (s->nb + 1) * RW);
   cudaMemset(s->picked, 0, 4 * s->total_picked);
   cudaMemset(s->swaps, 0, 8 * s->R);
   cudaMemset(s->swap_attempts, 0, 8 * s->R);
@@ -541,7 +541,7 @@ static int device_errors(cg_sim* s) {
   const long long RW = (long long)s->R * s->spec_w;
   cudaMemset(s->g_keys, 0xFF, 4 * Hg * RW);
   cudaMemset(s->g_bslot, 0xFF, 4 * Hg * RW);
-  cudaMemset(s->g_vals, 0, 8 * Hg * s->ncol * RW);
+  cudaMemset(s->g_vals, 0, 8 * Hg * (s->nb + 1) * RW);
   cudaMemset(s->picked, 0, 4 * s->total_picked);
   char msg[160];
   snprintf(msg, sizeof msg, "device error bits 0x%x (first at replica %d)", any, first);

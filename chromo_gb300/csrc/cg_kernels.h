@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <string>
 
 #include "cg_device.cuh"
@@ -39,9 +40,12 @@ struct MovePlan {
 };
 
 // Shared-memory header of one replica's CTA.
+constexpr int kDrawCache = 64;  // first draws of each in-flight move, precomputed by its warp
+
 struct SpecShared {
   WarpShared ws;
   MovePlan plan[kMaxW];
+  alignas(16) unsigned draws[kMaxW][kDrawCache];  // written as uint4 by init()
   int nused[kMaxW];
   unsigned long long t0;   // move counter (selects each move's random sub-stream)
   double run_dE;
@@ -49,6 +53,9 @@ struct SpecShared {
   unsigned accmask;
   int pad;
 };
+
+static_assert(offsetof(SpecShared, draws) % 16 == 0 && sizeof(unsigned) * kDrawCache % 16 == 0,
+              "the draw buffers are written with 16-byte stores");
 
 struct KArgs {
   RepDev* reps;
@@ -63,7 +70,8 @@ struct KArgs {
   const double* bonds;        // 6 doubles per bead (bond i -> i+1)
   long long* grid;            // ncol int64 per voxel
   const double* access_vol;   // per voxel, or null
-  int ncol;
+  int ncol;   // grid columns per voxel (2 or 4: rows padded to 16 or 32 bytes)
+  int hcol;   // columns of a voxel-hash entry (n_binders + 1)
   // per-replica global scratch for moves too large for shared memory
   int* g_keys;
   int* g_used;

@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
   long long* s_vals = reinterpret_cast<long long*>(base + a.off_vals);
   Pos* s_stage = reinterpret_cast<Pos*>(base + a.off_stage);
   int* s_idx = reinterpret_cast<int*>(base + a.off_idx);
-  const int ncol = a.ncol;
+  const int ncol = a.hcol;  // stride of the voxel-hash values
 
   {  // load replica parameters and controllers into shared memory
     const unsigned* src = reinterpret_cast<const unsigned*>(a.reps + rep);

@@ -31,21 +31,62 @@ __device__ __forceinline__ void add_delta(long long* vals, int ncol, int slot, i
   if (d != 0) atomicAdd((unsigned long long*)&vals[(long long)slot * ncol + col], (unsigned long long)d);
 }
 
+// Linear probing for `key` after its home slot `start` was found taken by
+// another key; sets `inserted` when the key claims a new slot.
+__device__ __forceinline__ int hash_probe(int* keys, int logH, int key, int start, bool& inserted,
+                                          unsigned& err) {
+  const unsigned mask = (1u << logH) - 1u;
+  unsigned h = ((unsigned)start + 1u) & mask;
+  for (unsigned it = 1; it <= mask; it++) {
+    int prev = atomicCAS(&keys[h], -1, key);
+    if (prev == -1) { inserted = true; return (int)h; }
+    if (prev == key) { inserted = false; return (int)h; }
+    h = (h + 1) & mask;
+  }
+  err |= E_SPIN;
+  return -1;
+}
+
 // Deposit +/- one bead's eight trilinear weights with binder states `st`
-// (packed int8) into the hash.
+// (packed int8) into the hash.  The eight home-slot claims are issued back to
+// back (independent shared-memory atomics in flight together); only a claim
+// that meets another key probes on.  The lane appends its new slots to the
+// used list with one counter update.
 template <typename Real>
 __device__ __forceinline__ void deposit_bead(const RepDev& rd, int ncol, int* keys, int* used,
                                              int* nused, long long* vals, int logH,
                                              const Real w[8], const int v[8], unsigned st,
                                              bool negate, unsigned& err) {
+  int slot[8], prev[8];
+#pragma unroll
+  for (int l = 0; l < 8; l++) {
+    slot[l] = (int)(((unsigned)v[l] * 0x9E3779B1u) >> (32 - logH));
+    prev[l] = atomicCAS(&keys[slot[l]], -1, v[l]);
+  }
+  unsigned fresh = 0;
+#pragma unroll
+  for (int l = 0; l < 8; l++) {
+    if (prev[l] == -1) {
+      fresh |= 1u << l;
+    } else if (prev[l] != v[l]) {
+      bool inserted = false;
+      slot[l] = hash_probe(keys, logH, v[l], slot[l], inserted, err);
+      if (slot[l] < 0) return;
+      if (inserted) fresh |= 1u << l;
+    }
+  }
+  if (fresh) {
+    int at = atomicAdd(nused, __popc(fresh));
+#pragma unroll
+    for (int l = 0; l < 8; l++)
+      if ((fresh >> l) & 1u) used[at++] = slot[l];
+  }
 #pragma unroll
   for (int l = 0; l < 8; l++) {
     long long q = q40(w[l]);
     if (negate) q = -q;
-    int slot = hash_slot(keys, used, nused, logH, v[l], err);
-    if (slot < 0) return;
-    add_delta(vals, ncol, slot, 0, q);
-    for (int b = 0; b < rd.nb; b++) add_delta(vals, ncol, slot, 1 + b, q * (long long)((st >> (8 * b)) & 0xFF));
+    add_delta(vals, ncol, slot[l], 0, q);
+    for (int b = 0; b < rd.nb; b++) add_delta(vals, ncol, slot[l], 1 + b, q * (long long)((st >> (8 * b)) & 0xFF));
   }
 }
 
@@ -62,17 +103,17 @@ __device__ __forceinline__ double chi_term64(const RepDev& rd, double V, long lo
 
 // Field dE over the touched voxels (fixed-point grid), FP64 arithmetic; also
 // stores the post-move grid values into the hash values for the commit.
-static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int ncol, const int* keys,
+static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
                                   long long& n_vox, double) {
   const RepDev& rd = ws.rd;
   double part = 0;
-  const long long* grid = a.grid + rd.vox_off * ncol;
+  const long long* grid = a.grid + rd.vox_off * a.ncol;
   for (int i = lane; i < nused; i += 32) {
     int slot = used[i];
     int v = keys[slot];
-    long long* d = vals + (long long)slot * ncol;
-    const long long* gv = grid + (long long)v * ncol;
+    long long* d = vals + (long long)slot * hcol;
+    const long long* gv = grid + (long long)v * a.ncol;
     long long g0 = gv[0], d0 = d[0];
     double V = rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin;
     double c = 0, rho[CG_MAX_BINDERS], dd[CG_MAX_BINDERS];
@@ -96,17 +137,17 @@ static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, i
 
 // FP32 arithmetic per voxel, FP64 accumulation; voxels at or near the volume
 // fraction limit take the FP64 branch so the 1e99 penalty is decided as in FP64.
-static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int ncol, const int* keys,
+static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
                                   long long& n_vox, float) {
   const RepDev& rd = ws.rd;
   double part = 0;
-  const long long* grid = a.grid + rd.vox_off * ncol;
+  const long long* grid = a.grid + rd.vox_off * a.ncol;
   for (int i = lane; i < nused; i += 32) {
     int slot = used[i];
     int v = keys[slot];
-    long long* d = vals + (long long)slot * ncol;
-    const long long* gv = grid + (long long)v * ncol;
+    long long* d = vals + (long long)slot * hcol;
+    const long long* gv = grid + (long long)v * a.ncol;
     long long g0 = gv[0], d0 = d[0];
     float sc = ws.f_scale, k = ws.f_k;
     double V = rd.vol_bin;
@@ -139,18 +180,18 @@ static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, i
   return warp_sum(part);
 }
 
-__device__ __forceinline__ void commit_grid(const RepDev& rd, const KArgs& a, int ncol, int* keys,
+__device__ __forceinline__ void commit_grid(const RepDev& rd, const KArgs& a, int hcol, int* keys,
                                             const int* used, long long* vals, int nused, int lane,
                                             bool accept) {
-  long long* grid = a.grid + rd.vox_off * ncol;
+  long long* grid = a.grid + rd.vox_off * a.ncol;
   for (int i = lane; i < nused; i += 32) {
     int slot = used[i];
     if (accept) {
       int v = keys[slot];
-      for (int c = 0; c < ncol; c++) grid[(long long)v * ncol + c] = vals[(long long)slot * ncol + c];
+      for (int c = 0; c < hcol; c++) grid[(long long)v * a.ncol + c] = vals[(long long)slot * hcol + c];
     }
     keys[slot] = -1;
-    for (int c = 0; c < ncol; c++) vals[(long long)slot * ncol + c] = 0;
+    for (int c = 0; c < hcol; c++) vals[(long long)slot * hcol + c] = 0;
   }
 }
 

@@ -30,20 +30,32 @@
 
 namespace cg {
 
-// Random numbers of one attempted move (its own counter space).
+// Random numbers of one attempted move (its own counter space).  Draw j is
+// word j & 3 of Philox block j >> 2.  The first kDrawCache draws are computed
+// at init by kDrawCache / 4 lanes at once into the warp's shared-memory
+// buffer, so a move's draws cost one Philox latency instead of a chain of
+// them; init() must be called by the whole warp.
 struct MoveRng {
   uint2 key, keyb;
   unsigned tlo, thi;
   unsigned long long pos, bpos;
   unsigned cctr;
   uint4 cache;
+  const unsigned* buf;
   bool fail;
-  __device__ void init(unsigned long long seed, int rep, unsigned long long t) {
+  __device__ void init(unsigned long long seed, int rep, unsigned long long t, unsigned* draws) {
     key = make_uint2((unsigned)seed ^ (unsigned)rep * 0x85EBCA6Bu, (unsigned)(seed >> 32) ^ 0x1B873593u);
     keyb = make_uint2(key.x ^ 0x68E31DA4u, key.y ^ 0xB5297A4Du);
     tlo = (unsigned)t;
     thi = (unsigned)(t >> 32);
     pos = 0; bpos = 0; cctr = 0xffffffffu; fail = false;
+    const unsigned lane = threadIdx.x & 31u;
+    if (lane < kDrawCache / 4) {
+      uint4 o = philox(make_uint4(lane, tlo, thi, 0x2545F491u), key);
+      reinterpret_cast<uint4*>(draws)[lane] = o;
+    }
+    __syncwarp();
+    buf = draws;
   }
   __device__ __forceinline__ unsigned at(unsigned long long j, bool& ok) const {
     ok = true;
@@ -51,12 +63,14 @@ struct MoveRng {
     return comp4(o, (unsigned)(j & 3)) >> 1;
   }
   __device__ __forceinline__ unsigned next() {
-    unsigned j = (unsigned)pos++, c = j >> 2;
+    unsigned long long j = pos++;
+    if (j < (unsigned long long)kDrawCache) return buf[j] >> 1;
+    unsigned c = (unsigned)(j >> 2);
     if (c != cctr) {
       cache = philox(make_uint4(c, tlo, thi, 0x2545F491u), key);
       cctr = c;
     }
-    return comp4(cache, j & 3u) >> 1;
+    return comp4(cache, (unsigned)j & 3u) >> 1;
   }
   __device__ __forceinline__ int state_at(unsigned long long k, int nt, bool& ok) const {
     ok = true;
@@ -98,7 +112,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
   const GridF& gf = sh.ws.gf;
   const WarpShared& ws = sh.ws;
   const long long N = rd.n_beads;
-  const int ncol = a.ncol;
+  const int ncol = a.hcol;  // stride of the voxel-hash values
   const V4<Pos>* r4 = reinterpret_cast<const V4<Pos>*>(a.r4) + rd.bead_off;
   const V4<Pos>* t34 = reinterpret_cast<const V4<Pos>*>(a.t34) + rd.bead_off;
   const V4<Pos>* t24 = reinterpret_cast<const V4<Pos>*>(a.t24) + rd.bead_off;
@@ -107,7 +121,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
   const double* bonds = a.bonds + rd.bead_off * 6;
   MovePlan& P = sh.plan[w];
   MoveRng g;
-  g.init(a.seed, rep, t);
+  g.init(a.seed, rep, t, sh.draws[w]);
   unsigned err = 0;
   const bool check_field = rd.field_kind != 0 && kind != CG_TANGENT_ROTATION;
   const bool density = rd.field_kind == 2;
@@ -182,7 +196,9 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
       for (int i = 0; i < 3; i++)
         for (int j = 0; j < 4; j++) M[i][j] = (Real)Md[i][j];
       if (m > a.stage_cap) { S.stage = gm.stage; gstage = 1; }
-      if (32 * m > (1LL << sm.logH)) { S.keys = gm.keys; S.used = gm.used; S.bslot = gm.bslot; S.vals = gm.vals; S.logH = gm.logH; gtab = 1; }
+      // at most 16 distinct voxels per bead (8 corners, old and new), so a
+      // table of 16 m slots never fills
+      if (16 * m > (1LL << sm.logH)) { S.keys = gm.keys; S.used = gm.used; S.bslot = gm.bslot; S.vals = gm.vals; S.logH = gm.logH; gtab = 1; }
       Pos* stage = reinterpret_cast<Pos*>(S.stage);
       double part = 0;
       int oob = 0;
@@ -457,14 +473,15 @@ __device__ void conflict_mask(const KArgs& a, SpecShared& sh, unsigned char* sme
       cm = __reduce_or_sync(kFull, cm);
     }
     cm &= (1u << w) - 1u;
-    for (int u = 0; u < w; u++) {
-      const MovePlan& U = sh.plan[u];
-      if (U.err || U.empty) continue;
-      if (P.kind == CG_TANGENT_ROTATION) {
+    if (P.kind == CG_TANGENT_ROTATION) {
+      // rotated beads of u against those of w and their neighbours
+      const int* lw = P.gstage ? gm.idx : sm.idx;
+      for (int u = 0; u < w; u++) {
+        const MovePlan& U = sh.plan[u];
+        if (U.err || U.empty) continue;
         const int* lu = U.gstage ? a.g_idx + ((long long)rep * a.spec_w + u) * a.g_stage_cap
                                  : reinterpret_cast<const int*>(smem + a.spec_off_warps +
                                                                 (size_t)u * a.warp_smem + a.off_idx);
-        const int* lw = P.gstage ? gm.idx : sm.idx;
         int hit = 0;
         for (int k = lane; k < P.m && !hit; k += 32) {
           int j = lw[k];
@@ -474,14 +491,21 @@ __device__ void conflict_mask(const KArgs& a, SpecShared& sh, unsigned char* sme
           }
         }
         if (__any_sync(kFull, hit)) cm |= 1u << u;
-      } else {
-        // beads written by u: [ind0, indf); beads read by w: the segment and,
-        // for position moves, its two neighbours
-        long long wlo = U.ind0, whi = (long long)U.indf - 1;
-        long long rlo = P.kind == CG_CHANGE_BINDING_STATE ? P.ind0 : (long long)P.ind0 - 1;
-        long long rhi = P.kind == CG_CHANGE_BINDING_STATE ? (long long)P.indf - 1 : (long long)P.indf;
-        if (wlo <= rhi && rlo <= whi) cm |= 1u << u;
       }
+    } else {
+      // lane u < w: beads written by u, [ind0, indf), against the beads read
+      // by w: the segment and, for position moves, its two neighbours
+      bool hit = false;
+      if (lane < w) {
+        const MovePlan& U = sh.plan[lane];
+        if (!U.err && !U.empty) {
+          const long long wlo = U.ind0, whi = (long long)U.indf - 1;
+          const long long rlo = P.kind == CG_CHANGE_BINDING_STATE ? P.ind0 : (long long)P.ind0 - 1;
+          const long long rhi = P.kind == CG_CHANGE_BINDING_STATE ? (long long)P.indf - 1 : (long long)P.indf;
+          hit = wlo <= rhi && rlo <= whi;
+        }
+      }
+      cm |= __ballot_sync(kFull, hit);
     }
   }
   if (lane == 0) P.cmask = cm;
@@ -493,7 +517,7 @@ __device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int w, int lane
                                  unsigned* bmask) {
   const MovePlan& P = sh.plan[w];
   const RepDev& rd = sh.ws.rd;
-  const int ncol = a.ncol;
+  const int ncol = a.ncol, hcol = a.hcol;
   V4<Pos>* r4w = reinterpret_cast<V4<Pos>*>(a.r4) + rd.bead_off;
   V4<Pos>* t34w = reinterpret_cast<V4<Pos>*>(a.t34) + rd.bead_off;
   V4<Pos>* t24w = reinterpret_cast<V4<Pos>*>(a.t24) + rd.bead_off;
@@ -538,10 +562,10 @@ __device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int w, int lane
     int slot = used[i];
     if (accept) {
       int v = keys[slot];
-      for (int cc = 0; cc < ncol; cc++) grid[(long long)v * ncol + cc] = vals[(long long)slot * ncol + cc];
+      for (int cc = 0; cc < hcol; cc++) grid[(long long)v * ncol + cc] = vals[(long long)slot * hcol + cc];
     }
     keys[slot] = -1;
-    for (int cc = 0; cc < ncol; cc++) vals[(long long)slot * ncol + cc] = 0;
+    for (int cc = 0; cc < hcol; cc++) vals[(long long)slot * hcol + cc] = 0;
     int b = bslot[i];
     if (b >= 0) { bkeys[b] = -1; bmask[b] = 0u; }
     bslot[i] = -1;
@@ -550,8 +574,10 @@ __device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int w, int lane
   if (lane == 0) sh.nused[w] = 0;
 }
 
+// 168 registers: two CTAs of 6 warps fit one SM's register file (measured
+// faster than 128 registers with 8 warps, which spills).
 template <typename Pos>
-__global__ void __launch_bounds__(256, 1) spec_kernel(KArgs a) {
+__global__ void __maxnreg__(168) spec_kernel(KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int W = a.spec_w;
@@ -561,7 +587,7 @@ __global__ void __launch_bounds__(256, 1) spec_kernel(KArgs a) {
   int* bkeys = reinterpret_cast<int*>(smem + a.spec_off_bkeys);
   unsigned* bmask = reinterpret_cast<unsigned*>(smem + a.spec_off_bmask);
   const int HB = 1 << a.spec_logHB;
-  const int ncol = a.ncol;
+  const int ncol = a.hcol;  // stride of the voxel-hash values
   unsigned char* wb = smem + a.spec_off_warps + (size_t)warp * a.warp_smem;
   WarpScratch sm, gm;
   sm.keys = reinterpret_cast<int*>(wb + a.off_keys);
@@ -626,40 +652,55 @@ __global__ void __launch_bounds__(256, 1) spec_kernel(KArgs a) {
           __syncthreads();
           if (warp < B) conflict_mask(a, sh, smem, rep, warp, lane, sm, gm, bmask);
           __syncthreads();
-          if (tid == 0) {
-            unsigned acc = 0;
-            int cut = B;
-            for (int w = 0; w < B; w++) {
-              MovePlan& P = sh.plan[w];
-              if (P.err) { cut = w; sh.stop = P.err; break; }
-              if (P.cmask & acc) { cut = w; break; }
-              c.num_attempt += 1;
+          // Resolve, computed by every warp from the plans (lane u reads move u):
+          // the batch stands up to the first move that failed or meets an
+          // earlier accepted move (everything before it stands, so "earlier
+          // accepted" is the accepted moves below it), or up to and including
+          // the first move whose voxels could not be registered.
+          const bool valid = lane < B;
+          const MovePlan& Pl = sh.plan[valid ? lane : 0];
+          const bool p_err = valid && Pl.err != 0;
+          const unsigned D = __ballot_sync(kFull, valid && !Pl.empty && Pl.dec);
+          const unsigned F = __ballot_sync(kFull, p_err || (valid && (Pl.cmask & D & ((1u << lane) - 1u))));
+          const unsigned RF = __ballot_sync(kFull, valid && Pl.regfail);
+          const int first_fail = F ? __ffs((int)F) - 1 : B;
+          int cut = first_fail;
+          if (RF && __ffs((int)RF) < cut) cut = __ffs((int)RF);
+          const unsigned acc = cut >= 32 ? D : (D & ((1u << cut) - 1u));
+          if (warp == 0) {
+            // bookkeeping of the standing moves, in move order where it is FP64
+            const bool stand = lane < cut;
+            const bool took = (acc >> lane) & 1u;
+            const unsigned sm_m = __reduce_add_sync(kFull, stand ? (unsigned)Pl.m : 0u);
+            const unsigned sm_v = __reduce_add_sync(kFull, stand ? (unsigned)Pl.nvox : 0u);
+            const unsigned ac_m = __reduce_add_sync(kFull, took ? (unsigned)Pl.m : 0u);
+            const unsigned ac_v = __reduce_add_sync(kFull, took ? (unsigned)Pl.nvox : 0u);
+            if (lane == 0) {
+              const unsigned n_acc = (unsigned)__popc(acc);
+              c.num_attempt += cut;
+              c.num_success += n_acc;
               unsigned long long* t = sh.ws.tally + kind * 6;
-              t[0] += 1;
-              t[2] += (unsigned long long)P.m;
-              t[3] += (unsigned long long)P.nvox;
-              if (!P.empty) {
-                if (P.dec) {
-                  acc |= 1u << w;
-                  c.num_success += 1;
-                  sh.run_dE += P.dE;
-                  t[1] += 1;
-                  t[4] += (unsigned long long)P.m;
-                  t[5] += (unsigned long long)P.nvox;
-                }
-                c.acc_rate = c.alpha * (P.dec ? 1.0 : 0.0) + (1 - c.alpha) * c.acc_rate;
+              t[0] += (unsigned long long)cut;
+              t[1] += n_acc;
+              t[2] += sm_m;
+              t[3] += sm_v;
+              t[4] += ac_m;
+              t[5] += ac_v;
+              double run = sh.run_dE, rate = c.acc_rate;
+              for (int w = 0; w < cut; w++) {
+                const MovePlan& P = sh.plan[w];
+                if (P.empty) continue;
+                if (P.dec) run += P.dE;
+                rate = c.alpha * (P.dec ? 1.0 : 0.0) + (1 - c.alpha) * rate;
               }
-              if (P.regfail) { cut = w + 1; break; }
+              sh.run_dE = run;
+              c.acc_rate = rate;
+              sh.t0 += (unsigned long long)cut;
+              if (cut == first_fail && first_fail < B && sh.plan[first_fail].err) sh.stop = sh.plan[first_fail].err;
             }
-            sh.cut = cut;
-            sh.t0 += (unsigned long long)cut;
-            sh.accmask = acc;
           }
-          __syncthreads();
-          const int cut = sh.cut;
           if (warp < B)
-            commit_and_clear<Pos>(a, sh, warp, lane, warp < cut && ((sh.accmask >> warp) & 1u), sm, gm,
-                                  bkeys, bmask);
+            commit_and_clear<Pos>(a, sh, warp, lane, warp < cut && ((acc >> warp) & 1u), sm, gm, bkeys, bmask);
           __syncthreads();
           done += cut;
           if (sh.stop) break;

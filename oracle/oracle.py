@@ -219,6 +219,9 @@ class OracleSystem:
         self.draw_pos, self.bstate_pos = dp.value, bp.value
         for i, c in enumerate(ctls):
             C.memmove(C.byref(c), C.byref(arr[i]), C.sizeof(Ctl))
+        if n == -3:  # window larger than the chain: ValueError in the reference
+            raise ValueError("bead selection window larger than the polymer "
+                             "(chromo/util/bead_selection.pyx:86-89)")
         if n < 0:
             raise RuntimeError(f"oracle mc_sim error {n}")
         return recs[:n]

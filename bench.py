@@ -294,12 +294,10 @@ def main():
     for k in range(e2e_steps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for rep in range(w.replicas):
-            c = chains[rep]
-            sim.set_chain(rep, r=c.r, t3=c.t3, t2=c.t2, states=c.states)
+        sim.set_chains([dict(r=c.r, t3=c.t3, t2=c.t2, states=c.states) for c in chains])
         sim.run_batched(1, steps_round, w.n_rungs, 11 + rank, sh)
-        snap = [sim.get_chain(rep) for rep in range(w.replicas)]
         sim.sync(sh)
+        snap = sim.get_chains()
         dt = time.perf_counter() - t0
         if k > 0:
             t_e2e += dt
@@ -340,8 +338,8 @@ def main():
                          "moves_per_launch": float(tal2[:, :, 0].sum()) / n_launch},
             "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
-                    "path": "C ABI: cg_set_chain x R (host FP64 -> pinned -> HBM), cg_run_batched, "
-                            "cg_get_chain x R"},
+                    "path": "C ABI: cg_set_chains (host FP64 -> pinned -> HBM, all replicas), "
+                            "cg_run_batched, cg_get_chains"},
             "plain": {"value": plain_value, "unit": "moves/s",
                       "workload": "one 10,000-bead chain, 60^3 grid, one binder, 300 MC steps",
                       "batched_over_plain": value / plain_value},

@@ -82,7 +82,7 @@ EXPORTS = [
     "cg_set_binding", "cg_set_controllers", "cg_get_controllers", "cg_deposit", "cg_get_density",
     "cg_run", "cg_sync", "cg_run_audit", "cg_energy", "cg_reset_running_energy", "cg_get_tally",
     "cg_reset_tally", "cg_exchange", "cg_get_chi", "cg_run_batched", "cg_get_launch_info",
-    "cg_field_energy_static", "cg_energies",
+    "cg_field_energy_static", "cg_energies", "cg_set_chains", "cg_get_chains",
 ]
 
 
@@ -124,6 +124,8 @@ def lib():
             "cg_get_launch_info": ([P, P, P, P], C.c_int),
             "cg_field_energy_static": ([C.POINTER(FieldParams), I64, P, P, P, P, P], C.c_int),
             "cg_energies": ([P, P, P], C.c_int),
+            "cg_set_chains": ([P, P, P, P, P], C.c_int),
+            "cg_get_chains": ([P, P, P, P, P], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -196,6 +198,44 @@ class Sim:
         st = np.empty((n, self.nb), dtype=np.int64)
         check(lib().cg_get_chain(self.h, rep, _ptr(r), _ptr(t3), _ptr(t2), _ptr(st)))
         return r, t3, t2, st
+
+    def set_chains(self, chains):
+        """Upload every replica's chain at once: ``chains[rep]`` is a mapping with
+        any of ``r``, ``t3``, ``t2``, ``states`` (missing keys are skipped)."""
+        keep = []
+
+        def table(key, dtype, width):
+            ptrs = (C.c_void_p * self.R)()
+            given = False
+            for rep, c in enumerate(chains):
+                a = c.get(key)
+                if a is None:
+                    continue
+                a = np.ascontiguousarray(a, dtype=dtype)
+                if a.size != int(self.n_beads[rep]) * width:
+                    raise ValueError(f"{key} of replica {rep} has the wrong size")
+                keep.append(a)
+                ptrs[rep] = a.ctypes.data
+                given = True
+            return ptrs if given else None
+
+        if len(chains) != self.R:
+            raise ValueError("one entry per replica")
+        check(lib().cg_set_chains(self.h, table("r", np.float64, 3), table("t3", np.float64, 3),
+                                  table("t2", np.float64, 3), table("states", np.int64, self.nb)))
+
+    def get_chains(self):
+        """Every replica's (r, t3, t2, states) in one call."""
+        out = [(np.empty((int(n), 3)), np.empty((int(n), 3)), np.empty((int(n), 3)),
+                np.empty((int(n), self.nb), dtype=np.int64)) for n in self.n_beads]
+        tabs = []
+        for k in range(4):
+            t = (C.c_void_p * self.R)()
+            for rep in range(self.R):
+                t[rep] = out[rep][k].ctypes.data
+            tabs.append(t)
+        check(lib().cg_get_chains(self.h, *tabs))
+        return out
 
     def set_field(self, rep, fp: FieldParams, access_vol=None):
         av = None if access_vol is None else np.ascontiguousarray(access_vol, dtype=np.float64)

@@ -153,12 +153,20 @@ class ReplicaBatch:
         return self.sim.chi()
 
     # ------------------------------------------------------------ read back
+    def push(self):
+        """Upload the host objects' positions, tangents and binding states (all
+        replicas in one call) and rebuild the densities."""
+        self.sim.set_chains([dict(r=p.r, t3=p.t3, t2=p.t2, states=p.states) for p in self.polymers])
+        self.sim.deposit(-1)
+        self.rebaseline()
+
     def pull(self):
         """Copy positions, tangents, binding states, densities, chi and controller
         state back into the host objects."""
         chi = self.sim.chi()
+        chains = self.sim.get_chains()
         for r, (p, f, ctrls) in enumerate(zip(self.polymers, self.fields, self.controllers)):
-            rr, t3, t2, st = self.sim.get_chain(r)
+            rr, t3, t2, st = chains[r]
             p.r[:] = rr
             p.t3[:] = t3
             p.t2[:] = t2

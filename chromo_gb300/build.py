@@ -52,7 +52,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if any(p.wait() != 0 for p in procs):
         raise RuntimeError("nvcc compilation failed")
     tmp = LIB.with_suffix(".so.tmp")
-    subprocess.check_call([nv, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)])
+    subprocess.check_call([nv, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

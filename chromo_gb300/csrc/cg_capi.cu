@@ -10,7 +10,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "cg_kernels.h"
@@ -165,6 +167,24 @@ static void unpack_pos(const unsigned char* in, long long n, double* dst) {
   }
 }
 
+// Run f(rep) for every replica on up to hardware_concurrency() host threads
+// (replicas taken in turn from a shared counter).
+template <class F>
+static void for_each_replica(int R, const F& f) {
+  unsigned nt = std::thread::hardware_concurrency();
+  if (nt < 1) nt = 1;
+  if (nt > 32) nt = 32;
+  if ((int)nt > R) nt = (unsigned)R;
+  std::atomic<int> next(0);
+  auto work = [&]() {
+    for (int r = next.fetch_add(1); r < R; r = next.fetch_add(1)) f(r);
+  };
+  std::vector<std::thread> pool;
+  for (unsigned t = 1; t < nt; t++) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+}
+
 extern "C" {
 
 const char* cg_last_error(void) { return g_err.c_str(); }
@@ -204,7 +224,7 @@ static int choose_shape(cg_sim* s, int w_req) {
   const size_t budget = std::min<size_t>(smem_per_sm / ctas_per_sm - 1024, 220 * 1024);
   const int lhb = 10;
   const long long sc = 48;
-  int lh = 12;
+  int lh = 10;  // at most 1,024 slots: the 32-bit split counters of a shared table cannot overflow
   for (; lh > 6; lh--) {
     s->layout(lh, sc);
     if (s->cta_layout(lhb, W) <= budget) break;
@@ -423,6 +443,98 @@ int cg_get_chain(cg_sim* s, int rep, double* r, double* t3, double* t2, int64_t*
     for (long long i = 0; i < n; i++)
       for (int b = 0; b < s->nb; b++) states[i * s->nb + b] = (pk[i] >> (8 * b)) & 0xFF;
   }
+  return CG_OK;
+}
+
+int cg_set_chains(cg_sim* s, const double* const* r, const double* const* t3, const double* const* t2,
+                  const int64_t* const* states) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  const long long N = s->total_beads;
+  const size_t pb = s->pos_bytes();
+  unsigned char* buf = s->staging(pb * N * 3 + 4 * N);
+  if (!buf) return fail(CG_ERR_NOMEM, "pinned staging allocation failed");
+  const double* const* src[3] = {r, t3, t2};
+  unsigned* pk = reinterpret_cast<unsigned*>(buf + pb * N * 3);
+  std::atomic<int> bad(0);
+  for_each_replica(s->R, [&](int rep) {
+    const long long n = s->n_beads[rep], off = s->bead_off[rep];
+    for (int k = 0; k < 3; k++) {
+      if (!src[k] || !src[k][rep]) continue;
+      const double* a = src[k][rep];
+      for (long long i = 0; i < 3 * n; i++)
+        if (!std::isfinite(a[i])) { bad.store(1); return; }
+      unsigned char* b = buf + pb * (N * k + off);
+      if (s->fp64) pack_pos<double>(a, n, b);
+      else pack_pos<float>(a, n, b);
+    }
+    if (states && states[rep]) {
+      for (long long i = 0; i < n; i++) {
+        unsigned w = 0;
+        for (int b = 0; b < s->nb; b++) {
+          const int64_t v = states[rep][i * s->nb + b];
+          if (v < 0 || v > CG_MAX_MARK) { bad.store(2); return; }
+          w |= (unsigned)v << (8 * b);
+        }
+        pk[off + i] = w;
+      }
+    }
+  });
+  if (bad.load() == 1) return fail(CG_ERR_NONFINITE, "non-finite position or tangent");
+  if (bad.load() == 2) return fail(CG_ERR_ARG, "binding states must be in 0..3");
+  // every replica given for an array, or none: one copy of the whole array
+  void* dst[3] = {s->r4, s->t34, s->t24};
+  for (int k = 0; k < 3; k++) {
+    if (!src[k]) continue;
+    bool all = true;
+    for (int rep = 0; rep < s->R; rep++) all = all && src[k][rep];
+    if (all) {
+      CUDA_TRY(cudaMemcpy(dst[k], buf + pb * N * k, pb * N, cudaMemcpyHostToDevice));
+    } else {
+      for (int rep = 0; rep < s->R; rep++)
+        if (src[k][rep])
+          CUDA_TRY(cudaMemcpy((char*)dst[k] + pb * s->bead_off[rep], buf + pb * (N * k + s->bead_off[rep]),
+                              pb * s->n_beads[rep], cudaMemcpyHostToDevice));
+    }
+  }
+  if (states) {
+    bool all = true;
+    for (int rep = 0; rep < s->R; rep++) all = all && states[rep];
+    if (all) {
+      CUDA_TRY(cudaMemcpy(s->states, pk, 4 * N, cudaMemcpyHostToDevice));
+    } else {
+      for (int rep = 0; rep < s->R; rep++)
+        if (states[rep])
+          CUDA_TRY(cudaMemcpy(s->states + s->bead_off[rep], pk + s->bead_off[rep], 4 * s->n_beads[rep],
+                              cudaMemcpyHostToDevice));
+    }
+  }
+  return CG_OK;
+}
+
+int cg_get_chains(cg_sim* s, double* const* r, double* const* t3, double* const* t2, int64_t* const* states) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  const long long N = s->total_beads;
+  const size_t pb = s->pos_bytes();
+  unsigned char* buf = s->staging(pb * N * 3 + 4 * N);
+  if (!buf) return fail(CG_ERR_NOMEM, "pinned staging allocation failed");
+  double* const* dst[3] = {r, t3, t2};
+  void* src[3] = {s->r4, s->t34, s->t24};
+  for (int k = 0; k < 3; k++)
+    if (dst[k]) CUDA_TRY(cudaMemcpy(buf + pb * N * k, src[k], pb * N, cudaMemcpyDeviceToHost));
+  unsigned* pk = reinterpret_cast<unsigned*>(buf + pb * N * 3);
+  if (states) CUDA_TRY(cudaMemcpy(pk, s->states, 4 * N, cudaMemcpyDeviceToHost));
+  for_each_replica(s->R, [&](int rep) {
+    const long long n = s->n_beads[rep], off = s->bead_off[rep];
+    for (int k = 0; k < 3; k++) {
+      if (!dst[k] || !dst[k][rep]) continue;
+      const unsigned char* b = buf + pb * (N * k + off);
+      if (s->fp64) unpack_pos<double>(b, n, dst[k][rep]);
+      else unpack_pos<float>(b, n, dst[k][rep]);
+    }
+    if (states && states[rep])
+      for (long long i = 0; i < n; i++)
+        for (int b = 0; b < s->nb; b++) states[rep][i * s->nb + b] = (pk[off + i] >> (8 * b)) & 0xFF;
+  });
   return CG_OK;
 }
 

@@ -27,8 +27,31 @@ __device__ __forceinline__ int hash_slot(int* keys, int* used, int* nused, int l
   return -1;
 }
 
-__device__ __forceinline__ void add_delta(long long* vals, int ncol, int slot, int col, long long d) {
-  if (d != 0) atomicAdd((unsigned long long*)&vals[(long long)slot * ncol + col], (unsigned long long)d);
+// Add d to column `col` of a hash entry.  Global-memory tables take one 64-bit
+// atomic.  Shared-memory tables (split = true) keep each column as two 32-bit
+// counters, d = hi * 2^21 + lo with lo in [0, 2^21): 32-bit shared atomics are
+// native and several times faster than 64-bit ones.  A shared table has at
+// most 1,024 slots and serves moves of m <= slots / 16 beads, so a column gets
+// at most 16 m <= 1,024 contributions of |d| < 2^42: |sum hi| < 2^10 * 3 * 2^19
+// and sum lo < 2^10 * 2^21, both below 2^31.
+__device__ __forceinline__ void add_delta(long long* vals, int ncol, int slot, int col, long long d,
+                                          bool split = false) {
+  if (d == 0) return;
+  long long* cell = &vals[(long long)slot * ncol + col];
+  if (split) {
+    int* half = reinterpret_cast<int*>(cell);
+    atomicAdd(half, (int)(d & 0x1FFFFF));
+    atomicAdd(half + 1, (int)(d >> 21));
+  } else {
+    atomicAdd((unsigned long long*)cell, (unsigned long long)d);
+  }
+}
+
+// Value of a hash column written by add_delta.
+__device__ __forceinline__ long long hash_delta(const long long* cell, bool split) {
+  if (!split) return *cell;
+  const int* half = reinterpret_cast<const int*>(cell);
+  return (long long)half[1] * 2097152LL + (long long)half[0];
 }
 
 // Linear probing for `key` after its home slot `start` was found taken by
@@ -56,7 +79,7 @@ template <typename Real>
 __device__ __forceinline__ void deposit_bead(const RepDev& rd, int ncol, int* keys, int* used,
                                              int* nused, long long* vals, int logH,
                                              const Real w[8], const int v[8], unsigned st,
-                                             bool negate, unsigned& err) {
+                                             bool negate, unsigned& err, bool split = false) {
   int slot[8], prev[8];
 #pragma unroll
   for (int l = 0; l < 8; l++) {
@@ -85,8 +108,9 @@ __device__ __forceinline__ void deposit_bead(const RepDev& rd, int ncol, int* ke
   for (int l = 0; l < 8; l++) {
     long long q = q40(w[l]);
     if (negate) q = -q;
-    add_delta(vals, ncol, slot[l], 0, q);
-    for (int b = 0; b < rd.nb; b++) add_delta(vals, ncol, slot[l], 1 + b, q * (long long)((st >> (8 * b)) & 0xFF));
+    add_delta(vals, ncol, slot[l], 0, q, split);
+    for (int b = 0; b < rd.nb; b++)
+      add_delta(vals, ncol, slot[l], 1 + b, q * (long long)((st >> (8 * b)) & 0xFF), split);
   }
 }
 
@@ -105,7 +129,7 @@ __device__ __forceinline__ double chi_term64(const RepDev& rd, double V, long lo
 // stores the post-move grid values into the hash values for the commit.
 static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
-                                  long long& n_vox, double) {
+                                  long long& n_vox, double, bool split = false) {
   const RepDev& rd = ws.rd;
   double part = 0;
   const long long* grid = a.grid + rd.vox_off * a.ncol;
@@ -114,11 +138,11 @@ static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, i
     int v = keys[slot];
     long long* d = vals + (long long)slot * hcol;
     const long long* gv = grid + (long long)v * a.ncol;
-    long long g0 = gv[0], d0 = d[0];
+    long long g0 = gv[0], d0 = hash_delta(d, split);
     double V = rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin;
     double c = 0, rho[CG_MAX_BINDERS], dd[CG_MAX_BINDERS];
     for (int b = 0; b < rd.nb; b++) {
-      long long gb = gv[1 + b], db = d[1 + b];
+      long long gb = gv[1 + b], db = hash_delta(d + 1 + b, split);
       rho[b] = ((double)gb * kFxInv) / V;
       dd[b] = ((double)db * kFxInv) / V;
       c += rd.pref[b] * (dd[b] * (2 * rho[b] + dd[b]));
@@ -139,7 +163,7 @@ static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, i
 // fraction limit take the FP64 branch so the 1e99 penalty is decided as in FP64.
 static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
-                                  long long& n_vox, float) {
+                                  long long& n_vox, float, bool split = false) {
   const RepDev& rd = ws.rd;
   double part = 0;
   const long long* grid = a.grid + rd.vox_off * a.ncol;
@@ -148,7 +172,7 @@ static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, i
     int v = keys[slot];
     long long* d = vals + (long long)slot * hcol;
     const long long* gv = grid + (long long)v * a.ncol;
-    long long g0 = gv[0], d0 = d[0];
+    long long g0 = gv[0], d0 = hash_delta(d, split);
     float sc = ws.f_scale, k = ws.f_k;
     double V = rd.vol_bin;
     if (rd.has_access) {
@@ -158,7 +182,7 @@ static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, i
     }
     float c = 0, rho[CG_MAX_BINDERS], dd[CG_MAX_BINDERS];
     for (int b = 0; b < rd.nb; b++) {
-      long long gb = gv[1 + b], db = d[1 + b];
+      long long gb = gv[1 + b], db = hash_delta(d + 1 + b, split);
       rho[b] = (float)gb * sc;
       dd[b] = (float)db * sc;
       c += ws.f_pref[b] * (dd[b] * (2.0f * rho[b] + dd[b]));

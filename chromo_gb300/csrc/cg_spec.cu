@@ -237,8 +237,8 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
           voxel_weights(rd, gf, r, w0, v0);
           voxel_weights(rd, gf, tr, w1, v1);
           unsigned s = st[i];
-          deposit_bead(rd, ncol, S.keys, S.used, nused, S.vals, S.logH, w0, v0, s, true, err);
-          deposit_bead(rd, ncol, S.keys, S.used, nused, S.vals, S.logH, w1, v1, s, false, err);
+          deposit_bead(rd, ncol, S.keys, S.used, nused, S.vals, S.logH, w0, v0, s, true, err, !gtab);
+          deposit_bead(rd, ncol, S.keys, S.used, nused, S.vals, S.logH, w1, v1, s, false, err, !gtab);
         }
       }
       err = __reduce_or_sync(kFull, err);
@@ -251,7 +251,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
         dEf = conf;
       }
       __syncwarp();
-      if (density) dEf += field_dE_voxels(ws, a, ncol, S.keys, S.used, S.vals, *nused, lane, nvox, (Real)0);
+      if (density) dEf += field_dE_voxels(ws, a, ncol, S.keys, S.used, S.vals, *nused, lane, nvox, (Real)0, !gtab);
     }
   } else if (kind == CG_TANGENT_ROTATION) {
     Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
@@ -399,7 +399,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
           for (int l = 0; l < 8; l++) {
             int slot = hash_slot(S.keys, S.used, nused, S.logH, v[l], err);
             if (slot < 0) break;
-            add_delta(S.vals, ncol, slot, 1 + bsel, q40(wv[l]) * (long long)(s_new - s_old));
+            add_delta(S.vals, ncol, slot, 1 + bsel, q40(wv[l]) * (long long)(s_new - s_old), !gtab);
           }
         }
       }
@@ -418,7 +418,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
       }
       __syncwarp();
       if (density) {
-        dEf += field_dE_voxels(ws, a, ncol, S.keys, S.used, S.vals, *nused, lane, nvox, (Real)0);
+        dEf += field_dE_voxels(ws, a, ncol, S.keys, S.used, S.vals, *nused, lane, nvox, (Real)0, !gtab);
         dEf += rd.intra[bsel] * (double)ddb;
       }
       if (lane == 0) P.bsel = bsel;

@@ -120,6 +120,17 @@ int cg_set_chain(cg_sim *sim, int32_t rep, const double *r, const double *t3, co
                  const int64_t *states, const int64_t *marks, const double *bonds);
 int cg_get_chain(cg_sim *sim, int32_t rep, double *r, double *t3, double *t2, int64_t *states);
 
+/* cg_set_chain / cg_get_chain for every replica in one call: r[rep], t3[rep],
+ * t2[rep] point to replica rep's [N_rep*3] arrays and states[rep] to its
+ * [N_rep*n_binders] array (a NULL array list, or a NULL entry, skips that
+ * array or replica).  The host-side conversion runs on several threads and
+ * each array crosses the bus in one copy; this is how a batch of chains is
+ * moved between the reference's per-polymer numpy arrays and the device. */
+int cg_set_chains(cg_sim *sim, const double *const *r, const double *const *t3,
+                  const double *const *t2, const int64_t *const *states);
+int cg_get_chains(cg_sim *sim, double *const *r, double *const *t3, double *const *t2,
+                  int64_t *const *states);
+
 /* Field of one replica; access_vol [G] or NULL when every voxel is fully
  * accessible (get_accessible_volumes, chromo/fields.pyx:714-768). */
 int cg_set_field(cg_sim *sim, int32_t rep, const cg_field_params *field, const double *access_vol);

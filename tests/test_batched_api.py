@@ -84,3 +84,22 @@ def test_run_exchange_permutes_chi_within_ladders():
         b.pull()
         assert [f.chi for f in fields] == list(got)
         assert np.all(np.abs(b.energy_drift()) < 1e-12)  # rebaselined after the swaps
+
+
+def test_all_replica_transfers_match_per_replica_calls():
+    """cg_set_chains / cg_get_chains move the same data as R single-replica calls."""
+    b, polys, _, _ = _batch(R=3)
+    with b:
+        b.run(3, 5)
+        b.sync()
+        whole = b.sim.get_chains()
+        for r in range(3):
+            single = b.sim.get_chain(r)
+            for x, y in zip(whole[r], single):
+                np.testing.assert_array_equal(x, y)
+        # push the host chains (the initial state) back and read them again
+        b.push()
+        again = b.sim.get_chains()
+        for r, p in enumerate(polys):
+            np.testing.assert_array_equal(again[r][0], p.r.astype(np.float32).astype(np.float64))
+            np.testing.assert_array_equal(again[r][3], p.states)

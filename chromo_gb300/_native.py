@@ -82,8 +82,10 @@ EXPORTS = [
     "cg_set_binding", "cg_set_controllers", "cg_get_controllers", "cg_deposit", "cg_get_density",
     "cg_run", "cg_sync", "cg_run_audit", "cg_energy", "cg_reset_running_energy", "cg_get_tally",
     "cg_reset_tally", "cg_exchange", "cg_get_chi", "cg_run_batched", "cg_get_launch_info",
-    "cg_field_energy_static", "cg_energies", "cg_set_chains", "cg_get_chains",
+    "cg_field_energy_static", "cg_energies", "cg_set_chains", "cg_get_chains", "cg_gradient",
+    "cg_sample_terms", "cg_get_samples",
 ]
+N_TERMS = 14
 
 
 def lib_path() -> Path:
@@ -126,6 +128,9 @@ def lib():
             "cg_energies": ([P, P, P], C.c_int),
             "cg_set_chains": ([P, P, P, P, P], C.c_int),
             "cg_get_chains": ([P, P, P, P, P], C.c_int),
+            "cg_gradient": ([P, P, P], C.c_int),
+            "cg_sample_terms": ([P, P], C.c_int),
+            "cg_get_samples": ([P, P, I32], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -292,6 +297,23 @@ class Sim:
         out = np.zeros((self.R, 5))
         check(lib().cg_energies(self.h, _ptr(out), stream))
         return out
+
+    def gradient(self, positions=True, terms=True):
+        """(dE/dr [total_beads, 3] FP32 or None, terms [R, 14] or None)."""
+        g = np.empty((int(self.n_beads.sum()), 3), dtype=np.float32) if positions else None
+        t = np.empty((self.R, N_TERMS)) if terms else None
+        check(lib().cg_gradient(self.h, _ptr(g), _ptr(t)))
+        return g, t
+
+    def sample_terms(self, stream=None):
+        check(lib().cg_sample_terms(self.h, stream))
+
+    def samples(self, reset=False):
+        """(sum T [R, 14], sum T T^T [R, 14, 14], count [R])."""
+        k = N_TERMS
+        out = np.empty((self.R, k + k * k + 1))
+        check(lib().cg_get_samples(self.h, _ptr(out), int(bool(reset))))
+        return out[:, :k], out[:, k:k + k * k].reshape(self.R, k, k), out[:, -1]
 
     def reset_running_energy(self):
         check(lib().cg_reset_running_energy(self.h))

@@ -22,6 +22,7 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 from . import _native as nat
+from .derivatives import observable_coefficients, reweighting_sensitivity, theta_coefficients
 from .fields import NullField, UniformDensityField
 from .mc import get_amplitude_bounds
 from .mc.mc_controller import SimpleControl, all_moves
@@ -151,6 +152,47 @@ class ReplicaBatch:
     @property
     def chi(self) -> np.ndarray:
         return self.sim.chi()
+
+    # ---------------------------------------------------------- derivatives
+    def _theta_coef(self, r):
+        p, f = self.polymers[r], self.fields[r]
+        binders = p.beads[0].binders
+        vol_bin = f.vol_bin if isinstance(f, UniformDensityField) else 1.0
+        return theta_coefficients([b.chemical_potential for b in binders],
+                                  float(getattr(p, "mu_adjust_factor", 1.0)),
+                                  [b.interaction_volume for b in binders], vol_bin)
+
+    def gradient(self):
+        """Per replica: dE/dr [N_r, 3] (FP32) and dE/d(chi, mu_0, mu_1, eps_00,
+        eps_11, eps_01) [6] (FP64) of the energy ``energies`` sums."""
+        g, T = self.sim.gradient()
+        per, off = [], 0
+        for p in self.polymers:
+            per.append(g[off:off + p.num_beads])
+            off += p.num_beads
+        theta = np.stack([self._theta_coef(r) @ T[r] for r in range(self.n_replicas)])
+        return per, theta
+
+    def sample(self, n_samples: int, steps_between: int, random_seed: int, stream=None):
+        """``n_samples`` times: ``steps_between`` MC steps, then add every
+        replica's energy terms to the running sums on the device."""
+        for k in range(int(n_samples)):
+            if steps_between:
+                self.sim.run(int(steps_between), int(random_seed) + k, stream)
+            self.sim.sample_terms(stream)
+        self.sim.sync(stream)
+
+    def sensitivities(self, reset: bool = False) -> np.ndarray:
+        """[R, n_binders + 1, 6]: d<O>/dtheta for O = mean occupancy of each
+        binder and the variance of the bead density over voxels, by
+        reweighting the sampled configurations (-Cov(O, dE/dtheta))."""
+        sum_t, sum_tt, count = self.sim.samples(reset)
+        out = []
+        for r, (p, f) in enumerate(zip(self.polymers, self.fields)):
+            n_vox = f.n_bins if isinstance(f, UniformDensityField) else 1
+            O = observable_coefficients(p.num_beads, n_vox, p.num_binders)
+            out.append(reweighting_sensitivity(sum_t[r], sum_tt[r], count[r], O, self._theta_coef(r)))
+        return np.stack(out)
 
     # ------------------------------------------------------------ read back
     def push(self):

@@ -88,6 +88,10 @@ struct cg_sim {
   int graph_rungs = -1;
   unsigned long long graph_seed = 0;
   cudaStream_t graph_stream = nullptr;
+  // derivatives: per-bead gradient, per-replica terms, running sums (allocated on first use)
+  float* grad = nullptr;
+  double* terms = nullptr;
+  double* acc = nullptr;
   // pinned host staging for chain uploads / downloads
   void* pinned = nullptr;
   size_t pinned_bytes = 0;
@@ -196,7 +200,7 @@ void cg_destroy(cg_sim* s) {
   void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
                   s->grid, s->access_vol, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
                   s->picked, s->d_picked_off, s->eout, s->aout, s->rep_of_rung, s->swaps,
-                  s->swap_attempts, s->xround};
+                  s->swap_attempts, s->xround, s->grad, s->terms, s->acc};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete s;
@@ -746,6 +750,44 @@ int cg_energies(cg_sim* s, double* out, void* stream) {
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(out, s->eout, sizeof(double) * 5 * s->R, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
+  return CG_OK;
+}
+
+static int ensure_derivative_buffers(cg_sim* s) {
+  if (!s->grad) CUDA_TRY(cudaMalloc(&s->grad, sizeof(float) * 3 * std::max(1LL, s->total_beads)));
+  if (!s->terms) CUDA_TRY(cudaMalloc(&s->terms, sizeof(double) * cg::kTerms * s->R));
+  if (!s->acc) {
+    CUDA_TRY(cudaMalloc(&s->acc, sizeof(double) * cg::kAccPerRep * s->R));
+    CUDA_TRY(cudaMemset(s->acc, 0, sizeof(double) * cg::kAccPerRep * s->R));
+  }
+  return CG_OK;
+}
+
+int cg_gradient(cg_sim* s, float* dEdr, double* terms) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (int rc = ensure_derivative_buffers(s)) return rc;
+  KArgs a = s->args();
+  if (dEdr) cg_launch_gradient(a, s->fp64 != 0, s->grad, s->max_beads, 0);
+  if (terms) cg_launch_terms(a, s->terms, nullptr, 0);
+  CUDA_TRY(cudaGetLastError());
+  if (dEdr) CUDA_TRY(cudaMemcpy(dEdr, s->grad, sizeof(float) * 3 * s->total_beads, cudaMemcpyDeviceToHost));
+  if (terms) CUDA_TRY(cudaMemcpy(terms, s->terms, sizeof(double) * cg::kTerms * s->R, cudaMemcpyDeviceToHost));
+  return CG_OK;
+}
+
+int cg_sample_terms(cg_sim* s, void* stream) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (int rc = ensure_derivative_buffers(s)) return rc;
+  cg_launch_terms(s->args(), nullptr, s->acc, (cudaStream_t)stream);
+  CUDA_TRY(cudaGetLastError());
+  return CG_OK;
+}
+
+int cg_get_samples(cg_sim* s, double* out, int reset) {
+  if (!s || !out) return fail(CG_ERR_ARG, "null argument");
+  if (int rc = ensure_derivative_buffers(s)) return rc;
+  CUDA_TRY(cudaMemcpy(out, s->acc, sizeof(double) * cg::kAccPerRep * s->R, cudaMemcpyDeviceToHost));
+  if (reset) CUDA_TRY(cudaMemset(s->acc, 0, sizeof(double) * cg::kAccPerRep * s->R));
   return CG_OK;
 }
 

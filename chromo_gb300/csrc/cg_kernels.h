@@ -119,5 +119,12 @@ void cg_launch_energy(const cg::KArgs& a, bool fp64, double* out, cudaStream_t s
 void cg_launch_chi_sum(const cg::KArgs& a, double* out, cudaStream_t s);
 // warps of the MC kernel that fit one SM's register file
 int cg_spec_warps_per_sm(bool fp64);
+
+namespace cg {
+constexpr int kTerms = 14;                                // energy terms per replica (cg_grad.cu)
+constexpr int kAccPerRep = kTerms + kTerms * kTerms + 1;  // running sums of T, T T^T, count
+}
+void cg_launch_gradient(const cg::KArgs& a, bool fp64, float* out, long long max_beads, cudaStream_t s);
+void cg_launch_terms(const cg::KArgs& a, double* terms, double* acc, cudaStream_t s);
 void cg_launch_exchange(const cg::KArgs& a, const double* eout, int n_rungs, long long round,
                         unsigned long long seed, cudaStream_t s);

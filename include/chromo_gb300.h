@@ -186,6 +186,27 @@ int cg_reset_running_energy(cg_sim *sim);
  * returns once out is filled. */
 int cg_energies(cg_sim *sim, double *out, void *stream);
 
+/* Derivatives of the energy cg_energy reports (elastic + binding + field in
+ * the form whose differences are the move dE); no counterpart in the
+ * reference, which has no derivatives.  dEdr [total beads x 3] FP32, replicas
+ * concatenated in creation order: dE/dr of every bead (the two bonds at the
+ * bead and the bead's eight trilinear weights), or NULL.  terms
+ * [n_replicas x 14] FP64, or NULL: [0] S = sum over voxels with vf <= vf_limit
+ * of (V/V_bead) vf^2 (= dE/dchi), [1..3] sum_v rho_b^2, [4..6] sum_v rho_0 rho_1,
+ * rho_0 rho_2, rho_1 rho_2, [7..9] number of beads with state_b == 2,
+ * [10..12] sum_i state_ib, [13] sum_v (bead density)^2; dE/d(mu_b) and
+ * dE/d(eps) are linear in them (field_prefactor, intranucleosome and
+ * cross-talk prefactors are linear in eps, chromo/fields.pyx:687-712).
+ * Synchronous. */
+int cg_gradient(cg_sim *sim, float *dEdr, double *terms);
+/* Add every replica's 14 terms T and their products T T^T to running sums on
+ * the device (enqueued on `stream`), for reweighting: the covariance of any
+ * two linear combinations of the terms follows from the sums. */
+int cg_sample_terms(cg_sim *sim, void *stream);
+/* Running sums [n_replicas x (14 + 196 + 1)]: sum T, sum T T^T (row major),
+ * number of samples; reset != 0 zeroes them after reading. */
+int cg_get_samples(cg_sim *sim, double *out, int32_t reset);
+
 /* Per-replica, per-move tallies [5 * 6]: attempts, accepts, beads moved,
  * voxels touched, beads moved in accepted moves, voxels touched in accepted
  * moves.  Used for the algorithmic-bytes roofline. */

@@ -147,41 +147,23 @@ class ClockSampler:
 
 
 def dist_init(args):
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    return rank, world, local
+    from chromo_gb300 import distributed
+    return distributed.init("nccl")
 
 
 def barrier(world):
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
+    from chromo_gb300 import distributed
+    distributed.barrier(world)
 
 
 def allreduce_max(x, world):
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from chromo_gb300 import distributed
+    return distributed.allreduce(x, "max", world)
 
 
 def allreduce_sum(x, world):
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    from chromo_gb300 import distributed
+    return distributed.allreduce(x, "sum", world)
 
 
 def reference_arm(args, rank, world):

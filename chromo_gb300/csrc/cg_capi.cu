@@ -62,6 +62,7 @@ struct cg_sim {
   void *r4 = nullptr, *t34 = nullptr, *t24 = nullptr;
   unsigned *states = nullptr, *marks = nullptr;
   double* bonds = nullptr;
+  float* bonds32 = nullptr;  // FP32 copy, 8 floats per bead: eb, g, ep, epp, eta, pad
   long long* grid = nullptr;
   double* access_vol = nullptr;
   int *g_keys = nullptr, *g_used = nullptr, *g_bslot = nullptr;
@@ -114,6 +115,7 @@ struct cg_sim {
     KArgs a{};
     a.reps = reps; a.ctl = ctl; a.n_ctl = n_ctl; a.n_reps = R; a.tally = tally;
     a.r4 = r4; a.t34 = t34; a.t24 = t24; a.states = states; a.marks = marks; a.bonds = bonds;
+    a.bonds32 = bonds32;
     a.grid = grid; a.access_vol = access_vol; a.ncol = ncol; a.hcol = nb + 1;
     a.g_keys = g_keys; a.g_used = g_used; a.g_bslot = g_bslot; a.g_vals = g_vals; a.g_logH = g_logH;
     a.g_stage = g_stage; a.g_idx = g_idx; a.g_stage_cap = g_stage_cap;
@@ -198,7 +200,7 @@ void cg_destroy(cg_sim* s) {
   if (s->graph) cudaGraphExecDestroy(s->graph);
   if (s->pinned) cudaFreeHost(s->pinned);
   void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
-                  s->grid, s->access_vol, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
+                  s->bonds32, s->grid, s->access_vol, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
                   s->picked, s->d_picked_off, s->eout, s->aout, s->rep_of_rung, s->swaps,
                   s->swap_attempts, s->xround, s->grad, s->terms, s->acc};
   for (void* p : ptrs)
@@ -302,6 +304,7 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   ALLOC(s->states, 4 * s->total_beads);
   ALLOC(s->marks, 4 * s->total_beads);
   ALLOC(s->bonds, 6 * 8 * s->total_beads);
+  ALLOC(s->bonds32, 8 * 4 * s->total_beads);
   ALLOC(s->grid, 8 * s->ncol * s->total_vox);
   if (s->nonuniform) ALLOC(s->access_vol, 8 * s->total_vox);
   ALLOC(s->g_keys, 4 * Hg * RW);
@@ -332,6 +335,7 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   cudaMemset(s->states, 0, 4 * s->total_beads);
   cudaMemset(s->marks, 0, 4 * s->total_beads);
   cudaMemset(s->bonds, 0, 48 * s->total_beads);
+  cudaMemset(s->bonds32, 0, 32 * s->total_beads);
   cudaMemset(s->grid, 0, 8 * s->ncol * s->total_vox);
   cudaMemset(s->g_keys, 0xFF, 4 * Hg * RW);
   cudaMemset(s->g_bslot, 0xFF, 4 * Hg * RW);
@@ -424,6 +428,10 @@ int cg_set_chain(cg_sim* s, int rep, const double* r, const double* t3, const do
     for (long long i = 0; i + 1 < n; i++)
       for (int j = 0; j < 5; j++) bb[6 * i + j] = bonds[5 * i + j];
     CUDA_TRY(cudaMemcpy(s->bonds + 6 * off, bb.data(), 8 * 6 * n, cudaMemcpyHostToDevice));
+    std::vector<float> bf(8 * n, 0.0f);
+    for (long long i = 0; i + 1 < n; i++)
+      for (int j = 0; j < 5; j++) bf[8 * i + j] = (float)bonds[5 * i + j];
+    CUDA_TRY(cudaMemcpy(s->bonds32 + 8 * off, bf.data(), 4 * 8 * n, cudaMemcpyHostToDevice));
   }
   return CG_OK;
 }

@@ -128,7 +128,10 @@ __device__ __forceinline__ double unif(unsigned x) {
   double a = (double)x * 0x1p-31;
   return __fma_rn(a, 0x1.00000002p-31, a);
 }
-__device__ __forceinline__ float unif32(unsigned x) { return (float)unif(x); }
+// x / (2^31 - 1) to within 2^-23 relative, in FP32 only: the fast paths below
+// use it with margins far above that error and fall back to unif() near a
+// decision boundary.
+__device__ __forceinline__ float unif32(unsigned x) { return (float)x * 4.656612873077393e-10f; }
 
 // floor(-log10(u + 1e-5) * window * 0.45 + 1.0001) (bead_selection.pyx:56-65)
 // evaluated in FP32 when the result is unambiguous, else in FP64, so the
@@ -139,6 +142,17 @@ __device__ __forceinline__ long long sel_floor(unsigned x, long long window) {
   float margin = 1e-3f + 1e-6f * y;
   if (y - fl > margin && fl + 1.0f - y > margin) return (long long)fl;
   return (long long)(-log10(unif(x) + 0.00001) * (double)window * 0.45 + 1.0001);
+}
+
+// int(unif(x) * n) (the bound_0 draw of crank_shaft, move_funcs.pyx:64): in
+// FP32 when the product is clear of an integer by more than its rounding
+// error (relative error below 2e-7), else in FP64; same integer either way.
+__device__ __forceinline__ long long scaled_index(unsigned x, long long n) {
+  float y = unif32(x) * (float)n;
+  float fl = floorf(y);
+  float margin = 1e-4f + 4e-7f * y;
+  if (y - fl > margin && fl + 1.0f - y > margin) return (long long)fl;
+  return (int)(unif(x) * (double)n);
 }
 
 // The Metropolis test u < exp(t) (mc_sim.pyx:164-171) with u = unif(x):
@@ -156,6 +170,55 @@ __device__ __forceinline__ bool metropolis(unsigned x, double t) {
     return false;
   }
   return u < exp(t);
+}
+
+// ---------------------------------------------------------------- FP32 sums
+// dE of the FP32 path is accumulated as an unevaluated sum hi + lo of two
+// binary32 numbers (Knuth's TwoSum; Dekker's renormalisation): error about
+// 2^-44 relative, and no FP64 instruction, which runs at 1/64 of the FP32
+// rate on GB300.  Both operands enter symmetrically (the TwoSum error term is
+// the exact rounding error), so a butterfly reduction leaves every lane with
+// the same bits.
+struct FF { float hi, lo; };
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  float s = a.hi + b.hi;
+  float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e += a.lo + b.lo;
+  float hi = s + e;
+  return FF{hi, e - (hi - s)};
+}
+__device__ __forceinline__ FF ff_add(FF a, float b) { return ff_add(a, FF{b, 0.0f}); }
+__device__ __forceinline__ double ff_d(FF a) { return (double)a.hi + (double)a.lo; }
+
+// Accumulator of the arithmetic of each storage type: FP64 storage sums in
+// FP64 (the reference's arithmetic), FP32 storage in FF.
+template <typename Real> struct AccOf { using type = double; };
+template <> struct AccOf<float> { using type = FF; };
+__device__ __forceinline__ void acc_add(double& s, double v) { s += v; }
+__device__ __forceinline__ void acc_add(FF& s, FF v) { s = ff_add(s, v); }
+__device__ __forceinline__ void acc_add(FF& s, float v) { s = ff_add(s, v); }
+__device__ __forceinline__ double acc_d(double v) { return v; }
+__device__ __forceinline__ double acc_d(FF v) { return ff_d(v); }
+template <typename A> __device__ __forceinline__ A acc_zero();
+template <> __device__ __forceinline__ double acc_zero<double>() { return 0.0; }
+template <> __device__ __forceinline__ FF acc_zero<FF>() { return FF{0.0f, 0.0f}; }
+
+// The Metropolis test of the FP32 path on t = -dE held as hi + lo: decided in
+// FP32 when u and exp(t) differ by more than 1e-4 relative (the FP32 errors of
+// u, exp and of dropping lo stay below 1e-5 for |t| <= 80), else by
+// metropolis() on the FP64 value of t.
+__device__ __forceinline__ bool metropolis_ff(unsigned x, FF t) {
+  const float th = t.hi;
+  if (th > 81.0f) return true;
+  if (th < -81.0f && x != 0u) return false;
+  if (th >= -80.0f && th <= 80.0f) {
+    const float u = unif32(x), e = expf(th);
+    if (u < e * 0.9999f) return true;
+    if (u > e * 1.0001f) return false;
+  }
+  return metropolis(x, ff_d(t));
 }
 
 // ---------------------------------------------------------------- bead selection
@@ -294,6 +357,16 @@ __device__ __forceinline__ Bond<Real> load_bond(const double* bonds, long long i
   return Bond<Real>{(Real)b[0], (Real)b[1], (Real)b[2], (Real)b[3], (Real)b[4]};
 }
 
+// Bond i of the storage type's arithmetic: FP64 parameters for FP64 storage,
+// their FP32 copy (one 16-byte and one 4-byte load) for FP32 storage.
+__device__ __forceinline__ Bond<double> bond_at(const double* b64, const float*, long long i, double) {
+  return load_bond<double>(b64, i);
+}
+__device__ __forceinline__ Bond<float> bond_at(const double*, const float* b32, long long i, float) {
+  const float4 q = *reinterpret_cast<const float4*>(b32 + 8 * i);
+  return Bond<float>{q.x, q.y, q.z, q.w, b32[8 * i + 4]};
+}
+
 template <typename Real>
 __device__ __forceinline__ Real e_pair(const Bond<Real>& b, const Real bend[3], Real par, const Real dp[3]) {
   Real x = par - b.g;
@@ -338,12 +411,19 @@ __device__ __forceinline__ double pair_dE_rev(const Bond<Real>& b, const Real r0
   return (double)e_pair(b, bt, pt, dpt) - (double)e_pair(b, bc, pc, dp);
 }
 
+// (x + y + z) / 2 as FF
+__device__ __forceinline__ FF half_sum3(float x, float y, float z) {
+  FF s = ff_add(FF{x, 0.0f}, y);
+  s = ff_add(s, z);
+  return FF{0.5f * s.hi, 0.5f * s.lo};
+}
+
 // FP32 evaluation of E_pair(trial) - E_pair(current) in difference form:
 // |b_t|^2 - |b_c|^2 = sum (b_t - b_c)(b_t + b_c) and likewise for the other
 // two terms, with the differences formed from the (small) input differences,
 // so the rounding error scales with dE rather than with E.
 // Forward bond (bead 1 moved; bead 0 and its tangent fixed).
-__device__ __forceinline__ double pair_dE_fwd(const Bond<float>& b, const float r0[3], const float r1[3],
+__device__ __forceinline__ FF pair_dE_fwd(const Bond<float>& b, const float r0[3], const float r1[3],
                                               const float tr1[3], const float t30[3],
                                               const float t31[3], const float tt31[3]) {
   float drt[3], dr[3], ddr[3];
@@ -361,11 +441,11 @@ __device__ __forceinline__ double pair_dE_fwd(const Bond<float>& b, const float 
     e_perp += ddp * (dpt + dp);
     e_bend += db * (bt + bc);
   }
-  return 0.5 * ((double)(b.eb * e_bend) + (double)(b.ep * e_par) + (double)(b.epp * e_perp));
+  return half_sum3(b.eb * e_bend, b.ep * e_par, b.epp * e_perp);
 }
 
 // Reverse bond (bead 0 moved; bead 1 fixed).
-__device__ __forceinline__ double pair_dE_rev(const Bond<float>& b, const float r0[3], const float tr0[3],
+__device__ __forceinline__ FF pair_dE_rev(const Bond<float>& b, const float r0[3], const float tr0[3],
                                               const float r1[3], const float t30[3],
                                               const float tt30[3], const float t31[3]) {
   float drt[3], dr[3], ddr[3], dt[3];
@@ -386,7 +466,7 @@ __device__ __forceinline__ double pair_dE_rev(const Bond<float>& b, const float 
     e_perp += ddp * (dpt + dp);
     e_bend += db * (bt + bc);
   }
-  return 0.5 * ((double)(b.eb * e_bend) + (double)(b.ep * e_par) + (double)(b.epp * e_perp));
+  return half_sum3(b.eb * e_bend, b.ep * e_par, b.epp * e_perp);
 }
 
 // ---------------------------------------------------------------- density field
@@ -482,13 +562,19 @@ __device__ __forceinline__ void voxel_weights(const RepDev&, const GridF& gf, co
 }
 
 __device__ __forceinline__ long long q40(double w) { return __double2ll_rn(w * kFxScale); }
-__device__ __forceinline__ long long q40(float w) { return __float2ll_rn(w * 1099511627776.0f); }
+__device__ __forceinline__ long long q40(float w) { return cgm_q40f(w); }
 
 // ---------------------------------------------------------------- warp helpers
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+__device__ __forceinline__ FF warp_sum(FF v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v = ff_add(v, FF{__shfl_xor_sync(kFull, v.hi, o), __shfl_xor_sync(kFull, v.lo, o)});
   return v;
 }
 __device__ __forceinline__ long long warp_sum_ll(long long v) {

@@ -24,6 +24,10 @@ struct WarpShared {
   float f_vb;     // bead volume
   float f_k;      // chi * vol_bin / bead volume
   float f_lim;    // vf_limit
+  // FP32 copies of the binding constants: free energy table, effective
+  // chemical potential (mu (2 - f) for mu > 0, else mu f), intranucleosome term
+  float f_bind[CG_MAX_BINDERS * (CG_MAX_MARK + 1) * (CG_MAX_MARK + 1)];
+  float f_me[CG_MAX_BINDERS], f_intra[CG_MAX_BINDERS];
   int nused;
   int pad[3];
 };
@@ -68,6 +72,7 @@ struct KArgs {
   unsigned* states;           // packed int8 binding states per bead
   unsigned* marks;            // packed int8 chemical_mods per bead
   const double* bonds;        // 6 doubles per bead (bond i -> i+1)
+  const float* bonds32;       // the same in FP32, 8 floats per bead (16-byte aligned rows)
   long long* grid;            // ncol int64 per voxel
   const double* access_vol;   // per voxel, or null
   int ncol;   // grid columns per voxel (2 or 4: rows padded to 16 or 32 bytes)

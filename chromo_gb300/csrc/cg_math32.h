@@ -97,4 +97,22 @@ CGM_FN float cgm_acosf(float x)
 /* 24-bit uniform in [0, 1) from a 31-bit draw (exact in binary32) */
 CGM_FN float cgm_unif24(unsigned x) { return (float)(x >> 7) * 5.9604644775390625e-08f; }
 
+/*
+ * round(w * 2^40), ties to even, for 0 <= w <= 1: the fixed-point value of a
+ * trilinear weight, with 32-bit conversions only (a conversion of a float to
+ * a 64-bit integer runs at the FP64 rate on GB300).  a = w * 2^30 is exact;
+ * w * 2^40 = floor(a) * 2^10 + f * 2^10 with f = a - floor(a) exact (Sterbenz
+ * for a >= 1, f = a below), and floor(a) * 2^10 is even, so rounding f * 2^10
+ * (exact: a power-of-two scaling of a number below 1) to nearest-even rounds
+ * the whole.  Equals llrint((double)w * 2^40) for every binary32 w in [0, 1]
+ * (checked exhaustively in the test suite).
+ */
+CGM_FN long long cgm_q40f(float w)
+{
+    float a = w * 1073741824.0f;
+    float fl = floorf(a);
+    float fr = (a - fl) * 1024.0f;
+    return (long long)(int)fl * 1024LL + (long long)(int)rintf(fr);
+}
+
 #endif /* CG_MATH32_H */

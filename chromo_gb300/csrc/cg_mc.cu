@@ -56,15 +56,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
     if (lane == 0) ws.nused = 0;
   }
   __syncwarp();
-  if (lane == 0) {
-    make_gridf(ws.rd, ws.gf);
-    for (int b = 0; b < CG_MAX_BINDERS; b++) ws.f_pref[b] = (float)ws.rd.pref[b];
-    for (int b = 0; b < CG_MAX_BINDERS * CG_MAX_BINDERS; b++) ws.f_xpref[b] = (float)ws.rd.xpref[b];
-    ws.f_scale = (float)(kFxInv / ws.rd.vol_bin);
-    ws.f_vb = (float)ws.rd.bead_vol;
-    ws.f_k = (float)(ws.rd.chi * (ws.rd.vol_bin / ws.rd.bead_vol));
-    ws.f_lim = (float)ws.rd.vf_limit;
-  }
+  if (lane == 0) setup_f32(ws);
   __syncwarp();
   using Real = Pos;
   const RepDev& rd = ws.rd;
@@ -79,6 +71,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
   unsigned* st = a.states + rd.bead_off;
   const unsigned* mk = a.marks + rd.bead_off;
   const double* bonds = a.bonds + rd.bead_off * 6;
+  const float* bonds32 = a.bonds32 + rd.bead_off * 8;
   // per-replica global scratch (used when a move is too large for shared memory)
   const long long gi = (long long)rep * a.spec_w;  // the replica's first warp region
   int* g_keys = a.g_keys + gi * (1 << a.g_logH);
@@ -113,7 +106,10 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
           if (lane == 0) c.num_attempt += 1;  // moves.pyx:151
           long long ind0 = 0, indf = 0, m = 0;
           int bsel = -1;
-          double dEp = 0, dEf = 0;
+          // dE = dEp (polymer) + dEs (field, FF for FP32 storage) + dEh (FP64 part)
+          using Acc = typename AccOf<Real>::type;
+          Acc dEp = acc_zero<Acc>(), dEs = acc_zero<Acc>();
+          double dEh = 0;
           long long nvox = 0;
           bool empty = false;
           int* keys = s_keys; int* used = s_used; long long* vals = s_vals; int logH = a.logH;
@@ -124,7 +120,8 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
             Real Md[3][4];
             if (kind == CG_CRANK_SHAFT) {  // move_funcs.pyx:39-101, 157-280
               Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
-              long long b0 = (int)(unif(g.next()) * (double)N);
+              const unsigned xb0 = g.next();
+              long long b0 = sizeof(Real) == 4 ? scaled_index(xb0, N) : (long long)(int)(unif(xb0) * (double)N);
               long long b1 = from_point(g, c.amp_bead, N, b0, err);
               if (b1 < 1) b1 = 1;
               check_bead_bounds(b0, b1, N, ind0, indf);
@@ -184,7 +181,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
               if (m > a.stage_cap) { stage = g_stage; }
               const bool smem_hash = 16 * m * 2 <= (1LL << a.logH);
               if (!smem_hash) { keys = g_keys; used = g_used; vals = g_vals; logH = a.g_logH; }
-              double part = 0;
+              Acc part = acc_zero<Acc>();
               int oob = 0;
               for (long long k = lane; k < m; k += 32) {
                 const long long i = ind0 + k;
@@ -211,12 +208,12 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
                 if (k == 0 && ind0 != 0) {  // continuous_dE_poly forward bond, polymers.pyx:1121-1131
                   Real r0[3], t30[3];
                   ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
-                  part += pair_dE_fwd(load_bond<Real>(bonds, i - 1), r0, r, tr, t30, t3, tt3);
+                  acc_add(part, pair_dE_fwd(bond_at(bonds, bonds32, i - 1, (Real)0), r0, r, tr, t30, t3, tt3));
                 }
                 if (k == m - 1 && indf != N) {  // reverse bond, polymers.pyx:1132-1142
                   Real r1[3], t31[3];
                   ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
-                  part += pair_dE_rev(load_bond<Real>(bonds, i), r, tr, r1, t3, tt3, t31);
+                  acc_add(part, pair_dE_rev(bond_at(bonds, bonds32, i, (Real)0), r, tr, r1, t3, tt3, t31));
                 }
                 if (check_field && rd.confine_kind) {
                   oob += out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
@@ -233,17 +230,17 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
               }
               err = __reduce_or_sync(kFull, err);
               dEp = warp_sum(part);
-              if (check_field) {
+              if (check_field && rd.confine_kind) {
                 int oo = __reduce_add_sync(kFull, (unsigned)oob);
                 double conf = 0;
                 conf += (double)(oo >> 16) * kEHugeField;
                 conf -= (double)(oo & 0xFFFF) * kEHugeField;
-                dEf = conf;
+                dEh = conf;
               }
               __syncwarp();
               if (density) {
                 int nu = ws.nused;
-                dEf += field_dE_voxels(ws, a, ncol, keys, used, vals, nu, lane, nvox, (Real)0);
+                field_dE_voxels(ws, a, ncol, keys, used, vals, nu, lane, nvox, dEs, dEh);
               }
             }
           } else if (kind == CG_TANGENT_ROTATION) {
@@ -292,7 +289,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
             }
             if (err) break;
             const unsigned long long axis_base = g.pos;
-            double part = 0;
+            Acc part = acc_zero<Acc>();
             Real sa, ca;
             rsincos(ang, &sa, &ca);
             for (long long k = lane; k < m; k += 32) {
@@ -318,18 +315,18 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
               }
               Pos* sg = stage + k * 9;
               for (int j = 0; j < 3; j++) { sg[3 + j] = (Pos)tt3[j]; sg[6 + j] = (Pos)tt2[j]; }
-              double de = 0;
+              Acc de = acc_zero<Acc>();
               if (i != 0) {
                 Real r0[3], t30[3];
                 ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
-                de += pair_dE_fwd(load_bond<Real>(bonds, i - 1), r0, r, r, t30, t3, tt3);
+                acc_add(de, pair_dE_fwd(bond_at(bonds, bonds32, i - 1, (Real)0), r0, r, r, t30, t3, tt3));
               }
               if (i + 1 != N) {
                 Real r1[3], t31[3];
                 ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
-                de += pair_dE_rev(load_bond<Real>(bonds, i), r, r, r1, t3, tt3, t31);
+                acc_add(de, pair_dE_rev(bond_at(bonds, bonds32, i, (Real)0), r, r, r1, t3, tt3, t31));
               }
-              part += de;
+              acc_add(part, de);
             }
             g.pos = axis_base + 2 * (unsigned long long)m;
             err = __reduce_or_sync(kFull, err);
@@ -347,7 +344,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
             if (m > a.stage_cap) idx = g_idx;
             const bool smem_hash = 8 * m * 2 <= (1LL << a.logH);
             if (!smem_hash) { keys = g_keys; used = g_used; vals = g_vals; logH = a.g_logH; }
-            double part = 0;
+            Acc part = acc_zero<Acc>();
             int dbl = 0;  // doubly-bound trial minus current, chosen binder (fields.pyx:1877-1937)
             for (long long k = lane; k < m; k += 32) {
               const long long i = ind0 + k;
@@ -357,33 +354,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
               unsigned sw = st[i], mw = mk[i];
               int s_old = (int)((sw >> (8 * bsel)) & 0xFF);
               // bead_binding_dE, polymers.pyx:1408-1538
-              double de = 0;
-              if (rd.max_binders != -1) {
-                int tot_t = 0, tot_c = 0;
-                for (int h = 0; h < rd.nb; h++) {
-                  int sh = (int)((sw >> (8 * h)) & 0xFF);
-                  tot_c += sh;
-                  tot_t += h == bsel ? s_new : sh;
-                }
-                if (tot_t > rd.max_binders) de += kEHugePoly * (double)(tot_t - rd.max_binders);
-                if (tot_c > rd.max_binders) de -= kEHugePoly * (double)(tot_c - rd.max_binders);
-              }
-              for (int b = 0; b < rd.nb; b++) {
-                int sc = (int)((sw >> (8 * b)) & 0xFF);
-                int stt = b == bsel ? s_new : sc;
-                int nm = (int)((mw >> (8 * b)) & 0xFF);
-                de += bind_f(rd, b, nm, stt);
-                de -= bind_f(rd, b, nm, sc);
-                if (rd.mu[b] > 0) {
-                  double me = rd.mu[b] * (-rd.mu_adjust + 2);
-                  de -= (double)stt * me;
-                  de += (double)sc * me;
-                } else {
-                  de -= (double)stt * rd.mu[b] * rd.mu_adjust;
-                  de += (double)sc * rd.mu[b] * rd.mu_adjust;
-                }
-              }
-              part += de;
+              acc_add(part, bead_bind_dE(ws, sw, mw, bsel, s_new, (Real)0));
               dbl += (s_new == 2 ? 1 : 0) - (s_old == 2 ? 1 : 0);
               idx[k] = s_new;
               if (density && s_new != s_old) {
@@ -411,13 +382,13 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
                 ld3(r4, ind0 + k, p);
                 oob += out_of_bounds(rd, p, true);
               }
-              dEf = (double)__reduce_add_sync(kFull, (unsigned)oob) * kEHugeField;
+              dEh = (double)__reduce_add_sync(kFull, (unsigned)oob) * kEHugeField;
             }
             __syncwarp();
             if (density) {
               int nu = ws.nused;
-              dEf += field_dE_voxels(ws, a, ncol, keys, used, vals, nu, lane, nvox, (Real)0);
-              dEf += rd.intra[bsel] * (double)ddb;
+              field_dE_voxels(ws, a, ncol, keys, used, vals, nu, lane, nvox, dEs, dEh);
+              add_intra(ws, bsel, ddb, dEs, dEh);
             }
           }
           if (AUDIT && g.fail) err |= E_STREAM;
@@ -426,9 +397,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
           int accepted = -1;
           if (!empty) {
             double dE = 0;
-            dE += dEp;
-            dE += dEf;
-            bool acc = metropolis(g.next(), -dE);
+            bool acc = decide(g.next(), dEp, dEs, dEh, &dE);
             if (AUDIT && g.fail) { err |= E_STREAM; break; }
             accepted = acc ? 1 : 0;
             if (acc) {
@@ -483,7 +452,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
           if (AUDIT && lane == 0 && nrec < a.a_max_recs) {
             cg_move_record rec;
             rec.kind = kind; rec.n_inds = (int)m; rec.ind0 = (int)ind0; rec.indf = (int)indf;
-            rec.dE_poly = empty ? 0.0 : dEp; rec.dE_field = empty ? 0.0 : dEf;
+            rec.dE_poly = empty ? 0.0 : acc_d(dEp); rec.dE_field = empty ? 0.0 : acc_d(dEs) + dEh;
             rec.accepted = accepted; rec.n_draws = (int)(g.pos - draw0);
             a.a_recs[nrec] = rec;
           }

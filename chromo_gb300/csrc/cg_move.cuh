@@ -8,6 +8,24 @@
 
 namespace cg {
 
+// FP32 copies of a replica's field and binding constants (one thread).
+__device__ __forceinline__ void setup_f32(WarpShared& ws) {
+  const RepDev& rd = ws.rd;
+  make_gridf(rd, ws.gf);
+  for (int b = 0; b < CG_MAX_BINDERS; b++) ws.f_pref[b] = (float)rd.pref[b];
+  for (int b = 0; b < CG_MAX_BINDERS * CG_MAX_BINDERS; b++) ws.f_xpref[b] = (float)rd.xpref[b];
+  ws.f_scale = (float)(kFxInv / rd.vol_bin);
+  ws.f_vb = (float)rd.bead_vol;
+  ws.f_k = (float)(rd.chi * (rd.vol_bin / rd.bead_vol));
+  ws.f_lim = (float)rd.vf_limit;
+  for (int i = 0; i < CG_MAX_BINDERS * (CG_MAX_MARK + 1) * (CG_MAX_MARK + 1); i++)
+    ws.f_bind[i] = (float)rd.bind_f[i];
+  for (int b = 0; b < CG_MAX_BINDERS; b++) {
+    ws.f_me[b] = (float)(rd.mu[b] > 0 ? rd.mu[b] * (-rd.mu_adjust + 2) : rd.mu[b] * rd.mu_adjust);
+    ws.f_intra[b] = (float)rd.intra[b];
+  }
+}
+
 // ---------------------------------------------------------------- hash insert
 __device__ __forceinline__ int hash_slot(int* keys, int* used, int* nused, int logH, int key,
                                          unsigned& err) {
@@ -126,10 +144,11 @@ __device__ __forceinline__ double chi_term64(const RepDev& rd, double V, long lo
 }
 
 // Field dE over the touched voxels (fixed-point grid), FP64 arithmetic; also
-// stores the post-move grid values into the hash values for the commit.
-static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
+// stores the post-move grid values into the hash values for the commit.  The
+// sum is added to `hard` (the FP64 part of the move's dE), nothing to `soft`.
+static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
-                                  long long& n_vox, double, bool split = false) {
+                                  long long& n_vox, double& soft, double& hard, bool split = false) {
   const RepDev& rd = ws.rd;
   double part = 0;
   const long long* grid = a.grid + rd.vox_off * a.ncol;
@@ -156,16 +175,21 @@ static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, i
     part += c;
   }
   n_vox = nused;
-  return warp_sum(part);
+  (void)soft;
+  hard += warp_sum(part);
 }
 
-// FP32 arithmetic per voxel, FP64 accumulation; voxels at or near the volume
-// fraction limit take the FP64 branch so the 1e99 penalty is decided as in FP64.
-static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
+// FP32 arithmetic per voxel, FF accumulation into `soft`; voxels at or near
+// the volume-fraction limit take the FP64 branch, summed into `hard`, so the
+// 1e99 penalty is decided as in FP64 (FP64 instructions only when some lane
+// met such a voxel).
+static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
-                                  long long& n_vox, float, bool split = false) {
+                                  long long& n_vox, FF& soft, double& hard, bool split = false) {
   const RepDev& rd = ws.rd;
-  double part = 0;
+  FF part = FF{0.0f, 0.0f};
+  double huge = 0;
+  bool rare = false;
   const long long* grid = a.grid + rd.vox_off * a.ncol;
   for (int i = lane; i < nused; i += 32) {
     int slot = used[i];
@@ -194,14 +218,17 @@ static __device__ double field_dE_voxels(const WarpShared& ws, const KArgs& a, i
     float vf0 = (float)g0 * sc * ws.f_vb;
     float dvf = (float)d0 * sc * ws.f_vb;
     if (vf0 > ws.f_lim - 1e-3f || vf0 + dvf > ws.f_lim - 1e-3f) {
-      part += (double)c + chi_term64(rd, V, g0, d0);
+      part = ff_add(part, c);
+      huge += chi_term64(rd, V, g0, d0);
+      rare = true;
     } else {
-      part += (double)(c + k * (dvf * (2.0f * vf0 + dvf)));
+      part = ff_add(part, c + k * (dvf * (2.0f * vf0 + dvf)));
     }
     d[0] = g0 + d0;
   }
   n_vox = nused;
-  return warp_sum(part);
+  soft = ff_add(soft, warp_sum(part));
+  if (__any_sync(kFull, rare)) hard += warp_sum(huge);
 }
 
 __device__ __forceinline__ void commit_grid(const RepDev& rd, const KArgs& a, int hcol, int* keys,
@@ -235,6 +262,99 @@ __device__ __forceinline__ int out_of_bounds(const RepDev& rd, const Real q[3], 
 
 __device__ __forceinline__ double bind_f(const RepDev& rd, int b, int nm, int s) {
   return rd.bind_f[(b * (CG_MAX_MARK + 1) + nm) * (CG_MAX_MARK + 1) + s];
+}
+
+// bead_binding_dE (chromo/polymers.pyx:1408-1538) of one bead whose binder
+// `bsel` goes from its current state (packed in sw, marks in mw) to s_new.
+// FP64 storage: the reference's FP64 arithmetic.
+__device__ __forceinline__ double bead_bind_dE(const WarpShared& ws, unsigned sw, unsigned mw, int bsel,
+                                               int s_new, double) {
+  const RepDev& rd = ws.rd;
+  double de = 0;
+  if (rd.max_binders != -1) {
+    int tot_t = 0, tot_c = 0;
+    for (int h = 0; h < rd.nb; h++) {
+      int shh = (int)((sw >> (8 * h)) & 0xFF);
+      tot_c += shh;
+      tot_t += h == bsel ? s_new : shh;
+    }
+    if (tot_t > rd.max_binders) de += kEHugePoly * (double)(tot_t - rd.max_binders);
+    if (tot_c > rd.max_binders) de -= kEHugePoly * (double)(tot_c - rd.max_binders);
+  }
+  for (int b = 0; b < rd.nb; b++) {
+    int sc = (int)((sw >> (8 * b)) & 0xFF);
+    int stt = b == bsel ? s_new : sc;
+    int nm = (int)((mw >> (8 * b)) & 0xFF);
+    de += bind_f(rd, b, nm, stt);
+    de -= bind_f(rd, b, nm, sc);
+    if (rd.mu[b] > 0) {
+      double me = rd.mu[b] * (-rd.mu_adjust + 2);
+      de -= (double)stt * me;
+      de += (double)sc * me;
+    } else {
+      de -= (double)stt * rd.mu[b] * rd.mu_adjust;
+      de += (double)sc * rd.mu[b] * rd.mu_adjust;
+    }
+  }
+  return de;
+}
+
+// FP32 storage: FP32 arithmetic on the FP32 copies of the table and of the
+// effective chemical potentials (terms of order 1 kT; error ~1e-7 kT).
+__device__ __forceinline__ float bead_bind_dE(const WarpShared& ws, unsigned sw, unsigned mw, int bsel,
+                                              int s_new, float) {
+  const RepDev& rd = ws.rd;
+  float de = 0;
+  if (rd.max_binders != -1) {
+    int tot_t = 0, tot_c = 0;
+    for (int h = 0; h < rd.nb; h++) {
+      int shh = (int)((sw >> (8 * h)) & 0xFF);
+      tot_c += shh;
+      tot_t += h == bsel ? s_new : shh;
+    }
+    if (tot_t > rd.max_binders) de += (float)kEHugePoly * (float)(tot_t - rd.max_binders);
+    if (tot_c > rd.max_binders) de -= (float)kEHugePoly * (float)(tot_c - rd.max_binders);
+  }
+  for (int b = 0; b < rd.nb; b++) {
+    int sc = (int)((sw >> (8 * b)) & 0xFF);
+    int stt = b == bsel ? s_new : sc;
+    int nm = (int)((mw >> (8 * b)) & 0xFF);
+    const float* tb = ws.f_bind + (b * (CG_MAX_MARK + 1) + nm) * (CG_MAX_MARK + 1);
+    de += (tb[stt] - tb[sc]) - ws.f_me[b] * (float)(stt - sc);
+  }
+  return de;
+}
+
+// intranucleosome term of a binding move (fields.pyx:1920-1933): into the
+// FP64 part for FP64 storage, into the FF part for FP32 storage
+__device__ __forceinline__ void add_intra(const WarpShared& ws, int bsel, int ddb, double&, double& hard) {
+  hard += ws.rd.intra[bsel] * (double)ddb;
+}
+__device__ __forceinline__ void add_intra(const WarpShared& ws, int bsel, int ddb, FF& soft, double&) {
+  soft = ff_add(soft, ws.f_intra[bsel] * (float)ddb);
+}
+
+// True when an FP64 value is +0 or -0 (integer test, no FP64 instruction)
+__device__ __forceinline__ bool is_zero64(double v) { return (__double_as_longlong(v) << 1) == 0; }
+
+// dE = dEp + soft + hard and the Metropolis decision on it.  FP64 storage:
+// dE = (0 + dEp) + hard in FP64, as the reference sums polymer and field dE
+// (mc_sim.pyx:144-171).  FP32 storage: decided on the FF sum when the FP64
+// part is empty.  *dE_out (if given) receives dE in FP64.
+__device__ __forceinline__ bool decide(unsigned x, double dEp, double, double hard, double* dE_out) {
+  double dE = 0;
+  dE += dEp;
+  dE += hard;
+  if (dE_out) *dE_out = dE;
+  return metropolis(x, -dE);
+}
+__device__ __forceinline__ bool decide(unsigned x, FF dEp, FF soft, double hard, double* dE_out) {
+  const FF s = ff_add(dEp, soft);
+  bool d;
+  if (is_zero64(hard)) d = metropolis_ff(x, FF{-s.hi, -s.lo});
+  else d = metropolis(x, -(ff_d(s) + hard));
+  if (dE_out) *dE_out = ff_d(s) + hard;
+  return d;
 }
 
 }  // namespace cg

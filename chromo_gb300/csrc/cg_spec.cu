@@ -119,6 +119,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
   const unsigned* st = a.states + rd.bead_off;
   const unsigned* mk = a.marks + rd.bead_off;
   const double* bonds = a.bonds + rd.bead_off * 6;
+  const float* bonds32 = a.bonds32 + rd.bead_off * 8;
   MovePlan& P = sh.plan[w];
   MoveRng g;
   g.init(a.seed, rep, t, sh.draws[w]);
@@ -126,7 +127,12 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
   const bool check_field = rd.field_kind != 0 && kind != CG_TANGENT_ROTATION;
   const bool density = rd.field_kind == 2;
   long long ind0 = 0, indf = 0, m = 0;
-  double dEp = 0, dEf = 0;
+  // dE = dEp (polymer) + dEs (field, FF for FP32 storage) + dEh (the FP64
+  // part: confinement penalties, voxels at the volume-fraction limit, and
+  // the whole field dE for FP64 storage)
+  using Acc = typename AccOf<Real>::type;
+  Acc dEp = acc_zero<Acc>(), dEs = acc_zero<Acc>();
+  double dEh = 0;
   long long nvox = 0;
   bool empty = false;
   int gtab = 0, gstage = 0;
@@ -137,7 +143,8 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
     Real Md[3][4];
     if (kind == CG_CRANK_SHAFT) {
       Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
-      long long b0 = (int)(unif(g.next()) * (double)N);
+      const unsigned xb0 = g.next();
+      long long b0 = sizeof(Real) == 4 ? scaled_index(xb0, N) : (long long)(int)(unif(xb0) * (double)N);
       long long b1 = from_point(g, c.amp_bead, N, b0, err);
       if (b1 < 1) b1 = 1;
       check_bead_bounds(b0, b1, N, ind0, indf);
@@ -200,7 +207,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
       // table of 16 m slots never fills
       if (16 * m > (1LL << sm.logH)) { S.keys = gm.keys; S.used = gm.used; S.bslot = gm.bslot; S.vals = gm.vals; S.logH = gm.logH; gtab = 1; }
       Pos* stage = reinterpret_cast<Pos*>(S.stage);
-      double part = 0;
+      Acc part = acc_zero<Acc>();
       int oob = 0;
       for (long long k = lane; k < m; k += 32) {
         const long long i = ind0 + k;
@@ -223,12 +230,12 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
         if (k == 0 && ind0 != 0) {
           Real r0[3], t30[3];
           ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
-          part += pair_dE_fwd(load_bond<Real>(bonds, i - 1), r0, r, tr, t30, t3, tt3);
+          acc_add(part, pair_dE_fwd(bond_at(bonds, bonds32, i - 1, (Real)0), r0, r, tr, t30, t3, tt3));
         }
         if (k == m - 1 && indf != N) {
           Real r1[3], t31[3];
           ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
-          part += pair_dE_rev(load_bond<Real>(bonds, i), r, tr, r1, t3, tt3, t31);
+          acc_add(part, pair_dE_rev(bond_at(bonds, bonds32, i, (Real)0), r, tr, r1, t3, tt3, t31));
         }
         if (check_field && rd.confine_kind) oob += out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
         if (density && fin) {
@@ -243,15 +250,15 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
       }
       err = __reduce_or_sync(kFull, err);
       dEp = warp_sum(part);
-      if (check_field) {
+      if (check_field && rd.confine_kind) {
         int oo = __reduce_add_sync(kFull, (unsigned)oob);
         double conf = 0;
         conf += (double)(oo >> 16) * kEHugeField;
         conf -= (double)(oo & 0xFFFF) * kEHugeField;
-        dEf = conf;
+        dEh = conf;
       }
       __syncwarp();
-      if (density) dEf += field_dE_voxels(ws, a, ncol, S.keys, S.used, S.vals, *nused, lane, nvox, (Real)0, !gtab);
+      if (density) field_dE_voxels(ws, a, ncol, S.keys, S.used, S.vals, *nused, lane, nvox, dEs, dEh, !gtab);
     }
   } else if (kind == CG_TANGENT_ROTATION) {
     Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
@@ -294,7 +301,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
     if (!err) {
       const unsigned long long axis_base = g.pos;
       Pos* stage = reinterpret_cast<Pos*>(S.stage);
-      double part = 0;
+      Acc part = acc_zero<Acc>();
       Real sa, ca;
       rsincos(ang, &sa, &ca);
       for (long long k = lane; k < m; k += 32) {
@@ -318,18 +325,18 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
         }
         Pos* sg = stage + k * 9;
         for (int j = 0; j < 3; j++) { sg[3 + j] = (Pos)tt3[j]; sg[6 + j] = (Pos)tt2[j]; }
-        double de = 0;
+        Acc de = acc_zero<Acc>();
         if (i != 0) {
           Real r0[3], t30[3];
           ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
-          de += pair_dE_fwd(load_bond<Real>(bonds, i - 1), r0, r, r, t30, t3, tt3);
+          acc_add(de, pair_dE_fwd(bond_at(bonds, bonds32, i - 1, (Real)0), r0, r, r, t30, t3, tt3));
         }
         if (i + 1 != N) {
           Real r1[3], t31[3];
           ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
-          de += pair_dE_rev(load_bond<Real>(bonds, i), r, r, r1, t3, tt3, t31);
+          acc_add(de, pair_dE_rev(bond_at(bonds, bonds32, i, (Real)0), r, r, r1, t3, tt3, t31));
         }
-        part += de;
+        acc_add(part, de);
       }
       g.pos = axis_base + 2 * (unsigned long long)m;
       dEp = warp_sum(part);
@@ -353,7 +360,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
       if (m > a.stage_cap) { S.idx = gm.idx; gstage = 1; }
       if (16 * m > (1LL << sm.logH)) { S.keys = gm.keys; S.used = gm.used; S.bslot = gm.bslot; S.vals = gm.vals; S.logH = gm.logH; gtab = 1; }
       int* idx = S.idx;
-      double part = 0;
+      Acc part = acc_zero<Acc>();
       int dbl = 0;
       for (long long k = lane; k < m; k += 32) {
         const long long i = ind0 + k;
@@ -361,33 +368,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
         int s_new = g.state_at(g.bpos + k, nt, ok);
         unsigned sw = st[i], mw = mk[i];
         int s_old = (int)((sw >> (8 * bsel)) & 0xFF);
-        double de = 0;
-        if (rd.max_binders != -1) {
-          int tot_t = 0, tot_c = 0;
-          for (int h = 0; h < rd.nb; h++) {
-            int shh = (int)((sw >> (8 * h)) & 0xFF);
-            tot_c += shh;
-            tot_t += h == bsel ? s_new : shh;
-          }
-          if (tot_t > rd.max_binders) de += kEHugePoly * (double)(tot_t - rd.max_binders);
-          if (tot_c > rd.max_binders) de -= kEHugePoly * (double)(tot_c - rd.max_binders);
-        }
-        for (int b = 0; b < rd.nb; b++) {
-          int sc = (int)((sw >> (8 * b)) & 0xFF);
-          int stt = b == bsel ? s_new : sc;
-          int nm = (int)((mw >> (8 * b)) & 0xFF);
-          de += bind_f(rd, b, nm, stt);
-          de -= bind_f(rd, b, nm, sc);
-          if (rd.mu[b] > 0) {
-            double me = rd.mu[b] * (-rd.mu_adjust + 2);
-            de -= (double)stt * me;
-            de += (double)sc * me;
-          } else {
-            de -= (double)stt * rd.mu[b] * rd.mu_adjust;
-            de += (double)sc * rd.mu[b] * rd.mu_adjust;
-          }
-        }
-        part += de;
+        acc_add(part, bead_bind_dE(ws, sw, mw, bsel, s_new, (Real)0));
         dbl += (s_new == 2 ? 1 : 0) - (s_old == 2 ? 1 : 0);
         idx[k] = s_new;
         if (density && s_new != s_old) {
@@ -414,12 +395,12 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
           ld3(r4, ind0 + k, p);
           oob += out_of_bounds(rd, p, true);
         }
-        dEf = (double)__reduce_add_sync(kFull, (unsigned)oob) * kEHugeField;
+        dEh = (double)__reduce_add_sync(kFull, (unsigned)oob) * kEHugeField;
       }
       __syncwarp();
       if (density) {
-        dEf += field_dE_voxels(ws, a, ncol, S.keys, S.used, S.vals, *nused, lane, nvox, (Real)0, !gtab);
-        dEf += rd.intra[bsel] * (double)ddb;
+        field_dE_voxels(ws, a, ncol, S.keys, S.used, S.vals, *nused, lane, nvox, dEs, dEh, !gtab);
+        add_intra(ws, bsel, ddb, dEs, dEh);
       }
       if (lane == 0) P.bsel = bsel;
     }
@@ -439,13 +420,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int w, in
     regfail = (int)__reduce_or_sync(kFull, (unsigned)regfail);
   }
   bool dec = false;
-  if (!err && !empty) {
-    double dE = 0;
-    dE += dEp;
-    dE += dEf;
-    dec = metropolis(g.next(), -dE);
-    if (lane == 0) P.dE = dE;
-  }
+  if (!err && !empty) dec = decide(g.next(), dEp, dEs, dEh, lane == 0 ? &P.dE : nullptr);
   if (lane == 0) {
     P.kind = kind; P.m = (int)m; P.ind0 = (int)ind0; P.indf = (int)indf;
     P.empty = empty ? 1 : 0; P.err = (int)err; P.regfail = regfail; P.dec = dec ? 1 : 0;
@@ -622,13 +597,7 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
   __syncthreads();
   if (tid == 0) {
     const RepDev& rd0 = sh.ws.rd;
-    make_gridf(rd0, sh.ws.gf);
-    for (int b = 0; b < CG_MAX_BINDERS; b++) sh.ws.f_pref[b] = (float)rd0.pref[b];
-    for (int b = 0; b < CG_MAX_BINDERS * CG_MAX_BINDERS; b++) sh.ws.f_xpref[b] = (float)rd0.xpref[b];
-    sh.ws.f_scale = (float)(kFxInv / rd0.vol_bin);
-    sh.ws.f_vb = (float)rd0.bead_vol;
-    sh.ws.f_k = (float)(rd0.chi * (rd0.vol_bin / rd0.bead_vol));
-    sh.ws.f_lim = (float)rd0.vf_limit;
+    setup_f32(sh.ws);
     sh.t0 = rd0.draw_pos;
     sh.run_dE = rd0.run_dE;
     sh.stop = 0;

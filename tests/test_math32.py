@@ -1,5 +1,7 @@
 """The deterministic FP32 sin/cos/acos used by the FP32-storage path, against
-FP64 libm (numpy), within a few ulp over the argument ranges the moves use."""
+FP64 libm (numpy), within a few ulp over the argument ranges the moves use;
+and the 32-bit-conversion fixed-point rounding of trilinear weights against
+llrint(w * 2^40) for every binary32 weight in [0, 1]."""
 import ctypes
 import subprocess
 from pathlib import Path
@@ -17,12 +19,19 @@ def lib(tmp_path_factory):
     src.write_text(f'#include "{HDR}"\n'
                    "void sc(const float* x, float* s, float* c, int n)"
                    "{ for (int i = 0; i < n; i++) cgm_sincosf(x[i], s + i, c + i); }\n"
-                   "void ac(const float* x, float* y, int n) { for (int i = 0; i < n; i++) y[i] = cgm_acosf(x[i]); }\n")
+                   "void ac(const float* x, float* y, int n) { for (int i = 0; i < n; i++) y[i] = cgm_acosf(x[i]); }\n"
+                   "#include <string.h>\n"
+                   "long long q40_bad(unsigned lo, unsigned hi) { long long bad = 0;"
+                   " for (unsigned b = lo; ; b++) { float w; memcpy(&w, &b, 4);"
+                   " if (cgm_q40f(w) != llrint((double)w * 1099511627776.0)) bad++;"
+                   " if (b == hi) break; } return bad; }\n")
     so = d / "m32.so"
     subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-ffp-contract=off", "-o", str(so), str(src), "-lm"])
     L = ctypes.CDLL(str(so))
     L.sc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
     L.ac.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    L.q40_bad.argtypes = [ctypes.c_uint, ctypes.c_uint]
+    L.q40_bad.restype = ctypes.c_longlong
     return L
 
 
@@ -53,3 +62,10 @@ def test_acos_accuracy(lib):
     ref = np.arccos(x.astype(np.float64))
     assert np.max(np.abs(y - ref)) < 5e-7
     assert y[-4] == 0.0 or abs(y[-4] - np.pi) < 1e-6
+
+
+def test_fixed_point_weights_exhaustive(lib):
+    """cgm_q40f(w) == llrint(w * 2^40) for all 1,065,353,217 binary32 values
+    in [0, 1] (0x00000000 .. 0x3F800000): the GPU deposits weights with
+    32-bit conversions only and must produce the oracle's int64 grid."""
+    assert lib.q40_bad(0, 0x3F800000) == 0

@@ -217,7 +217,13 @@ def main():
     sh = stream.cuda_stream
     w = wl.make_workload(args.workload, seed_offset=rank)
     chains = wl.make_chains(w)
-    sim = wl.build_sim(w, chains)
+    # launch shape (warps per replica, lanes per move) picked by the autotuner
+    # on scratch copies of this workload (untimed; cached per problem)
+    from chromo_gb300 import autotune
+    shape, tune_table = autotune.tune(
+        lambda W, G: wl.build_sim(w, chains, warps_per_block=W, lanes_per_move=G),
+        w.lengths, [[w.nbins] * 3] * w.replicas, w.n_binders)
+    sim = wl.build_sim(w, chains, warps_per_block=shape[0], lanes_per_move=shape[1])
     steps_round = w.steps_per_round
     moves_round = w.replicas * steps_round * w.moves_per_step
     # ---- warm-up rounds (graph capture happens on the first)
@@ -312,7 +318,10 @@ def main():
                        "beads_total": nbeads, "mc_steps_per_step": steps_round,
                        "attempted_moves_per_step": int(attempts / args.steps),
                        "l2": "inputs larger than L2 (grids 256 x 1.5 MB + chains > 129 MB)",
-                       "graph": "one exchange round captured in a CUDA graph, replayed per step"},
+                       "graph": "one exchange round captured in a CUDA graph, replayed per step",
+                       "launch_shape": dict(zip(("warps_per_replica", "lanes_per_move", "moves_in_flight",
+                                                 "hash_slots"), sim.launch_shape())),
+                       "autotune_moves_per_s": {k: round(v) for k, v in tune_table.items()}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "spec_kernel<float>", "peak_source": peak_kind,

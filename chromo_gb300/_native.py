@@ -72,7 +72,7 @@ class Config(C.Structure):
         ("n_replicas", C.c_int32), ("pos_fp64", C.c_int32), ("n_binders", C.c_int32),
         ("warps_per_block", C.c_int32), ("n_beads", C.POINTER(C.c_int64)),
         ("grid_dims", C.POINTER(C.c_int32)), ("max_segment", C.c_int64),
-        ("max_tangent", C.c_int64), ("nonuniform_access", C.c_int32), ("pad", C.c_int32),
+        ("max_tangent", C.c_int64), ("nonuniform_access", C.c_int32), ("lanes_per_move", C.c_int32),
     ]
 
 
@@ -83,7 +83,7 @@ EXPORTS = [
     "cg_run", "cg_sync", "cg_run_audit", "cg_energy", "cg_reset_running_energy", "cg_get_tally",
     "cg_reset_tally", "cg_exchange", "cg_get_chi", "cg_run_batched", "cg_get_launch_info",
     "cg_field_energy_static", "cg_energies", "cg_set_chains", "cg_get_chains", "cg_gradient",
-    "cg_sample_terms", "cg_get_samples",
+    "cg_sample_terms", "cg_get_samples", "cg_get_launch_shape", "cg_mc_warps_per_sm",
 ]
 N_TERMS = 14
 
@@ -124,6 +124,8 @@ def lib():
             "cg_get_chi": ([P, P], C.c_int),
             "cg_run_batched": ([P, I64, I64, I32, C.c_uint64, P], C.c_int),
             "cg_get_launch_info": ([P, P, P, P], C.c_int),
+            "cg_get_launch_shape": ([P, P, P, P, P], C.c_int),
+            "cg_mc_warps_per_sm": ([I32, I32], C.c_int),
             "cg_field_energy_static": ([C.POINTER(FieldParams), I64, P, P, P, P, P], C.c_int),
             "cg_energies": ([P, P, P], C.c_int),
             "cg_set_chains": ([P, P, P, P, P], C.c_int),
@@ -138,6 +140,14 @@ def lib():
             f.restype = res
         _lib = L
     return _lib
+
+
+def mc_warps_per_sm(pos_fp64: bool, lanes_per_move: int) -> int:
+    """Warps of the MC kernel that fit one SM's register file (needs a GPU)."""
+    n = lib().cg_mc_warps_per_sm(int(bool(pos_fp64)), int(lanes_per_move))
+    if n < 0:
+        raise ValueError(f"no MC kernel for lanes_per_move={lanes_per_move} (pos_fp64={pos_fp64})")
+    return n
 
 
 def check(rc):
@@ -156,7 +166,7 @@ class Sim:
     """Owner of one cg_sim handle (R replicas resident on the GPU)."""
 
     def __init__(self, n_beads, grid_dims, n_binders, *, pos_fp64=False, max_segment=152,
-                 max_tangent=1, warps_per_block=0, nonuniform_access=False):
+                 max_tangent=1, warps_per_block=0, nonuniform_access=False, lanes_per_move=0):
         L = lib()
         self.n_beads = np.ascontiguousarray(n_beads, dtype=np.int64)
         self.grid_dims = np.ascontiguousarray(grid_dims, dtype=np.int32).reshape(-1, 3)
@@ -175,6 +185,7 @@ class Sim:
         cfg.max_segment = int(max_segment)
         cfg.max_tangent = int(max_tangent)
         cfg.nonuniform_access = int(bool(nonuniform_access))
+        cfg.lanes_per_move = int(lanes_per_move)
         h = C.c_void_p()
         check(L.cg_create(C.byref(cfg), C.byref(h)))
         self.h = h
@@ -337,6 +348,12 @@ class Sim:
     def run_batched(self, n_rounds, n_steps, n_rungs, seed, stream=None):
         check(lib().cg_run_batched(self.h, int(n_rounds), int(n_steps), int(n_rungs),
                                    int(seed) & (2**64 - 1), stream))
+
+    def launch_shape(self):
+        """(warps per replica, lanes per move, moves in flight, shared voxel-table slots)."""
+        w, g, f, hs = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        check(lib().cg_get_launch_shape(self.h, C.byref(w), C.byref(g), C.byref(f), C.byref(hs)))
+        return w.value, g.value, f.value, hs.value
 
     def launch_info(self):
         w, hs, k = C.c_int32(), C.c_int32(), C.c_int64()

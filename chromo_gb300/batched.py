@@ -42,10 +42,15 @@ class ReplicaBatch:
     that chain; ``controllers``: one list of move controllers per chain
     (default: ``all_moves`` with SimpleControl and the chain's own
     amplitude bounds, as ``chromo.mc.polymer_in_field`` sets up);
-    ``precision``: "fp32" (default) or "fp64" position storage."""
+    ``precision``: "fp32" (default) or "fp64" position storage;
+    ``warps_per_block`` / ``lanes_per_move``: the kernel's launch shape (0:
+    chosen by the library); ``autotune=True`` times the candidate shapes on
+    scratch copies of this batch first (``chromo_gb300.autotune``) and uses
+    the fastest (results cached per problem)."""
 
     def __init__(self, polymers: Sequence, fields: Sequence, controllers: Optional[List[list]] = None,
-                 *, precision: str = "fp32", warps_per_block: int = 0):
+                 *, precision: str = "fp32", warps_per_block: int = 0, lanes_per_move: int = 0,
+                 autotune: bool = False):
         self.polymers = list(polymers)
         self.fields = list(fields)
         R = len(self.polymers)
@@ -76,20 +81,33 @@ class ReplicaBatch:
         for ctrls in self.controllers:
             s, t = _bounds(ctrls)
             seg, tan = max(seg, s), max(tan, t)
-        nonuni = any(isinstance(f, UniformDensityField) and not f.uniform_access for f in self.fields)
-        self.sim = nat.Sim([p.num_beads for p in self.polymers], [_grid_dims(f) for f in self.fields],
-                           nb, pos_fp64=(precision == "fp64"), max_segment=seg, max_tangent=tan,
-                           warps_per_block=warps_per_block, nonuniform_access=nonuni)
-        for r, (p, f, ctrls) in enumerate(zip(self.polymers, self.fields, self.controllers)):
-            self.sim.set_chain(r, r=p.r, t3=p.t3, t2=p.t2, states=p.states, marks=p.chemical_mods,
-                               bonds=p.bond_parameters())
-            uni = isinstance(f, UniformDensityField)
-            self.sim.set_field(r, _field_struct(p, f),
-                               access_vol=f.access_vols if (nonuni and uni) else None)
-            self.sim.set_binding(r, _binding_struct(p))
-            self.sim.set_controllers(r, [_ctl_struct(c) for c in ctrls])
-        self.sim.deposit(-1)
+        self._nb, self._seg, self._tan = nb, seg, tan
+        self._fp64 = precision == "fp64"
+        self._nonuni = any(isinstance(f, UniformDensityField) and not f.uniform_access for f in self.fields)
+        self.tuning = None
+        if autotune:
+            from . import autotune as at
+            (warps_per_block, lanes_per_move), self.tuning = at.tune(
+                self._make_sim, [p.num_beads for p in self.polymers],
+                [_grid_dims(f) for f in self.fields], nb, self._fp64)
+        self.sim = self._make_sim(warps_per_block, lanes_per_move)
         self.rebaseline()
+
+    def _make_sim(self, warps_per_block: int, lanes_per_move: int) -> "nat.Sim":
+        """A resident simulation of this batch's chains, fields and controllers."""
+        sim = nat.Sim([p.num_beads for p in self.polymers], [_grid_dims(f) for f in self.fields],
+                      self._nb, pos_fp64=self._fp64, max_segment=self._seg, max_tangent=self._tan,
+                      warps_per_block=warps_per_block, nonuniform_access=self._nonuni,
+                      lanes_per_move=lanes_per_move)
+        for r, (p, f, ctrls) in enumerate(zip(self.polymers, self.fields, self.controllers)):
+            sim.set_chain(r, r=p.r, t3=p.t3, t2=p.t2, states=p.states, marks=p.chemical_mods,
+                          bonds=p.bond_parameters())
+            uni = isinstance(f, UniformDensityField)
+            sim.set_field(r, _field_struct(p, f), access_vol=f.access_vols if (self._nonuni and uni) else None)
+            sim.set_binding(r, _binding_struct(p))
+            sim.set_controllers(r, [_ctl_struct(c) for c in ctrls])
+        sim.deposit(-1)
+        return sim
 
     # ------------------------------------------------------------------ running
     @property

@@ -78,9 +78,9 @@ struct cg_sim {
   int* rep_of_rung = nullptr;
   unsigned long long *swaps = nullptr, *swap_attempts = nullptr, *xround = nullptr;
   // shared-memory layout
-  int logH = 0, warp_smem = 0, off_keys = 0, off_used = 0, off_bslot = 0, off_vals = 0, off_stage = 0,
+  int logH = 0, warp_smem = 0, off_draws = 0, off_keys = 0, off_used = 0, off_bslot = 0, off_vals = 0, off_stage = 0,
       off_idx = 0;
-  int spec_w = 1, spec_logHB = 11, spec_off_bkeys = 0, spec_off_bmask = 0, spec_off_warps = 0;
+  int spec_w = 1, spec_g = 32, spec_s = 1, spec_logHB = 11, spec_off_bkeys = 0, spec_off_bmask = 0, spec_off_warps = 0;
   long long stage_cap = 0;
   size_t spec_bytes = 0;
   // captured batched graph
@@ -120,21 +120,23 @@ struct cg_sim {
     a.g_keys = g_keys; a.g_used = g_used; a.g_bslot = g_bslot; a.g_vals = g_vals; a.g_logH = g_logH;
     a.g_stage = g_stage; a.g_idx = g_idx; a.g_stage_cap = g_stage_cap;
     a.picked = picked; a.picked_off = d_picked_off;
-    a.wpb = wpb; a.logH = logH; a.stage_cap = stage_cap; a.warp_smem = warp_smem;
+    a.wpb = wpb; a.logH = logH; a.stage_cap = stage_cap; a.warp_smem = warp_smem; a.off_draws = off_draws;
     a.off_keys = off_keys; a.off_used = off_used; a.off_vals = off_vals; a.off_stage = off_stage;
     a.off_idx = off_idx; a.off_bslot = off_bslot;
-    a.spec_w = spec_w; a.spec_logHB = spec_logHB; a.spec_off_bkeys = spec_off_bkeys;
+    a.spec_w = spec_w; a.spec_g = spec_g; a.spec_s = spec_s; a.spec_logHB = spec_logHB; a.spec_off_bkeys = spec_off_bkeys;
     a.spec_off_bmask = spec_off_bmask; a.spec_off_warps = spec_off_warps;
     a.rep_of_rung = rep_of_rung; a.swaps = swaps; a.swap_attempts = swap_attempts;
     a.xround = xround;
     return a;
   }
 
-  // Per-warp region for hash capacity 2^lh and staging capacity sc (offsets
-  // within the region); returns the region size.
+  // Region of one move slot for voxel-table capacity 2^lh and staging
+  // capacity sc (offsets within the region; the draw buffer first, 16-byte
+  // aligned); returns the region size, a multiple of 16 bytes.
   int layout(int lh, long long sc) {
     size_t H = size_t(1) << lh;
     size_t o = 0;
+    off_draws = (int)o; o += 4 * cg::kDrawCache;
     off_keys = (int)o; o += 4 * H;
     off_used = (int)o; o += 4 * H;
     off_bslot = (int)o; o += 4 * H;
@@ -147,8 +149,9 @@ struct cg_sim {
     logH = lh; stage_cap = sc; warp_smem = (int)o;
     return warp_smem;
   }
-  // CTA layout: header, block voxel table (2^lhb entries), W warp regions.
-  size_t cta_layout(int lhb, int W) {
+  // CTA layout: header, block voxel table (2^lhb entries), one region per
+  // move slot (W warps of 32 / G slots).
+  size_t cta_layout(int lhb, int W, int G) {
     size_t o = align16(sizeof(cg::SpecShared));
     spec_off_bkeys = (int)o; o += 4 * (size_t(1) << lhb);
     spec_off_bmask = (int)o; o += 4 * (size_t(1) << lhb);
@@ -156,7 +159,9 @@ struct cg_sim {
     spec_off_warps = (int)o;
     spec_logHB = lhb;
     spec_w = W;
-    return o + (size_t)W * warp_smem;
+    spec_g = G;
+    spec_s = W * (32 / G);
+    return o + (size_t)spec_s * warp_smem;
   }
 };
 
@@ -208,37 +213,46 @@ void cg_destroy(cg_sim* s) {
   delete s;
 }
 
-// Moves in flight per replica: the largest W <= kMaxW for which every
-// replica's CTA is resident at once (ceil(R / SMs) CTAs per SM, W warps each,
-// within the register file).
-static int default_warps(const cg_sim* s) {
-  const long long ctas = (s->R + s->n_sm - 1) / std::max(1, s->n_sm);
-  const long long W = cg_spec_warps_per_sm(s->fp64 != 0) / std::max(1LL, ctas);
-  return (int)std::min<long long>(cg::kMaxW, std::max<long long>(1, W));
+// Lanes per move when the caller leaves it to the library: 16 for FP32
+// storage, 32 for FP64 storage (the only shape built for it).
+static int default_lanes(const cg_sim* s, int g_req) {
+  if (s->fp64) return 32;
+  return g_req > 0 ? g_req : 16;
 }
 
-static int choose_shape(cg_sim* s, int w_req) {
-  // One CTA per replica with W warps (moves in flight).  Enough CTAs must be
-  // resident per SM for every replica to run at once; each warp region gets
-  // the largest voxel hash that then fits.
+// Warps per replica: the largest W <= kMaxW for which every replica's CTA is
+// resident at once (ceil(R / SMs) CTAs per SM, W warps each, within the
+// register file), and at most 32 moves in flight.
+static int default_warps(const cg_sim* s, int G) {
+  const long long ctas = (s->R + s->n_sm - 1) / std::max(1, s->n_sm);
+  const long long W = cg_spec_warps_per_sm(s->fp64 != 0, G) / std::max(1LL, ctas);
+  const long long wmax = std::min<long long>(cg::kMaxW, cg::kMaxS / (32 / G));
+  return (int)std::min<long long>(wmax, std::max<long long>(1, W));
+}
+
+static int choose_shape(cg_sim* s, int w_req, int g_req) {
+  // One CTA per replica with W warps of 32 / G moves each.  Enough CTAs must
+  // be resident per SM for every replica to run at once; each move slot gets
+  // the largest voxel table that then fits.
   const size_t smem_per_sm = 227 * 1024;
   long long ctas_per_sm = (s->R + s->n_sm - 1) / std::max(1, s->n_sm);
   if (ctas_per_sm < 1) ctas_per_sm = 1;
-  int W = w_req > 0 ? w_req : default_warps(s);
+  const int G = default_lanes(s, g_req);
+  int W = w_req > 0 ? w_req : default_warps(s, G);
   if (W > cg::kMaxW) W = cg::kMaxW;
-  s->spec_w = W;
+  if (W * (32 / G) > cg::kMaxS) W = cg::kMaxS / (32 / G);
   const size_t budget = std::min<size_t>(smem_per_sm / ctas_per_sm - 1024, 220 * 1024);
   const int lhb = 10;
-  const long long sc = 48;
+  const long long sc = G == 32 ? 48 : 32;
   int lh = 10;  // at most 1,024 slots: the 32-bit split counters of a shared table cannot overflow
   for (; lh > 6; lh--) {
     s->layout(lh, sc);
-    if (s->cta_layout(lhb, W) <= budget) break;
+    if (s->cta_layout(lhb, W, G) <= budget) break;
   }
   s->layout(lh, sc);
-  s->spec_bytes = s->cta_layout(lhb, W);
+  s->spec_bytes = s->cta_layout(lhb, W, G);
   s->wpb = 1;
-  cudaError_t e = cg_set_spec_smem(s->fp64 != 0, (int)s->spec_bytes);
+  cudaError_t e = cg_set_spec_smem(s->fp64 != 0, G, (int)s->spec_bytes);
   if (e == cudaSuccess) e = cg_set_mc_smem(s->fp64 != 0, (int)(s->spec_off_warps + s->warp_smem));
   if (e != cudaSuccess) return fail(CG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
   return CG_OK;
@@ -281,16 +295,28 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   s->g_logH = next_log2(32 * s->max_segment);
   s->g_stage_cap = std::max(s->max_segment, s->max_tangent);
   const long long Hg = 1LL << s->g_logH;
-  {
-    int W = cfg->warps_per_block > 0 ? cfg->warps_per_block : default_warps(s);
-    s->spec_w = W > cg::kMaxW ? cg::kMaxW : W;
+  if (cfg->lanes_per_move != 0 && !cg_spec_shape_ok(s->fp64 != 0, cfg->lanes_per_move)) {
+    cg_destroy(s);
+    return fail(CG_ERR_ARG, "lanes_per_move must be 8, 16 or 32 (32 with FP64 storage)");
   }
-  const long long RW = (long long)s->R * s->spec_w;
-  // tangent-rotation bitmaps: one per (replica, warp)
+  if (cfg->warps_per_block < 0 || cfg->warps_per_block > cg::kMaxW) {
+    cg_destroy(s);
+    return fail(CG_ERR_ARG, "warps_per_block must be in 0..12");
+  }
+  {
+    const int G = default_lanes(s, cfg->lanes_per_move);
+    int W = cfg->warps_per_block > 0 ? cfg->warps_per_block : default_warps(s, G);
+    if (W * (32 / G) > cg::kMaxS) W = cg::kMaxS / (32 / G);
+    s->spec_w = W;
+    s->spec_g = G;
+    s->spec_s = W * (32 / G);
+  }
+  const long long RW = (long long)s->R * s->spec_s;
+  // tangent-rotation bitmaps: one per (replica, move slot)
   s->total_picked = 0;
   for (int r = 0; r < s->R; r++) {
     s->picked_off[r] = s->total_picked;
-    s->total_picked += (long long)s->spec_w * ((s->n_beads[r] + 31) / 32);
+    s->total_picked += (long long)s->spec_s * ((s->n_beads[r] + 31) / 32);
   }
   auto M = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes == 0 ? 16 : bytes); };
   cudaError_t e = cudaSuccess;
@@ -368,7 +394,7 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   cudaMemcpy(s->reps, rd.data(), sizeof(RepDev) * s->R, cudaMemcpyHostToDevice);
   e = cudaGetLastError();
   if (e != cudaSuccess) { cg_destroy(s); return fail(CG_ERR_CUDA, cudaGetErrorString(e)); }
-  int rc = choose_shape(s, cfg->warps_per_block);
+  int rc = choose_shape(s, s->spec_w, s->spec_g);
   if (rc) { cg_destroy(s); return rc; }
   *out = s;
   return CG_OK;
@@ -662,7 +688,7 @@ static int device_errors(cg_sim* s) {
   for (int r = 0; r < s->R; r++) rd[r].err = 0;
   cudaMemcpy(s->reps, rd.data(), sizeof(RepDev) * s->R, cudaMemcpyHostToDevice);
   const long long Hg = 1LL << s->g_logH;
-  const long long RW = (long long)s->R * s->spec_w;
+  const long long RW = (long long)s->R * s->spec_s;
   cudaMemset(s->g_keys, 0xFF, 4 * Hg * RW);
   cudaMemset(s->g_bslot, 0xFF, 4 * Hg * RW);
   cudaMemset(s->g_vals, 0, 8 * Hg * (s->nb + 1) * RW);
@@ -875,6 +901,20 @@ int cg_run_batched(cg_sim* s, int64_t n_rounds, int64_t n_steps, int32_t n_rungs
   CUDA_TRY(cudaGraphLaunch(s->graph, st));
   s->kernels += n_rounds;
   return CG_OK;
+}
+
+int cg_get_launch_shape(cg_sim* s, int32_t* wpb, int32_t* lanes, int32_t* in_flight, int32_t* hash_slots) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (wpb) *wpb = s->spec_w;
+  if (lanes) *lanes = s->spec_g;
+  if (in_flight) *in_flight = s->spec_s;
+  if (hash_slots) *hash_slots = 1 << s->logH;
+  return CG_OK;
+}
+
+int cg_mc_warps_per_sm(int32_t pos_fp64, int32_t lanes) {
+  if (!cg_spec_shape_ok(pos_fp64 != 0, lanes)) return -1;
+  return cg_spec_warps_per_sm(pos_fp64 != 0, lanes);
 }
 
 int cg_get_launch_info(cg_sim* s, int32_t* wpb, int32_t* hash_slots, int64_t* kernels) {

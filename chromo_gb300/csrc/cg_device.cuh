@@ -23,6 +23,9 @@ constexpr int kMaxIter = 4096;                          // cap on resampling loo
 
 // device-side error bits (mapped to cg_status on the host)
 enum : unsigned { E_WINDOW = 1u, E_STREAM = 2u, E_NONFINITE = 4u, E_SPIN = 8u };
+// internal: a move's shared-memory voxel table filled up (the move is then
+// evaluated again with its global-memory table; never reported)
+constexpr unsigned E_OVF = 16u;
 
 template <typename T> struct alignas(4 * sizeof(T)) V4 { T x, y, z, w; };
 
@@ -173,12 +176,10 @@ __device__ __forceinline__ bool metropolis(unsigned x, double t) {
 }
 
 // ---------------------------------------------------------------- FP32 sums
-// dE of the FP32 path is accumulated as an unevaluated sum hi + lo of two
-// binary32 numbers (Knuth's TwoSum; Dekker's renormalisation): error about
-// 2^-44 relative, and no FP64 instruction, which runs at 1/64 of the FP32
-// rate on GB300.  Both operands enter symmetrically (the TwoSum error term is
-// the exact rounding error), so a butterfly reduction leaves every lane with
-// the same bits.
+// FF: unevaluated sum hi + lo of two binary32 numbers (Knuth's TwoSum with
+// Dekker's renormalisation), for the three terms of one bond's energy.  Both
+// operands enter symmetrically (the TwoSum error term is the exact rounding
+// error).
 struct FF { float hi, lo; };
 
 __device__ __forceinline__ FF ff_add(FF a, FF b) {
@@ -190,35 +191,71 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
   return FF{hi, e - (hi - s)};
 }
 __device__ __forceinline__ FF ff_add(FF a, float b) { return ff_add(a, FF{b, 0.0f}); }
-__device__ __forceinline__ double ff_d(FF a) { return (double)a.hi + (double)a.lo; }
+
+// True when an FP64 value is +0 or -0 (integer test, no FP64 instruction)
+__device__ __forceinline__ bool is_zero64(double v) { return (__double_as_longlong(v) << 1) == 0; }
+
+// dE of the FP32 path in fixed point: every FP32 energy term is rounded to a
+// multiple of 2^-30 kT (error at most 2^-31 kT per term) and the terms are
+// summed exactly in int64.  The sum therefore does not depend on the order of
+// the terms -- on how beads and voxels are spread over lanes, or on the order
+// in which voxels were first touched -- and needs no FP64 instruction (FP64
+// runs at 1/64 of the FP32 rate on GB300).  Terms of 2^20 kT or more, and
+// non-finite ones, go to an FP64 side sum `hard` (rare: a 1e25 max_binders
+// penalty, an extreme bond).
+constexpr double kFxEInv = 1.0 / 1073741824.0;  // kT per fixed-point unit
+
+// round(x * 2^30), ties to even, for |x| < 2^20, with 32-bit conversions only:
+// a = |x| 2^10 < 2^30 is exact, floor(a) 2^20 is even, and (a - floor(a)) 2^20
+// is exact, so rounding that fraction rounds the whole.
+__device__ __forceinline__ long long q30(float x) {
+  const float a = fabsf(x) * 1024.0f;
+  const float fl = floorf(a);
+  const long long q = (long long)(int)fl * 1048576LL + (long long)(int)rintf((a - fl) * 1048576.0f);
+  return x < 0.0f ? -q : q;
+}
+
+struct Fx {
+  long long q;  // sum of the terms in units of 2^-30 kT
+  double hard;  // FP64 sum of the terms outside the fixed-point range
+};
 
 // Accumulator of the arithmetic of each storage type: FP64 storage sums in
-// FP64 (the reference's arithmetic), FP32 storage in FF.
+// FP64 (the reference's arithmetic), FP32 storage in fixed point.
 template <typename Real> struct AccOf { using type = double; };
-template <> struct AccOf<float> { using type = FF; };
+template <> struct AccOf<float> { using type = Fx; };
 __device__ __forceinline__ void acc_add(double& s, double v) { s += v; }
-__device__ __forceinline__ void acc_add(FF& s, FF v) { s = ff_add(s, v); }
-__device__ __forceinline__ void acc_add(FF& s, float v) { s = ff_add(s, v); }
+__device__ __forceinline__ void acc_add(Fx& s, float x) {
+  if (fabsf(x) < 1048576.0f) s.q += q30(x);
+  else s.hard += (double)x;
+}
+__device__ __forceinline__ void acc_add(Fx& s, FF v) { acc_add(s, v.hi); acc_add(s, v.lo); }
+__device__ __forceinline__ void acc_add(Fx& s, const Fx& v) {
+  s.q += v.q;
+  if (!is_zero64(v.hard)) s.hard += v.hard;
+}
 __device__ __forceinline__ double acc_d(double v) { return v; }
-__device__ __forceinline__ double acc_d(FF v) { return ff_d(v); }
+__device__ __forceinline__ double acc_d(const Fx& v) { return (double)v.q * kFxEInv + v.hard; }
 template <typename A> __device__ __forceinline__ A acc_zero();
 template <> __device__ __forceinline__ double acc_zero<double>() { return 0.0; }
-template <> __device__ __forceinline__ FF acc_zero<FF>() { return FF{0.0f, 0.0f}; }
+template <> __device__ __forceinline__ Fx acc_zero<Fx>() { return Fx{0, 0.0}; }
 
-// The Metropolis test of the FP32 path on t = -dE held as hi + lo: decided in
-// FP32 when u and exp(t) differ by more than 1e-4 relative (the FP32 errors of
-// u, exp and of dropping lo stay below 1e-5 for |t| <= 80), else by
-// metropolis() on the FP64 value of t.
-__device__ __forceinline__ bool metropolis_ff(unsigned x, FF t) {
-  const float th = t.hi;
-  if (th > 81.0f) return true;
-  if (th < -81.0f && x != 0u) return false;
-  if (th >= -80.0f && th <= 80.0f) {
-    const float u = unif32(x), e = expf(th);
-    if (u < e * 0.9999f) return true;
-    if (u > e * 1.0001f) return false;
+// The Metropolis test of the FP32 path on dE = q 2^-30 + hard: decided in
+// FP32 when `hard` is empty and u and exp(-dE) differ by more than 1e-4
+// relative (the FP32 errors of u, of exp and of converting q stay below 1e-5
+// for |dE| <= 80), else by metropolis() on the FP64 value of dE.
+__device__ __forceinline__ bool metropolis_fx(unsigned x, long long q, double hard) {
+  if (is_zero64(hard)) {
+    const float th = -(float)q * 9.313225746154785e-10f;
+    if (th > 81.0f) return true;
+    if (th < -81.0f && x != 0u) return false;
+    if (th >= -80.0f && th <= 80.0f) {
+      const float u = unif32(x), e = expf(th);
+      if (u < e * 0.9999f) return true;
+      if (u > e * 1.0001f) return false;
+    }
   }
-  return metropolis(x, ff_d(t));
+  return metropolis(x, -((double)q * kFxEInv + hard));
 }
 
 // ---------------------------------------------------------------- bead selection
@@ -571,12 +608,43 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
   return v;
 }
-__device__ __forceinline__ FF warp_sum(FF v) {
+// Reductions over aligned groups of G lanes (G = 8, 16, 32): every lane of a
+// group ends with the group's total.  Must be called by the whole warp.
+template <int G> __device__ __forceinline__ double gsum(double v) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1)
-    v = ff_add(v, FF{__shfl_xor_sync(kFull, v.hi, o), __shfl_xor_sync(kFull, v.lo, o)});
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
   return v;
 }
+template <int G> __device__ __forceinline__ long long gsum(long long v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+template <int G> __device__ __forceinline__ int gsum(int v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+template <int G> __device__ __forceinline__ unsigned gor(unsigned v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v |= __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+// The group's votes as G bits (lane gl of the group -> bit gl).
+template <int G> __device__ __forceinline__ unsigned gballot(bool p) {
+  const unsigned b = __ballot_sync(kFull, p);
+  if (G == 32) return b;
+  return (b >> ((threadIdx.x & 31u) & ~(unsigned)(G - 1))) & ((1u << (G & 31)) - 1u);
+}
+template <int G> __device__ __forceinline__ bool gany(bool p) { return gballot<G>(p) != 0u; }
+// Fixed-point sums are exact; the FP64 side sum is reduced only when some
+// lane of the group holds one.
+template <int G> __device__ __forceinline__ Fx gsum(Fx v) {
+  v.q = gsum<G>(v.q);
+  if (gany<G>(!is_zero64(v.hard))) v.hard = gsum<G>(v.hard);
+  return v;
+}
+__device__ __forceinline__ Fx warp_sum(Fx v) { return gsum<32>(v); }
 __device__ __forceinline__ long long warp_sum_ll(long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);

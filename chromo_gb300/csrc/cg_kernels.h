@@ -32,7 +32,8 @@ struct WarpShared {
   int pad[3];
 };
 
-constexpr int kMaxW = 8;
+constexpr int kMaxW = 12;  // warps per replica CTA (12 x 32 threads x 168 registers fill one SM)
+constexpr int kMaxS = 32;  // moves in flight per replica (one bit each in 32-bit masks)
 
 // Outcome of one speculatively evaluated move.
 struct MovePlan {
@@ -44,13 +45,12 @@ struct MovePlan {
 };
 
 // Shared-memory header of one replica's CTA.
-constexpr int kDrawCache = 64;  // first draws of each in-flight move, precomputed by its warp
+constexpr int kDrawCache = 64;  // first draws of each in-flight move, precomputed by its lanes
 
 struct SpecShared {
   WarpShared ws;
-  MovePlan plan[kMaxW];
-  alignas(16) unsigned draws[kMaxW][kDrawCache];  // written as uint4 by init()
-  int nused[kMaxW];
+  MovePlan plan[kMaxS];
+  int nused[kMaxS];
   unsigned long long t0;   // move counter (selects each move's random sub-stream)
   double run_dE;
   int cut, stop;
@@ -58,8 +58,7 @@ struct SpecShared {
   int pad;
 };
 
-static_assert(offsetof(SpecShared, draws) % 16 == 0 && sizeof(unsigned) * kDrawCache % 16 == 0,
-              "the draw buffers are written with 16-byte stores");
+static_assert(sizeof(unsigned) * kDrawCache % 16 == 0, "the draw buffers are written with 16-byte stores");
 
 struct KArgs {
   RepDev* reps;
@@ -88,13 +87,15 @@ struct KArgs {
   long long g_stage_cap;
   unsigned* picked;           // tangent-rotation bitmaps
   const long long* picked_off;
-  // launch shape and shared-memory layout (bytes within one warp's region)
+  // launch shape and shared-memory layout (bytes within one move slot's
+  // region; the audit kernel uses the first region for its single move)
   long long n_steps;
   int wpb, logH;
   long long stage_cap;
-  int warp_smem, off_keys, off_used, off_bslot, off_vals, off_stage, off_idx;
-  // multi-warp layout: header, block voxel table, then one region per warp
-  int spec_w, spec_logHB, spec_off_bkeys, spec_off_bmask, spec_off_warps;
+  int warp_smem, off_draws, off_keys, off_used, off_bslot, off_vals, off_stage, off_idx;
+  // CTA layout: header, block voxel table, then one region per move slot;
+  // spec_w warps of 32 / spec_g groups, spec_s = spec_w * 32 / spec_g slots
+  int spec_w, spec_g, spec_s, spec_logHB, spec_off_bkeys, spec_off_bmask, spec_off_warps;
   unsigned long long seed;
   // audit mode
   int audit_rep;
@@ -116,14 +117,16 @@ struct KArgs {
 
 void cg_launch_mc(const cg::KArgs& a, bool fp64, bool audit, cudaStream_t s);
 void cg_launch_spec(const cg::KArgs& a, bool fp64, size_t smem_bytes, cudaStream_t s);
-cudaError_t cg_set_spec_smem(bool fp64, int bytes);
+cudaError_t cg_set_spec_smem(bool fp64, int lanes_per_move, int bytes);
+// whether an MC kernel is built for (storage, lanes per move)
+bool cg_spec_shape_ok(bool fp64, int lanes_per_move);
 cudaError_t cg_set_mc_smem(bool fp64, int bytes);
 void cg_launch_deposit(const cg::KArgs& a, bool fp64, int rep, int n_reps_launch, long long max_beads,
                        cudaStream_t s);
 void cg_launch_energy(const cg::KArgs& a, bool fp64, double* out, cudaStream_t s);
 void cg_launch_chi_sum(const cg::KArgs& a, double* out, cudaStream_t s);
 // warps of the MC kernel that fit one SM's register file
-int cg_spec_warps_per_sm(bool fp64);
+int cg_spec_warps_per_sm(bool fp64, int lanes_per_move);
 
 namespace cg {
 constexpr int kTerms = 14;                                // energy terms per replica (cg_grad.cu)

@@ -132,6 +132,77 @@ __device__ __forceinline__ void deposit_bead(const RepDev& rd, int ncol, int* ke
   }
 }
 
+// Add the signed fixed-point contributions q[l] (bead weight; times the packed
+// binder states `st` for the binder columns) to the eight voxels v[l] of a
+// move's voxel table; contributions of zero claim nothing.  The home-slot
+// claims are issued back to back; only a claim that meets another key probes
+// on.  A table that cannot take a new voxel, or whose count of voxels passes
+// `cap`, sets `full_bit` in err (E_OVF for an optimistic shared table, after
+// which the caller starts the move again in its global table; E_SPIN where
+// the table was sized for the worst case).
+__device__ __forceinline__ void claim_add8(const RepDev& rd, int hcol, int* keys, int* used, int* nused,
+                                           long long* vals, int logH, const int v[8], const long long q[8],
+                                           unsigned st, unsigned& err, bool split, int cap,
+                                           unsigned full_bit) {
+  int slot[8], prev[8];
+#pragma unroll
+  for (int l = 0; l < 8; l++) {
+    slot[l] = (int)(((unsigned)v[l] * 0x9E3779B1u) >> (32 - logH));
+    prev[l] = q[l] != 0 ? atomicCAS(&keys[slot[l]], -1, v[l]) : v[l];
+  }
+  unsigned fresh = 0;
+#pragma unroll
+  for (int l = 0; l < 8; l++) {
+    if (prev[l] == -1) {
+      fresh |= 1u << l;
+    } else if (prev[l] != v[l]) {
+      bool inserted = false;
+      unsigned e = 0;
+      slot[l] = hash_probe(keys, logH, v[l], slot[l], inserted, e);
+      if (slot[l] < 0) { err |= full_bit; break; }
+      if (inserted) fresh |= 1u << l;
+    }
+  }
+  if (fresh) {
+    int at = atomicAdd(nused, __popc(fresh));
+#pragma unroll
+    for (int l = 0; l < 8; l++)
+      if ((fresh >> l) & 1u) used[at++] = slot[l];
+    if (at > cap) err |= full_bit;
+  }
+  if (err & full_bit) return;
+#pragma unroll
+  for (int l = 0; l < 8; l++) {
+    if (q[l] == 0) continue;
+    add_delta(vals, hcol, slot[l], 0, q[l], split);
+    for (int b = 0; b < rd.nb; b++)
+      add_delta(vals, hcol, slot[l], 1 + b, q[l] * (long long)((st >> (8 * b)) & 0xFF), split);
+  }
+}
+
+// Remove one bead's old trilinear weights (w0 at voxels v0) and add its new
+// ones (w1 at v1).  When both lie in the same eight voxels (the same lower
+// corner) each voxel gets one contribution q(w1) - q(w0) and the second set
+// is empty: fewer claims and atomics than two separate deposits, the same
+// integer sums.  Both sets go through the same two calls whatever the case,
+// so lanes of a warp do not diverge on it.
+template <typename Real>
+__device__ __forceinline__ void deposit_pair(const RepDev& rd, int hcol, int* keys, int* used, int* nused,
+                                             long long* vals, int logH, const Real w0[8], const int v0[8],
+                                             const Real w1[8], const int v1[8], unsigned st, unsigned& err,
+                                             bool split, int cap, unsigned full_bit) {
+  const bool same = v0[0] == v1[0];
+  long long qa[8], qb[8];
+#pragma unroll
+  for (int l = 0; l < 8; l++) {
+    const long long q0 = q40(w0[l]), q1 = q40(w1[l]);
+    qa[l] = same ? q1 - q0 : -q0;
+    qb[l] = same ? 0 : q1;
+  }
+  claim_add8(rd, hcol, keys, used, nused, vals, logH, v0, qa, st, err, split, cap, full_bit);
+  claim_add8(rd, hcol, keys, used, nused, vals, logH, v1, qb, st, err, split, cap, full_bit);
+}
+
 // chi term of one voxel in FP64 (fields.pyx:1792-1875 with the vf_limit branch)
 __device__ __forceinline__ double chi_term64(const RepDev& rd, double V, long long g0, long long d0) {
   double vf0 = ((double)g0 * kFxInv) / V * rd.bead_vol;
@@ -146,13 +217,16 @@ __device__ __forceinline__ double chi_term64(const RepDev& rd, double V, long lo
 // Field dE over the touched voxels (fixed-point grid), FP64 arithmetic; also
 // stores the post-move grid values into the hash values for the commit.  The
 // sum is added to `hard` (the FP64 part of the move's dE), nothing to `soft`.
+// Called by the whole warp; lane gl of each group of G lanes takes voxels
+// gl, gl + G, ... of its group's table.
+template <int G = 32>
 static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
                                   long long& n_vox, double& soft, double& hard, bool split = false) {
   const RepDev& rd = ws.rd;
   double part = 0;
   const long long* grid = a.grid + rd.vox_off * a.ncol;
-  for (int i = lane; i < nused; i += 32) {
+  for (int i = lane; i < nused; i += G) {
     int slot = used[i];
     int v = keys[slot];
     long long* d = vals + (long long)slot * hcol;
@@ -176,22 +250,21 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
   }
   n_vox = nused;
   (void)soft;
-  hard += warp_sum(part);
+  hard += gsum<G>(part);
 }
 
-// FP32 arithmetic per voxel, FF accumulation into `soft`; voxels at or near
-// the volume-fraction limit take the FP64 branch, summed into `hard`, so the
-// 1e99 penalty is decided as in FP64 (FP64 instructions only when some lane
-// met such a voxel).
+// FP32 arithmetic per voxel, fixed-point accumulation into `soft`; voxels at
+// or near the volume-fraction limit take the FP64 branch (into the FP64 side
+// sum), so the 1e99 penalty is decided as in FP64.
+template <int G = 32>
 static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
-                                  long long& n_vox, FF& soft, double& hard, bool split = false) {
+                                  long long& n_vox, Fx& soft, double& hard, bool split = false) {
   const RepDev& rd = ws.rd;
-  FF part = FF{0.0f, 0.0f};
-  double huge = 0;
-  bool rare = false;
+  Fx part = Fx{0, 0.0};
   const long long* grid = a.grid + rd.vox_off * a.ncol;
-  for (int i = lane; i < nused; i += 32) {
+  (void)hard;
+  for (int i = lane; i < nused; i += G) {
     int slot = used[i];
     int v = keys[slot];
     long long* d = vals + (long long)slot * hcol;
@@ -218,17 +291,15 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
     float vf0 = (float)g0 * sc * ws.f_vb;
     float dvf = (float)d0 * sc * ws.f_vb;
     if (vf0 > ws.f_lim - 1e-3f || vf0 + dvf > ws.f_lim - 1e-3f) {
-      part = ff_add(part, c);
-      huge += chi_term64(rd, V, g0, d0);
-      rare = true;
+      acc_add(part, c);
+      part.hard += chi_term64(rd, V, g0, d0);
     } else {
-      part = ff_add(part, c + k * (dvf * (2.0f * vf0 + dvf)));
+      acc_add(part, c + k * (dvf * (2.0f * vf0 + dvf)));
     }
     d[0] = g0 + d0;
   }
   n_vox = nused;
-  soft = ff_add(soft, warp_sum(part));
-  if (__any_sync(kFull, rare)) hard += warp_sum(huge);
+  acc_add(soft, gsum<G>(part));
 }
 
 __device__ __forceinline__ void commit_grid(const RepDev& rd, const KArgs& a, int hcol, int* keys,
@@ -330,12 +401,9 @@ __device__ __forceinline__ float bead_bind_dE(const WarpShared& ws, unsigned sw,
 __device__ __forceinline__ void add_intra(const WarpShared& ws, int bsel, int ddb, double&, double& hard) {
   hard += ws.rd.intra[bsel] * (double)ddb;
 }
-__device__ __forceinline__ void add_intra(const WarpShared& ws, int bsel, int ddb, FF& soft, double&) {
-  soft = ff_add(soft, ws.f_intra[bsel] * (float)ddb);
+__device__ __forceinline__ void add_intra(const WarpShared& ws, int bsel, int ddb, Fx& soft, double&) {
+  acc_add(soft, ws.f_intra[bsel] * (float)ddb);
 }
-
-// True when an FP64 value is +0 or -0 (integer test, no FP64 instruction)
-__device__ __forceinline__ bool is_zero64(double v) { return (__double_as_longlong(v) << 1) == 0; }
 
 // dE = dEp + soft + hard and the Metropolis decision on it.  FP64 storage:
 // dE = (0 + dEp) + hard in FP64, as the reference sums polymer and field dE
@@ -348,13 +416,13 @@ __device__ __forceinline__ bool decide(unsigned x, double dEp, double, double ha
   if (dE_out) *dE_out = dE;
   return metropolis(x, -dE);
 }
-__device__ __forceinline__ bool decide(unsigned x, FF dEp, FF soft, double hard, double* dE_out) {
-  const FF s = ff_add(dEp, soft);
-  bool d;
-  if (is_zero64(hard)) d = metropolis_ff(x, FF{-s.hi, -s.lo});
-  else d = metropolis(x, -(ff_d(s) + hard));
-  if (dE_out) *dE_out = ff_d(s) + hard;
+__device__ __forceinline__ bool decide(unsigned x, const Fx& dEp, const Fx& soft, double hard,
+                                       double* dE_out) {
+  const long long q = dEp.q + soft.q;
+  if (!is_zero64(dEp.hard)) hard += dEp.hard;
+  if (!is_zero64(soft.hard)) hard += soft.hard;
+  const bool d = metropolis_fx(x, q, hard);
+  if (dE_out) *dE_out = (double)q * kFxEInv + hard;
   return d;
 }
-
 }  // namespace cg

@@ -1,0 +1,807 @@
+// cg_spec.cuh -- the production MC kernel: several moves of a replica in flight.
+//
+// One CTA per replica, W warps, each warp split into 32 / G groups of G lanes
+// (G = 8, 16 or 32).  Every group evaluates one move, so S = W * 32 / G moves
+// are in flight.  Within one controller's cycle (same move kind, fixed
+// amplitudes) the next S attempted moves are evaluated at once, group s taking
+// move t0 + s, all against the state before the batch.  Then:
+//
+//   * each move's read/write footprint -- the beads it reads or writes and
+//     the voxels it touches -- is compared with the footprints of the earlier
+//     moves of the batch (beads by index range, voxels through a block-wide
+//     voxel -> move-bitmask table);
+//   * walking the batch in order, move s stands iff no earlier *accepted*
+//     move's footprint meets its own; the first move that fails, and every
+//     later one, is evaluated again in the next batch on the updated state;
+//   * the standing accepted moves are committed; their footprints are
+//     disjoint, so the commits do not interact.
+//
+// The result is exactly that of applying the moves one after the other (a
+// rejected move changes nothing; an accepted move only changes its own
+// footprint), for every W and G: each attempted move takes its random numbers
+// from its own Philox4x32-10 sub-stream, indexed by (replica, move number,
+// draw number), and the FP32 path sums dE exactly in fixed point, so neither
+// the spread of beads and voxels over lanes nor the order of hash claims
+// changes a bit.  Acceptance statistics and the controllers' amplitude updates
+// are applied in move order as in the one-move-at-a-time loop
+// (chromo/mc/mc_sim.pyx:88-182).
+//
+// Several moves per warp: a move of a few beads (the mean segment of the
+// benchmark's moves is 4-20 beads) leaves most of a warp's lanes idle, and the
+// scalar part of a move (draws, bead selection, rotation, Metropolis) is
+// computed redundantly by all lanes of its group; with G = 16 or 8 one warp
+// instruction serves 2 or 4 moves.  Every warp-collective operation below is
+// executed by the whole warp with per-group masks, so groups may diverge only
+// in code without collectives.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "cg_device.cuh"
+#include "cg_kernels.h"
+#include "cg_move.cuh"
+
+namespace cg {
+
+// Random numbers of one attempted move (its own counter space).  Draw j is
+// word j & 3 of Philox block j >> 2.  The first kDrawCache draws are computed
+// at init by the move's G lanes into its shared-memory buffer, so a move's
+// draws cost one Philox latency instead of a chain of them; init() must be
+// called by the whole warp.
+struct MoveRng {
+  uint2 key, keyb;
+  unsigned tlo, thi;
+  unsigned long long pos, bpos;
+  unsigned cctr;
+  uint4 cache;
+  const unsigned* buf;
+  bool fail;
+  template <int G>
+  __device__ void init(unsigned long long seed, int rep, unsigned long long t, unsigned* draws, int gl) {
+    key = make_uint2((unsigned)seed ^ (unsigned)rep * 0x85EBCA6Bu, (unsigned)(seed >> 32) ^ 0x1B873593u);
+    keyb = make_uint2(key.x ^ 0x68E31DA4u, key.y ^ 0xB5297A4Du);
+    tlo = (unsigned)t;
+    thi = (unsigned)(t >> 32);
+    pos = 0; bpos = 0; cctr = 0xffffffffu; fail = false;
+    for (int j = gl; j < kDrawCache / 4; j += G) {
+      uint4 o = philox(make_uint4((unsigned)j, tlo, thi, 0x2545F491u), key);
+      reinterpret_cast<uint4*>(draws)[j] = o;
+    }
+    __syncwarp();
+    buf = draws;
+  }
+  __device__ __forceinline__ unsigned at(unsigned long long j, bool& ok) const {
+    ok = true;
+    uint4 o = philox(make_uint4((unsigned)(j >> 2), tlo, thi, 0x2545F491u), key);
+    return comp4(o, (unsigned)(j & 3)) >> 1;
+  }
+  __device__ __forceinline__ unsigned next() {
+    unsigned long long j = pos++;
+    if (j < (unsigned long long)kDrawCache) return buf[j] >> 1;
+    unsigned c = (unsigned)(j >> 2);
+    if (c != cctr) {
+      cache = philox(make_uint4(c, tlo, thi, 0x2545F491u), key);
+      cctr = c;
+    }
+    return comp4(cache, (unsigned)j & 3u) >> 1;
+  }
+  __device__ __forceinline__ int state_at(unsigned long long k, int nt, bool& ok) const {
+    ok = true;
+    uint4 o = philox(make_uint4((unsigned)(k >> 2), tlo, thi, 0x7F4A7C15u), keyb);
+    return (int)__umulhi(comp4(o, (unsigned)(k & 3)), (unsigned)(nt + 1));
+  }
+};
+
+__device__ __forceinline__ int block_insert(int* bkeys, int logHB, int key) {
+  const unsigned mask = (1u << logHB) - 1u;
+  unsigned h = ((unsigned)key * 0x9E3779B1u) >> (32 - logHB);
+  for (int it = 0; it < 64; it++) {
+    int prev = atomicCAS(&bkeys[h], -1, key);
+    if (prev == -1 || prev == key) return (int)h;
+    h = (h + 1) & mask;
+  }
+  return -1;
+}
+
+// Scratch of one move slot: its shared-memory region, or the slot's global
+// region for moves too large for shared memory.
+struct SlotScratch {
+  int* keys;
+  int* used;
+  int* bslot;
+  long long* vals;
+  int logH;
+  void* stage;
+  int* idx;
+  unsigned* picked;
+};
+
+__device__ __forceinline__ void use_table(SlotScratch& S, const SlotScratch& from) {
+  S.keys = from.keys; S.used = from.used; S.bslot = from.bslot; S.vals = from.vals; S.logH = from.logH;
+}
+
+// Drop the entries a move left in a voxel table (keys, values, block slots).
+__device__ __forceinline__ void clear_table(const SlotScratch& T, int hcol, int nu, int gl, int G) {
+  for (int i = gl; i < nu; i += G) {
+    const int slot = T.used[i];
+    T.keys[slot] = -1;
+    for (int cc = 0; cc < hcol; cc++) T.vals[(long long)slot * hcol + cc] = 0;
+    T.bslot[i] = -1;
+  }
+}
+
+// Evaluate move t of the batch in slot s (group lanes gl = 0..G-1); `live`
+// is false for the groups of a partly filled batch, which run the warp's
+// collectives with empty work.
+template <typename Pos, int G>
+__device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, int gl, bool live, int kind,
+                              const cg_move_ctl& c, unsigned long long t, unsigned* draws,
+                              const SlotScratch& sm, const SlotScratch& gm, int* bkeys, unsigned* bmask,
+                              int logHB) {
+  using Real = Pos;
+  using Acc = typename AccOf<Real>::type;
+  const RepDev& rd = sh.ws.rd;
+  const GridF& gf = sh.ws.gf;
+  const WarpShared& ws = sh.ws;
+  const long long N = rd.n_beads;
+  const int hcol = a.hcol;  // stride of the voxel-table values
+  const V4<Pos>* r4 = reinterpret_cast<const V4<Pos>*>(a.r4) + rd.bead_off;
+  const V4<Pos>* t34 = reinterpret_cast<const V4<Pos>*>(a.t34) + rd.bead_off;
+  const V4<Pos>* t24 = reinterpret_cast<const V4<Pos>*>(a.t24) + rd.bead_off;
+  const unsigned* st = a.states + rd.bead_off;
+  const unsigned* mk = a.marks + rd.bead_off;
+  const double* bonds = a.bonds + rd.bead_off * 6;
+  const float* bonds32 = a.bonds32 + rd.bead_off * 8;
+  MovePlan& P = sh.plan[s];
+  MoveRng g;
+  g.init<G>(a.seed, rep, t, draws, gl);
+  unsigned err = 0;
+  const bool check_field = rd.field_kind != 0 && kind != CG_TANGENT_ROTATION;
+  const bool density = rd.field_kind == 2;
+  long long ind0 = 0, indf = 0, m = 0;
+  // dE = dEp (polymer) + dEs (field; fixed point for FP32 storage) + dEh (the
+  // FP64 part: confinement penalties, and the whole field dE for FP64 storage)
+  Acc dEp = acc_zero<Acc>(), dEs = acc_zero<Acc>();
+  double dEh = 0;
+  long long nvox = 0;
+  bool empty = !live;
+  int gtab = 0, gstage = 0;
+  SlotScratch S = sm;
+  int* nused = &sh.nused[s];
+  const int Hs = 1 << sm.logH;
+
+  if (kind <= CG_SLIDE) {
+    Real M[3][4];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 4; j++) M[i][j] = i == j ? (Real)1 : (Real)0;
+    if (live) {
+      if (kind == CG_CRANK_SHAFT) {
+        Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
+        const unsigned xb0 = g.next();
+        long long b0 = sizeof(Real) == 4 ? scaled_index(xb0, N) : (long long)(int)(unif(xb0) * (double)N);
+        long long b1 = from_point(g, c.amp_bead, N, b0, err);
+        if (b1 < 1) b1 = 1;
+        check_bead_bounds(b0, b1, N, ind0, indf);
+        long long ia, ib;
+        if (ind0 == indf - 1 && ind0 == 0) { ia = indf; ib = ind0; }
+        else if (ind0 == indf - 1 && ind0 == N - 1) { ia = ind0; ib = ind0 - 1; }
+        else if (ind0 == 0 && indf == N) { ia = indf - 1; ib = ind0; }
+        else if (ind0 == 0) { ia = indf; ib = ind0; }
+        else if (indf == N) { ia = indf - 1; ib = ind0 - 1; }
+        else { ia = indf; ib = ind0 - 1; }
+        if (!err) {
+          Real pa[3], pb[3], dir[3], p[3];
+          ld3(r4, ia, pa); ld3(r4, ib, pb);
+          for (int i = 0; i < 3; i++) dir[i] = pa[i] - pb[i];
+          Real mag = rsqrt_(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+          if (mag < (Real)1E-5) sphere<Real>(g, dir);
+          else { Real sc = (Real)1 / mag; for (int i = 0; i < 3; i++) dir[i] = dir[i] * sc; }
+          long long ip;
+          if (ind0 == 0 && indf != N) ip = indf;
+          else if (ind0 != 0 && indf == N) ip = ind0 - 1;
+          else if (ind0 == 0 && indf == N) ip = ind0;
+          else ip = ind0 - 1;
+          ld3(r4, ip, p);
+          axis_rotation(dir, p, ang, M);
+        }
+      } else if (kind == CG_END_PIVOT) {
+        Real ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
+        long long lhs = g.next() & 1u;
+        if (lhs == 1) { ind0 = 0; indf = from_left(g, c.amp_bead, N, err) + 1; }
+        else { ind0 = N - from_left(g, c.amp_bead, N, err); indf = N; }
+        Real axis[3], p[3];
+        sphere<Real>(g, axis);
+        long long ip;
+        if (ind0 == 0 && indf != N) ip = indf;
+        else if (ind0 != 0 && indf == N) ip = ind0 - 1;
+        else if (ind0 == 0 && indf == N && lhs == 1) ip = indf - 1;
+        else ip = ind0;
+        if (!err) {
+          ld3(r4, ip, p);
+          axis_rotation(axis, p, ang, M);
+        }
+      } else {
+        Real amp = (Real)c.amp_move * uni<Real>(g.next()), d[3];
+        sphere<Real>(g, d);
+        for (int i = 0; i < 3; i++) M[i][3] = d[i] * amp;
+        long long b0 = g.next() % (unsigned)N;
+        long long b1 = from_point(g, c.amp_bead, N, b0, err);
+        check_bead_bounds(b0, b1, N, ind0, indf);
+      }
+    }
+    m = (!live || err) ? 0 : indf - ind0;
+    if (live && !err && m == 0) empty = true;
+    if (m > a.stage_cap) { S.stage = gm.stage; gstage = 1; }
+    // voxel table: shared when the move's at most 16 m voxels surely fit, or
+    // optimistically (a few distinct voxels per bead in practice) up to m <=
+    // slots / 4 with a fallback to the global table on overflow; global beyond
+    const bool sure = 16 * m <= Hs;
+    if (!sure && 4 * m > Hs) { use_table(S, gm); gtab = 1; }
+    Pos* stage = reinterpret_cast<Pos*>(S.stage);
+    Acc part = acc_zero<Acc>();
+    int oob = 0;
+    bool ovf = false;
+    for (int pass = 0; pass < 2; pass++) {
+      if (pass == 1) {
+        if (!__any_sync(kFull, ovf)) break;
+        if (ovf) clear_table(S, hcol, *nused, gl, G);
+        __syncwarp();
+        if (ovf) {
+          if (gl == 0) *nused = 0;
+          use_table(S, gm);
+          gtab = 1;
+          part = acc_zero<Acc>();
+          oob = 0;
+        }
+        __syncwarp();
+      }
+      const bool run = pass == 0 || ovf;
+      const int cap = gtab ? (1 << gm.logH) : (sure ? Hs : (3 * Hs) / 4);
+      const unsigned full_bit = (gtab || sure) ? E_SPIN : E_OVF;
+      unsigned e = 0;
+      for (long long k = gl; run && k < m; k += G) {
+        if (e & E_OVF) break;
+        const long long i = ind0 + k;
+        V4<Pos> R = r4[i], T3 = t34[i], T2 = t24[i];
+        Real r[3] = {R.x, R.y, R.z}, t3[3] = {T3.x, T3.y, T3.z}, t2[3] = {T2.x, T2.y, T2.z};
+        Real tr[3], tt3[3], tt2[3];
+        if (kind == CG_SLIDE) {
+          for (int j = 0; j < 3; j++) { tr[j] = r[j] + M[j][3]; tt3[j] = t3[j]; tt2[j] = t2[j]; }
+        } else {
+          for (int j = 0; j < 3; j++) {
+            Real er = 0, e3 = 0, e2 = 0;
+            for (int q = 0; q < 3; q++) { er += M[j][q] * r[q]; e3 += M[j][q] * t3[q]; e2 += M[j][q] * t2[q]; }
+            tr[j] = er + M[j][3]; tt3[j] = e3; tt2[j] = e2;
+          }
+        }
+        const bool fin = isfinite(tr[0]) && isfinite(tr[1]) && isfinite(tr[2]);
+        if (!fin) e |= E_NONFINITE;
+        Pos* sg = stage + k * 9;
+        for (int j = 0; j < 3; j++) { sg[j] = (Pos)tr[j]; sg[3 + j] = (Pos)tt3[j]; sg[6 + j] = (Pos)tt2[j]; }
+        if (k == 0 && ind0 != 0) {
+          Real r0[3], t30[3];
+          ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
+          acc_add(part, pair_dE_fwd(bond_at(bonds, bonds32, i - 1, (Real)0), r0, r, tr, t30, t3, tt3));
+        }
+        if (k == m - 1 && indf != N) {
+          Real r1[3], t31[3];
+          ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
+          acc_add(part, pair_dE_rev(bond_at(bonds, bonds32, i, (Real)0), r, tr, r1, t3, tt3, t31));
+        }
+        if (check_field && rd.confine_kind) oob += out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
+        if (density && fin) {
+          Real w0[8], w1[8];
+          int v0[8], v1[8];
+          voxel_weights(rd, gf, r, w0, v0);
+          voxel_weights(rd, gf, tr, w1, v1);
+          deposit_pair(rd, hcol, S.keys, S.used, nused, S.vals, S.logH, w0, v0, w1, v1, st[i], e, !gtab,
+                       cap, full_bit);
+        }
+      }
+      e = gor<G>(e);
+      ovf = (e & E_OVF) != 0;
+      err |= e & ~E_OVF;
+    }
+    err = gor<G>(err);
+    dEp = gsum<G>(part);
+    if (check_field && rd.confine_kind) {
+      int oo = gsum<G>(oob);
+      double conf = 0;
+      conf += (double)(oo >> 16) * kEHugeField;
+      conf -= (double)(oo & 0xFFFF) * kEHugeField;
+      dEh = conf;
+    }
+    __syncwarp();
+    if (density)
+      field_dE_voxels<G>(ws, a, hcol, S.keys, S.used, S.vals, *nused, gl, nvox, dEs, dEh, !gtab);
+  } else if (kind == CG_TANGENT_ROTATION) {
+    Real ang = 0;
+    long long n = 0;
+    if (live) {
+      ang = (Real)c.amp_move * (uni<Real>(g.next()) - (Real)0.5);
+      n = (long long)(g.next() % (unsigned)c.amp_bead) + 1;
+      if (n > N) err |= E_WINDOW;
+    }
+    m = (!live || err) ? 0 : n;
+    if (m > a.stage_cap) { S.stage = gm.stage; S.idx = gm.idx; gstage = 1; }
+    int* idx = S.idx;
+    // n distinct random beads, drawn in order with redraws (get_inds): G
+    // candidates per round, the first fresh ones taken in draw order
+    long long got = 0;
+    int it = 0;
+    const unsigned lt = (1u << gl) - 1u;
+    const unsigned gmask = G == 32 ? kFull : ((1u << (G & 31)) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(G - 1));
+    for (;;) {
+      bool want = live && !err && got < m;
+      if (want && ++it > kMaxIter) { err |= E_SPIN; want = false; }
+      if (!__any_sync(kFull, want)) break;
+      bool ok;
+      const unsigned x = g.at(g.pos + gl, ok);
+      const long long cand = want ? (long long)(x % (unsigned)N) : -1 - (long long)(threadIdx.x & 31u);
+      const unsigned grp = __match_any_sync(kFull, cand) & gmask;
+      const unsigned gshift = G == 32 ? 0u : ((threadIdx.x & 31u) & ~(unsigned)(G - 1));
+      const bool first = ((grp >> gshift) & lt) == 0;
+      const bool fresh = want && first && !((S.picked[cand >> 5] >> (cand & 31)) & 1u);
+      const unsigned bal = gballot<G>(fresh);
+      const long long need = m - got;
+      const int cnt = __popc(bal);
+      const int rank = __popc(bal & lt);
+      if (fresh && rank < need) {
+        idx[got + rank] = (int)cand;
+        atomicOr(&S.picked[cand >> 5], 1u << (cand & 31));
+      }
+      if (want) {
+        long long consumed;
+        if (cnt >= need) {
+          unsigned b = bal;
+          for (long long q = 1; q < need; q++) b &= b - 1;
+          consumed = __ffs((int)b);
+          got = m;
+        } else {
+          consumed = G;
+          got += cnt;
+        }
+        g.pos += consumed;
+      }
+      __syncwarp();
+    }
+    err = gor<G>(err);
+    if (err) m = 0;
+    const unsigned long long axis_base = g.pos;
+    Pos* stage = reinterpret_cast<Pos*>(S.stage);
+    Acc part = acc_zero<Acc>();
+    Real sa, ca;
+    rsincos(ang, &sa, &ca);
+    for (long long k = gl; k < m; k += G) {
+      const long long i = idx[k];
+      bool ok1, ok2;
+      unsigned xa = g.at(axis_base + 2 * k, ok1), xb = g.at(axis_base + 2 * k + 1, ok2);
+      Real axis[3];
+      sphere_from<Real>(xa, xb, axis);
+      const Real origin[3] = {0, 0, 0};
+      Real M[3][4];
+      axis_rotation_sc(axis, origin, sa, ca, M);
+      Real r[3], t3[3], t2[3], tt3[3], tt2[3];
+      ld3(r4, i, r); ld3(t34, i, t3); ld3(t24, i, t2);
+      for (int j = 0; j < 3; j++) {
+        Real e3 = 0, e2 = 0;
+        for (int q = 0; q < 3; q++) { e3 += M[j][q] * t3[q]; e2 += M[j][q] * t2[q]; }
+        tt3[j] = e3; tt2[j] = e2;
+      }
+      Pos* sg = stage + k * 9;
+      for (int j = 0; j < 3; j++) { sg[3 + j] = (Pos)tt3[j]; sg[6 + j] = (Pos)tt2[j]; }
+      Acc de = acc_zero<Acc>();
+      if (i != 0) {
+        Real r0[3], t30[3];
+        ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
+        acc_add(de, pair_dE_fwd(bond_at(bonds, bonds32, i - 1, (Real)0), r0, r, r, t30, t3, tt3));
+      }
+      if (i + 1 != N) {
+        Real r1[3], t31[3];
+        ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
+        acc_add(de, pair_dE_rev(bond_at(bonds, bonds32, i, (Real)0), r, r, r1, t3, tt3, t31));
+      }
+      acc_add(part, de);
+    }
+    g.pos = axis_base + 2 * (unsigned long long)m;
+    dEp = gsum<G>(part);
+    // the picked marks only serve the redraws of this move
+    for (long long k = gl; k < m; k += G) {
+      int i = idx[k];
+      atomicAnd(&S.picked[i >> 5], ~(1u << (i & 31)));
+    }
+    __syncwarp();
+    if (m > 0) {
+      ind0 = idx[0];
+      indf = ind0 + 1;
+    }
+  } else {
+    int bsel = 0;
+    if (live) {
+      bsel = (int)(g.next() % (unsigned)rd.nb);
+      long long b0 = g.next() % (unsigned)N;
+      long long b1 = from_point(g, c.amp_bead, N, b0, err);
+      if (!err) check_bead_bounds(b0, b1, N, ind0, indf);
+    }
+    m = (!live || err) ? 0 : indf - ind0;
+    const int nt = rd.sites[bsel];
+    if (m > a.stage_cap) { S.idx = gm.idx; gstage = 1; }
+    if (8 * m > Hs) { use_table(S, gm); gtab = 1; }
+    int* idx = S.idx;
+    Acc part = acc_zero<Acc>();
+    int dbl = 0;
+    for (long long k = gl; k < m; k += G) {
+      const long long i = ind0 + k;
+      bool ok;
+      int s_new = g.state_at(g.bpos + k, nt, ok);
+      unsigned sw = st[i], mw = mk[i];
+      int s_old = (int)((sw >> (8 * bsel)) & 0xFF);
+      acc_add(part, bead_bind_dE(ws, sw, mw, bsel, s_new, (Real)0));
+      dbl += (s_new == 2 ? 1 : 0) - (s_old == 2 ? 1 : 0);
+      idx[k] = s_new;
+      if (density && s_new != s_old) {
+        Real p[3], wv[8];
+        int v[8];
+        ld3(r4, i, p);
+        voxel_weights(rd, gf, p, wv, v);
+#pragma unroll
+        for (int l = 0; l < 8; l++) {
+          int slot = hash_slot(S.keys, S.used, nused, S.logH, v[l], err);
+          if (slot < 0) break;
+          add_delta(S.vals, hcol, slot, 1 + bsel, q40(wv[l]) * (long long)(s_new - s_old), !gtab);
+        }
+      }
+    }
+    g.bpos += (unsigned long long)m;
+    err = gor<G>(err);
+    dEp = gsum<G>(part);
+    const int ddb = gsum<G>(dbl);
+    if (check_field && rd.field_kind == 1 && rd.confine_kind == 2) {
+      int oob = 0;
+      for (long long k = gl; k < m; k += G) {
+        double p[3];
+        ld3(r4, ind0 + k, p);
+        oob += out_of_bounds(rd, p, true);
+      }
+      dEh = (double)gsum<G>(oob) * kEHugeField;
+    }
+    __syncwarp();
+    if (density) {
+      field_dE_voxels<G>(ws, a, hcol, S.keys, S.used, S.vals, *nused, gl, nvox, dEs, dEh, !gtab);
+      if (m > 0) add_intra(ws, bsel, ddb, dEs, dEh);
+    }
+    if (gl == 0 && live) P.bsel = bsel;
+  }
+  err = gor<G>(err);
+  // register the touched voxels for the conflict test
+  int regfail = 0;
+  if (density && check_field) {
+    const int nu = (live && !err && !empty) ? *nused : 0;
+    for (int i = gl; i < nu; i += G) {
+      int v = S.keys[S.used[i]];
+      int b = block_insert(bkeys, logHB, v);
+      S.bslot[i] = b;
+      if (b < 0) regfail = 1;
+      else atomicOr(&bmask[b], 1u << s);
+    }
+    regfail = (int)gor<G>((unsigned)regfail);
+  }
+  bool dec = false;
+  if (live && !err && !empty) dec = decide(g.next(), dEp, dEs, dEh, gl == 0 ? &P.dE : nullptr);
+  if (gl == 0 && live) {
+    P.kind = kind; P.m = (int)m; P.ind0 = (int)ind0; P.indf = (int)indf;
+    P.empty = empty ? 1 : 0; P.err = (int)err; P.regfail = regfail; P.dec = dec ? 1 : 0;
+    P.nvox = (int)nvox; P.gtab = gtab; P.gstage = gstage;
+  }
+}
+
+// Bits of earlier moves of the batch (u < s) whose footprint meets move s's.
+template <int G>
+__device__ void conflict_mask(const KArgs& a, SpecShared& sh, unsigned char* smem, int rep, int s, int gl,
+                              bool live, int kind, int B, const SlotScratch& sm, const SlotScratch& gm,
+                              const unsigned* bmask) {
+  MovePlan& P = sh.plan[s];
+  const RepDev& rd = sh.ws.rd;
+  const bool act = live && !P.err && !P.empty;
+  unsigned cm = 0;
+  if (rd.field_kind == 2 && kind != CG_TANGENT_ROTATION) {
+    const int nu = act ? sh.nused[s] : 0;
+    const int* bs = P.gtab ? gm.bslot : sm.bslot;
+    for (int i = gl; i < nu; i += G) {
+      int b = bs[i];
+      if (b >= 0) cm |= bmask[b];
+    }
+    cm = gor<G>(cm);
+  }
+  cm &= (1u << s) - 1u;
+  if (kind == CG_TANGENT_ROTATION) {
+    // rotated beads of u against those of s and their neighbours
+    const int* lw = P.gstage ? gm.idx : sm.idx;
+    for (int u = 0; u < B; u++) {
+      const MovePlan& U = sh.plan[u];
+      int hit = 0;
+      if (act && u < s && !U.err && !U.empty) {
+        const int* lu = U.gstage ? a.g_idx + ((long long)rep * a.spec_s + u) * a.g_stage_cap
+                                 : reinterpret_cast<const int*>(smem + a.spec_off_warps +
+                                                                (size_t)u * a.warp_smem + a.off_idx);
+        for (int k = gl; k < P.m && !hit; k += G) {
+          int j = lw[k];
+          for (int q = 0; q < U.m; q++) {
+            int d = lu[q] - j;
+            if (d >= -1 && d <= 1) { hit = 1; break; }
+          }
+        }
+      }
+      if (gany<G>(hit)) cm |= 1u << u;
+    }
+  } else {
+    // lane gl takes the earlier moves u = u0 + gl: beads written by u,
+    // [ind0, indf), against the beads read by s -- the segment and, for
+    // position moves, its two neighbours
+    for (int u0 = 0; u0 < B; u0 += G) {
+      const int u = u0 + gl;
+      bool hit = false;
+      if (act && u < s) {
+        const MovePlan& U = sh.plan[u];
+        if (!U.err && !U.empty) {
+          const long long wlo = U.ind0, whi = (long long)U.indf - 1;
+          const long long rlo = P.kind == CG_CHANGE_BINDING_STATE ? P.ind0 : (long long)P.ind0 - 1;
+          const long long rhi = P.kind == CG_CHANGE_BINDING_STATE ? (long long)P.indf - 1 : (long long)P.indf;
+          hit = wlo <= rhi && rlo <= whi;
+        }
+      }
+      cm |= gballot<G>(hit) << u0;
+    }
+  }
+  if (gl == 0 && live) P.cmask = cm;
+}
+
+template <typename Pos, int G>
+__device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int s, int gl, bool accept,
+                                 const SlotScratch& sm, const SlotScratch& gm, int* bkeys, unsigned* bmask) {
+  const MovePlan& P = sh.plan[s];
+  const RepDev& rd = sh.ws.rd;
+  const int ncol = a.ncol, hcol = a.hcol;
+  V4<Pos>* r4w = reinterpret_cast<V4<Pos>*>(a.r4) + rd.bead_off;
+  V4<Pos>* t34w = reinterpret_cast<V4<Pos>*>(a.t34) + rd.bead_off;
+  V4<Pos>* t24w = reinterpret_cast<V4<Pos>*>(a.t24) + rd.bead_off;
+  unsigned* st = a.states + rd.bead_off;
+  const Pos* stage = reinterpret_cast<const Pos*>(P.gstage ? gm.stage : sm.stage);
+  const int* idx = P.gstage ? gm.idx : sm.idx;
+  int* keys = P.gtab ? gm.keys : sm.keys;
+  int* used = P.gtab ? gm.used : sm.used;
+  int* bslot = P.gtab ? gm.bslot : sm.bslot;
+  long long* vals = P.gtab ? gm.vals : sm.vals;
+  const int m = P.m;
+  if (accept) {
+    if (P.kind <= CG_SLIDE) {
+      for (int k = gl; k < m; k += G) {
+        const Pos* sg = stage + (long long)k * 9;
+        const long long i = (long long)P.ind0 + k;
+        r4w[i] = V4<Pos>{sg[0], sg[1], sg[2], (Pos)0};
+        if (P.kind != CG_SLIDE) {
+          t34w[i] = V4<Pos>{sg[3], sg[4], sg[5], (Pos)0};
+          t24w[i] = V4<Pos>{sg[6], sg[7], sg[8], (Pos)0};
+        }
+      }
+    } else if (P.kind == CG_TANGENT_ROTATION) {
+      for (int k = gl; k < m; k += G) {
+        const Pos* sg = stage + (long long)k * 9;
+        const long long i = idx[k];
+        t34w[i] = V4<Pos>{sg[3], sg[4], sg[5], (Pos)0};
+        t24w[i] = V4<Pos>{sg[6], sg[7], sg[8], (Pos)0};
+      }
+    } else {
+      for (int k = gl; k < m; k += G) {
+        const long long i = (long long)P.ind0 + k;
+        unsigned sw = st[i];
+        sw = (sw & ~(0xFFu << (8 * P.bsel))) | ((unsigned)idx[k] << (8 * P.bsel));
+        st[i] = sw;
+      }
+    }
+  }
+  const int nu = sh.nused[s];
+  long long* grid = a.grid + rd.vox_off * ncol;
+  for (int i = gl; i < nu; i += G) {
+    int slot = used[i];
+    if (accept) {
+      int v = keys[slot];
+      for (int cc = 0; cc < hcol; cc++) grid[(long long)v * ncol + cc] = vals[(long long)slot * hcol + cc];
+    }
+    keys[slot] = -1;
+    for (int cc = 0; cc < hcol; cc++) vals[(long long)slot * hcol + cc] = 0;
+    int b = bslot[i];
+    if (b >= 0) { bkeys[b] = -1; bmask[b] = 0u; }
+    bslot[i] = -1;
+  }
+}
+
+// 168 registers: two CTAs of 6 warps fit one SM's register file (measured
+// faster than 128 registers with 8 warps, which spills).
+template <typename Pos, int G>
+__global__ void __maxnreg__(168) spec_kernel(KArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int GPW = 32 / G;  // move groups per warp
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int gl = lane & (G - 1);
+  const int slot = warp * GPW + lane / G;
+  const int Sn = a.spec_s;
+  const int rep = blockIdx.x;
+  if (rep >= a.n_reps) return;
+  SpecShared& sh = *reinterpret_cast<SpecShared*>(smem);
+  int* bkeys = reinterpret_cast<int*>(smem + a.spec_off_bkeys);
+  unsigned* bmask = reinterpret_cast<unsigned*>(smem + a.spec_off_bmask);
+  const int HB = 1 << a.spec_logHB;
+  const int hcol = a.hcol;
+  unsigned char* wb = smem + a.spec_off_warps + (size_t)slot * a.warp_smem;
+  unsigned* draws = reinterpret_cast<unsigned*>(wb + a.off_draws);
+  SlotScratch sm, gm;
+  sm.keys = reinterpret_cast<int*>(wb + a.off_keys);
+  sm.used = reinterpret_cast<int*>(wb + a.off_used);
+  sm.bslot = reinterpret_cast<int*>(wb + a.off_bslot);
+  sm.vals = reinterpret_cast<long long*>(wb + a.off_vals);
+  sm.logH = a.logH;
+  sm.stage = wb + a.off_stage;
+  sm.idx = reinterpret_cast<int*>(wb + a.off_idx);
+  const long long gi = (long long)rep * Sn + slot;
+  const long long Hg = 1LL << a.g_logH;
+  gm.keys = a.g_keys + gi * Hg;
+  gm.used = a.g_used + gi * Hg;
+  gm.bslot = a.g_bslot + gi * Hg;
+  gm.vals = a.g_vals + gi * Hg * hcol;
+  gm.logH = a.g_logH;
+  gm.stage = reinterpret_cast<Pos*>(a.g_stage) + gi * a.g_stage_cap * 9;
+  gm.idx = a.g_idx + gi * a.g_stage_cap;
+  {
+    const unsigned* src = reinterpret_cast<const unsigned*>(a.reps + rep);
+    unsigned* dst = reinterpret_cast<unsigned*>(&sh.ws.rd);
+    for (int i = tid; i < (int)(sizeof(RepDev) / 4); i += blockDim.x) dst[i] = src[i];
+    const unsigned* cs = reinterpret_cast<const unsigned*>(a.ctl + (long long)rep * 5);
+    unsigned* cd = reinterpret_cast<unsigned*>(sh.ws.ctl);
+    for (int i = tid; i < (int)(5 * sizeof(cg_move_ctl) / 4); i += blockDim.x) cd[i] = cs[i];
+    for (int i = tid; i < HB; i += blockDim.x) { bkeys[i] = -1; bmask[i] = 0u; }
+    for (int i = tid; i < 30; i += blockDim.x) sh.ws.tally[i] = 0;
+    for (int i = gl; i < (1 << a.logH); i += G) { sm.keys[i] = -1; sm.bslot[i] = -1; }
+    for (int i = gl; i < (1 << a.logH) * hcol; i += G) sm.vals[i] = 0;
+    if (gl == 0) sh.nused[slot] = 0;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const RepDev& rd0 = sh.ws.rd;
+    setup_f32(sh.ws);
+    sh.t0 = rd0.draw_pos;
+    sh.run_dE = rd0.run_dE;
+    sh.stop = 0;
+    sh.cut = 0;
+  }
+  __syncthreads();
+  const long long words = (sh.ws.rd.n_beads + 31) / 32;
+  sm.picked = gm.picked = a.picked + a.picked_off[rep] + slot * words;
+
+  for (long long step = 0; step < a.n_steps; step++) {
+    for (int ci = 0; ci < a.n_ctl; ci++) {
+      cg_move_ctl& c = sh.ws.ctl[ci];
+      const int kind = (int)c.move_kind;
+      if (c.move_on == 1) {
+        long long done = 0;
+        while (done < c.num_per_cycle) {
+          const int B = (int)(c.num_per_cycle - done < Sn ? c.num_per_cycle - done : Sn);
+          const bool wlive = warp * GPW < B;  // the warp has a move of this batch
+          const bool live = slot < B;
+          if (wlive)
+            evaluate_move<Pos, G>(a, sh, rep, slot, gl, live, kind, c, sh.t0 + (unsigned long long)slot,
+                                  draws, sm, gm, bkeys, bmask, a.spec_logHB);
+          __syncthreads();
+          if (wlive) conflict_mask<G>(a, sh, smem, rep, slot, gl, live, kind, B, sm, gm, bmask);
+          __syncthreads();
+          // Resolve, computed by every warp from the plans (lane u reads move u):
+          // the batch stands up to the first move that failed or meets an
+          // earlier accepted move (everything before it stands, so "earlier
+          // accepted" is the accepted moves below it), or up to and including
+          // the first move whose voxels could not be registered.
+          const bool valid = lane < B;
+          const MovePlan& Pl = sh.plan[valid ? lane : 0];
+          const bool p_err = valid && Pl.err != 0;
+          const unsigned D = __ballot_sync(kFull, valid && !Pl.empty && Pl.dec);
+          const unsigned F = __ballot_sync(kFull, p_err || (valid && (Pl.cmask & D & ((1u << lane) - 1u))));
+          const unsigned RF = __ballot_sync(kFull, valid && Pl.regfail);
+          const int first_fail = F ? __ffs((int)F) - 1 : B;
+          int cut = first_fail;
+          if (RF && __ffs((int)RF) < cut) cut = __ffs((int)RF);
+          const unsigned acc = cut >= 32 ? D : (D & ((1u << cut) - 1u));
+          if (warp == 0) {
+            // bookkeeping of the standing moves, in move order where it is FP64
+            const bool stand = lane < cut;
+            const bool took = (acc >> lane) & 1u;
+            const unsigned sm_m = __reduce_add_sync(kFull, stand ? (unsigned)Pl.m : 0u);
+            const unsigned sm_v = __reduce_add_sync(kFull, stand ? (unsigned)Pl.nvox : 0u);
+            const unsigned ac_m = __reduce_add_sync(kFull, took ? (unsigned)Pl.m : 0u);
+            const unsigned ac_v = __reduce_add_sync(kFull, took ? (unsigned)Pl.nvox : 0u);
+            if (lane == 0) {
+              const unsigned n_acc = (unsigned)__popc(acc);
+              c.num_attempt += cut;
+              c.num_success += n_acc;
+              unsigned long long* t = sh.ws.tally + kind * 6;
+              t[0] += (unsigned long long)cut;
+              t[1] += n_acc;
+              t[2] += sm_m;
+              t[3] += sm_v;
+              t[4] += ac_m;
+              t[5] += ac_v;
+              double run = sh.run_dE, rate = c.acc_rate;
+              for (int w = 0; w < cut; w++) {
+                const MovePlan& P = sh.plan[w];
+                if (P.empty) continue;
+                if (P.dec) run += P.dE;
+                rate = c.alpha * (P.dec ? 1.0 : 0.0) + (1 - c.alpha) * rate;
+              }
+              sh.run_dE = run;
+              c.acc_rate = rate;
+              sh.t0 += (unsigned long long)cut;
+              if (cut == first_fail && first_fail < B && sh.plan[first_fail].err) sh.stop = sh.plan[first_fail].err;
+            }
+          }
+          if (wlive && live)
+            commit_and_clear<Pos, G>(a, sh, slot, gl, slot < cut && ((acc >> slot) & 1u), sm, gm, bkeys, bmask);
+          __syncwarp();
+          if (live && gl == 0) sh.nused[slot] = 0;
+          __syncthreads();
+          done += cut;
+          if (sh.stop) break;
+        }
+      }
+      if (sh.stop) break;
+      if (tid == 0 && c.ctrl_kind == 1) {  // SimpleControl.update_amplitudes, mc_controller.py:126-189
+        double acc = c.acc_rate;
+        if (acc < 0.5) {
+          double prop = c.amp_move * 0.95;
+          if (prop > c.move_lo) c.amp_move = prop;
+          else {
+            c.amp_move = c.move_hi;
+            double nb = (double)(c.amp_bead - 1);
+            c.amp_bead = (long long)(c.bead_lo > nb ? c.bead_lo : nb);
+          }
+        } else if (acc > 0.5) {
+          double prop = c.amp_move / 0.95;
+          if (prop < c.move_hi) c.amp_move = prop;
+          else {
+            c.amp_move = c.move_lo;
+            double nb = (double)(c.amp_bead + 1);
+            c.amp_bead = (long long)(c.bead_hi < nb ? c.bead_hi : nb);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (sh.stop) break;
+  }
+  __syncthreads();
+  {
+    unsigned* cd = reinterpret_cast<unsigned*>(a.ctl + (long long)rep * 5);
+    const unsigned* cs = reinterpret_cast<const unsigned*>(sh.ws.ctl);
+    for (int i = tid; i < (int)(5 * sizeof(cg_move_ctl) / 4); i += blockDim.x) cd[i] = cs[i];
+  }
+  if (tid == 0) {
+    RepDev* out = a.reps + rep;
+    out->draw_pos = sh.t0;
+    out->run_dE = sh.run_dE;
+    out->err = (unsigned)sh.stop;
+    unsigned long long* t = a.tally + (long long)rep * 30;
+    for (int i = 0; i < 30; i++) t[i] += sh.ws.tally[i];
+  }
+}
+
+}  // namespace cg
+
+// Launch, shared-memory opt-in and register count of one instantiation.
+#define CG_SPEC_INSTANTIATE(Pos, G, NAME)                                                          \
+  void cg_launch_spec_##NAME(const cg::KArgs& a, size_t smem, cudaStream_t s) {                    \
+    cg::spec_kernel<Pos, G><<<a.n_reps, 32 * a.spec_w, smem, s>>>(a);                              \
+  }                                                                                                \
+  cudaError_t cg_spec_smem_##NAME(int bytes) {                                                     \
+    return cudaFuncSetAttribute(cg::spec_kernel<Pos, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                bytes);                                                            \
+  }                                                                                                \
+  int cg_spec_regs_##NAME() {                                                                      \
+    cudaFuncAttributes at;                                                                         \
+    return cudaFuncGetAttributes(&at, cg::spec_kernel<Pos, G>) == cudaSuccess ? at.numRegs : 0;    \
+  }

@@ -138,11 +138,12 @@ def binder_names(nb):
     return ["HP1", "PRC1", "B3"][:nb]
 
 
-def build_sim(w: Workload, chains=None, pos_fp64=False, warps_per_block=0) -> nat.Sim:
+def build_sim(w: Workload, chains=None, pos_fp64=False, warps_per_block=0, lanes_per_move=0) -> nat.Sim:
     chains = chains if chains is not None else make_chains(w)
     R, nb = w.replicas, w.n_binders
     sim = nat.Sim(w.lengths, [[w.nbins] * 3] * R, nb, pos_fp64=pos_fp64, max_segment=152,
-                  max_tangent=int(max(w.lengths)), warps_per_block=warps_per_block)
+                  max_tangent=int(max(w.lengths)), warps_per_block=warps_per_block,
+                  lanes_per_move=lanes_per_move)
     width = w.nbins * VOXEL
     vint = 4.0 / 3.0 * np.pi * R_INT ** 3
     pref, intra, xpref = field_prefactors(w.eps, [vint] * nb, w.cross, binder_names(nb), VOXEL ** 3)

@@ -103,7 +103,8 @@ typedef struct {
     int64_t max_segment;       /* largest bead amplitude of a segment move + 1 */
     int64_t max_tangent;       /* largest bead amplitude of tangent_rotation */
     int32_t nonuniform_access; /* 1: per-voxel accessible volumes are uploaded */
-    int32_t pad;
+    int32_t lanes_per_move;    /* lanes evaluating one move: 8, 16 or 32 (FP64 storage: 32);
+                                  0: chosen by the library */
 } cg_config;
 
 /* Allocate device state for R replicas.  Replaces constructing the reference's
@@ -232,6 +233,18 @@ int cg_run_batched(cg_sim *sim, int64_t n_rounds, int64_t n_steps, int32_t n_run
  * library launched since creation. */
 int cg_get_launch_info(cg_sim *sim, int32_t *warps_per_block, int32_t *hash_slots,
                        int64_t *kernels_launched);
+
+/* Launch shape of the MC kernel: warps per replica CTA, lanes per move, moves
+ * in flight per replica (warps * 32 / lanes) and shared voxel-table slots per
+ * move.  No counterpart in the reference (its loop runs one move at a time);
+ * the autotuner (chromo_gb300.autotune) reads it. */
+int cg_get_launch_shape(cg_sim *sim, int32_t *warps_per_block, int32_t *lanes_per_move,
+                        int32_t *moves_in_flight, int32_t *hash_slots);
+
+/* Warps of the MC kernel for (storage precision, lanes per move) that fit one
+ * SM's register file, or -1 for a shape that is not built.  No counterpart in
+ * the reference; the autotuner derives its candidate shapes from it. */
+int cg_mc_warps_per_sm(int32_t pos_fp64, int32_t lanes_per_move);
 
 /* Field energy of one chain, allocating nothing (no counterpart in the
  * reference).  Deposits the chain into a fixed-point density grid and writes

@@ -28,25 +28,32 @@ def _small(nrep=6, n=1500, nbins=12, nb=2):
     return w
 
 
+SHAPES_FP32 = [(1, 32), (2, 32), (4, 32), (8, 32), (1, 16), (3, 16), (6, 16), (1, 8), (4, 8), (8, 8)]
+SHAPES_FP64 = [(1, 32), (2, 32), (4, 32), (8, 32)]
+
+
 @pytest.mark.parametrize("fp64", [False, True])
 def test_moves_in_flight_equal_sequential(fp64):
+    """Every launch shape (W warps of 32 / G moves each, up to 32 moves in
+    flight) against one move at a time (W = 1, G = 32)."""
     w = _small()
     chains = wl.make_chains(w)
     out = {}
-    for W in (1, 2, 4, 8):
-        sim = wl.build_sim(w, chains, pos_fp64=fp64, warps_per_block=W)
-        assert sim.launch_info()[0] == W
+    shapes = SHAPES_FP64 if fp64 else SHAPES_FP32
+    for W, G in shapes:
+        sim = wl.build_sim(w, chains, pos_fp64=fp64, warps_per_block=W, lanes_per_move=G)
+        assert sim.launch_shape()[:3] == (W, G, W * 32 // G)
         sim.run(6, 99)
         sim.sync()
-        out[W] = ([sim.get_chain(r) for r in range(w.replicas)],
+        out[(W, G)] = ([sim.get_chain(r) for r in range(w.replicas)],
                   [sim.density(r) for r in range(w.replicas)],
                   [[(c.amp_move, c.amp_bead, c.num_attempt, c.num_success, c.acc_rate)
                     for c in sim.get_controllers(r)] for r in range(w.replicas)],
                   np.stack([sim.tally(r) for r in range(w.replicas)]))
         sim.close()
-    base = out[1]
-    for W in (2, 4, 8):
-        chains_w, dens_w, ctl_w, tal_w = out[W]
+    base = out[(1, 32)]
+    for shape in shapes[1:]:
+        chains_w, dens_w, ctl_w, tal_w = out[shape]
         for r in range(w.replicas):
             for a, b in zip(base[0][r], chains_w[r]):
                 np.testing.assert_array_equal(a, b)
@@ -55,9 +62,10 @@ def test_moves_in_flight_equal_sequential(fp64):
         np.testing.assert_array_equal(base[3], tal_w)
 
 
-def test_grid_consistent_after_parallel_run():
+@pytest.mark.parametrize("lanes", [8, 16, 32])
+def test_grid_consistent_after_parallel_run(lanes):
     w = _small(nrep=4, n=3000, nbins=16)
-    sim = wl.build_sim(w, warps_per_block=8)
+    sim = wl.build_sim(w, warps_per_block=8, lanes_per_move=lanes)
     sim.run(10, 3)
     sim.sync()
     inc = [sim.density(r) for r in range(w.replicas)]

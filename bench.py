@@ -80,6 +80,22 @@ def profile_case(args):
                       "algorithmic_bytes": wl.algorithmic_bytes(tal, w.n_binders)}), flush=True)
 
 
+TUNE_WARMUP, TUNE_STEPS = 62, 31  # one exchange round of warm-up, then half a round timed
+
+
+def _tune_child(workload, rank, local):
+    """Autotune the launch shape of this rank's workload (fills the cache)."""
+    import torch
+    torch.cuda.set_device(local)
+    from chromo_gb300 import autotune
+    from chromo_gb300 import workloads as wl
+    w = wl.make_workload(workload, seed_offset=rank)
+    chains = wl.make_chains(w)
+    autotune.tune(lambda W, G: wl.build_sim(w, chains, warps_per_block=W, lanes_per_move=G),
+                  w.lengths, [[w.nbins] * 3] * w.replicas, w.n_binders, steps=TUNE_STEPS,
+                  warmup=TUNE_WARMUP)
+
+
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -201,6 +217,14 @@ def main():
     if args.impl == "reference":
         reference_arm(args, rank, world)
         return
+    # wall seconds of each untimed setup phase and timed leg, reported with the line
+    phases, t_last = {}, [time.perf_counter()]
+
+    def mark(name):
+        now = time.perf_counter()
+        phases[name] = round(now - t_last[0], 2)
+        t_last[0] = now
+
     # CPU baseline first (spawned workers, before this process touches the GPU)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -216,14 +240,26 @@ def main():
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     w = wl.make_workload(args.workload, seed_offset=rank)
+    mark("cpu_baseline_and_import")
     chains = wl.make_chains(w)
+    mark("make_chains")
     # launch shape (warps per replica, lanes per move) picked by the autotuner
-    # on scratch copies of this workload (untimed; cached per problem)
+    # on scratch copies of this workload (untimed; cached per problem).  The
+    # tuning runs in a child process so that its scratch allocations leave
+    # no trace in this process's device memory.
     from chromo_gb300 import autotune
+    import multiprocessing as mp
+    child = mp.get_context("spawn").Process(target=_tune_child, args=(args.workload, rank, local))
+    child.start()
+    child.join()
     shape, tune_table = autotune.tune(
         lambda W, G: wl.build_sim(w, chains, warps_per_block=W, lanes_per_move=G),
-        w.lengths, [[w.nbins] * 3] * w.replicas, w.n_binders)
+        w.lengths, [[w.nbins] * 3] * w.replicas, w.n_binders, steps=TUNE_STEPS, warmup=TUNE_WARMUP)
+    mark("autotune")
     sim = wl.build_sim(w, chains, warps_per_block=shape[0], lanes_per_move=shape[1])
+    if w.mu_rungs:
+        sim.set_mu_ladder(w.mu_rungs, 0)
+    mark("build_sim")
     steps_round = w.steps_per_round
     moves_round = w.replicas * steps_round * w.moves_per_step
     # ---- warm-up rounds (graph capture happens on the first)
@@ -249,6 +285,7 @@ def main():
     attempts = float(tal[:, :, 0].sum())
     total_attempts = allreduce_sum(attempts, world)
     value = total_attempts / (ms_max / 1000.0)
+    mark("warmup_and_timed")
     # ---- roofline: MC kernel alone, CUDA events per launch
     sim.reset_tally()
     n_launch = 5
@@ -274,6 +311,26 @@ def main():
         hit = re.search(r"DRAM bytes per attempted move \| ([0-9.]+)", prof.read_text())
         if hit:
             traffic = float(hit.group(1)) * float(tal2[:, :, 0].sum()) / n_launch
+    mark("roofline_launches")
+    # ---- energy drift: FP64 energies recomputed on the device (cg_energies)
+    # around three MC launches (~3e4 moves per replica, no exchange) against
+    # the running sum of accepted dE.  Includes the reference's tangent-rotation
+    # rule (adjacent rotated beads each see the other's current tangent,
+    # chromo/polymers.pyx:1074-1080), so it is not rounding alone.
+    en0 = sim.energies(sh)
+    for i in range(3):
+        sim.run(steps_round, 301 + i, sh)
+    sim.sync(sh)
+    en1 = sim.energies(sh)
+    d_true = en1[:, :3].sum(1) - en0[:, :3].sum(1)
+    d_run = en1[:, 3] - en0[:, 3]
+    drift_abs = np.abs(d_true - d_run)
+    drift = {"max_abs_kT": float(drift_abs.max()), "median_abs_kT": float(np.median(drift_abs)),
+             "max_rel_to_energy": float((drift_abs / np.maximum(1.0, np.abs(en1[:, :3].sum(1)))).max()),
+             "moves_per_replica": int(3 * steps_round * w.moves_per_step),
+             "how": "FP64 full-energy recompute on the device before and after 3 MC launches "
+                    "vs the running sum of accepted dE"}
+    mark("energy_drift")
     # ---- e2e through the C ABI with host buffers
     h2d = d2h = 0
     pos_b = 16
@@ -293,6 +350,7 @@ def main():
     h2d = nbeads * (3 * pos_b + 4)
     d2h = nbeads * (3 * pos_b + 4)
     e2e_value = allreduce_sum(moves_round * e2e_steps, world) / allreduce_max(t_e2e, world)
+    mark("e2e")
     # ---- plain single chain (one CTA) on the same kernel
     wp = wl.make_workload("plain", seed_offset=rank)
     psim = wl.build_sim(wp)
@@ -308,6 +366,7 @@ def main():
     p_att = float(psim.tally(0)[:, 0].sum())
     plain_value = p_att / (pe0.elapsed_time(pe1) / 1000.0)
     launches = args.steps * (3 if w.n_rungs else 1)
+    mark("plain")
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "moves/s", "n_gpus": world,
@@ -334,8 +393,10 @@ def main():
             "plain": {"value": plain_value, "unit": "moves/s",
                       "workload": "one 10,000-bead chain, 60^3 grid, one binder, 300 MC steps",
                       "batched_over_plain": value / plain_value},
+            "energy_drift": drift,
             "gpu_launches": launches,
             "clocks": clocks.summary(),
+            "phase_seconds": phases,
         }
         if cpu is not None:
             out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}

@@ -84,6 +84,7 @@ EXPORTS = [
     "cg_reset_tally", "cg_exchange", "cg_get_chi", "cg_run_batched", "cg_get_launch_info",
     "cg_field_energy_static", "cg_energies", "cg_set_chains", "cg_get_chains", "cg_gradient",
     "cg_sample_terms", "cg_get_samples", "cg_get_launch_shape", "cg_mc_warps_per_sm",
+    "cg_set_mu_ladder", "cg_get_mu", "cg_get_swap_counts",
 ]
 N_TERMS = 14
 
@@ -126,6 +127,9 @@ def lib():
             "cg_get_launch_info": ([P, P, P, P], C.c_int),
             "cg_get_launch_shape": ([P, P, P, P, P], C.c_int),
             "cg_mc_warps_per_sm": ([I32, I32], C.c_int),
+            "cg_set_mu_ladder": ([P, I32, I32], C.c_int),
+            "cg_get_mu": ([P, I32, P], C.c_int),
+            "cg_get_swap_counts": ([P, P, P, P, P], C.c_int),
             "cg_field_energy_static": ([C.POINTER(FieldParams), I64, P, P, P, P, P], C.c_int),
             "cg_energies": ([P, P, P], C.c_int),
             "cg_set_chains": ([P, P, P, P, P], C.c_int),
@@ -344,6 +348,21 @@ class Sim:
         out = np.zeros(self.R)
         check(lib().cg_get_chi(self.h, _ptr(out)))
         return out
+
+    def set_mu_ladder(self, mu_rungs, binder=0):
+        """Exchange mu of ``binder`` between neighbouring mu rungs (0: off)."""
+        check(lib().cg_set_mu_ladder(self.h, int(mu_rungs), int(binder)))
+
+    def mu(self, binder=0):
+        out = np.zeros(self.R)
+        check(lib().cg_get_mu(self.h, int(binder), _ptr(out)))
+        return out
+
+    def swap_counts(self):
+        """Accepted / attempted chi and mu swaps per lower slot of each pair."""
+        arrs = [np.zeros(self.R, dtype=np.uint64) for _ in range(4)]
+        check(lib().cg_get_swap_counts(self.h, *[_ptr(a) for a in arrs]))
+        return dict(zip(("chi_swaps", "chi_attempts", "mu_swaps", "mu_attempts"), arrs))
 
     def run_batched(self, n_rounds, n_steps, n_rungs, seed, stream=None):
         check(lib().cg_run_batched(self.h, int(n_rounds), int(n_steps), int(n_rungs),

@@ -122,10 +122,14 @@ class ReplicaBatch:
             self.sim.run(int(num_mc_steps), int(random_seed), stream)
 
     def run_exchange(self, n_rounds: int, steps_per_round: int, n_rungs: int, random_seed: int,
-                     stream=None):
+                     stream=None, mu_rungs: int = 0, mu_binder: int = 0):
         """``n_rounds`` of (``steps_per_round`` MC steps, one exchange) under a
-        CUDA graph.  Ladders are n_rungs consecutive replicas; the swaps change
-        field energies outside of any move, so the drift baseline is reset."""
+        CUDA graph.  Ladders are n_rungs consecutive replicas; with
+        ``mu_rungs`` > 1 replicas form grids of mu_rungs x n_rungs and the
+        chemical potential of binder ``mu_binder`` is also exchanged between
+        neighbouring mu rungs.  The swaps change energies outside of any move,
+        so the drift baseline is reset."""
+        self.sim.set_mu_ladder(int(mu_rungs), int(mu_binder))
         self.sim.run_batched(int(n_rounds), int(steps_per_round), int(n_rungs), int(random_seed), stream)
         self.sim.sync(stream)
         self.rebaseline()
@@ -171,14 +175,21 @@ class ReplicaBatch:
     def chi(self) -> np.ndarray:
         return self.sim.chi()
 
+    def mu(self, binder: int = 0) -> np.ndarray:
+        """Chemical potential of ``binder`` on every replica (moved by mu-ladder exchange)."""
+        return self.sim.mu(binder)
+
     # ---------------------------------------------------------- derivatives
-    def _theta_coef(self, r):
+    def _theta_coef(self, r, mus=None):
         p, f = self.polymers[r], self.fields[r]
         binders = p.beads[0].binders
         vol_bin = f.vol_bin if isinstance(f, UniformDensityField) else 1.0
-        return theta_coefficients([b.chemical_potential for b in binders],
-                                  float(getattr(p, "mu_adjust_factor", 1.0)),
+        mu = [b.chemical_potential for b in binders] if mus is None else [m[r] for m in mus]
+        return theta_coefficients(mu, float(getattr(p, "mu_adjust_factor", 1.0)),
                                   [b.interaction_volume for b in binders], vol_bin)
+
+    def _device_mus(self):
+        return [self.sim.mu(b) for b in range(self.polymers[0].num_binders)]
 
     def gradient(self):
         """Per replica: dE/dr [N_r, 3] (FP32) and dE/d(chi, mu_0, mu_1, eps_00,
@@ -188,7 +199,8 @@ class ReplicaBatch:
         for p in self.polymers:
             per.append(g[off:off + p.num_beads])
             off += p.num_beads
-        theta = np.stack([self._theta_coef(r) @ T[r] for r in range(self.n_replicas)])
+        mus = self._device_mus()
+        theta = np.stack([self._theta_coef(r, mus) @ T[r] for r in range(self.n_replicas)])
         return per, theta
 
     def sample(self, n_samples: int, steps_between: int, random_seed: int, stream=None):
@@ -205,11 +217,12 @@ class ReplicaBatch:
         binder and the variance of the bead density over voxels, by
         reweighting the sampled configurations (-Cov(O, dE/dtheta))."""
         sum_t, sum_tt, count = self.sim.samples(reset)
+        mus = self._device_mus()
         out = []
         for r, (p, f) in enumerate(zip(self.polymers, self.fields)):
             n_vox = f.n_bins if isinstance(f, UniformDensityField) else 1
             O = observable_coefficients(p.num_beads, n_vox, p.num_binders)
-            out.append(reweighting_sensitivity(sum_t[r], sum_tt[r], count[r], O, self._theta_coef(r)))
+            out.append(reweighting_sensitivity(sum_t[r], sum_tt[r], count[r], O, self._theta_coef(r, mus)))
         return np.stack(out)
 
     # ------------------------------------------------------------ read back

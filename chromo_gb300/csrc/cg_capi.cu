@@ -77,6 +77,9 @@ struct cg_sim {
   long long* aout = nullptr;
   int* rep_of_rung = nullptr;
   unsigned long long *swaps = nullptr, *swap_attempts = nullptr, *xround = nullptr;
+  int mu_rungs = 0, mu_binder = 0;
+  double* nbound = nullptr;
+  unsigned long long *mu_swaps = nullptr, *mu_swap_attempts = nullptr;
   // shared-memory layout
   int logH = 0, warp_smem = 0, off_draws = 0, off_keys = 0, off_used = 0, off_bslot = 0, off_vals = 0, off_stage = 0,
       off_idx = 0;
@@ -127,6 +130,8 @@ struct cg_sim {
     a.spec_off_bmask = spec_off_bmask; a.spec_off_warps = spec_off_warps;
     a.rep_of_rung = rep_of_rung; a.swaps = swaps; a.swap_attempts = swap_attempts;
     a.xround = xround;
+    a.mu_rungs = mu_rungs; a.mu_binder = mu_binder; a.nbound = nbound;
+    a.mu_swaps = mu_swaps; a.mu_swap_attempts = mu_swap_attempts;
     return a;
   }
 
@@ -207,17 +212,19 @@ void cg_destroy(cg_sim* s) {
   void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
                   s->bonds32, s->grid, s->access_vol, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
                   s->picked, s->d_picked_off, s->eout, s->aout, s->rep_of_rung, s->swaps,
-                  s->swap_attempts, s->xround, s->grad, s->terms, s->acc};
+                  s->swap_attempts, s->xround, s->grad, s->terms, s->acc, s->nbound, s->mu_swaps,
+                  s->mu_swap_attempts};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete s;
 }
 
-// Lanes per move when the caller leaves it to the library: 16 for FP32
-// storage, 32 for FP64 storage (the only shape built for it).
+// Lanes per move when the caller leaves it to the library: 32 (the fastest
+// shape measured on the batched benchmark workload; the autotuner picks
+// others where they win), and always 32 for FP64 storage.
 static int default_lanes(const cg_sim* s, int g_req) {
   if (s->fp64) return 32;
-  return g_req > 0 ? g_req : 16;
+  return g_req > 0 ? g_req : 32;
 }
 
 // Warps per replica: the largest W <= kMaxW for which every replica's CTA is
@@ -347,6 +354,9 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   ALLOC(s->swaps, 8 * s->R);
   ALLOC(s->swap_attempts, 8 * s->R);
   ALLOC(s->xround, 8);
+  ALLOC(s->nbound, 8 * s->R);
+  ALLOC(s->mu_swaps, 8 * s->R);
+  ALLOC(s->mu_swap_attempts, 8 * s->R);
 #undef ALLOC
   if (e != cudaSuccess) {
     cg_destroy(s);
@@ -370,6 +380,9 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   cudaMemset(s->swaps, 0, 8 * s->R);
   cudaMemset(s->swap_attempts, 0, 8 * s->R);
   cudaMemset(s->xround, 0, 8);
+  cudaMemset(s->nbound, 0, 8 * s->R);
+  cudaMemset(s->mu_swaps, 0, 8 * s->R);
+  cudaMemset(s->mu_swap_attempts, 0, 8 * s->R);
   cudaMemcpy(s->d_picked_off, s->picked_off.data(), 8 * s->R, cudaMemcpyHostToDevice);
   std::vector<int> ror(s->R);
   for (int r = 0; r < s->R; r++) ror[r] = r;
@@ -853,9 +866,50 @@ static int enqueue_exchange(cg_sim* s, int n_rungs, long long round, uint64_t se
   return CG_OK;
 }
 
+// chi rungs per row (n_rungs) against the replica count and the mu ladder
+static int check_rungs(const cg_sim* s, long long n_rungs) {
+  if (s->mu_rungs > 1) {
+    if (n_rungs < 1 || s->R % (n_rungs * s->mu_rungs))
+      return fail(CG_ERR_ARG, "with a mu ladder, n_rungs * mu_rungs must divide n_replicas");
+    return CG_OK;
+  }
+  if (n_rungs < 2 || s->R % n_rungs) return fail(CG_ERR_ARG, "n_rungs must be >= 2 and divide n_replicas");
+  return CG_OK;
+}
+
+int cg_set_mu_ladder(cg_sim* s, int32_t mu_rungs, int32_t binder) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (mu_rungs != 0 && (mu_rungs < 2 || s->R % mu_rungs))
+    return fail(CG_ERR_ARG, "mu_rungs must be 0 or >= 2 and divide n_replicas");
+  if (binder < 0 || binder >= s->nb) return fail(CG_ERR_ARG, "binder index out of range");
+  s->mu_rungs = mu_rungs;
+  s->mu_binder = binder;
+  if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }  // arguments are baked into it
+  return CG_OK;
+}
+
+int cg_get_mu(cg_sim* s, int32_t binder, double* mu) {
+  if (!s || !mu) return fail(CG_ERR_ARG, "null argument");
+  if (binder < 0 || binder >= s->nb) return fail(CG_ERR_ARG, "binder index out of range");
+  std::vector<RepDev> rd(s->R);
+  CUDA_TRY(cudaMemcpy(rd.data(), s->reps, sizeof(RepDev) * s->R, cudaMemcpyDeviceToHost));
+  for (int r = 0; r < s->R; r++) mu[r] = rd[r].mu[binder];
+  return CG_OK;
+}
+
+int cg_get_swap_counts(cg_sim* s, uint64_t* chi_swaps, uint64_t* chi_attempts, uint64_t* mu_swaps,
+                       uint64_t* mu_attempts) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  uint64_t* dst[4] = {chi_swaps, chi_attempts, mu_swaps, mu_attempts};
+  unsigned long long* src[4] = {s->swaps, s->swap_attempts, s->mu_swaps, s->mu_swap_attempts};
+  for (int k = 0; k < 4; k++)
+    if (dst[k]) CUDA_TRY(cudaMemcpy(dst[k], src[k], 8 * s->R, cudaMemcpyDeviceToHost));
+  return CG_OK;
+}
+
 int cg_exchange(cg_sim* s, int n_rungs, int64_t round, uint64_t seed, void* stream) {
   if (!s) return fail(CG_ERR_ARG, "null sim");
-  if (n_rungs < 2 || s->R % n_rungs) return fail(CG_ERR_ARG, "n_rungs must be >= 2 and divide n_replicas");
+  if (int rc = check_rungs(s, n_rungs)) return rc;
   enqueue_exchange(s, n_rungs, round, seed, (cudaStream_t)stream);
   CUDA_TRY(cudaGetLastError());
   return CG_OK;
@@ -873,7 +927,8 @@ int cg_run_batched(cg_sim* s, int64_t n_rounds, int64_t n_steps, int32_t n_rungs
                    void* stream) {
   if (!s) return fail(CG_ERR_ARG, "null sim");
   if (n_rounds < 1 || n_steps < 1) return fail(CG_ERR_ARG, "n_rounds and n_steps must be >= 1");
-  if (n_rungs && (n_rungs < 2 || s->R % n_rungs)) return fail(CG_ERR_ARG, "n_rungs must be 0 or divide n_replicas");
+  if (n_rungs)
+    if (int rc = check_rungs(s, n_rungs)) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   if (!(s->graph && s->graph_rounds == n_rounds && s->graph_steps == n_steps && s->graph_rungs == n_rungs &&
         s->graph_seed == seed && s->graph_stream == st)) {

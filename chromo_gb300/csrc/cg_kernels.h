@@ -107,10 +107,16 @@ struct KArgs {
   long long a_max_recs;
   long long* a_out;
   // replica exchange
-  int* rep_of_rung;
+  int* rep_of_rung;            // parameter slot -> replica holding that slot's (chi, mu)
   unsigned long long* swaps;
   unsigned long long* swap_attempts;
   unsigned long long* xround;  // exchange rounds performed (graph replays)
+  // mu ladder: mu_rungs > 1 arranges slots as [grid][mu rung][chi rung] and
+  // also swaps mu of binder mu_binder between neighbouring mu rungs
+  int mu_rungs, mu_binder;
+  double* nbound;              // per replica: bound sites of binder mu_binder
+  unsigned long long* mu_swaps;
+  unsigned long long* mu_swap_attempts;
 };
 
 }  // namespace cg

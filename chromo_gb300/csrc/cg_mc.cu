@@ -638,6 +638,14 @@ __global__ void chi_sum_kernel(KArgs a, double* out) {
   }
   const double t = block_sum(sx, sh);
   if (threadIdx.x == 0) out[rep * 5 + 4] = t;
+  if (a.mu_rungs > 1) {  // bound sites of the mu-ladder binder (exact integer sum)
+    const unsigned* st = a.states + rd.bead_off;
+    const int sh8 = 8 * a.mu_binder;
+    long long nbl = 0;
+    for (long long i = threadIdx.x; i < rd.n_beads; i += blockDim.x) nbl += (st[i] >> sh8) & 0xFFu;
+    const double nbt = block_sum((double)nbl, sh);
+    if (threadIdx.x == 0) a.nbound[rep] = nbt;
+  }
 }
 
 // ---------------------------------------------------------------- replica exchange
@@ -654,7 +662,7 @@ __global__ void exchange_kernel(KArgs a, const double* eout, int n_rungs, long l
   const long long round = round_sh;
   const int parity = (int)(round & 1);
   const int ladders = a.n_reps / n_rungs;
-  const int per = n_rungs / 2;
+  const int per = n_rungs / 2;  // no chi pairs for n_rungs = 1 (a mu-only ladder)
   for (int t = threadIdx.x; t < ladders * per; t += blockDim.x) {
     const int ladder = t / per, pair = t % per;
     if (2 * pair + 1 + parity >= n_rungs) continue;
@@ -673,6 +681,42 @@ __global__ void exchange_kernel(KArgs a, const double* eout, int n_rungs, long l
       a.swaps[ra] += 1;
     }
     a.swap_attempts[ra] += 1;
+  }
+  __syncthreads();
+  // mu swaps between neighbouring mu rungs (same chi rung) of each grid of
+  // mu_rungs x n_rungs slots: the mu-dependent energy of replica r is
+  // -m(mu_r) N_r with m(mu) = mu (2 - f) for mu > 0, mu f otherwise
+  // (chromo/polymers.pyx:1520-1531), N_r its bound sites of the binder, so a
+  // swap changes the energy by dE = m_a(mu_a) N_a + m_b(mu_b) N_b
+  // - m_a(mu_b) N_a - m_b(mu_a) N_b and is accepted iff u < exp(-dE).
+  if (a.mu_rungs > 1) {
+    const int nm = a.mu_rungs, b = a.mu_binder;
+    const int grids = a.n_reps / (nm * n_rungs);
+    const int mper = nm / 2;
+    for (int t = threadIdx.x; t < grids * n_rungs * mper; t += blockDim.x) {
+      const int grid = t / (n_rungs * mper), rest = t % (n_rungs * mper);
+      const int crung = rest / mper, pair = rest % mper;
+      const int mr = 2 * pair + parity;
+      if (mr + 1 >= nm) continue;
+      const int sa = (grid * nm + mr) * n_rungs + crung, sb = sa + n_rungs;
+      const int ia = a.rep_of_rung[sa], ib = a.rep_of_rung[sb];
+      const double mua = a.reps[ia].mu[b], mub = a.reps[ib].mu[b];
+      const double fa = a.reps[ia].mu_adjust, fb = a.reps[ib].mu_adjust;
+      auto eff = [](double mu, double f) { return mu > 0 ? mu * (-f + 2) : mu * f; };
+      const double na = a.nbound[ia], nb = a.nbound[ib];
+      const double dE = eff(mua, fa) * na + eff(mub, fb) * nb - eff(mub, fa) * na - eff(mua, fb) * nb;
+      uint4 o = philox(make_uint4((unsigned)round, (unsigned)(round >> 32), (unsigned)sa, 0x5BE0CD19u),
+                       make_uint2((unsigned)seed ^ 0xA4093822u, (unsigned)(seed >> 32)));
+      const double u = (double)(o.x >> 1) / kRandMax;
+      if (u < exp(-dE)) {
+        a.reps[ia].mu[b] = mub;
+        a.reps[ib].mu[b] = mua;
+        a.rep_of_rung[sa] = ib;
+        a.rep_of_rung[sb] = ia;
+        a.mu_swaps[sa] += 1;
+      }
+      a.mu_swap_attempts[sa] += 1;
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0 && round_in < 0) a.xround[0] += 1;

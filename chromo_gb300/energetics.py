@@ -30,15 +30,13 @@ def dss_parameters(bead_length, lp):
     """(delta, eps_bend, gamma, eps_par, eps_perp, eta) per bond."""
     t = dss_table()
     bl = np.asarray(bead_length, dtype=np.float64)
-    n = len(bl)
-    delta, eb, g, ep, epp, eta = (np.zeros(n) for _ in range(6))
-    for i in range(n):
-        delta[i] = bl[i] / lp
-        eb[i] = np.interp(delta[i], t[:, 0], t[:, 1]) / delta[i]
-        g[i] = np.interp(delta[i], t[:, 0], t[:, 2]) * delta[i] * lp
-        ep[i] = np.interp(delta[i], t[:, 0], t[:, 3]) / (delta[i] * lp ** 2)
-        epp[i] = np.interp(delta[i], t[:, 0], t[:, 4]) / (delta[i] * lp ** 2)
-        eta[i] = np.interp(delta[i], t[:, 0], t[:, 5]) / lp
+    # element-wise the same arithmetic as one np.interp call per bond
+    delta = bl / lp
+    eb = np.interp(delta, t[:, 0], t[:, 1]) / delta
+    g = np.interp(delta, t[:, 0], t[:, 2]) * delta * lp
+    ep = np.interp(delta, t[:, 0], t[:, 3]) / (delta * lp ** 2)
+    epp = np.interp(delta, t[:, 0], t[:, 4]) / (delta * lp ** 2)
+    eta = np.interp(delta, t[:, 0], t[:, 5]) / lp
     return delta, eb, g, ep, epp, eta
 
 

@@ -10,7 +10,8 @@ Sizes follow the benchmark configurations of this path:
               chi ladder of 16 rungs in [0.5, 2.0] (16 ladders of 16 rungs).
 * ``diff``    64 chains of 5,000 beads, 40^3 grids, binders as ``batched``.
 * ``large``   32 chains of 100,000 beads, 100^3 grids, chi ladder of 8 rungs
-              times a sweep of 4 mu_A values.
+              times a sweep of 4 mu_A values (one grid of 4 x 8 parameter slots:
+              chi exchanged along rows, mu_A along columns).
 
 Chains are seeded Gaussian walks (16.5 nm spacing, lp = 53 nm) and every
 replica runs all five moves under SimpleControl with the reference's
@@ -72,6 +73,7 @@ class Workload:
     n_rungs: int
     seed: int
     steps_per_round: int = 62    # ~1e4 attempted moves per replica per exchange round
+    mu_rungs: int = 0            # > 1: grids of mu_rungs x n_rungs, mu_A exchanged along mu rungs
     replicas: int = field(init=False)
 
     def __post_init__(self):
@@ -109,7 +111,7 @@ def make_workload(name: str, seed_offset: int = 0) -> Workload:
         mu = np.stack([mu_a, rng.uniform(-1.0, 0.0, size=R)], axis=1)
         chi = np.tile(np.linspace(0.5, 2.0, rungs), R // rungs)
         return Workload("large", np.full(R, 100000), 100, 2, mu, chi, [-4.0, -3.0],
-                        [{"PRC1": 1.0}, {}], 50, rungs, BASE_SEED + 4 + seed_offset)
+                        [{"PRC1": 1.0}, {}], 50, rungs, BASE_SEED + 4 + seed_offset, mu_rungs=4)
     raise ValueError(f"unknown workload {name}")
 
 

@@ -223,6 +223,23 @@ int cg_reset_tally(cg_sim *sim);
 int cg_exchange(cg_sim *sim, int32_t n_rungs, int64_t round, uint64_t seed, void *stream);
 int cg_get_chi(cg_sim *sim, double *chi);
 
+/* Two-dimensional ladder (no counterpart in the reference): with mu_rungs >= 2
+ * the parameter slots form grids of mu_rungs x n_rungs (slot = (grid * mu_rungs
+ * + mu rung) * n_rungs + chi rung, replica r starting in slot r), and every
+ * exchange round after its chi swaps also proposes, for mu-rung pairs
+ * (2i+p, 2i+1+p) at the same chi rung, to swap the chemical potential of
+ * binder `binder`, accepted with probability min(1, exp(-dE)), dE the change
+ * of sum_r -m(mu_r) N_r (m(mu) = mu (2 - f) for mu > 0, mu f otherwise, f the
+ * annealing factor; N_r the replica's bound sites of that binder,
+ * chromo/polymers.pyx:1520-1531).  n_rungs = 1 gives a mu-only ladder.
+ * mu_rungs = 0 switches it off. */
+int cg_set_mu_ladder(cg_sim *sim, int32_t mu_rungs, int32_t binder);
+int cg_get_mu(cg_sim *sim, int32_t binder, double *mu);
+/* Accepted and attempted swaps per lower slot of each pair [n_replicas] each
+ * (any pointer may be NULL). */
+int cg_get_swap_counts(cg_sim *sim, uint64_t *chi_swaps, uint64_t *chi_attempts, uint64_t *mu_swaps,
+                       uint64_t *mu_attempts);
+
 /* Batched run: n_rounds x (n_steps MC steps on every replica, then one
  * exchange round), captured once in a CUDA graph and replayed.  n_rungs = 0
  * disables exchange. */

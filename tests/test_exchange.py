@@ -140,3 +140,81 @@ def test_batched_rounds_exchange_after_mc():
             cur = got
     finally:
         sim.close()
+
+
+def mu_uniform(seed, round_, slot):
+    o = philox4x32_10([round_ & MASK, (round_ >> 32) & MASK, slot, 0x5BE0CD19],
+                      [(seed & MASK) ^ 0xA4093822, (seed >> 32) & MASK])
+    return (o[0] >> 1) / 2147483647.0
+
+
+def expected_mu_exchange(mu, nbound, ror, n_chi, n_mu, round_, seed, f=1.0, tie=1e-9):
+    """The mu pass of one exchange round on the host: slots of each grid are
+    (mu rung m, chi rung c) -> (grid * n_mu + m) * n_chi + c; pairs (2i+p,
+    2i+1+p) of mu rungs at equal chi rung swap mu iff u < exp(-dE), dE the
+    change of sum_r -m(mu_r) N_r, m(mu) = mu (2 - f) for mu > 0 else mu f."""
+    mu, ror = mu.copy(), ror.copy()
+    parity = round_ & 1
+    swaps = ties = 0
+    eff = lambda x: x * (2 - f) if x > 0 else x * f
+    for grid in range(len(mu) // (n_chi * n_mu)):
+        for c in range(n_chi):
+            for pair in range(n_mu // 2):
+                m = 2 * pair + parity
+                if m + 1 >= n_mu:
+                    continue
+                sa = (grid * n_mu + m) * n_chi + c
+                sb = sa + n_chi
+                ia, ib = ror[sa], ror[sb]
+                na, nb = nbound[ia], nbound[ib]
+                dE = eff(mu[ia]) * na + eff(mu[ib]) * nb - eff(mu[ib]) * na - eff(mu[ia]) * nb
+                u = mu_uniform(seed, round_, sa)
+                ties += abs(u - np.exp(-dE)) < tie
+                if u < np.exp(-dE):
+                    mu[ia], mu[ib] = mu[ib], mu[ia]
+                    ror[sa], ror[sb] = ib, ia
+                    swaps += 1
+    return mu, ror, swaps, ties
+
+
+@pytest.mark.gpu
+def test_mu_ladder_rounds_match_host_rule():
+    """Two-dimensional ladder: 8 replicas as one grid of 4 mu rungs x 2 chi
+    rungs; each round swaps chi along the rows, then mu of binder 0 along the
+    columns, both against the host restatement of the rules."""
+    pytest.importorskip("torch")
+    from chromo_gb300 import workloads as wl
+    R, n_chi, n_mu = 8, 2, 4
+    rng = np.random.default_rng(9)
+    mu = np.stack([np.repeat([-0.5, -0.45, -0.4, -0.35], n_chi), rng.uniform(-1, 0, size=R)], axis=1)
+    w = wl.Workload("mu_ladder", np.full(R, 400), 10, 2, mu, np.tile([0.8, 1.2], n_mu),
+                    [-4.0, -3.0], [{"PRC1": 1.0}, {}], 50, n_chi, wl.BASE_SEED + 12)
+    sim = wl.build_sim(w)
+    try:
+        sim.set_mu_ladder(n_mu, 0)
+        seed = 0xBEEF_0001
+        ror = np.arange(R)
+        chi, cur_mu = sim.chi(), sim.mu(0)
+        np.testing.assert_array_equal(cur_mu, mu[:, 0])
+        mu_total = 0
+        for rnd in range(10):
+            sim.run(2, 300 + rnd)
+            sim.sync()
+            S = _chi_sums(sim, w)
+            nbound = np.array([sim.get_chain(r)[3][:, 0].sum() for r in range(R)], dtype=np.float64)
+            want_chi, ror, _, ties_c = expected_exchange(chi, S, ror, n_chi, rnd, seed)
+            want_mu, ror, swaps, ties_m = expected_mu_exchange(cur_mu, nbound, ror, n_chi, n_mu, rnd, seed)
+            sim.exchange(n_chi, rnd, seed)
+            sim.sync()
+            chi, cur_mu = sim.chi(), sim.mu(0)
+            if not (ties_c or ties_m):
+                np.testing.assert_array_equal(chi, want_chi)
+                np.testing.assert_array_equal(cur_mu, want_mu)
+            mu_total += swaps
+        # the other binder's mu never moves
+        np.testing.assert_array_equal(sim.mu(1), mu[:, 1])
+        counts = sim.swap_counts()
+        assert int(counts["mu_swaps"].sum()) == mu_total
+        assert 0 < mu_total < int(counts["mu_attempts"].sum())
+    finally:
+        sim.close()

@@ -35,13 +35,28 @@ WORKLOAD_DESC = ("batched replicas: 256 chains, lengths log-uniform in [2000, 20
                  "in [0.5, 2.0], exchange every 62 MC steps (~1e4 moves per replica)")
 
 
+WORKLOAD_DESCS = {
+    "batched": WORKLOAD_DESC,
+    "large": ("large batched: 32 chains of 100,000 beads, each in its own periodic 4000 nm box with a "
+              "100^3 grid of 40 nm voxels; FP32 positions, int64 fixed-point density; two binders; "
+              "one grid of 4 mu_A values x 8 chi rungs in [0.5, 2.0], chi and mu_A exchanged every 62 "
+              "MC steps (~1e4 moves per replica)"),
+    "diff": ("batched + differentiation: 64 chains of 5,000 beads, 40^3 grids (40 nm voxels), two "
+             "binders, no exchange; dE/dr and dE/d(chi, mu_A, mu_B, eps_AA, eps_BB, eps_AB) kernels "
+             "and 1e6 on-device reweighting samples reported under 'derivatives'"),
+}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "large", "diff"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "large", "diff"],
+                    help="batched: 256 replicas (the headline); large: 32 x 100,000 beads with a "
+                         "chi x mu ladder; diff: 64 x 5,000 beads plus the derivative kernels and 1e6 "
+                         "reweighting samples")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-budget", type=float, default=2.0)
     ap.add_argument("--profile", action="store_true",
@@ -59,7 +74,7 @@ def profile_case(args):
     from chromo_gb300.build import build
     build()
     from chromo_gb300 import workloads as wl
-    w = wl.make_workload("diff")
+    w = wl.make_workload("profile")
     sim = wl.build_sim(w)
     sh = torch.cuda.current_stream().cuda_stream
     sim.run(w.steps_per_round, 1, sh)
@@ -80,7 +95,7 @@ def profile_case(args):
                       "algorithmic_bytes": wl.algorithmic_bytes(tal, w.n_binders)}), flush=True)
 
 
-TUNE_WARMUP, TUNE_STEPS = 62, 31  # one exchange round of warm-up, then half a round timed
+TUNE_WARMUP, TUNE_STEPS = 186, 62  # the timed region's state: three rounds of warm-up, one timed
 
 
 def _tune_child(workload, rank, local):
@@ -94,6 +109,56 @@ def _tune_child(workload, rank, local):
     autotune.tune(lambda W, G: wl.build_sim(w, chains, warps_per_block=W, lanes_per_move=G),
                   w.lengths, [[w.nbins] * 3] * w.replicas, w.n_binders, steps=TUNE_STEPS,
                   warmup=TUNE_WARMUP)
+
+
+def derivatives_leg(sim, w, stream):
+    """Batched + differentiation: the backward kernels (dE/dr of every bead in
+    FP32 and the 14 energy terms per replica, cg_gradient) timed over five
+    calls, then 1e6 sampled configurations (every replica sampled after each
+    MC step, T and T T^T summed on the device by cg_sample_terms) and the
+    reweighting sensitivities d<O>/dtheta = -Cov(O, dE/dtheta) they give."""
+    import math
+    import numpy as np
+    import torch
+    from chromo_gb300 import workloads as wl
+    from chromo_gb300.derivatives import (THETA_NAMES, observable_coefficients,
+                                          reweighting_sensitivity, theta_coefficients)
+    sh = stream.cuda_stream
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(5):
+        grad, terms = sim.gradient()
+    grad_ms = (time.perf_counter() - t0) / 5 * 1e3
+    per_rep = int(math.ceil(1e6 / w.replicas))
+    sim.samples(reset=True)
+    sim.reset_tally()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(per_rep):
+        sim.run(1, 7000 + k, sh)
+        sim.sample_terms(sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sim.sync(sh)
+    ms = e0.elapsed_time(e1)
+    sum_t, sum_tt, count = sim.samples()
+    moves = float(sum(sim.tally(r)[:, 0].sum() for r in range(sim.R)))
+    vint = 4.0 / 3.0 * np.pi * wl.R_INT ** 3
+    O = observable_coefficients(int(w.lengths[0]), w.nbins ** 3, w.n_binders)
+    sens = np.stack([reweighting_sensitivity(sum_t[r], sum_tt[r], count[r], O,
+                                             theta_coefficients(w.mu[r], 1.0, [vint] * w.n_binders,
+                                                                wl.VOXEL ** 3))
+                     for r in range(sim.R)])
+    names = [f"occupancy_{b}" for b in range(w.n_binders)] + ["density_variance"]
+    mean = {f"d<{o}>/d{t}": float(sens[:, i, j].mean()) for i, o in enumerate(names)
+            for j, t in enumerate(THETA_NAMES) if (o.startswith("occ") and t in ("chi", "mu_0", "mu_1"))
+            or (o == "density_variance" and t == "chi")}
+    return {"gradient_ms_per_call": grad_ms,
+            "gradient": "dE/dr of all %d beads (FP32) + 14 energy terms per replica" % int(w.lengths.sum()),
+            "sampled_configurations": int(count.sum()), "sampling_s": ms / 1e3,
+            "configurations_per_s": float(count.sum()) / (ms / 1e3),
+            "mc_moves_during_sampling": moves,
+            "mean_sensitivities_over_replicas": mean}
 
 
 def load_peaks():
@@ -196,7 +261,7 @@ def reference_arm(args, rank, world):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD_DESC if args.workload == "batched" else args.workload,
+        "config": {"workload": WORKLOAD_DESCS[args.workload],
                    "replicas": int(w.replicas)},
         "cpu_baseline": {"value": res["value"], "unit": "moves/s", "cores": res["cores"],
                          "kind": res["kind"], "sample": res["sample"]},
@@ -225,11 +290,6 @@ def main():
         phases[name] = round(now - t_last[0], 2)
         t_last[0] = now
 
-    # CPU baseline first (spawned workers, before this process touches the GPU)
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        from oracle import refbench
-        cpu = refbench.run(args.workload, budget=args.cpu_budget, n_procs=os.cpu_count())
     import numpy as np
     import torch
     from chromo_gb300.build import build
@@ -240,7 +300,7 @@ def main():
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     w = wl.make_workload(args.workload, seed_offset=rank)
-    mark("cpu_baseline_and_import")
+    mark("import_and_build")
     chains = wl.make_chains(w)
     mark("make_chains")
     # launch shape (warps per replica, lanes per move) picked by the autotuner
@@ -367,16 +427,26 @@ def main():
     plain_value = p_att / (pe0.elapsed_time(pe1) / 1000.0)
     launches = args.steps * (3 if w.n_rungs else 1)
     mark("plain")
+    deriv = derivatives_leg(sim, w, stream) if args.workload == "diff" else None
+    mark("derivatives")
+    # CPU baseline last (spawned workers), so that the host cores it loads do
+    # not share the timed GPU legs' power and memory budget
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import refbench
+        cpu = refbench.run(args.workload, budget=args.cpu_budget, n_procs=os.cpu_count())
+    mark("cpu_baseline")
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "moves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Gaussian-walk chains, Markov mark tracks)",
-            "config": {"workload": WORKLOAD_DESC, "replicas": int(w.replicas),
+            "config": {"workload": WORKLOAD_DESCS[args.workload], "replicas": int(w.replicas),
                        "beads_total": nbeads, "mc_steps_per_step": steps_round,
                        "attempted_moves_per_step": int(attempts / args.steps),
-                       "l2": "inputs larger than L2 (grids 256 x 1.5 MB + chains > 129 MB)",
+                       "l2": "inputs larger than L2 (%.0f MB of grids and chains > 129 MB)"
+                             % ((w.replicas * w.nbins ** 3 * 32 + nbeads * 104) / 1e6),
                        "graph": "one exchange round captured in a CUDA graph, replayed per step",
                        "launch_shape": dict(zip(("warps_per_replica", "lanes_per_move", "moves_in_flight",
                                                  "hash_slots"), sim.launch_shape())),
@@ -398,6 +468,8 @@ def main():
             "clocks": clocks.summary(),
             "phase_seconds": phases,
         }
+        if deriv is not None:
+            out["derivatives"] = deriv
         if cpu is not None:
             out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         print(json.dumps(out), flush=True)

@@ -8,7 +8,10 @@ Sizes follow the benchmark configurations of this path:
               its own 40^3 grid, two binders (eps_AA = -4, eps_BB = -3,
               eps_AB = +1 stored on A; mu_A, mu_B ~ U[-1, 0] per replica),
               chi ladder of 16 rungs in [0.5, 2.0] (16 ladders of 16 rungs).
-* ``diff``    64 chains of 5,000 beads, 40^3 grids, binders as ``batched``.
+* ``diff``    64 chains of 5,000 beads, 40^3 grids, binders as ``batched``
+              (the batched + differentiation configuration; no exchange).
+* ``profile`` 256 chains of 5,000 beads: the CTA shape of ``batched`` with
+              fixed lengths, a bounded case for profilers.
 * ``large``   32 chains of 100,000 beads, 100^3 grids, chi ladder of 8 rungs
               times a sweep of 4 mu_A values (one grid of 4 x 8 parameter slots:
               chi exchanged along rows, mu_A along columns).
@@ -99,11 +102,17 @@ def make_workload(name: str, seed_offset: int = 0) -> Workload:
         chi = np.tile(np.linspace(0.5, 2.0, rungs), R // rungs)
         return Workload("batched", lengths, 40, 2, mu, chi, [-4.0, -3.0], [{"PRC1": 1.0}, {}],
                         50, rungs, BASE_SEED + 2 + seed_offset)
-    if name == "diff":  # fixed-length chains for profiling; the same CTA shape as "batched"
+    if name == "diff":  # batched + differentiation: 64 chains of 5,000 beads, no exchange
+        R = 64
+        mu = rng.uniform(-1.0, 0.0, size=(R, 2))
+        chi = np.full(R, 1.0)
+        return Workload("diff", np.full(R, 5000), 40, 2, mu, chi, [-4.0, -3.0],
+                        [{"PRC1": 1.0}, {}], 50, 0, BASE_SEED + 3 + seed_offset)
+    if name == "profile":  # fixed-length chains for profilers; the same CTA shape as "batched"
         R = 256
         mu = rng.uniform(-1.0, 0.0, size=(R, 2))
         chi = np.tile(np.linspace(0.5, 2.0, 16), R // 16)
-        return Workload("diff", np.full(R, 5000), 40, 2, mu, chi, [-4.0, -3.0],
+        return Workload("profile", np.full(R, 5000), 40, 2, mu, chi, [-4.0, -3.0],
                         [{"PRC1": 1.0}, {}], 50, 16, BASE_SEED + 3 + seed_offset)
     if name == "large":
         R, rungs = 32, 8

@@ -555,6 +555,29 @@ __device__ void conflict_mask(const KArgs& a, SpecShared& sh, unsigned char* sme
   if (gl == 0 && live) P.cmask = cm;
 }
 
+// SimpleControl.update_amplitudes (chromo/mc/mc_controller.py:126-189)
+__device__ __forceinline__ void update_amplitudes(cg_move_ctl& c) {
+  if (c.ctrl_kind != 1) return;
+  double acc = c.acc_rate;
+  if (acc < 0.5) {
+    double prop = c.amp_move * 0.95;
+    if (prop > c.move_lo) c.amp_move = prop;
+    else {
+      c.amp_move = c.move_hi;
+      double nb = (double)(c.amp_bead - 1);
+      c.amp_bead = (long long)(c.bead_lo > nb ? c.bead_lo : nb);
+    }
+  } else if (acc > 0.5) {
+    double prop = c.amp_move / 0.95;
+    if (prop < c.move_hi) c.amp_move = prop;
+    else {
+      c.amp_move = c.move_lo;
+      double nb = (double)(c.amp_bead + 1);
+      c.amp_bead = (long long)(c.bead_hi < nb ? c.bead_hi : nb);
+    }
+  }
+}
+
 template <typename Pos, int G>
 __device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int s, int gl, bool accept,
                                  const SlotScratch& sm, const SlotScratch& gm, int* bkeys, unsigned* bmask) {
@@ -750,26 +773,7 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
         }
       }
       if (sh.stop) break;
-      if (tid == 0 && c.ctrl_kind == 1) {  // SimpleControl.update_amplitudes, mc_controller.py:126-189
-        double acc = c.acc_rate;
-        if (acc < 0.5) {
-          double prop = c.amp_move * 0.95;
-          if (prop > c.move_lo) c.amp_move = prop;
-          else {
-            c.amp_move = c.move_hi;
-            double nb = (double)(c.amp_bead - 1);
-            c.amp_bead = (long long)(c.bead_lo > nb ? c.bead_lo : nb);
-          }
-        } else if (acc > 0.5) {
-          double prop = c.amp_move / 0.95;
-          if (prop < c.move_hi) c.amp_move = prop;
-          else {
-            c.amp_move = c.move_lo;
-            double nb = (double)(c.amp_bead + 1);
-            c.amp_bead = (long long)(c.bead_hi < nb ? c.bead_hi : nb);
-          }
-        }
-      }
+      if (tid == 0) update_amplitudes(c);
       __syncthreads();
     }
     if (sh.stop) break;

@@ -89,6 +89,11 @@ CASES = {
     # null field with a spherical confinement (confinement dE only)
     "null_spherical": dict(n=200, binders=[("HP1", -0.4, -4.0, {})], null_field=True,
                            confine=("Spherical", 400.0), steps=4, moves="all", seed=15, run=20),
+    # spherical confinement of a density field with accessible volumes computed
+    # for the voxels the sphere cuts (assume_fully_accessible=0)
+    "sphere_access": dict(n=120, nbins=16, vox=40.0, binders=[("HP1", -0.4, -4.0, {})], chi=1.0,
+                          confine=("Spherical", 300.0), access=True, steps=4, moves="all", seed=17,
+                          run=20),
     # large amplitudes without adaptation: long segments, many tangent beads
     "big_amps": dict(n=160, nbins=8, vox=40.0, binders=[("HP1", -0.4, -4.0, {})], chi=1.0,
                      steps=30, moves="big", seed=16, run=20),
@@ -122,8 +127,11 @@ def make_field(cfg, p, binders):
         ct, cl = cfg["confine"]
         return NullField([p], confine_type=ct, confine_length=cl)
     w = cfg["nbins"] * cfg["vox"]
+    ct, cl = cfg.get("confine", ("", 0.0))
     return UniformDensityField([p], binders, w, cfg["nbins"], w, cfg["nbins"], w, cfg["nbins"],
-                               chi=cfg["chi"], vf_limit=cfg.get("vf_limit", 0.5))
+                               confine_type=ct, confine_length=cl, chi=cfg["chi"],
+                               assume_fully_accessible=0 if cfg.get("access") else 1,
+                               vf_limit=cfg.get("vf_limit", 0.5))
 
 
 def make_controllers(cfg, p):
@@ -283,6 +291,8 @@ def run_case(name, cfg):
         states1=np.asarray(p.states).copy(), density1=density_of(field),
         density0=None if not uniform else None,
         E_elastic1=p.compute_E(),
+        access_vols=(np.array([field.access_vols[i] for i in range(field.n_bins)])
+                     if uniform and cfg.get("access") else None),
     )
     out = {k: v for k, v in out.items() if v is not None}
     np.savez_compressed(OUT / f"{name}.npz", **out)

@@ -25,7 +25,7 @@ def oracle_system(g, pos="f64", fixed_density=0, state="0"):
         max_binders=int(g["max_binders"]), field_kind=int(g["field_kind"]),
         confine_kind=int(g["confine_kind"]), confine_length=float(g["confine_length"]),
         nxyz=tuple(int(x) for x in g["nxyz"]), widths=tuple(float(x) for x in g["widths"]),
-        chi=float(g["chi"]), vf_limit=float(g["vf_limit"]),
+        access_vol=g.get("access_vols"), chi=float(g["chi"]), vf_limit=float(g["vf_limit"]),
         bead_vol=4.0 / 3.0 * np.pi * float(g["bead_rad"]) ** 3,
         pref=g["pref"], intra=g["intra"], xpref=g["xpref"], pos=pos,
         fixed_density=fixed_density)
@@ -51,8 +51,9 @@ def gpu_sim(g, pos_fp64, state="0"):
     ctl0 = g["ctl0"]
     max_seg = int(max(max(row[1], row[5]) for k, row in enumerate(ctl0) if k != 3)) + 2
     max_tan = int(max(ctl0[3][1], ctl0[3][5]))
+    access = g.get("access_vols")
     sim = nat.Sim([n], [list(g["nxyz"])], nb, pos_fp64=pos_fp64, max_segment=max_seg,
-                  max_tangent=max_tan)
+                  max_tangent=max_tan, nonuniform_access=access is not None)
     sim.set_chain(0, r=g["r" + state], t3=g["t3" + state], t2=g["t2" + state],
                   states=g["states" + state], marks=g["marks"],
                   bonds=bonds_array(g["eps_bend"], g["gamma"], g["eps_par"], g["eps_perp"], g["eta"]))
@@ -61,7 +62,7 @@ def gpu_sim(g, pos_fp64, state="0"):
         confine_length=float(g["confine_length"]), nxyz=g["nxyz"], widths=g["widths"],
         n_binders=nb, chi=float(g["chi"]), vf_limit=float(g["vf_limit"]),
         bead_vol=4.0 / 3.0 * np.pi * float(g["bead_rad"]) ** 3, pref=g["pref"], intra=g["intra"],
-        xpref=g["xpref"]))
+        xpref=g["xpref"]), access_vol=access)
     sim.set_binding(0, binding_params(sites=g["sites"], e_mod=g["e_mod"], e_nomod=g["e_nomod"],
                                       mu=g["mu"], mu_adjust_factor=float(g["mu_adjust_factor"]),
                                       max_binders=int(g["max_binders"])))

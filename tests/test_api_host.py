@@ -51,6 +51,22 @@ def test_field_prefactors_match_reference(name):
     assert f.vol_bin == pytest.approx(w[0] * w[1] * w[2] / (n[0] * n[1] * n[2]))
 
 
+@pytest.mark.parametrize("name", [c for c in CASES if "access_vols" in load(c)])
+def test_accessible_volumes_match_reference(name):
+    """Voxels cut by a spherical confinement get the fraction of a 20^3 point
+    lattice inside the sphere (chromo/fields.pyx:714-951), as the reference
+    computed them for the golden case."""
+    g = load(name)
+    p, binders = _poly_from_golden(g)
+    n = [int(x) for x in g["nxyz"]]
+    w = [float(x) for x in g["widths"]]
+    f = UniformDensityField([p], binders, w[0], n[0], w[1], n[1], w[2], n[2], confine_type="Spherical",
+                            confine_length=float(g["confine_length"]), chi=float(g["chi"]),
+                            assume_fully_accessible=0)
+    assert not f.uniform_access
+    np.testing.assert_array_equal(f.access_vols, g["access_vols"])
+
+
 def test_binder_presets_and_lookup():
     assert cb.get_by_name("HP1") is cb.hp1
     assert cb.get_by_name("PRC1") is cb.prc1

@@ -23,8 +23,11 @@ def _setup(g):
     if int(g["field_kind"]) == 2:
         n = [int(x) for x in g["nxyz"]]
         w = [float(x) for x in g["widths"]]
+        ct = {0: "", 1: "Spherical", 2: "Cubical"}[int(g["confine_kind"])]
         f = UniformDensityField([p], binders, w[0], n[0], w[1], n[1], w[2], n[2],
-                                chi=float(g["chi"]), vf_limit=float(g["vf_limit"]))
+                                confine_type=ct, confine_length=float(g["confine_length"]),
+                                chi=float(g["chi"]), vf_limit=float(g["vf_limit"]),
+                                assume_fully_accessible=0 if "access_vols" in g else 1)
     else:
         ct = {1: "Spherical", 2: "Cubical"}[int(g["confine_kind"])]
         f = NullField([p], confine_type=ct, confine_length=float(g["confine_length"]))

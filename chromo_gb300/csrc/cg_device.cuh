@@ -139,29 +139,35 @@ __device__ __forceinline__ float unif32(unsigned x) { return (float)x * 4.656612
 // floor(-log10(u + 1e-5) * window * 0.45 + 1.0001) (bead_selection.pyx:56-65)
 // evaluated in FP32 when the result is unambiguous, else in FP64, so the
 // integer equals the reference's FP64 value.
+static __device__ __noinline__ long long sel_floor64(unsigned x, long long window) {
+  return (long long)(-log10(unif(x) + 0.00001) * (double)window * 0.45 + 1.0001);
+}
 __device__ __forceinline__ long long sel_floor(unsigned x, long long window) {
   float y = -log10f(unif32(x) + 0.00001f) * (float)window * 0.45f + 1.0001f;
   float fl = floorf(y);
   float margin = 1e-3f + 1e-6f * y;
   if (y - fl > margin && fl + 1.0f - y > margin) return (long long)fl;
-  return (long long)(-log10(unif(x) + 0.00001) * (double)window * 0.45 + 1.0001);
+  return sel_floor64(x, window);
 }
 
 // int(unif(x) * n) (the bound_0 draw of crank_shaft, move_funcs.pyx:64): in
 // FP32 when the product is clear of an integer by more than its rounding
 // error (relative error below 2e-7), else in FP64; same integer either way.
+static __device__ __noinline__ long long scaled_index64(unsigned x, long long n) {
+  return (int)(unif(x) * (double)n);
+}
 __device__ __forceinline__ long long scaled_index(unsigned x, long long n) {
   float y = unif32(x) * (float)n;
   float fl = floorf(y);
   float margin = 1e-4f + 4e-7f * y;
   if (y - fl > margin && fl + 1.0f - y > margin) return (long long)fl;
-  return (int)(unif(x) * (double)n);
+  return scaled_index64(x, n);
 }
 
 // The Metropolis test u < exp(t) (mc_sim.pyx:164-171) with u = unif(x):
 // decided in FP32 away from the boundary, in FP64 near it; same outcome as
 // the FP64 comparison.
-__device__ __forceinline__ bool metropolis(unsigned x, double t) {
+static __device__ __noinline__ bool metropolis(unsigned x, double t) {
   double u = unif(x);
   if (t != t) return false;
   if (t > 80.0) return true;

@@ -27,24 +27,6 @@ __device__ __forceinline__ void setup_f32(WarpShared& ws) {
 }
 
 // ---------------------------------------------------------------- hash insert
-__device__ __forceinline__ int hash_slot(int* keys, int* used, int* nused, int logH, int key,
-                                         unsigned& err) {
-  unsigned mask = (1u << logH) - 1u;
-  unsigned h = ((unsigned)key * 0x9E3779B1u) >> (32 - logH);
-  for (int it = 0; it <= (int)mask; it++) {
-    int prev = atomicCAS(&keys[h], -1, key);
-    if (prev == -1) {
-      int idx = atomicAdd(nused, 1);
-      used[idx] = (int)h;
-      return (int)h;
-    }
-    if (prev == key) return (int)h;
-    h = (h + 1) & mask;
-  }
-  err |= E_SPIN;
-  return -1;
-}
-
 // Add d to column `col` of a hash entry.  Global-memory tables take one 64-bit
 // atomic.  Shared-memory tables (split = true) keep each column as two 32-bit
 // counters, d = hi * 2^21 + lo with lo in [0, 2^21): 32-bit shared atomics are
@@ -73,19 +55,43 @@ __device__ __forceinline__ long long hash_delta(const long long* cell, bool spli
 }
 
 // Linear probing for `key` after its home slot `start` was found taken by
-// another key; sets `inserted` when the key claims a new slot.
-__device__ __forceinline__ int hash_probe(int* keys, int logH, int key, int start, bool& inserted,
-                                          unsigned& err) {
+// another key: the slot, plus 1 << 30 when the key claimed it new, or -1 when
+// the table is full (out of line: the loop is rare and would be inlined at
+// every claim).
+static __device__ __noinline__ int hash_probe_packed(int* keys, int logH, int key, int start) {
   const unsigned mask = (1u << logH) - 1u;
   unsigned h = ((unsigned)start + 1u) & mask;
   for (unsigned it = 1; it <= mask; it++) {
     int prev = atomicCAS(&keys[h], -1, key);
-    if (prev == -1) { inserted = true; return (int)h; }
-    if (prev == key) { inserted = false; return (int)h; }
+    if (prev == -1) return (int)h | (1 << 30);
+    if (prev == key) return (int)h;
     h = (h + 1) & mask;
   }
-  err |= E_SPIN;
   return -1;
+}
+__device__ __forceinline__ int hash_probe(int* keys, int logH, int key, int start, bool& inserted,
+                                          unsigned& err) {
+  const int r = hash_probe_packed(keys, logH, key, start);
+  if (r < 0) { err |= E_SPIN; return -1; }
+  inserted = (r >> 30) & 1;
+  return r & ((1 << 30) - 1);
+}
+
+// Claim (or find) the slot of `key`; a new slot is appended to the used list.
+__device__ __forceinline__ int hash_slot(int* keys, int* used, int* nused, int logH, int key,
+                                         unsigned& err) {
+  const unsigned h = ((unsigned)key * 0x9E3779B1u) >> (32 - logH);
+  int prev = atomicCAS(&keys[h], -1, key);
+  int slot = (int)h;
+  bool fresh = prev == -1;
+  if (!fresh && prev != key) {
+    const int r = hash_probe_packed(keys, logH, key, (int)h);
+    if (r < 0) { err |= E_SPIN; return -1; }
+    fresh = (r >> 30) & 1;
+    slot = r & ((1 << 30) - 1);
+  }
+  if (fresh) used[atomicAdd(nused, 1)] = slot;
+  return slot;
 }
 
 // Deposit +/- one bead's eight trilinear weights with binder states `st`
@@ -204,7 +210,7 @@ __device__ __forceinline__ void deposit_pair(const RepDev& rd, int hcol, int* ke
 }
 
 // chi term of one voxel in FP64 (fields.pyx:1792-1875 with the vf_limit branch)
-__device__ __forceinline__ double chi_term64(const RepDev& rd, double V, long long g0, long long d0) {
+static __device__ __noinline__ double chi_term64(const RepDev& rd, double V, long long g0, long long d0) {
   double vf0 = ((double)g0 * kFxInv) / V * rd.bead_vol;
   double vf1 = ((double)(g0 + d0) * kFxInv) / V * rd.bead_vol;
   double k = rd.chi * (V / rd.bead_vol);
@@ -317,18 +323,19 @@ __device__ __forceinline__ void commit_grid(const RepDev& rd, const KArgs& a, in
   }
 }
 
-// confinement count of one position (chromo/fields.pyx:121-202)
+// confinement count of one position (chromo/fields.pyx:121-202); out of
+// line: confinement is off in periodic boxes and its FP64 arithmetic would
+// otherwise sit in the hot loop's code
+static __device__ __noinline__ int out_of_bounds3(const RepDev& rd, double x, double y, double z, bool trial) {
+  if (rd.confine_kind == 1) return sqrt(x * x + y * y + z * z) > rd.confine_length ? 1 : 0;
+  if (rd.confine_kind == 2 && trial)
+    return (fabs(x) > rd.confine_length / 2 ? 1 : 0) + (fabs(y) > rd.confine_length / 2 ? 1 : 0) +
+           (fabs(z) > rd.confine_length / 2 ? 1 : 0);
+  return 0;
+}
 template <typename Real>
 __device__ __forceinline__ int out_of_bounds(const RepDev& rd, const Real q[3], bool trial) {
-  const double p[3] = {(double)q[0], (double)q[1], (double)q[2]};
-  if (rd.confine_kind == 1)
-    return sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]) > rd.confine_length ? 1 : 0;
-  if (rd.confine_kind == 2 && trial) {
-    int o = 0;
-    for (int j = 0; j < 3; j++) o += fabs(p[j]) > rd.confine_length / 2 ? 1 : 0;
-    return o;
-  }
-  return 0;
+  return out_of_bounds3(rd, (double)q[0], (double)q[1], (double)q[2], trial);
 }
 
 __device__ __forceinline__ double bind_f(const RepDev& rd, int b, int nm, int s) {

@@ -42,6 +42,15 @@
 
 namespace cg {
 
+// Draw j (>= kDrawCache) of a move's sub-stream: word j & 3 of Philox block
+// j >> 2.  Out of line: few moves draw this many numbers, and inlined at every
+// draw site the rounds would fill the instruction cache.
+static __device__ __noinline__ unsigned move_draw_slow(uint2 key, unsigned tlo, unsigned thi,
+                                                       unsigned long long j) {
+  uint4 o = philox(make_uint4((unsigned)(j >> 2), tlo, thi, 0x2545F491u), key);
+  return comp4(o, (unsigned)j & 3u) >> 1;
+}
+
 // Random numbers of one attempted move (its own counter space).  Draw j is
 // word j & 3 of Philox block j >> 2.  The first kDrawCache draws are computed
 // at init by the move's G lanes into its shared-memory buffer, so a move's
@@ -51,8 +60,6 @@ struct MoveRng {
   uint2 key, keyb;
   unsigned tlo, thi;
   unsigned long long pos, bpos;
-  unsigned cctr;
-  uint4 cache;
   const unsigned* buf;
   bool fail;
   template <int G>
@@ -61,7 +68,7 @@ struct MoveRng {
     keyb = make_uint2(key.x ^ 0x68E31DA4u, key.y ^ 0xB5297A4Du);
     tlo = (unsigned)t;
     thi = (unsigned)(t >> 32);
-    pos = 0; bpos = 0; cctr = 0xffffffffu; fail = false;
+    pos = 0; bpos = 0; fail = false;
     for (int j = gl; j < kDrawCache / 4; j += G) {
       uint4 o = philox(make_uint4((unsigned)j, tlo, thi, 0x2545F491u), key);
       reinterpret_cast<uint4*>(draws)[j] = o;
@@ -77,12 +84,7 @@ struct MoveRng {
   __device__ __forceinline__ unsigned next() {
     unsigned long long j = pos++;
     if (j < (unsigned long long)kDrawCache) return buf[j] >> 1;
-    unsigned c = (unsigned)(j >> 2);
-    if (c != cctr) {
-      cache = philox(make_uint4(c, tlo, thi, 0x2545F491u), key);
-      cctr = c;
-    }
-    return comp4(cache, (unsigned)j & 3u) >> 1;
+    return move_draw_slow(key, tlo, thi, j);
   }
   __device__ __forceinline__ int state_at(unsigned long long k, int nt, bool& ok) const {
     ok = true;

@@ -244,10 +244,16 @@ class Sim:
         check(lib().cg_set_chains(self.h, table("r", np.float64, 3), table("t3", np.float64, 3),
                                   table("t2", np.float64, 3), table("states", np.int64, self.nb)))
 
-    def get_chains(self):
-        """Every replica's (r, t3, t2, states) in one call."""
-        out = [(np.empty((int(n), 3)), np.empty((int(n), 3)), np.empty((int(n), 3)),
-                np.empty((int(n), self.nb), dtype=np.int64)) for n in self.n_beads]
+    def get_chains(self, out=None):
+        """Every replica's (r, t3, t2, states) in one call; ``out`` (the list a
+        previous call returned) is filled in place instead of new arrays."""
+        if out is None:
+            out = [(np.empty((int(n), 3)), np.empty((int(n), 3)), np.empty((int(n), 3)),
+                    np.empty((int(n), self.nb), dtype=np.int64)) for n in self.n_beads]
+        elif len(out) != self.R or any(
+                o[0].shape != (int(n), 3) or o[3].shape != (int(n), self.nb) or o[3].dtype != np.int64
+                or not all(a.flags.c_contiguous for a in o) for o, n in zip(out, self.n_beads)):
+            raise ValueError("out must be a list of (r, t3, t2, states) arrays as get_chains returns")
         tabs = []
         for k in range(4):
             t = (C.c_void_p * self.R)()

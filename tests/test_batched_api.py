@@ -99,7 +99,8 @@ def test_all_replica_transfers_match_per_replica_calls():
                 np.testing.assert_array_equal(x, y)
         # push the host chains (the initial state) back and read them again
         b.push()
-        again = b.sim.get_chains()
+        again = b.sim.get_chains(out=whole)  # filled in place
+        assert again is whole
         for r, p in enumerate(polys):
             np.testing.assert_array_equal(again[r][0], p.r.astype(np.float32).astype(np.float64))
             np.testing.assert_array_equal(again[r][3], p.states)

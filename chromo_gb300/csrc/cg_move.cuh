@@ -209,6 +209,20 @@ __device__ __forceinline__ void deposit_pair(const RepDev& rd, int hcol, int* ke
   claim_add8(rd, hcol, keys, used, nused, vals, logH, v1, qb, st, err, split, cap, full_bit);
 }
 
+// One voxel's grid row -- bead weight, then one column per binder -- with
+// 16-byte loads (rows are 2 or 4 int64 columns, 16- or 32-byte aligned).
+__device__ __forceinline__ void load_row(const long long* gv, int ncol, long long row[4]) {
+  const longlong2 lo = *reinterpret_cast<const longlong2*>(gv);
+  row[0] = lo.x;
+  row[1] = lo.y;
+  row[2] = row[3] = 0;
+  if (ncol == 4) {
+    const longlong2 hi = reinterpret_cast<const longlong2*>(gv)[1];
+    row[2] = hi.x;
+    row[3] = hi.y;
+  }
+}
+
 // chi term of one voxel in FP64 (fields.pyx:1792-1875 with the vf_limit branch)
 static __device__ __noinline__ double chi_term64(const RepDev& rd, double V, long long g0, long long d0) {
   double vf0 = ((double)g0 * kFxInv) / V * rd.bead_vol;
@@ -236,20 +250,26 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
     int slot = used[i];
     int v = keys[slot];
     long long* d = vals + (long long)slot * hcol;
-    const long long* gv = grid + (long long)v * a.ncol;
-    long long g0 = gv[0], d0 = hash_delta(d, split);
+    long long row[4];
+    load_row(grid + (long long)v * a.ncol, a.ncol, row);
+    long long g0 = row[0], d0 = hash_delta(d, split);
     double V = rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin;
     double c = 0, rho[CG_MAX_BINDERS], dd[CG_MAX_BINDERS];
-    for (int b = 0; b < rd.nb; b++) {
-      long long gb = gv[1 + b], db = hash_delta(d + 1 + b, split);
+#pragma unroll
+    for (int b = 0; b < CG_MAX_BINDERS; b++) {
+      if (b >= rd.nb) break;
+      long long gb = row[1 + b], db = hash_delta(d + 1 + b, split);
       rho[b] = ((double)gb * kFxInv) / V;
       dd[b] = ((double)db * kFxInv) / V;
       c += rd.pref[b] * (dd[b] * (2 * rho[b] + dd[b]));
       d[1 + b] = gb + db;
     }
-    for (int b = 0; b < rd.nb; b++)
-      for (int e = 0; e < rd.nb; e++)
-        c += rd.xpref[b * CG_MAX_BINDERS + e] * (rho[b] * dd[e] + dd[b] * rho[e] + dd[b] * dd[e]);
+#pragma unroll
+    for (int b = 0; b < CG_MAX_BINDERS; b++)
+#pragma unroll
+      for (int e = 0; e < CG_MAX_BINDERS; e++)
+        if (b < rd.nb && e < rd.nb)
+          c += rd.xpref[b * CG_MAX_BINDERS + e] * (rho[b] * dd[e] + dd[b] * rho[e] + dd[b] * dd[e]);
     c += chi_term64(rd, V, g0, d0);
     d[0] = g0 + d0;
     part += c;
@@ -274,8 +294,9 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
     int slot = used[i];
     int v = keys[slot];
     long long* d = vals + (long long)slot * hcol;
-    const long long* gv = grid + (long long)v * a.ncol;
-    long long g0 = gv[0], d0 = hash_delta(d, split);
+    long long row[4];
+    load_row(grid + (long long)v * a.ncol, a.ncol, row);
+    long long g0 = row[0], d0 = hash_delta(d, split);
     float sc = ws.f_scale, k = ws.f_k;
     double V = rd.vol_bin;
     if (rd.has_access) {
@@ -284,16 +305,21 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
       k = (float)(rd.chi * (V / rd.bead_vol));
     }
     float c = 0, rho[CG_MAX_BINDERS], dd[CG_MAX_BINDERS];
-    for (int b = 0; b < rd.nb; b++) {
-      long long gb = gv[1 + b], db = hash_delta(d + 1 + b, split);
+#pragma unroll
+    for (int b = 0; b < CG_MAX_BINDERS; b++) {
+      if (b >= rd.nb) break;
+      long long gb = row[1 + b], db = hash_delta(d + 1 + b, split);
       rho[b] = (float)gb * sc;
       dd[b] = (float)db * sc;
       c += ws.f_pref[b] * (dd[b] * (2.0f * rho[b] + dd[b]));
       d[1 + b] = gb + db;
     }
-    for (int b = 0; b < rd.nb; b++)
-      for (int e = 0; e < rd.nb; e++)
-        c += ws.f_xpref[b * CG_MAX_BINDERS + e] * (rho[b] * dd[e] + dd[b] * rho[e] + dd[b] * dd[e]);
+#pragma unroll
+    for (int b = 0; b < CG_MAX_BINDERS; b++)
+#pragma unroll
+      for (int e = 0; e < CG_MAX_BINDERS; e++)
+        if (b < rd.nb && e < rd.nb)
+          c += ws.f_xpref[b * CG_MAX_BINDERS + e] * (rho[b] * dd[e] + dd[b] * rho[e] + dd[b] * dd[e]);
     float vf0 = (float)g0 * sc * ws.f_vb;
     float dvf = (float)d0 * sc * ws.f_vb;
     if (vf0 > ws.f_lim - 1e-3f || vf0 + dvf > ws.f_lim - 1e-3f) {

@@ -628,9 +628,12 @@ __device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int s, int gl, 
   long long* grid = a.grid + rd.vox_off * ncol;
   for (int i = gl; i < nu; i += G) {
     int slot = used[i];
-    if (accept) {
-      int v = keys[slot];
-      for (int cc = 0; cc < hcol; cc++) grid[(long long)v * ncol + cc] = vals[(long long)slot * hcol + cc];
+    if (accept) {  // the voxel's post-move row, stored with 16-byte stores (padding column stays 0)
+      const int v = keys[slot];
+      const long long* src = vals + (long long)slot * hcol;
+      longlong2* dst = reinterpret_cast<longlong2*>(grid + (long long)v * ncol);
+      dst[0] = make_longlong2(src[0], src[1]);
+      if (ncol == 4) dst[1] = make_longlong2(hcol > 2 ? src[2] : 0, hcol > 3 ? src[3] : 0);
     }
     keys[slot] = -1;
     for (int cc = 0; cc < hcol; cc++) vals[(long long)slot * hcol + cc] = 0;

@@ -38,6 +38,7 @@ int fail(int code, const std::string& msg) {
   } while (0)
 
 size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+size_t align32(size_t x) { return (x + 31) & ~size_t(31); }
 
 int next_log2(long long x) {
   int l = 0;
@@ -137,7 +138,8 @@ struct cg_sim {
 
   // Region of one move slot for voxel-table capacity 2^lh and staging
   // capacity sc (offsets within the region; the draw buffer first, 16-byte
-  // aligned); returns the region size, a multiple of 16 bytes.
+  // aligned; the staged 4-vectors 32-byte aligned); returns the region size,
+  // a multiple of 32 bytes.
   int layout(int lh, long long sc) {
     size_t H = size_t(1) << lh;
     size_t o = 0;
@@ -147,10 +149,11 @@ struct cg_sim {
     off_bslot = (int)o; o += 4 * H;
     o = align16(o);
     off_vals = (int)o; o += 8 * H * (nb + 1);
-    off_stage = (int)o; o += sc * 9 * scal_bytes();
+    o = align32(o);  // staged 4-vectors: 16 bytes (FP32) or 32 bytes (FP64) each
+    off_stage = (int)o; o += sc * 12 * scal_bytes();
     o = align16(o);
     off_idx = (int)o; o += 4 * sc;
-    o = align16(o);
+    o = align32(o);
     logH = lh; stage_cap = sc; warp_smem = (int)o;
     return warp_smem;
   }
@@ -160,7 +163,7 @@ struct cg_sim {
     size_t o = align16(sizeof(cg::SpecShared));
     spec_off_bkeys = (int)o; o += 4 * (size_t(1) << lhb);
     spec_off_bmask = (int)o; o += 4 * (size_t(1) << lhb);
-    o = align16(o);
+    o = align32(o);
     spec_off_warps = (int)o;
     spec_logHB = lhb;
     spec_w = W;
@@ -344,7 +347,7 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   ALLOC(s->g_used, 4 * Hg * RW);
   ALLOC(s->g_bslot, 4 * Hg * RW);
   ALLOC(s->g_vals, 8 * Hg * (s->nb + 1) * RW);
-  ALLOC(s->g_stage, s->scal_bytes() * 9 * s->g_stage_cap * RW);
+  ALLOC(s->g_stage, s->scal_bytes() * 12 * s->g_stage_cap * RW);
   ALLOC(s->g_idx, 4 * s->g_stage_cap * RW);
   ALLOC(s->picked, 4 * s->total_picked);
   ALLOC(s->d_picked_off, 8 * s->R);

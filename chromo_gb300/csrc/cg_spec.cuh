@@ -238,7 +238,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     // slots / 4 with a fallback to the global table on overflow; global beyond
     const bool sure = 16 * m <= Hs;
     if (!sure && 4 * m > Hs) { use_table(S, gm); gtab = 1; }
-    Pos* stage = reinterpret_cast<Pos*>(S.stage);
+    V4<Pos>* stage = reinterpret_cast<V4<Pos>*>(S.stage);  // r, t3, t2 of each moved bead
     Acc part = acc_zero<Acc>();
     int oob = 0;
     bool ovf = false;
@@ -277,8 +277,9 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
         }
         const bool fin = isfinite(tr[0]) && isfinite(tr[1]) && isfinite(tr[2]);
         if (!fin) e |= E_NONFINITE;
-        Pos* sg = stage + k * 9;
-        for (int j = 0; j < 3; j++) { sg[j] = (Pos)tr[j]; sg[3 + j] = (Pos)tt3[j]; sg[6 + j] = (Pos)tt2[j]; }
+        stage[3 * k] = V4<Pos>{(Pos)tr[0], (Pos)tr[1], (Pos)tr[2], (Pos)0};
+        stage[3 * k + 1] = V4<Pos>{(Pos)tt3[0], (Pos)tt3[1], (Pos)tt3[2], (Pos)0};
+        stage[3 * k + 2] = V4<Pos>{(Pos)tt2[0], (Pos)tt2[1], (Pos)tt2[2], (Pos)0};
         if (k == 0 && ind0 != 0) {
           Real r0[3], t30[3];
           ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
@@ -369,7 +370,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     err = gor<G>(err);
     if (err) m = 0;
     const unsigned long long axis_base = g.pos;
-    Pos* stage = reinterpret_cast<Pos*>(S.stage);
+    V4<Pos>* stage = reinterpret_cast<V4<Pos>*>(S.stage);
     Acc part = acc_zero<Acc>();
     Real sa, ca;
     rsincos(ang, &sa, &ca);
@@ -389,8 +390,8 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
         for (int q = 0; q < 3; q++) { e3 += M[j][q] * t3[q]; e2 += M[j][q] * t2[q]; }
         tt3[j] = e3; tt2[j] = e2;
       }
-      Pos* sg = stage + k * 9;
-      for (int j = 0; j < 3; j++) { sg[3 + j] = (Pos)tt3[j]; sg[6 + j] = (Pos)tt2[j]; }
+      stage[3 * k + 1] = V4<Pos>{(Pos)tt3[0], (Pos)tt3[1], (Pos)tt3[2], (Pos)0};
+      stage[3 * k + 2] = V4<Pos>{(Pos)tt2[0], (Pos)tt2[1], (Pos)tt2[2], (Pos)0};
       Acc de = acc_zero<Acc>();
       if (i != 0) {
         Real r0[3], t30[3];
@@ -590,7 +591,7 @@ __device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int s, int gl, 
   V4<Pos>* t34w = reinterpret_cast<V4<Pos>*>(a.t34) + rd.bead_off;
   V4<Pos>* t24w = reinterpret_cast<V4<Pos>*>(a.t24) + rd.bead_off;
   unsigned* st = a.states + rd.bead_off;
-  const Pos* stage = reinterpret_cast<const Pos*>(P.gstage ? gm.stage : sm.stage);
+  const V4<Pos>* stage = reinterpret_cast<const V4<Pos>*>(P.gstage ? gm.stage : sm.stage);
   const int* idx = P.gstage ? gm.idx : sm.idx;
   int* keys = P.gtab ? gm.keys : sm.keys;
   int* used = P.gtab ? gm.used : sm.used;
@@ -600,20 +601,18 @@ __device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int s, int gl, 
   if (accept) {
     if (P.kind <= CG_SLIDE) {
       for (int k = gl; k < m; k += G) {
-        const Pos* sg = stage + (long long)k * 9;
         const long long i = (long long)P.ind0 + k;
-        r4w[i] = V4<Pos>{sg[0], sg[1], sg[2], (Pos)0};
+        r4w[i] = stage[3 * k];
         if (P.kind != CG_SLIDE) {
-          t34w[i] = V4<Pos>{sg[3], sg[4], sg[5], (Pos)0};
-          t24w[i] = V4<Pos>{sg[6], sg[7], sg[8], (Pos)0};
+          t34w[i] = stage[3 * k + 1];
+          t24w[i] = stage[3 * k + 2];
         }
       }
     } else if (P.kind == CG_TANGENT_ROTATION) {
       for (int k = gl; k < m; k += G) {
-        const Pos* sg = stage + (long long)k * 9;
         const long long i = idx[k];
-        t34w[i] = V4<Pos>{sg[3], sg[4], sg[5], (Pos)0};
-        t24w[i] = V4<Pos>{sg[6], sg[7], sg[8], (Pos)0};
+        t34w[i] = stage[3 * k + 1];
+        t24w[i] = stage[3 * k + 2];
       }
     } else {
       for (int k = gl; k < m; k += G) {
@@ -647,7 +646,7 @@ __device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int s, int gl, 
 // faster than 128 registers with 8 warps, which spills).
 template <typename Pos, int G>
 __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(32) unsigned char smem[];
   constexpr int GPW = 32 / G;  // move groups per warp
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int gl = lane & (G - 1);
@@ -677,7 +676,7 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
   gm.bslot = a.g_bslot + gi * Hg;
   gm.vals = a.g_vals + gi * Hg * hcol;
   gm.logH = a.g_logH;
-  gm.stage = reinterpret_cast<Pos*>(a.g_stage) + gi * a.g_stage_cap * 9;
+  gm.stage = reinterpret_cast<V4<Pos>*>(a.g_stage) + gi * a.g_stage_cap * 3;
   gm.idx = a.g_idx + gi * a.g_stage_cap;
   {
     const unsigned* src = reinterpret_cast<const unsigned*>(a.reps + rep);

@@ -164,7 +164,34 @@ __global__ void terms_kernel(KArgs a, double* terms, double* acc) {
       loc[10 + b] += (double)s;
     }
   }
-  if (rd.field_kind == 2) {
+  if (rd.field_kind == 2 && !rd.has_access) {
+    // Uniform voxel volume V: every term is a sum of products of fixed-point
+    // grid values times one constant, so the raw products are summed (no FP64
+    // division per voxel; GB300 runs FP64 at 1/64 of the FP32 rate) and
+    // scaled once.  vf <= vf_limit <=> g0 <= vf_limit / (2^-40 Vb / V).
+    const long long* grid = a.grid + rd.vox_off * a.ncol;
+    const double u = kFxInv / rd.vol_bin;          // density per fixed-point unit
+    const double c = u * rd.bead_vol;              // volume fraction per unit
+    const double gmax = rd.vf_limit / c;
+    double s00 = 0, s00_lim = 0, sbb[CG_MAX_BINDERS] = {0, 0, 0}, sx[3] = {0, 0, 0};
+    for (long long v = threadIdx.x; v < rd.n_vox; v += blockDim.x) {
+      const double g0 = (double)grid[v * a.ncol];
+      double gb[CG_MAX_BINDERS] = {0, 0, 0};
+      for (int b = 0; b < rd.nb; b++) gb[b] = (double)grid[v * a.ncol + 1 + b];
+      const double q = g0 * g0;
+      s00 += q;
+      if (g0 <= gmax) s00_lim += q;
+      for (int b = 0; b < CG_MAX_BINDERS; b++) sbb[b] += gb[b] * gb[b];
+      sx[0] += gb[0] * gb[1];
+      sx[1] += gb[0] * gb[2];
+      sx[2] += gb[1] * gb[2];
+    }
+    const double u2 = u * u;
+    loc[0] += (rd.vol_bin / rd.bead_vol) * (c * c) * s00_lim;
+    for (int b = 0; b < CG_MAX_BINDERS; b++) loc[1 + b] += u2 * sbb[b];
+    for (int k = 0; k < 3; k++) loc[4 + k] += u2 * sx[k];
+    loc[13] += u2 * s00;
+  } else if (rd.field_kind == 2) {
     const long long* grid = a.grid + rd.vox_off * a.ncol;
     for (long long v = threadIdx.x; v < rd.n_vox; v += blockDim.x) {
       const double V = rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin;

@@ -327,6 +327,10 @@ def main():
         sim.run_batched(1, steps_round, w.n_rungs, 11 + rank, sh)
     sim.sync(sh)
     sim.reset_tally()
+    # the state the timed rounds start from (chains and move controllers),
+    # restored for the end-to-end leg so that both legs do the same MC work
+    start_chains = sim.get_chains()
+    start_ctl = [sim.get_controllers(r) for r in range(w.replicas)]
     # ---- timed rounds
     barrier(world)
     torch.cuda.synchronize()
@@ -394,20 +398,31 @@ def main():
     # ---- e2e through the C ABI with host buffers
     h2d = d2h = 0
     pos_b = 16
+    # A host-driven loop: every round uploads its input chains from host
+    # memory (all replicas: positions, tangents, binding states), rebuilds the
+    # densities, runs one exchange round and reads the resulting chains back;
+    # the next round's input is that snapshot.  The first round is untimed.
     e2e_steps = max(2, min(args.steps, 5))
     t_e2e = 0.0
-    snap = None  # host snapshot buffers, allocated by the first (untimed) step and reused
+    # start from the state the timed rounds started from (the chains are
+    # uploaded by the first, untimed round)
+    for r in range(w.replicas):
+        sim.set_controllers(r, start_ctl[r])
+    inp = start_chains
+    spare, other = sim.get_chains(), sim.get_chains()  # two host snapshot buffers, allocated untimed
     for k in range(e2e_steps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sim.set_chains([dict(r=c.r, t3=c.t3, t2=c.t2, states=c.states) for c in chains])
+        sim.set_chains([dict(r=r, t3=t3, t2=t2, states=st) for r, t3, t2, st in inp])
         sim.deposit(-1)  # the densities of the uploaded chains
         sim.run_batched(1, steps_round, w.n_rungs, 11 + rank, sh)
         sim.sync(sh)
-        snap = sim.get_chains(out=snap)
+        out = sim.get_chains(out=spare)
         dt = time.perf_counter() - t0
         if k > 0:
             t_e2e += dt
+        spare = other if k == 0 else inp  # the start snapshot is never overwritten
+        inp = out
     nbeads = int(w.lengths.sum())
     h2d = nbeads * (3 * pos_b + 4)
     d2h = nbeads * (3 * pos_b + 4)
@@ -460,8 +475,9 @@ def main():
                          "moves_per_launch": float(tal2[:, :, 0].sum()) / n_launch},
             "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
-                    "path": "C ABI: cg_set_chains (host FP64 -> pinned -> HBM, all replicas), "
-                            "cg_deposit, cg_run_batched, cg_get_chains (into reused host arrays)"},
+                    "path": "C ABI, host-driven rounds: cg_set_chains (the previous round's host "
+                            "snapshot, FP64 -> pinned -> HBM, all replicas), cg_deposit, cg_run_batched, "
+                            "cg_get_chains (into reused host arrays)"},
             "plain": {"value": plain_value, "unit": "moves/s",
                       "workload": "one 10,000-bead chain, 60^3 grid, one binder, 300 MC steps",
                       "batched_over_plain": value / plain_value},

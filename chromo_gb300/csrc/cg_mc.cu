@@ -628,7 +628,18 @@ __global__ void chi_sum_kernel(KArgs a, double* out) {
   const int rep = blockIdx.x;
   const RepDev& rd = a.reps[rep];
   double sx = 0;
-  if (rd.field_kind == 2) {
+  if (rd.field_kind == 2 && !rd.has_access) {
+    // uniform voxel volume: S = (V / Vb) c^2 sum g0^2 with c = 2^-40 Vb / V the
+    // volume fraction per fixed-point unit (no FP64 division per voxel)
+    const long long* grid = a.grid + rd.vox_off * a.ncol;
+    double s00 = 0;
+    for (long long v = threadIdx.x; v < rd.n_vox; v += blockDim.x) {
+      const double g0 = (double)grid[v * a.ncol];
+      s00 += g0 * g0;
+    }
+    const double c = kFxInv / rd.vol_bin * rd.bead_vol;
+    sx = (rd.vol_bin / rd.bead_vol) * (c * c) * s00;
+  } else if (rd.field_kind == 2) {
     const long long* grid = a.grid + rd.vox_off * a.ncol;
     for (long long v = threadIdx.x; v < rd.n_vox; v += blockDim.x) {
       double V = rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin;

@@ -241,9 +241,11 @@ static int default_warps(const cg_sim* s, int G) {
 }
 
 static int choose_shape(cg_sim* s, int w_req, int g_req) {
-  // One CTA per replica with W warps of 32 / G moves each.  Enough CTAs must
-  // be resident per SM for every replica to run at once; each move slot gets
-  // the largest voxel table that then fits.
+  // One CTA per replica with W warps of 32 / G moves each.  The CTAs that can
+  // be resident per SM -- those every replica needs to run at once, or fewer
+  // when the register file holds fewer CTAs of W warps (the replicas then run
+  // in waves) -- share the SM's shared memory; each move slot gets the
+  // largest voxel table that then fits.
   const size_t smem_per_sm = 227 * 1024;
   long long ctas_per_sm = (s->R + s->n_sm - 1) / std::max(1, s->n_sm);
   if (ctas_per_sm < 1) ctas_per_sm = 1;
@@ -251,6 +253,8 @@ static int choose_shape(cg_sim* s, int w_req, int g_req) {
   int W = w_req > 0 ? w_req : default_warps(s, G);
   if (W > cg::kMaxW) W = cg::kMaxW;
   if (W * (32 / G) > cg::kMaxS) W = cg::kMaxS / (32 / G);
+  const long long reg_ctas = std::max(1, cg_spec_warps_per_sm(s->fp64 != 0, G) / W);
+  if (ctas_per_sm > reg_ctas) ctas_per_sm = reg_ctas;
   const size_t budget = std::min<size_t>(smem_per_sm / ctas_per_sm - 1024, 220 * 1024);
   const int lhb = 10;
   const long long sc = G == 32 ? 48 : 32;

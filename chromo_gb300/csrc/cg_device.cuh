@@ -549,13 +549,12 @@ __device__ __forceinline__ void make_gridf(const RepDev& rd, GridF& gf) {
   gf.nxy = rd.nx * rd.ny;
 }
 
-// Exact reference arithmetic (FP64 storage).
-__device__ __forceinline__ void voxel_weights(const RepDev& rd, const GridF&, const double pos[3],
-                                              double w[8], int v[8]) {
+// Per axis: the lower and upper voxel of a bead and the lower voxel's weight
+// (fields.pyx:1524-1673).  Exact reference arithmetic (FP64 storage).
+__device__ __forceinline__ void voxel_axes(const RepDev& rd, const GridF&, const double pos[3],
+                                           double wl[3], int lo[3], int hi[3]) {
   const double width[3] = {rd.wx, rd.wy, rd.wz};
   const int n[3] = {rd.nx, rd.ny, rd.nz};
-  double wl[3];
-  int lo[3], hi[3];
 #pragma unroll
   for (int j = 0; j < 3; j++) {
     double d = width[j] / (double)n[j];
@@ -566,22 +565,11 @@ __device__ __forceinline__ void voxel_weights(const RepDev& rd, const GridF&, co
     hi[j] = lo[j] + 1 == n[j] ? 0 : lo[j] + 1;
     wl[j] = 1 - (x / d - (double)ind);
   }
-#pragma unroll
-  for (int l = 0; l < 8; l++) {
-    int bx = l & 1, by = (l >> 1) & 1, bz = (l >> 2) & 1;
-    double fx = bx ? (1 - wl[0]) : wl[0];
-    double fy = by ? (1 - wl[1]) : wl[1];
-    double fz = bz ? (1 - wl[2]) : wl[2];
-    w[l] = fx * fy * fz;
-    v[l] = (bx ? hi[0] : lo[0]) + rd.nx * ((by ? hi[1] : lo[1]) + rd.ny * (bz ? hi[2] : lo[2]));
-  }
 }
 
 // FP32 arithmetic (FP32 storage): same construction, one reciprocal multiply.
-__device__ __forceinline__ void voxel_weights(const RepDev&, const GridF& gf, const float pos[3],
-                                              float w[8], int v[8]) {
-  float wl[3];
-  int lo[3], hi[3];
+__device__ __forceinline__ void voxel_axes(const RepDev&, const GridF& gf, const float pos[3],
+                                           float wl[3], int lo[3], int hi[3]) {
 #pragma unroll
   for (int j = 0; j < 3; j++) {
     float x = pymodf(pos[j] + gf.half_w[j], gf.w[j]) - gf.half_d[j];
@@ -593,15 +581,29 @@ __device__ __forceinline__ void voxel_weights(const RepDev&, const GridF& gf, co
     hi[j] = lo[j] + 1 == gf.n[j] ? 0 : lo[j] + 1;
     wl[j] = 1 - (t - fl);
   }
+}
+
+// Corner l (bit 0: x, bit 1: y, bit 2: z upper) of the eight trilinear
+// weights and its voxel index.
+template <typename Real>
+__device__ __forceinline__ void voxel_corner(const GridF& gf, const Real wl[3], const int lo[3],
+                                             const int hi[3], int l, Real& w, int& v) {
+  const int bx = l & 1, by = (l >> 1) & 1, bz = (l >> 2) & 1;
+  const Real fx = bx ? (1 - wl[0]) : wl[0];
+  const Real fy = by ? (1 - wl[1]) : wl[1];
+  const Real fz = bz ? (1 - wl[2]) : wl[2];
+  w = fx * fy * fz;
+  v = (bx ? hi[0] : lo[0]) + gf.nx * (by ? hi[1] : lo[1]) + gf.nxy * (bz ? hi[2] : lo[2]);
+}
+
+template <typename Real>
+__device__ __forceinline__ void voxel_weights(const RepDev& rd, const GridF& gf, const Real pos[3],
+                                              Real w[8], int v[8]) {
+  Real wl[3];
+  int lo[3], hi[3];
+  voxel_axes(rd, gf, pos, wl, lo, hi);
 #pragma unroll
-  for (int l = 0; l < 8; l++) {
-    int bx = l & 1, by = (l >> 1) & 1, bz = (l >> 2) & 1;
-    float fx = bx ? (1 - wl[0]) : wl[0];
-    float fy = by ? (1 - wl[1]) : wl[1];
-    float fz = bz ? (1 - wl[2]) : wl[2];
-    w[l] = fx * fy * fz;
-    v[l] = (bx ? hi[0] : lo[0]) + gf.nx * (by ? hi[1] : lo[1]) + gf.nxy * (bz ? hi[2] : lo[2]);
-  }
+  for (int l = 0; l < 8; l++) voxel_corner(gf, wl, lo, hi, l, w[l], v[l]);
 }
 
 __device__ __forceinline__ long long q40(double w) { return __double2ll_rn(w * kFxScale); }

@@ -186,6 +186,57 @@ __device__ __forceinline__ void claim_add8(const RepDev& rd, int hcol, int* keys
   }
 }
 
+// Claim (or find) the slots of up to NQ voxels per lane of a group of G lanes
+// (v[j] where want[j]); the group appends its new slots to the used list
+// with one counter update.  Every lane's home-slot claims are issued back to
+// back; only a claim that meets another key probes on.  A table that cannot
+// take a new voxel (slot -1), or whose count of voxels passes `cap` (every
+// lane of the group), sets `full_bit` in err.  Called by the whole warp.
+template <int G, int NQ>
+__device__ __forceinline__ void claim_slots(int* keys, int* used, int* nused, int logH, const int (&v)[NQ],
+                                            const bool (&want)[NQ], int (&slot)[NQ], unsigned& err,
+                                            int cap, unsigned full_bit, int gl) {
+  int prev[NQ];
+  bool fresh[NQ];
+#pragma unroll
+  for (int j = 0; j < NQ; j++) {
+    slot[j] = (int)(((unsigned)v[j] * 0x9E3779B1u) >> (32 - logH));
+    prev[j] = want[j] ? atomicCAS(&keys[slot[j]], -1, v[j]) : v[j];
+  }
+#pragma unroll
+  for (int j = 0; j < NQ; j++) {
+    fresh[j] = prev[j] == -1;
+    if (!fresh[j] && prev[j] != v[j]) {
+      const int r = hash_probe_packed(keys, logH, v[j], slot[j]);
+      if (r < 0) {
+        err |= full_bit;
+        slot[j] = -1;
+      } else {
+        fresh[j] = (r >> 30) & 1;
+        slot[j] = r & ((1 << 30) - 1);
+      }
+    }
+  }
+  const unsigned lt = (1u << gl) - 1u;
+  unsigned bal[NQ];
+  int cnt = 0;
+#pragma unroll
+  for (int j = 0; j < NQ; j++) {
+    bal[j] = gballot<G>(fresh[j]);
+    cnt += __popc(bal[j]);
+  }
+  int base = 0;
+  if (gl == 0 && cnt) base = atomicAdd(nused, cnt);
+  base = __shfl_sync(kFull, base, (int)((threadIdx.x & 31u) & ~(unsigned)(G - 1)));
+  int at = base;
+#pragma unroll
+  for (int j = 0; j < NQ; j++) {
+    if (fresh[j]) used[at + __popc(bal[j] & lt)] = slot[j];
+    at += __popc(bal[j]);
+  }
+  if (at > cap) err |= full_bit;
+}
+
 // Remove one bead's old trilinear weights (w0 at voxels v0) and add its new
 // ones (w1 at v1).  When both lie in the same eight voxels (the same lower
 // corner) each voxel gets one contribution q(w1) - q(w0) and the second set

@@ -76,13 +76,9 @@ struct MoveRng {
     __syncwarp();
     buf = draws;
   }
-  __device__ __forceinline__ unsigned at(unsigned long long j, bool& ok) const {
-    ok = true;
-    uint4 o = philox(make_uint4((unsigned)(j >> 2), tlo, thi, 0x2545F491u), key);
-    return comp4(o, (unsigned)(j & 3)) >> 1;
-  }
-  __device__ __forceinline__ unsigned next() {
-    unsigned long long j = pos++;
+  __device__ __forceinline__ unsigned next() { return word(pos++); }
+  // draw j, from the cache when it holds it
+  __device__ __forceinline__ unsigned word(unsigned long long j) const {
     if (j < (unsigned long long)kDrawCache) return buf[j] >> 1;
     return move_draw_slow(key, tlo, thi, j);
   }
@@ -192,17 +188,16 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
         else { ia = indf; ib = ind0 - 1; }
         if (!err) {
           Real pa[3], pb[3], dir[3], p[3];
-          ld3(r4, ia, pa); ld3(r4, ib, pb);
-          for (int i = 0; i < 3; i++) dir[i] = pa[i] - pb[i];
-          Real mag = rsqrt_(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
-          if (mag < (Real)1E-5) sphere<Real>(g, dir);
-          else { Real sc = (Real)1 / mag; for (int i = 0; i < 3; i++) dir[i] = dir[i] * sc; }
-          long long ip;
+          long long ip;  // the fulcrum bead, loaded with the two axis beads
           if (ind0 == 0 && indf != N) ip = indf;
           else if (ind0 != 0 && indf == N) ip = ind0 - 1;
           else if (ind0 == 0 && indf == N) ip = ind0;
           else ip = ind0 - 1;
-          ld3(r4, ip, p);
+          ld3(r4, ia, pa); ld3(r4, ib, pb); ld3(r4, ip, p);
+          for (int i = 0; i < 3; i++) dir[i] = pa[i] - pb[i];
+          Real mag = rsqrt_(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+          if (mag < (Real)1E-5) sphere<Real>(g, dir);
+          else { Real sc = (Real)1 / mag; for (int i = 0; i < 3; i++) dir[i] = dir[i] * sc; }
           axis_rotation(dir, p, ang, M);
         }
       } else if (kind == CG_END_PIVOT) {
@@ -260,44 +255,85 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       const int cap = gtab ? (1 << gm.logH) : (sure ? Hs : (3 * Hs) / 4);
       const unsigned full_bit = (gtab || sure) ? E_SPIN : E_OVF;
       unsigned e = 0;
-      for (long long k = gl; run && k < m; k += G) {
-        if (e & E_OVF) break;
-        const long long i = ind0 + k;
-        V4<Pos> R = r4[i], T3 = t34[i], T2 = t24[i];
-        Real r[3] = {R.x, R.y, R.z}, t3[3] = {T3.x, T3.y, T3.z}, t2[3] = {T2.x, T2.y, T2.z};
-        Real tr[3], tt3[3], tt2[3];
-        if (kind == CG_SLIDE) {
-          for (int j = 0; j < 3; j++) { tr[j] = r[j] + M[j][3]; tt3[j] = t3[j]; tt2[j] = t2[j]; }
-        } else {
-          for (int j = 0; j < 3; j++) {
-            Real er = 0, e3 = 0, e2 = 0;
-            for (int q = 0; q < 3; q++) { er += M[j][q] * r[q]; e3 += M[j][q] * t3[q]; e2 += M[j][q] * t2[q]; }
-            tr[j] = er + M[j][3]; tt3[j] = e3; tt2[j] = e2;
+      // Eight lanes per bead, lane gl taking trilinear corner gl & 7 of bead
+      // gl >> 3 of each pass: every lane transforms its bead (the eight
+      // copies are the same arithmetic), corner lane 0 adds the bead's
+      // elastic and confinement terms, lanes 0-2 stage its r, t3, t2, and
+      // each lane removes its corner's old weight and adds the new one.  When
+      // the old and new weights lie in the same eight voxels (the same lower
+      // corner) the corner gets one contribution q(w1) - q(w0); contributions
+      // of zero claim nothing.
+      constexpr int BP = G / 8;
+      const int kc = gl >> 3, cl = gl & 7;
+      for (long long kb = 0; __any_sync(kFull, run && kb < m && !(e & E_OVF)); kb += BP) {
+        const long long k = kb + kc;
+        const bool act = run && k < m && !(e & E_OVF);
+        int vq[2] = {0, 0};
+        long long q[2] = {0, 0};
+        unsigned sw = 0;
+        if (act) {
+          const long long i = ind0 + k;
+          // corner lane 0 of the first bead takes the bond to its fixed left
+          // neighbour, corner lane 1 of the last bead the bond to its fixed
+          // right neighbour; their beads and bond parameters are loaded with
+          // the moved bead's (in-range indices on every lane)
+          const bool left = cl == 0 && k == 0 && ind0 != 0;
+          const bool right = cl == 1 && k == m - 1 && indf != N;
+          const long long in = left ? i - 1 : (right ? i + 1 : i);
+          const V4<Pos> RN = r4[in], TN = t34[in];
+          const Bond<Real> bn = bond_at(bonds, bonds32, right ? i : in, (Real)0);
+          V4<Pos> R = r4[i], T3 = t34[i], T2 = t24[i];
+          Real r[3] = {R.x, R.y, R.z}, t3[3] = {T3.x, T3.y, T3.z}, t2[3] = {T2.x, T2.y, T2.z};
+          Real tr[3], tt3[3], tt2[3];
+          if (kind == CG_SLIDE) {
+            for (int j = 0; j < 3; j++) { tr[j] = r[j] + M[j][3]; tt3[j] = t3[j]; tt2[j] = t2[j]; }
+          } else {
+            for (int j = 0; j < 3; j++) {
+              Real er = 0, e3 = 0, e2 = 0;
+              for (int qq = 0; qq < 3; qq++) { er += M[j][qq] * r[qq]; e3 += M[j][qq] * t3[qq]; e2 += M[j][qq] * t2[qq]; }
+              tr[j] = er + M[j][3]; tt3[j] = e3; tt2[j] = e2;
+            }
+          }
+          const bool fin = isfinite(tr[0]) && isfinite(tr[1]) && isfinite(tr[2]);
+          if (!fin) e |= E_NONFINITE;
+          if (cl < 3) {
+            Real o[3];
+            for (int j = 0; j < 3; j++) o[j] = cl == 0 ? tr[j] : (cl == 1 ? tt3[j] : tt2[j]);
+            stage[3 * k + cl] = V4<Pos>{(Pos)o[0], (Pos)o[1], (Pos)o[2], (Pos)0};
+          }
+          const Real rn[3] = {(Real)RN.x, (Real)RN.y, (Real)RN.z}, tn[3] = {(Real)TN.x, (Real)TN.y, (Real)TN.z};
+          if (left) acc_add(part, pair_dE_fwd(bn, rn, r, tr, tn, t3, tt3));
+          if (right) acc_add(part, pair_dE_rev(bn, r, tr, rn, t3, tt3, tn));
+          if (cl == 0 && check_field && rd.confine_kind)
+            oob += out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
+          if (density && fin) {
+            Real wl0[3], wl1[3], w0, w1;
+            int lo0[3], hi0[3], lo1[3], hi1[3];
+            voxel_axes(rd, gf, r, wl0, lo0, hi0);
+            voxel_axes(rd, gf, tr, wl1, lo1, hi1);
+            voxel_corner(gf, wl0, lo0, hi0, cl, w0, vq[0]);
+            voxel_corner(gf, wl1, lo1, hi1, cl, w1, vq[1]);
+            const bool same = lo0[0] == lo1[0] && lo0[1] == lo1[1] && lo0[2] == lo1[2];
+            const long long q0 = q40(w0), q1 = q40(w1);
+            q[0] = same ? q1 - q0 : -q0;
+            q[1] = same ? 0 : q1;
+            sw = st[i];
           }
         }
-        const bool fin = isfinite(tr[0]) && isfinite(tr[1]) && isfinite(tr[2]);
-        if (!fin) e |= E_NONFINITE;
-        stage[3 * k] = V4<Pos>{(Pos)tr[0], (Pos)tr[1], (Pos)tr[2], (Pos)0};
-        stage[3 * k + 1] = V4<Pos>{(Pos)tt3[0], (Pos)tt3[1], (Pos)tt3[2], (Pos)0};
-        stage[3 * k + 2] = V4<Pos>{(Pos)tt2[0], (Pos)tt2[1], (Pos)tt2[2], (Pos)0};
-        if (k == 0 && ind0 != 0) {
-          Real r0[3], t30[3];
-          ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
-          acc_add(part, pair_dE_fwd(bond_at(bonds, bonds32, i - 1, (Real)0), r0, r, tr, t30, t3, tt3));
-        }
-        if (k == m - 1 && indf != N) {
-          Real r1[3], t31[3];
-          ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
-          acc_add(part, pair_dE_rev(bond_at(bonds, bonds32, i, (Real)0), r, tr, r1, t3, tt3, t31));
-        }
-        if (check_field && rd.confine_kind) oob += out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
-        if (density && fin) {
-          Real w0[8], w1[8];
-          int v0[8], v1[8];
-          voxel_weights(rd, gf, r, w0, v0);
-          voxel_weights(rd, gf, tr, w1, v1);
-          deposit_pair(rd, hcol, S.keys, S.used, nused, S.vals, S.logH, w0, v0, w1, v1, st[i], e, !gtab,
-                       cap, full_bit);
+        if (density) {
+          const bool want[2] = {q[0] != 0, q[1] != 0};
+          int slot[2];
+          claim_slots<G, 2>(S.keys, S.used, nused, S.logH, vq, want, slot, e, cap, full_bit, gl);
+          if (!(e & full_bit)) {
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+              if (!want[j]) continue;
+              add_delta(S.vals, hcol, slot[j], 0, q[j], !gtab);
+              for (int b = 0; b < rd.nb; b++)
+                add_delta(S.vals, hcol, slot[j], 1 + b, q[j] * (long long)((sw >> (8 * b)) & 0xFF), !gtab);
+            }
+          }
+          e = gor<G>(e);  // a full table ends the group's passes together
         }
       }
       e = gor<G>(e);
@@ -337,8 +373,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       bool want = live && !err && got < m;
       if (want && ++it > kMaxIter) { err |= E_SPIN; want = false; }
       if (!__any_sync(kFull, want)) break;
-      bool ok;
-      const unsigned x = g.at(g.pos + gl, ok);
+      const unsigned x = g.word(g.pos + gl);
       const long long cand = want ? (long long)(x % (unsigned)N) : -1 - (long long)(threadIdx.x & 31u);
       const unsigned grp = __match_any_sync(kFull, cand) & gmask;
       const unsigned gshift = G == 32 ? 0u : ((threadIdx.x & 31u) & ~(unsigned)(G - 1));
@@ -376,15 +411,20 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     rsincos(ang, &sa, &ca);
     for (long long k = gl; k < m; k += G) {
       const long long i = idx[k];
-      bool ok1, ok2;
-      unsigned xa = g.at(axis_base + 2 * k, ok1), xb = g.at(axis_base + 2 * k + 1, ok2);
+      // the bead, both neighbours and both bonds, loaded together (in-range
+      // indices at the chain ends, where the term is skipped)
+      const bool hl = i != 0, hr = i + 1 != N;
+      const long long il = hl ? i - 1 : i, ir = hr ? i + 1 : i;
+      Real r[3], t3[3], t2[3], tt3[3], tt2[3], r0[3], t30[3], r1[3], t31[3];
+      ld3(r4, i, r); ld3(t34, i, t3); ld3(t24, i, t2);
+      ld3(r4, il, r0); ld3(t34, il, t30); ld3(r4, ir, r1); ld3(t34, ir, t31);
+      const Bond<Real> bl = bond_at(bonds, bonds32, il, (Real)0), br = bond_at(bonds, bonds32, i, (Real)0);
+      const unsigned xa = g.word(axis_base + 2 * k), xb = g.word(axis_base + 2 * k + 1);
       Real axis[3];
       sphere_from<Real>(xa, xb, axis);
       const Real origin[3] = {0, 0, 0};
       Real M[3][4];
       axis_rotation_sc(axis, origin, sa, ca, M);
-      Real r[3], t3[3], t2[3], tt3[3], tt2[3];
-      ld3(r4, i, r); ld3(t34, i, t3); ld3(t24, i, t2);
       for (int j = 0; j < 3; j++) {
         Real e3 = 0, e2 = 0;
         for (int q = 0; q < 3; q++) { e3 += M[j][q] * t3[q]; e2 += M[j][q] * t2[q]; }
@@ -393,16 +433,8 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       stage[3 * k + 1] = V4<Pos>{(Pos)tt3[0], (Pos)tt3[1], (Pos)tt3[2], (Pos)0};
       stage[3 * k + 2] = V4<Pos>{(Pos)tt2[0], (Pos)tt2[1], (Pos)tt2[2], (Pos)0};
       Acc de = acc_zero<Acc>();
-      if (i != 0) {
-        Real r0[3], t30[3];
-        ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
-        acc_add(de, pair_dE_fwd(bond_at(bonds, bonds32, i - 1, (Real)0), r0, r, r, t30, t3, tt3));
-      }
-      if (i + 1 != N) {
-        Real r1[3], t31[3];
-        ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
-        acc_add(de, pair_dE_rev(bond_at(bonds, bonds32, i, (Real)0), r, r, r1, t3, tt3, t31));
-      }
+      if (hl) acc_add(de, pair_dE_fwd(bl, r0, r, r, t30, t3, tt3));
+      if (hr) acc_add(de, pair_dE_rev(br, r, r, r1, t3, tt3, t31));
       acc_add(part, de);
     }
     g.pos = axis_base + 2 * (unsigned long long)m;
@@ -432,26 +464,40 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     int* idx = S.idx;
     Acc part = acc_zero<Acc>();
     int dbl = 0;
-    for (long long k = gl; k < m; k += G) {
-      const long long i = ind0 + k;
-      bool ok;
-      int s_new = g.state_at(g.bpos + k, nt, ok);
-      unsigned sw = st[i], mw = mk[i];
-      int s_old = (int)((sw >> (8 * bsel)) & 0xFF);
-      acc_add(part, bead_bind_dE(ws, sw, mw, bsel, s_new, (Real)0));
-      dbl += (s_new == 2 ? 1 : 0) - (s_old == 2 ? 1 : 0);
-      idx[k] = s_new;
-      if (density && s_new != s_old) {
-        Real p[3], wv[8];
-        int v[8];
-        ld3(r4, i, p);
-        voxel_weights(rd, gf, p, wv, v);
-#pragma unroll
-        for (int l = 0; l < 8; l++) {
-          int slot = hash_slot(S.keys, S.used, nused, S.logH, v[l], err);
-          if (slot < 0) break;
-          add_delta(S.vals, hcol, slot, 1 + bsel, q40(wv[l]) * (long long)(s_new - s_old), !gtab);
+    // eight lanes per bead as for the position moves: corner lane 0 takes the
+    // binding free energy, each lane the change of its corner's binder column
+    constexpr int BP = G / 8;
+    const int kc = gl >> 3, cl = gl & 7;
+    for (long long kb = 0; __any_sync(kFull, kb < m); kb += BP) {
+      const long long k = kb + kc;
+      int vq[1] = {0};
+      bool want[1] = {false};
+      long long q = 0;
+      if (k < m) {
+        const long long i = ind0 + k;
+        bool ok;
+        int s_new = g.state_at(g.bpos + k, nt, ok);
+        unsigned sw = st[i], mw = mk[i];
+        int s_old = (int)((sw >> (8 * bsel)) & 0xFF);
+        if (cl == 0) {
+          acc_add(part, bead_bind_dE(ws, sw, mw, bsel, s_new, (Real)0));
+          dbl += (s_new == 2 ? 1 : 0) - (s_old == 2 ? 1 : 0);
+          idx[k] = s_new;
         }
+        if (density && s_new != s_old) {
+          Real p[3], wl[3], w;
+          int lo[3], hi[3];
+          ld3(r4, i, p);
+          voxel_axes(rd, gf, p, wl, lo, hi);
+          voxel_corner(gf, wl, lo, hi, cl, w, vq[0]);
+          q = q40(w) * (long long)(s_new - s_old);
+          want[0] = true;
+        }
+      }
+      if (density) {
+        int slot[1];
+        claim_slots<G, 1>(S.keys, S.used, nused, S.logH, vq, want, slot, err, 1 << S.logH, E_SPIN, gl);
+        if (want[0] && slot[0] >= 0) add_delta(S.vals, hcol, slot[0], 1 + bsel, q, !gtab);
       }
     }
     g.bpos += (unsigned long long)m;

@@ -42,6 +42,14 @@ struct MovePlan {
   unsigned cmask;
   int nvox, gtab, gstage, bsel, pad;
   double dE;
+  // block-wide deposit of a position move (its beads' corners spread over
+  // every thread of the CTA): the proposal's transform and table kind in,
+  // the two boundary bond terms, the confinement counts and the error bits out
+  int blk, sure, oob;
+  unsigned derr;
+  long long pq[2];
+  double ph[2];
+  double M[12];
 };
 
 // Shared-memory header of one replica's CTA.

@@ -186,16 +186,17 @@ __device__ __forceinline__ void claim_add8(const RepDev& rd, int hcol, int* keys
   }
 }
 
-// Claim (or find) the slots of up to NQ voxels per lane of a group of G lanes
-// (v[j] where want[j]); the group appends its new slots to the used list
-// with one counter update.  Every lane's home-slot claims are issued back to
-// back; only a claim that meets another key probes on.  A table that cannot
-// take a new voxel (slot -1), or whose count of voxels passes `cap` (every
-// lane of the group), sets `full_bit` in err.  Called by the whole warp.
-template <int G, int NQ>
+// Claim (or find) the slots of up to NQ voxels per lane (v[j] where
+// want[j]) in a table shared by the lanes `peers` (this lane's bit set); the
+// peers append their new slots to the used list with one counter update.
+// Every lane's home-slot claims are issued back to back; only a claim that
+// meets another key probes on.  A table that cannot take a new voxel (slot
+// -1), or whose count of voxels passes `cap` (every peer), sets `full_bit` in
+// err.  Called by the whole warp.
+template <int NQ>
 __device__ __forceinline__ void claim_slots(int* keys, int* used, int* nused, int logH, const int (&v)[NQ],
                                             const bool (&want)[NQ], int (&slot)[NQ], unsigned& err,
-                                            int cap, unsigned full_bit, int gl) {
+                                            int cap, unsigned full_bit, unsigned peers) {
   int prev[NQ];
   bool fresh[NQ];
 #pragma unroll
@@ -217,17 +218,18 @@ __device__ __forceinline__ void claim_slots(int* keys, int* used, int* nused, in
       }
     }
   }
-  const unsigned lt = (1u << gl) - 1u;
+  const unsigned lane = threadIdx.x & 31u, lt = (1u << lane) - 1u;
+  const int leader = __ffs((int)peers) - 1;
   unsigned bal[NQ];
   int cnt = 0;
 #pragma unroll
   for (int j = 0; j < NQ; j++) {
-    bal[j] = gballot<G>(fresh[j]);
+    bal[j] = __ballot_sync(kFull, fresh[j]) & peers;
     cnt += __popc(bal[j]);
   }
   int base = 0;
-  if (gl == 0 && cnt) base = atomicAdd(nused, cnt);
-  base = __shfl_sync(kFull, base, (int)((threadIdx.x & 31u) & ~(unsigned)(G - 1)));
+  if ((int)lane == leader && cnt) base = atomicAdd(nused, cnt);
+  base = __shfl_sync(kFull, base, leader);
   int at = base;
 #pragma unroll
   for (int j = 0; j < NQ; j++) {
@@ -235,6 +237,21 @@ __device__ __forceinline__ void claim_slots(int* keys, int* used, int* nused, in
     at += __popc(bal[j]);
   }
   if (at > cap) err |= full_bit;
+}
+
+// The lanes of this lane's aligned group of G lanes.
+template <int G>
+__device__ __forceinline__ unsigned group_mask() {
+  if (G == 32) return kFull;
+  return ((1u << (G & 31)) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(G - 1));
+}
+
+// Add a corner's contribution q to a voxel-table slot: the bead column, and
+// q times the bead's state for each binder column (states packed as bytes).
+__device__ __forceinline__ void add_corner(long long* vals, int hcol, int slot, long long q, unsigned sw, int nb,
+                                           bool split) {
+  add_delta(vals, hcol, slot, 0, q, split);
+  for (int b = 0; b < nb; b++) add_delta(vals, hcol, slot, 1 + b, q * (long long)((sw >> (8 * b)) & 0xFF), split);
 }
 
 // Remove one bead's old trilinear weights (w0 at voxels v0) and add its new

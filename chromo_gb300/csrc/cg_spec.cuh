@@ -127,14 +127,177 @@ __device__ __forceinline__ void clear_table(const SlotScratch& T, int hcol, int 
   }
 }
 
+// A position move's bead data in global memory (one replica).
+template <typename Pos>
+struct ChainView {
+  const V4<Pos>* r4;
+  const V4<Pos>* t34;
+  const V4<Pos>* t24;
+  const unsigned* st;
+  const double* bonds;
+  const float* bonds32;
+  __device__ ChainView(const KArgs& a, const RepDev& rd)
+      : r4(reinterpret_cast<const V4<Pos>*>(a.r4) + rd.bead_off),
+        t34(reinterpret_cast<const V4<Pos>*>(a.t34) + rd.bead_off),
+        t24(reinterpret_cast<const V4<Pos>*>(a.t24) + rd.bead_off),
+        st(a.states + rd.bead_off), bonds(a.bonds + rd.bead_off * 6), bonds32(a.bonds32 + rd.bead_off * 8) {}
+};
+
+// Corner cl of bead k of a position move (transform M; segment [ind0, indf)
+// of m beads of a chain of N): transforms the bead, stages its r, t3, t2
+// (corner lanes 0-2), takes the bond to a fixed left neighbour (corner lane 0
+// of the first bead, `left`) or to a fixed right neighbour (corner lane 1 of
+// the last bead, `right`) into `pterm`, counts the confinement crossings
+// (corner lane 0), and returns the corner's voxel-table contributions: q[0]
+// at vq[0] (old weight removed; the weight change when the old and new
+// weights lie in the same eight voxels) and q[1] at vq[1] (new weight
+// otherwise), with the bead's binder states in sw.  The neighbour beads and
+// bond parameters are loaded with the moved bead (in-range indices on every
+// lane).
+template <typename Pos, typename Acc>
+__device__ __forceinline__ void bead_task(const RepDev& rd, const GridF& gf, const ChainView<Pos>& cv, int kind,
+                                          const Pos (&M)[3][4], long long N, long long ind0, long long indf,
+                                          long long m, long long k, int cl, V4<Pos>* stage, bool density,
+                                          bool conf, int (&vq)[2], long long (&q)[2], unsigned& sw,
+                                          unsigned& e, bool& left, bool& right, Acc& pterm, int& oob) {
+  using Real = Pos;
+  const long long i = ind0 + k;
+  left = cl == 0 && k == 0 && ind0 != 0;
+  right = cl == 1 && k == m - 1 && indf != N;
+  const long long in = left ? i - 1 : (right ? i + 1 : i);
+  const V4<Pos> RN = cv.r4[in], TN = cv.t34[in];
+  const Bond<Real> bn = bond_at(cv.bonds, cv.bonds32, right ? i : in, (Real)0);
+  const V4<Pos> R = cv.r4[i], T3 = cv.t34[i], T2 = cv.t24[i];
+  const unsigned swi = density ? cv.st[i] : 0u;
+  const Real r[3] = {R.x, R.y, R.z}, t3[3] = {T3.x, T3.y, T3.z}, t2[3] = {T2.x, T2.y, T2.z};
+  Real tr[3], tt3[3], tt2[3];
+  if (kind == CG_SLIDE) {
+    for (int j = 0; j < 3; j++) { tr[j] = r[j] + M[j][3]; tt3[j] = t3[j]; tt2[j] = t2[j]; }
+  } else {
+    for (int j = 0; j < 3; j++) {
+      Real er = 0, e3 = 0, e2 = 0;
+      for (int qq = 0; qq < 3; qq++) { er += M[j][qq] * r[qq]; e3 += M[j][qq] * t3[qq]; e2 += M[j][qq] * t2[qq]; }
+      tr[j] = er + M[j][3]; tt3[j] = e3; tt2[j] = e2;
+    }
+  }
+  const bool fin = isfinite(tr[0]) && isfinite(tr[1]) && isfinite(tr[2]);
+  if (!fin) e |= E_NONFINITE;
+  if (cl < 3) {
+    Real o[3];
+    for (int j = 0; j < 3; j++) o[j] = cl == 0 ? tr[j] : (cl == 1 ? tt3[j] : tt2[j]);
+    stage[3 * k + cl] = V4<Pos>{(Pos)o[0], (Pos)o[1], (Pos)o[2], (Pos)0};
+  }
+  const Real rn[3] = {(Real)RN.x, (Real)RN.y, (Real)RN.z}, tn[3] = {(Real)TN.x, (Real)TN.y, (Real)TN.z};
+  pterm = acc_zero<Acc>();
+  if (left) acc_add(pterm, pair_dE_fwd(bn, rn, r, tr, tn, t3, tt3));
+  if (right) acc_add(pterm, pair_dE_rev(bn, r, tr, rn, t3, tt3, tn));
+  oob = 0;
+  if (cl == 0 && conf) oob = out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
+  if (density && fin) {
+    Real wl0[3], wl1[3], w0, w1;
+    int lo0[3], hi0[3], lo1[3], hi1[3];
+    voxel_axes(rd, gf, r, wl0, lo0, hi0);
+    voxel_axes(rd, gf, tr, wl1, lo1, hi1);
+    voxel_corner(gf, wl0, lo0, hi0, cl, w0, vq[0]);
+    voxel_corner(gf, wl1, lo1, hi1, cl, w1, vq[1]);
+    const bool same = lo0[0] == lo1[0] && lo0[1] == lo1[1] && lo0[2] == lo1[2];
+    const long long q0 = q40(w0), q1 = q40(w1);
+    q[0] = same ? q1 - q0 : -q0;
+    q[1] = same ? 0 : q1;
+    sw = swi;
+  }
+}
+
+// A bond term kept in a move plan (fixed-point part and FP64 part).
+__device__ __forceinline__ void store_acc(long long& q, double& h, const Fx& v) { q = v.q; h = v.hard; }
+__device__ __forceinline__ void store_acc(long long& q, double& h, double v) { q = 0; h = v; }
+template <typename Acc> __device__ __forceinline__ Acc load_acc(long long q, double h);
+template <> __device__ __forceinline__ Fx load_acc<Fx>(long long q, double h) { return Fx{q, h}; }
+template <> __device__ __forceinline__ double load_acc<double>(long long, double h) { return h; }
+
+// Deposit of the batch's position moves that use their slot's shared voxel
+// table (plan.blk), by every thread of the CTA: the moves' bead corners, in
+// move order, are dealt out to the threads (eight per bead), so a move of
+// many beads no longer holds the batch back while the other warps wait.
+// Claims append to each move's used list once per warp and move; the bond
+// terms, confinement counts and error bits go to the move's plan.  A move
+// whose optimistic table overflows (E_OVF) is skipped from then on; its warp
+// deposits it again in its global table.  Called by every thread.
+template <typename Pos>
+__device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, int kind) {
+  using Acc = typename AccOf<Pos>::type;
+  unsigned char* smem = reinterpret_cast<unsigned char*>(&sh);
+  const RepDev& rd = sh.ws.rd;
+  const GridF& gf = sh.ws.gf;
+  const ChainView<Pos> cv(a, rd);
+  const long long N = rd.n_beads;
+  const bool conf = rd.field_kind != 0 && rd.confine_kind;
+  const int Hs = 1 << a.logH, hcol = a.hcol;
+  int total = 0;
+  for (int s = 0; s < B; s++)
+    if (sh.plan[s].blk) total += 8 * sh.plan[s].m;
+  for (int t0 = 0; t0 < total; t0 += (int)blockDim.x) {
+    const int t = t0 + (int)threadIdx.x;
+    int s = 0, base = 0;
+    if (t < total) {
+      for (;; s++) {
+        const int n = sh.plan[s].blk ? 8 * sh.plan[s].m : 0;
+        if (t < base + n) break;
+        base += n;
+      }
+    }
+    MovePlan& P = sh.plan[s];
+    const bool act = t < total && !(P.derr & E_OVF);
+    const long long k = (t - base) >> 3;
+    const int cl = (t - base) & 7;
+    unsigned char* wb = smem + a.spec_off_warps + (size_t)s * a.warp_smem;
+    int vq[2] = {0, 0};
+    long long q[2] = {0, 0};
+    unsigned sw = 0, e = 0;
+    if (act) {
+      Pos M[3][4];
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 4; j++) M[i][j] = (Pos)P.M[4 * i + j];
+      V4<Pos>* stage = P.gstage ? reinterpret_cast<V4<Pos>*>(a.g_stage) +
+                                      ((long long)rep * a.spec_s + s) * a.g_stage_cap * 3
+                                : reinterpret_cast<V4<Pos>*>(wb + a.off_stage);
+      bool left, right;
+      Acc pterm;
+      int oob;
+      bead_task<Pos, Acc>(rd, gf, cv, kind, M, N, P.ind0, P.indf, P.m, k, cl, stage, true, conf, vq, q, sw, e,
+                          left, right, pterm, oob);
+      if (left) store_acc(P.pq[0], P.ph[0], pterm);
+      if (right) store_acc(P.pq[1], P.ph[1], pterm);
+      if (oob) atomicAdd(&P.oob, oob);
+    }
+    const unsigned peers = __match_any_sync(kFull, t < total ? s : -1);
+    int* keys = reinterpret_cast<int*>(wb + a.off_keys);
+    int* used = reinterpret_cast<int*>(wb + a.off_used);
+    long long* vals = reinterpret_cast<long long*>(wb + a.off_vals);
+    const bool want[2] = {q[0] != 0, q[1] != 0};
+    const unsigned full_bit = P.sure ? E_SPIN : E_OVF;
+    int slot[2];
+    claim_slots<2>(keys, used, &sh.nused[s], a.logH, vq, want, slot, e, P.sure ? Hs : (3 * Hs) / 4, full_bit,
+                   peers);
+    if (!(e & full_bit)) {
+#pragma unroll
+      for (int j = 0; j < 2; j++)
+        if (want[j]) add_corner(vals, hcol, slot[j], q[j], sw, rd.nb, true);
+    }
+    if (e) atomicOr(&P.derr, e);
+  }
+}
+
 // Evaluate move t of the batch in slot s (group lanes gl = 0..G-1); `live`
-// is false for the groups of a partly filled batch, which run the warp's
-// collectives with empty work.
+// is false for the groups of a partly filled batch and for the warps without
+// a move, which run the collectives and block barriers with empty work.
+// Every thread of the CTA calls it (position moves hold two block barriers
+// around the block-wide deposit); B is the batch's number of moves.
 template <typename Pos, int G>
 __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, int gl, bool live, int kind,
                               const cg_move_ctl& c, unsigned long long t, unsigned* draws,
                               const SlotScratch& sm, const SlotScratch& gm, int* bkeys, unsigned* bmask,
-                              int logHB) {
+                              int logHB, int B) {
   using Real = Pos;
   using Acc = typename AccOf<Real>::type;
   const RepDev& rd = sh.ws.rd;
@@ -151,7 +314,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
   const float* bonds32 = a.bonds32 + rd.bead_off * 8;
   MovePlan& P = sh.plan[s];
   MoveRng g;
-  g.init<G>(a.seed, rep, t, draws, gl);
+  if (__any_sync(kFull, live)) g.init<G>(a.seed, rep, t, draws, gl);
   unsigned err = 0;
   const bool check_field = rd.field_kind != 0 && kind != CG_TANGENT_ROTATION;
   const bool density = rd.field_kind == 2;
@@ -168,6 +331,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
   const int Hs = 1 << sm.logH;
 
   if (kind <= CG_SLIDE) {
+    const ChainView<Pos> cv(a, rd);
     Real M[3][4];
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 4; j++) M[i][j] = i == j ? (Real)1 : (Real)0;
@@ -234,9 +398,39 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     const bool sure = 16 * m <= Hs;
     if (!sure && 4 * m > Hs) { use_table(S, gm); gtab = 1; }
     V4<Pos>* stage = reinterpret_cast<V4<Pos>*>(S.stage);  // r, t3, t2 of each moved bead
+    // moves with a shared table are deposited by the whole CTA
+    const bool blk = density && m > 0 && !gtab;
+    if (gl == 0 && live) {
+      P.blk = blk ? 1 : 0;
+      P.sure = sure ? 1 : 0;
+      P.m = (int)m;
+      P.ind0 = (int)ind0;
+      P.indf = (int)indf;
+      P.gstage = gstage;
+      P.oob = 0;
+      P.derr = 0;
+      P.pq[0] = P.pq[1] = 0;
+      P.ph[0] = P.ph[1] = 0;
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 4; j++) P.M[4 * i + j] = (double)M[i][j];
+    }
+    __syncthreads();
+    block_deposit<Pos>(a, sh, rep, B, kind);
+    __syncthreads();
     Acc part = acc_zero<Acc>();
     int oob = 0;
     bool ovf = false;
+    if (blk) {
+      const unsigned eb = P.derr;
+      ovf = (eb & E_OVF) != 0;
+      err |= eb & ~E_OVF;
+      if (gl == 0) {
+        acc_add(part, load_acc<Acc>(P.pq[0], P.ph[0]));
+        acc_add(part, load_acc<Acc>(P.pq[1], P.ph[1]));
+        oob = P.oob;
+      }
+    }
+    const unsigned peers = group_mask<G>();
     for (int pass = 0; pass < 2; pass++) {
       if (pass == 1) {
         if (!__any_sync(kFull, ovf)) break;
@@ -251,18 +445,13 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
         }
         __syncwarp();
       }
-      const bool run = pass == 0 || ovf;
+      // pass 0: the moves the CTA did not deposit; pass 1: overflowed ones
+      const bool run = pass == 0 ? !blk : ovf;
       const int cap = gtab ? (1 << gm.logH) : (sure ? Hs : (3 * Hs) / 4);
       const unsigned full_bit = (gtab || sure) ? E_SPIN : E_OVF;
       unsigned e = 0;
-      // Eight lanes per bead, lane gl taking trilinear corner gl & 7 of bead
-      // gl >> 3 of each pass: every lane transforms its bead (the eight
-      // copies are the same arithmetic), corner lane 0 adds the bead's
-      // elastic and confinement terms, lanes 0-2 stage its r, t3, t2, and
-      // each lane removes its corner's old weight and adds the new one.  When
-      // the old and new weights lie in the same eight voxels (the same lower
-      // corner) the corner gets one contribution q(w1) - q(w0); contributions
-      // of zero claim nothing.
+      // the group's own deposit: eight lanes per bead, lane gl taking
+      // trilinear corner gl & 7 of bead gl >> 3 of each pass
       constexpr int BP = G / 8;
       const int kc = gl >> 3, cl = gl & 7;
       for (long long kb = 0; __any_sync(kFull, run && kb < m && !(e & E_OVF)); kb += BP) {
@@ -272,72 +461,28 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
         long long q[2] = {0, 0};
         unsigned sw = 0;
         if (act) {
-          const long long i = ind0 + k;
-          // corner lane 0 of the first bead takes the bond to its fixed left
-          // neighbour, corner lane 1 of the last bead the bond to its fixed
-          // right neighbour; their beads and bond parameters are loaded with
-          // the moved bead's (in-range indices on every lane)
-          const bool left = cl == 0 && k == 0 && ind0 != 0;
-          const bool right = cl == 1 && k == m - 1 && indf != N;
-          const long long in = left ? i - 1 : (right ? i + 1 : i);
-          const V4<Pos> RN = r4[in], TN = t34[in];
-          const Bond<Real> bn = bond_at(bonds, bonds32, right ? i : in, (Real)0);
-          V4<Pos> R = r4[i], T3 = t34[i], T2 = t24[i];
-          Real r[3] = {R.x, R.y, R.z}, t3[3] = {T3.x, T3.y, T3.z}, t2[3] = {T2.x, T2.y, T2.z};
-          Real tr[3], tt3[3], tt2[3];
-          if (kind == CG_SLIDE) {
-            for (int j = 0; j < 3; j++) { tr[j] = r[j] + M[j][3]; tt3[j] = t3[j]; tt2[j] = t2[j]; }
-          } else {
-            for (int j = 0; j < 3; j++) {
-              Real er = 0, e3 = 0, e2 = 0;
-              for (int qq = 0; qq < 3; qq++) { er += M[j][qq] * r[qq]; e3 += M[j][qq] * t3[qq]; e2 += M[j][qq] * t2[qq]; }
-              tr[j] = er + M[j][3]; tt3[j] = e3; tt2[j] = e2;
-            }
-          }
-          const bool fin = isfinite(tr[0]) && isfinite(tr[1]) && isfinite(tr[2]);
-          if (!fin) e |= E_NONFINITE;
-          if (cl < 3) {
-            Real o[3];
-            for (int j = 0; j < 3; j++) o[j] = cl == 0 ? tr[j] : (cl == 1 ? tt3[j] : tt2[j]);
-            stage[3 * k + cl] = V4<Pos>{(Pos)o[0], (Pos)o[1], (Pos)o[2], (Pos)0};
-          }
-          const Real rn[3] = {(Real)RN.x, (Real)RN.y, (Real)RN.z}, tn[3] = {(Real)TN.x, (Real)TN.y, (Real)TN.z};
-          if (left) acc_add(part, pair_dE_fwd(bn, rn, r, tr, tn, t3, tt3));
-          if (right) acc_add(part, pair_dE_rev(bn, r, tr, rn, t3, tt3, tn));
-          if (cl == 0 && check_field && rd.confine_kind)
-            oob += out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
-          if (density && fin) {
-            Real wl0[3], wl1[3], w0, w1;
-            int lo0[3], hi0[3], lo1[3], hi1[3];
-            voxel_axes(rd, gf, r, wl0, lo0, hi0);
-            voxel_axes(rd, gf, tr, wl1, lo1, hi1);
-            voxel_corner(gf, wl0, lo0, hi0, cl, w0, vq[0]);
-            voxel_corner(gf, wl1, lo1, hi1, cl, w1, vq[1]);
-            const bool same = lo0[0] == lo1[0] && lo0[1] == lo1[1] && lo0[2] == lo1[2];
-            const long long q0 = q40(w0), q1 = q40(w1);
-            q[0] = same ? q1 - q0 : -q0;
-            q[1] = same ? 0 : q1;
-            sw = st[i];
-          }
+          bool left, right;
+          Acc pterm;
+          int ob;
+          bead_task<Pos, Acc>(rd, gf, cv, kind, M, N, ind0, indf, m, k, cl, stage, density,
+                              check_field && rd.confine_kind, vq, q, sw, e, left, right, pterm, ob);
+          if (left || right) acc_add(part, pterm);
+          oob += ob;
         }
         if (density) {
           const bool want[2] = {q[0] != 0, q[1] != 0};
           int slot[2];
-          claim_slots<G, 2>(S.keys, S.used, nused, S.logH, vq, want, slot, e, cap, full_bit, gl);
+          claim_slots<2>(S.keys, S.used, nused, S.logH, vq, want, slot, e, cap, full_bit, peers);
           if (!(e & full_bit)) {
 #pragma unroll
-            for (int j = 0; j < 2; j++) {
-              if (!want[j]) continue;
-              add_delta(S.vals, hcol, slot[j], 0, q[j], !gtab);
-              for (int b = 0; b < rd.nb; b++)
-                add_delta(S.vals, hcol, slot[j], 1 + b, q[j] * (long long)((sw >> (8 * b)) & 0xFF), !gtab);
-            }
+            for (int j = 0; j < 2; j++)
+              if (want[j]) add_corner(S.vals, hcol, slot[j], q[j], sw, rd.nb, !gtab);
           }
           e = gor<G>(e);  // a full table ends the group's passes together
         }
       }
       e = gor<G>(e);
-      ovf = (e & E_OVF) != 0;
+      if (run) ovf = (e & E_OVF) != 0;
       err |= e & ~E_OVF;
     }
     err = gor<G>(err);
@@ -496,7 +641,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       }
       if (density) {
         int slot[1];
-        claim_slots<G, 1>(S.keys, S.used, nused, S.logH, vq, want, slot, err, 1 << S.logH, E_SPIN, gl);
+        claim_slots<1>(S.keys, S.used, nused, S.logH, vq, want, slot, err, 1 << S.logH, E_SPIN, group_mask<G>());
         if (want[0] && slot[0] >= 0) add_delta(S.vals, hcol, slot[0], 1 + bsel, q, !gtab);
       }
     }
@@ -760,9 +905,8 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
           const int B = (int)(c.num_per_cycle - done < Sn ? c.num_per_cycle - done : Sn);
           const bool wlive = warp * GPW < B;  // the warp has a move of this batch
           const bool live = slot < B;
-          if (wlive)
-            evaluate_move<Pos, G>(a, sh, rep, slot, gl, live, kind, c, sh.t0 + (unsigned long long)slot,
-                                  draws, sm, gm, bkeys, bmask, a.spec_logHB);
+          evaluate_move<Pos, G>(a, sh, rep, slot, gl, live, kind, c, sh.t0 + (unsigned long long)slot, draws,
+                                sm, gm, bkeys, bmask, a.spec_logHB, B);
           __syncthreads();
           if (wlive) conflict_mask<G>(a, sh, smem, rep, slot, gl, live, kind, B, sm, gm, bmask);
           __syncthreads();
@@ -800,12 +944,15 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
               t[3] += sm_v;
               t[4] += ac_m;
               t[5] += ac_v;
+              // acc = alpha * x + (1 - alpha) * acc with x in {0, 1}, where
+              // alpha * x is alpha or 0 exactly: one FP64 multiply-add chain
               double run = sh.run_dE, rate = c.acc_rate;
+              const double alpha = c.alpha, beta = 1 - c.alpha;
               for (int w = 0; w < cut; w++) {
                 const MovePlan& P = sh.plan[w];
                 if (P.empty) continue;
                 if (P.dec) run += P.dE;
-                rate = c.alpha * (P.dec ? 1.0 : 0.0) + (1 - c.alpha) * rate;
+                rate = (P.dec ? alpha : 0.0) + beta * rate;
               }
               sh.run_dE = run;
               c.acc_rate = rate;

@@ -49,7 +49,7 @@ struct MovePlan {
   unsigned derr;
   long long pq[2];
   double ph[2];
-  double M[12];
+  double M[12];  // the 3 x 4 transform, stored in the position type
 };
 
 // Shared-memory header of one replica's CTA.

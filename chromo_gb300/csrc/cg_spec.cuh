@@ -256,8 +256,9 @@ __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, in
     unsigned sw = 0, e = 0;
     if (act) {
       Pos M[3][4];
+      const Pos* Mp = reinterpret_cast<const Pos*>(P.M);
       for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 4; j++) M[i][j] = (Pos)P.M[4 * i + j];
+        for (int j = 0; j < 4; j++) M[i][j] = Mp[4 * i + j];
       V4<Pos>* stage = P.gstage ? reinterpret_cast<V4<Pos>*>(a.g_stage) +
                                       ((long long)rep * a.spec_s + s) * a.g_stage_cap * 3
                                 : reinterpret_cast<V4<Pos>*>(wb + a.off_stage);
@@ -326,6 +327,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
   long long nvox = 0;
   bool empty = !live;
   int gtab = 0, gstage = 0;
+  unsigned cmb = 0;  // position moves: conflicts with earlier moves of the batch
   SlotScratch S = sm;
   int* nused = &sh.nused[s];
   const int Hs = 1 << sm.logH;
@@ -409,13 +411,27 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       P.gstage = gstage;
       P.oob = 0;
       P.derr = 0;
+      P.cmask = 0;
       P.pq[0] = P.pq[1] = 0;
       P.ph[0] = P.ph[1] = 0;
+      Pos* Mp = reinterpret_cast<Pos*>(P.M);  // in the position type: no conversions
       for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 4; j++) P.M[4 * i + j] = (double)M[i][j];
+        for (int j = 0; j < 4; j++) Mp[4 * i + j] = M[i][j];
     }
     __syncthreads();
     block_deposit<Pos>(a, sh, rep, B, kind);
+    // earlier moves u of the batch whose written beads [ind0, indf) meet the
+    // beads this move reads (its segment and both neighbours); a move with no
+    // beads (failed or empty) is never accepted, so it needs no exclusion
+    for (int u0 = 0; u0 < B; u0 += G) {
+      const int u = u0 + gl;
+      bool hit = false;
+      if (m > 0 && u < s) {
+        const MovePlan& U = sh.plan[u];
+        hit = U.m > 0 && (long long)U.ind0 <= indf && ind0 - 1 <= (long long)U.indf - 1;
+      }
+      cmb |= gballot<G>(hit) << u0;
+    }
     __syncthreads();
     Acc part = acc_zero<Acc>();
     int oob = 0;
@@ -509,9 +525,12 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     if (m > a.stage_cap) { S.stage = gm.stage; S.idx = gm.idx; gstage = 1; }
     int* idx = S.idx;
     // n distinct random beads, drawn in order with redraws (get_inds): G
-    // candidates per round, the first fresh ones taken in draw order
+    // candidates per round, the first fresh ones taken in draw order.  Beads
+    // taken in a round that another round follows are marked in the slot's
+    // bitmap, which later rounds consult (a move of fewer beads than G
+    // usually needs one round and touches no bitmap).
     long long got = 0;
-    int it = 0;
+    int it = 0, rounds = 0;
     const unsigned lt = (1u << gl) - 1u;
     const unsigned gmask = G == 32 ? kFull : ((1u << (G & 31)) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(G - 1));
     for (;;) {
@@ -523,16 +542,17 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       const unsigned grp = __match_any_sync(kFull, cand) & gmask;
       const unsigned gshift = G == 32 ? 0u : ((threadIdx.x & 31u) & ~(unsigned)(G - 1));
       const bool first = ((grp >> gshift) & lt) == 0;
-      const bool fresh = want && first && !((S.picked[cand >> 5] >> (cand & 31)) & 1u);
+      const bool fresh = want && first && !(rounds > 0 && ((S.picked[cand >> 5] >> (cand & 31)) & 1u));
       const unsigned bal = gballot<G>(fresh);
       const long long need = m - got;
       const int cnt = __popc(bal);
       const int rank = __popc(bal & lt);
       if (fresh && rank < need) {
         idx[got + rank] = (int)cand;
-        atomicOr(&S.picked[cand >> 5], 1u << (cand & 31));
+        if (cnt < need) atomicOr(&S.picked[cand >> 5], 1u << (cand & 31));
       }
       if (want) {
+        rounds++;
         long long consumed;
         if (cnt >= need) {
           unsigned b = bal;
@@ -548,6 +568,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       __syncwarp();
     }
     err = gor<G>(err);
+    const long long marked = rounds > 1 ? got : 0;  // beads whose marks are cleared below
     if (err) m = 0;
     const unsigned long long axis_base = g.pos;
     V4<Pos>* stage = reinterpret_cast<V4<Pos>*>(S.stage);
@@ -585,7 +606,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     g.pos = axis_base + 2 * (unsigned long long)m;
     dEp = gsum<G>(part);
     // the picked marks only serve the redraws of this move
-    for (long long k = gl; k < m; k += G) {
+    for (long long k = gl; k < marked; k += G) {
       int i = idx[k];
       atomicAnd(&S.picked[i >> 5], ~(1u << (i & 31)));
     }
@@ -667,17 +688,33 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
   }
   err = gor<G>(err);
   // register the touched voxels for the conflict test
+  // (position moves: the moves that registered a voxel first are this
+  // move's conflicts if earlier in the batch; a later move that registered
+  // it first learns of this one through its plan's mask)
   int regfail = 0;
   if (density && check_field) {
     const int nu = (live && !err && !empty) ? *nused : 0;
+    const unsigned below = (1u << s) - 1u, above = ~((2u << s) - 1u);
     for (int i = gl; i < nu; i += G) {
       int v = S.keys[S.used[i]];
       int b = block_insert(bkeys, logHB, v);
       S.bslot[i] = b;
-      if (b < 0) regfail = 1;
-      else atomicOr(&bmask[b], 1u << s);
+      if (b < 0) {
+        regfail = 1;
+      } else {
+        const unsigned prior = atomicOr(&bmask[b], 1u << s);
+        if (kind <= CG_SLIDE) {
+          cmb |= prior & below;
+          for (unsigned later = prior & above; later; later &= later - 1)
+            atomicOr(&sh.plan[__ffs((int)later) - 1].cmask, 1u << s);
+        }
+      }
     }
     regfail = (int)gor<G>((unsigned)regfail);
+  }
+  if (kind <= CG_SLIDE) {
+    cmb = gor<G>(cmb);
+    if (gl == 0 && live) atomicOr(&P.cmask, cmb);
   }
   bool dec = false;
   if (live && !err && !empty) dec = decide(g.next(), dEp, dEs, dEh, gl == 0 ? &P.dE : nullptr);
@@ -908,8 +945,10 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
           evaluate_move<Pos, G>(a, sh, rep, slot, gl, live, kind, c, sh.t0 + (unsigned long long)slot, draws,
                                 sm, gm, bkeys, bmask, a.spec_logHB, B);
           __syncthreads();
-          if (wlive) conflict_mask<G>(a, sh, smem, rep, slot, gl, live, kind, B, sm, gm, bmask);
-          __syncthreads();
+          if (kind > CG_SLIDE) {  // position moves set their masks while evaluating
+            if (wlive) conflict_mask<G>(a, sh, smem, rep, slot, gl, live, kind, B, sm, gm, bmask);
+            __syncthreads();
+          }
           // Resolve, computed by every warp from the plans (lane u reads move u):
           // the batch stands up to the first move that failed or meets an
           // earlier accepted move (everything before it stands, so "earlier

@@ -143,23 +143,29 @@ struct ChainView {
         st(a.states + rd.bead_off), bonds(a.bonds + rd.bead_off * 6), bonds32(a.bonds32 + rd.bead_off * 8) {}
 };
 
-// Corner cl of bead k of a position move (transform M; segment [ind0, indf)
-// of m beads of a chain of N): transforms the bead, stages its r, t3, t2
-// (corner lanes 0-2), takes the bond to a fixed left neighbour (corner lane 0
-// of the first bead, `left`) or to a fixed right neighbour (corner lane 1 of
+// Lanes per bead of the position-move deposit; each lane takes 8 / kLanesPerBead
+// of the bead's trilinear corners.
+constexpr int kLanesPerBead = 4;
+constexpr int kCornersPerLane = 8 / kLanesPerBead;
+
+// Lane cl (0..kLanesPerBead-1) of bead k of a position move (transform M;
+// segment [ind0, indf) of m beads of a chain of N): transforms the bead,
+// stages its r, t3, t2 (lanes 0-2), takes the bond to a fixed left neighbour
+// (lane 0 of the first bead, `left`) or to a fixed right neighbour (lane 1 of
 // the last bead, `right`) into `pterm`, counts the confinement crossings
-// (corner lane 0), and returns the corner's voxel-table contributions: q[0]
-// at vq[0] (old weight removed; the weight change when the old and new
-// weights lie in the same eight voxels) and q[1] at vq[1] (new weight
-// otherwise), with the bead's binder states in sw.  The neighbour beads and
-// bond parameters are loaded with the moved bead (in-range indices on every
-// lane).
+// (lane 0), and returns the voxel-table contributions of its corners c =
+// cl * kCornersPerLane + j: q[2j] at vq[2j] (old weight removed; the weight
+// change when the old and new weights lie in the same eight voxels) and
+// q[2j+1] at vq[2j+1] (new weight otherwise), with the bead's binder states
+// in sw.  The neighbour beads and bond parameters are loaded with the moved
+// bead (in-range indices on every lane).
 template <typename Pos, typename Acc>
 __device__ __forceinline__ void bead_task(const RepDev& rd, const GridF& gf, const ChainView<Pos>& cv, int kind,
                                           const Pos (&M)[3][4], long long N, long long ind0, long long indf,
                                           long long m, long long k, int cl, V4<Pos>* stage, bool density,
-                                          bool conf, int (&vq)[2], long long (&q)[2], unsigned& sw,
-                                          unsigned& e, bool& left, bool& right, Acc& pterm, int& oob) {
+                                          bool conf, int (&vq)[2 * kCornersPerLane],
+                                          long long (&q)[2 * kCornersPerLane], unsigned& sw, unsigned& e,
+                                          bool& left, bool& right, Acc& pterm, int& oob) {
   using Real = Pos;
   const long long i = ind0 + k;
   left = cl == 0 && k == 0 && ind0 != 0;
@@ -194,16 +200,21 @@ __device__ __forceinline__ void bead_task(const RepDev& rd, const GridF& gf, con
   oob = 0;
   if (cl == 0 && conf) oob = out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
   if (density && fin) {
-    Real wl0[3], wl1[3], w0, w1;
+    Real wl0[3], wl1[3];
     int lo0[3], hi0[3], lo1[3], hi1[3];
     voxel_axes(rd, gf, r, wl0, lo0, hi0);
     voxel_axes(rd, gf, tr, wl1, lo1, hi1);
-    voxel_corner(gf, wl0, lo0, hi0, cl, w0, vq[0]);
-    voxel_corner(gf, wl1, lo1, hi1, cl, w1, vq[1]);
     const bool same = lo0[0] == lo1[0] && lo0[1] == lo1[1] && lo0[2] == lo1[2];
-    const long long q0 = q40(w0), q1 = q40(w1);
-    q[0] = same ? q1 - q0 : -q0;
-    q[1] = same ? 0 : q1;
+#pragma unroll
+    for (int j = 0; j < kCornersPerLane; j++) {
+      const int c = cl * kCornersPerLane + j;
+      Real w0, w1;
+      voxel_corner(gf, wl0, lo0, hi0, c, w0, vq[2 * j]);
+      voxel_corner(gf, wl1, lo1, hi1, c, w1, vq[2 * j + 1]);
+      const long long q0 = q40(w0), q1 = q40(w1);
+      q[2 * j] = same ? q1 - q0 : -q0;
+      q[2 * j + 1] = same ? 0 : q1;
+    }
     sw = swi;
   }
 }
@@ -233,26 +244,31 @@ __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, in
   const long long N = rd.n_beads;
   const bool conf = rd.field_kind != 0 && rd.confine_kind;
   const int Hs = 1 << a.logH, hcol = a.hcol;
-  int total = 0;
-  for (int s = 0; s < B; s++)
-    if (sh.plan[s].blk) total += 8 * sh.plan[s].m;
+  // lane j of every warp holds the end of move j's tasks in the batch's
+  // task list (kLanesPerBead per bead of the moves with plan.blk)
+  const int lane = (int)(threadIdx.x & 31u);
+  int end = (lane < B && sh.plan[lane].blk) ? kLanesPerBead * sh.plan[lane].m : 0;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, end, o);
+    if (lane >= o) end += y;
+  }
+  const int total = __shfl_sync(kFull, end, 31);
   for (int t0 = 0; t0 < total; t0 += (int)blockDim.x) {
     const int t = t0 + (int)threadIdx.x;
-    int s = 0, base = 0;
-    if (t < total) {
-      for (;; s++) {
-        const int n = sh.plan[s].blk ? 8 * sh.plan[s].m : 0;
-        if (t < base + n) break;
-        base += n;
-      }
-    }
+    // the task's move: the number of moves whose tasks end at or before t
+    int s = 0;
+    for (int j = 0; j < B; j++) s += __shfl_sync(kFull, end, j) <= t ? 1 : 0;
+    const int before = __shfl_sync(kFull, end, s > 0 ? s - 1 : 0);
+    int base = s > 0 ? before : 0;
+    if (t >= total) s = base = 0;
     MovePlan& P = sh.plan[s];
     const bool act = t < total && !(P.derr & E_OVF);
-    const long long k = (t - base) >> 3;
-    const int cl = (t - base) & 7;
+    const long long k = (t - base) / kLanesPerBead;
+    const int cl = (t - base) % kLanesPerBead;
     unsigned char* wb = smem + a.spec_off_warps + (size_t)s * a.warp_smem;
-    int vq[2] = {0, 0};
-    long long q[2] = {0, 0};
+    int vq[2 * kCornersPerLane] = {};
+    long long q[2 * kCornersPerLane] = {};
     unsigned sw = 0, e = 0;
     if (act) {
       Pos M[3][4];
@@ -275,14 +291,16 @@ __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, in
     int* keys = reinterpret_cast<int*>(wb + a.off_keys);
     int* used = reinterpret_cast<int*>(wb + a.off_used);
     long long* vals = reinterpret_cast<long long*>(wb + a.off_vals);
-    const bool want[2] = {q[0] != 0, q[1] != 0};
+    bool want[2 * kCornersPerLane];
+#pragma unroll
+    for (int j = 0; j < 2 * kCornersPerLane; j++) want[j] = q[j] != 0;
     const unsigned full_bit = P.sure ? E_SPIN : E_OVF;
-    int slot[2];
-    claim_slots<2>(keys, used, &sh.nused[s], a.logH, vq, want, slot, e, P.sure ? Hs : (3 * Hs) / 4, full_bit,
-                   peers);
+    int slot[2 * kCornersPerLane];
+    claim_slots<2 * kCornersPerLane>(keys, used, &sh.nused[s], a.logH, vq, want, slot, e,
+                                     P.sure ? Hs : (3 * Hs) / 4, full_bit, peers);
     if (!(e & full_bit)) {
 #pragma unroll
-      for (int j = 0; j < 2; j++)
+      for (int j = 0; j < 2 * kCornersPerLane; j++)
         if (want[j]) add_corner(vals, hcol, slot[j], q[j], sw, rd.nb, true);
     }
     if (e) atomicOr(&P.derr, e);
@@ -466,15 +484,15 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       const int cap = gtab ? (1 << gm.logH) : (sure ? Hs : (3 * Hs) / 4);
       const unsigned full_bit = (gtab || sure) ? E_SPIN : E_OVF;
       unsigned e = 0;
-      // the group's own deposit: eight lanes per bead, lane gl taking
-      // trilinear corner gl & 7 of bead gl >> 3 of each pass
-      constexpr int BP = G / 8;
-      const int kc = gl >> 3, cl = gl & 7;
+      // the group's own deposit: kLanesPerBead lanes per bead, lane gl
+      // taking part gl % kLanesPerBead of bead gl / kLanesPerBead of a pass
+      constexpr int BP = G / kLanesPerBead;
+      const int kc = gl / kLanesPerBead, cl = gl % kLanesPerBead;
       for (long long kb = 0; __any_sync(kFull, run && kb < m && !(e & E_OVF)); kb += BP) {
         const long long k = kb + kc;
         const bool act = run && k < m && !(e & E_OVF);
-        int vq[2] = {0, 0};
-        long long q[2] = {0, 0};
+        int vq[2 * kCornersPerLane] = {};
+        long long q[2 * kCornersPerLane] = {};
         unsigned sw = 0;
         if (act) {
           bool left, right;
@@ -486,12 +504,14 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
           oob += ob;
         }
         if (density) {
-          const bool want[2] = {q[0] != 0, q[1] != 0};
-          int slot[2];
-          claim_slots<2>(S.keys, S.used, nused, S.logH, vq, want, slot, e, cap, full_bit, peers);
+          bool want[2 * kCornersPerLane];
+#pragma unroll
+          for (int j = 0; j < 2 * kCornersPerLane; j++) want[j] = q[j] != 0;
+          int slot[2 * kCornersPerLane];
+          claim_slots<2 * kCornersPerLane>(S.keys, S.used, nused, S.logH, vq, want, slot, e, cap, full_bit, peers);
           if (!(e & full_bit)) {
 #pragma unroll
-            for (int j = 0; j < 2; j++)
+            for (int j = 0; j < 2 * kCornersPerLane; j++)
               if (want[j]) add_corner(S.vals, hcol, slot[j], q[j], sw, rd.nb, !gtab);
           }
           e = gor<G>(e);  // a full table ends the group's passes together

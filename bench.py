@@ -442,6 +442,20 @@ def main():
     psim.sync(sh)
     p_att = float(psim.tally(0)[:, 0].sum())
     plain_value = p_att / (pe0.elapsed_time(pe1) / 1000.0)
+    psim.close()
+    # the same chain with one move in flight (one warp, no speculative
+    # batching): the kernel run strictly one move after the other
+    ssim = wl.build_sim(wp, warps_per_block=1)
+    ssim.run(20, 5, sh)
+    ssim.sync(sh)
+    ssim.reset_tally()
+    pe0.record(stream)
+    ssim.run(100, 6, sh)
+    pe1.record(stream)
+    torch.cuda.synchronize()
+    ssim.sync(sh)
+    seq_value = float(ssim.tally(0)[:, 0].sum()) / (pe0.elapsed_time(pe1) / 1000.0)
+    ssim.close()
     launches = args.steps * (3 if w.n_rungs else 1)
     mark("plain")
     deriv = derivatives_leg(sim, w, stream) if args.workload == "diff" else None
@@ -480,7 +494,10 @@ def main():
                             "cg_get_chains (into reused host arrays)"},
             "plain": {"value": plain_value, "unit": "moves/s",
                       "workload": "one 10,000-bead chain, 60^3 grid, one binder, 300 MC steps",
-                      "batched_over_plain": value / plain_value},
+                      "batched_over_plain": value / plain_value,
+                      "one_move_in_flight": {"value": seq_value, "unit": "moves/s",
+                                             "workload": "the same chain, one warp, 100 MC steps",
+                                             "batched_over": value / seq_value}},
             "energy_drift": drift,
             "gpu_launches": launches,
             "clocks": clocks.summary(),

@@ -520,8 +520,8 @@ __device__ __forceinline__ bool decide(unsigned x, double dEp, double, double ha
 __device__ __forceinline__ bool decide(unsigned x, const Fx& dEp, const Fx& soft, double hard,
                                        double* dE_out) {
   const long long q = dEp.q + soft.q;
-  if (!is_zero64(dEp.hard)) hard += dEp.hard;
-  if (!is_zero64(soft.hard)) hard += soft.hard;
+  if (!is_zero64(dEp.hard)) hard = add_hard(hard, dEp.hard);
+  if (!is_zero64(soft.hard)) hard = add_hard(hard, soft.hard);
   const bool d = metropolis_fx(x, q, hard);
   if (dE_out) *dE_out = (double)q * kFxEInv + hard;
   return d;

@@ -16,6 +16,7 @@
 // unit trilinear weight); the grid itself is int64 fixed point, so a deposit
 // is exactly undone by the opposite deposit and the grid never depends on the
 // order of updates.
+#include <mutex>
 #include <cuda_runtime.h>
 
 #include "cg_device.cuh"
@@ -758,8 +759,20 @@ void cg_launch_mc(const cg::KArgs& a, bool fp64, bool audit, cudaStream_t s) {
   else cg::launch_mc_t<float>(a, audit, blocks, s);
 }
 
+// Raised only (the attribute is shared by every simulation in the process;
+// see cg_set_spec_smem).
 cudaError_t cg_set_mc_smem(bool fp64, int bytes) {
-  return fp64 ? cg::set_smem_t<double>(bytes) : cg::set_smem_t<float>(bytes);
+  static std::mutex mu;
+  static int cur[64][2];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  int* c = dev >= 0 && dev < 64 ? &cur[dev][fp64 ? 1 : 0] : nullptr;
+  if (c && bytes <= *c) return cudaSuccess;
+  e = fp64 ? cg::set_smem_t<double>(bytes) : cg::set_smem_t<float>(bytes);
+  if (e == cudaSuccess && c) *c = bytes;
+  return e;
 }
 
 void cg_launch_deposit(const cg::KArgs& a, bool fp64, int rep, int n_reps_launch, long long max_beads,

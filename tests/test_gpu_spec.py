@@ -72,3 +72,24 @@ def test_grid_consistent_after_parallel_run(lanes):
     sim.deposit(-1)
     for r in range(w.replicas):
         np.testing.assert_array_equal(sim.density(r), inc[r])
+
+
+def test_smaller_layout_does_not_break_a_live_simulation():
+    """The MC kernel's dynamic shared-memory limit is a per-kernel attribute
+    shared by every simulation in the process: creating a simulation with a
+    smaller CTA layout (one warp) must leave a live one with a larger layout
+    (twelve warps) able to launch."""
+    from chromo_gb300 import workloads as wl
+    w = wl.make_workload("plain")
+    chains = wl.make_chains(w)
+    big = wl.build_sim(w, chains, warps_per_block=12)
+    small = wl.build_sim(w, chains, warps_per_block=1)
+    try:
+        small.run(1, 3)
+        big.run(1, 3)
+        big.sync()
+        small.sync()
+        assert big.tally(0)[:, 0].sum() > 0
+    finally:
+        small.close()
+        big.close()

@@ -158,6 +158,11 @@ class BinderCollection:
             raise ValueError("only orient='records' is supported")
         return [dict(r) for r in self._rows]
 
+    def copy(self):
+        """A copy of the table: new rows, with the nested cross-talk dicts
+        shared, as a pandas deep copy leaves object cells."""
+        return BinderCollection(self._rows)
+
     def equals(self, other):
         return isinstance(other, BinderCollection) and self._rows == other._rows
 

@@ -44,6 +44,10 @@ WORKLOAD_DESCS = {
     "diff": ("batched + differentiation: 64 chains of 5,000 beads, 40^3 grids (40 nm voxels), two "
              "binders, no exchange; dE/dr and dE/d(chi, mu_A, mu_B, eps_AA, eps_BB, eps_AB) kernels "
              "and 1e6 on-device reweighting samples reported under 'derivatives'"),
+    "sphere": ("confined batched: 256 chains of 5,000 beads, each confined to a sphere of radius "
+               "700 nm inside its 1600 nm box with a 40^3 grid of 40 nm voxels (Spherical "
+               "confinement; per-voxel accessible volumes at the surface); two binders; chi ladder "
+               "of 16 rungs in [0.5, 2.0], exchange every 62 MC steps (~1e4 moves per replica)"),
 }
 
 
@@ -53,7 +57,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "large", "diff"],
+    ap.add_argument("--workload", default="batched", choices=["batched", "large", "diff", "sphere"],
                     help="batched: 256 replicas (the headline); large: 32 x 100,000 beads with a "
                          "chi x mu ladder; diff: 64 x 5,000 beads plus the derivative kernels and 1e6 "
                          "reweighting samples")

@@ -66,6 +66,10 @@ struct cg_sim {
   float* bonds32 = nullptr;  // FP32 copy, 8 floats per bead: eb, g, ep, epp, eta, pad
   long long* grid = nullptr;
   double* access_vol = nullptr;
+  // per voxel, from the accessible volume V: the FP32 density scale
+  // 2^-40 / V and V / bead volume (the chi term's factor without chi)
+  float* access_sc = nullptr;
+  double* access_vb = nullptr;
   int *g_keys = nullptr, *g_used = nullptr, *g_bslot = nullptr;
   long long* g_vals = nullptr;
   int g_logH = 0;
@@ -120,7 +124,8 @@ struct cg_sim {
     a.reps = reps; a.ctl = ctl; a.n_ctl = n_ctl; a.n_reps = R; a.tally = tally;
     a.r4 = r4; a.t34 = t34; a.t24 = t24; a.states = states; a.marks = marks; a.bonds = bonds;
     a.bonds32 = bonds32;
-    a.grid = grid; a.access_vol = access_vol; a.ncol = ncol; a.hcol = nb + 1;
+    a.grid = grid; a.access_vol = access_vol; a.access_sc = access_sc; a.access_vb = access_vb;
+    a.ncol = ncol; a.hcol = nb + 1;
     a.g_keys = g_keys; a.g_used = g_used; a.g_bslot = g_bslot; a.g_vals = g_vals; a.g_logH = g_logH;
     a.g_stage = g_stage; a.g_idx = g_idx; a.g_stage_cap = g_stage_cap;
     a.picked = picked; a.picked_off = d_picked_off;
@@ -213,7 +218,7 @@ void cg_destroy(cg_sim* s) {
   if (s->graph) cudaGraphExecDestroy(s->graph);
   if (s->pinned) cudaFreeHost(s->pinned);
   void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
-                  s->bonds32, s->grid, s->access_vol, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
+                  s->bonds32, s->grid, s->access_vol, s->access_sc, s->access_vb, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
                   s->picked, s->d_picked_off, s->eout, s->aout, s->rep_of_rung, s->swaps,
                   s->swap_attempts, s->xround, s->grad, s->terms, s->acc, s->nbound, s->mu_swaps,
                   s->mu_swap_attempts};
@@ -347,6 +352,8 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   ALLOC(s->bonds32, 8 * 4 * s->total_beads);
   ALLOC(s->grid, 8 * s->ncol * s->total_vox);
   if (s->nonuniform) ALLOC(s->access_vol, 8 * s->total_vox);
+  if (s->nonuniform) ALLOC(s->access_sc, 4 * s->total_vox);
+  if (s->nonuniform) ALLOC(s->access_vb, 8 * s->total_vox);
   ALLOC(s->g_keys, 4 * Hg * RW);
   ALLOC(s->g_used, 4 * Hg * RW);
   ALLOC(s->g_bslot, 4 * Hg * RW);
@@ -623,8 +630,20 @@ int cg_set_field(cg_sim* s, int rep, const cg_field_params* f, const double* acc
   for (int b = 0; b < CG_MAX_BINDERS; b++) { d.pref[b] = f->pref[b]; d.intra[b] = f->intra[b]; }
   for (int b = 0; b < CG_MAX_BINDERS * CG_MAX_BINDERS; b++) d.xpref[b] = f->xpref[b];
   d.has_access = access_vol ? 1 : 0;
-  if (access_vol)
-    CUDA_TRY(cudaMemcpy(s->access_vol + s->vox_off[rep], access_vol, 8 * s->n_vox[rep], cudaMemcpyHostToDevice));
+  if (access_vol) {
+    // the factors the MC kernel's FP32 field terms need per voxel, in the
+    // same FP64 arithmetic the kernel would do per touched voxel
+    const long long nv = s->n_vox[rep];
+    std::vector<float> sc(nv);
+    std::vector<double> vb(nv);
+    for (long long v = 0; v < nv; v++) {
+      sc[v] = (float)((1.0 / 1099511627776.0) / access_vol[v]);
+      vb[v] = access_vol[v] / f->bead_vol;
+    }
+    CUDA_TRY(cudaMemcpy(s->access_vol + s->vox_off[rep], access_vol, 8 * nv, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(s->access_sc + s->vox_off[rep], sc.data(), 4 * nv, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(s->access_vb + s->vox_off[rep], vb.data(), 8 * nv, cudaMemcpyHostToDevice));
+  }
   return put_rep(s, rep, &d);
 }
 

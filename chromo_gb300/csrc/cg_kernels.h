@@ -82,6 +82,8 @@ struct KArgs {
   const float* bonds32;       // the same in FP32, 8 floats per bead (16-byte aligned rows)
   long long* grid;            // ncol int64 per voxel
   const double* access_vol;   // per voxel, or null
+  const float* access_sc;     // per voxel: (float)(2^-40 / V), with access_vol
+  const double* access_vb;    // per voxel: V / bead volume, with access_vol
   int ncol;   // grid columns per voxel (2 or 4: rows padded to 16 or 32 bytes)
   int hcol;   // columns of a voxel-hash entry (n_binders + 1)
   // per-replica global scratch for moves too large for shared memory

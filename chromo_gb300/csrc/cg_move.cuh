@@ -366,11 +366,9 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
     load_row(grid + (long long)v * a.ncol, a.ncol, row);
     long long g0 = row[0], d0 = hash_delta(d, split);
     float sc = ws.f_scale, k = ws.f_k;
-    double V = rd.vol_bin;
-    if (rd.has_access) {
-      V = a.access_vol[rd.vox_off + v];
-      sc = (float)(kFxInv / V);
-      k = (float)(rd.chi * (V / rd.bead_vol));
+    if (rd.has_access) {  // per-voxel factors precomputed from V (no FP64 division here)
+      sc = a.access_sc[rd.vox_off + v];
+      k = (float)(rd.chi * a.access_vb[rd.vox_off + v]);
     }
     float c = 0, rho[CG_MAX_BINDERS], dd[CG_MAX_BINDERS];
 #pragma unroll
@@ -392,7 +390,7 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
     float dvf = (float)d0 * sc * ws.f_vb;
     if (vf0 > ws.f_lim - 1e-3f || vf0 + dvf > ws.f_lim - 1e-3f) {
       acc_add(part, c);
-      part.hard += chi_term64(rd, V, g0, d0);
+      part.hard += chi_term64(rd, rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin, g0, d0);
     } else {
       acc_add(part, c + k * (dvf * (2.0f * vf0 + dvf)));
     }

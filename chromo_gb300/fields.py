@@ -53,6 +53,31 @@ class NullField(FieldBase):
         self.confine_length = confine_length
 
 
+def spherical_accessible_volumes(nx, ny, nz, dx, dy, dz, radius, vol_bin, n_side=20):
+    """Per-voxel volume inside a sphere of ``radius`` centred in an nx x ny x
+    nz grid of dx x dy x dz voxels of volume ``vol_bin`` (chromo/fields.pyx:
+    714-951): the full voxel away from the surface, else the voxel volume
+    times the fraction of an n_side^3 point lattice in the voxel that lies
+    inside."""
+    n_bins = nx * ny * nz
+    vols = np.full(n_bins, vol_bin)
+    idx = np.arange(n_bins)
+    ix, iy, iz = idx % nx, (idx // nx) % ny, idx // (nx * ny)
+    nxyz = np.array([nx, ny, nz])
+    cen = np.stack([ix, iy, iz], axis=1) - (nxyz - 1) / 2
+    coords = cen @ np.diag([dx, dy, dz])
+    buffer_dist = np.sqrt(2) / 4 * max(dx, dy, dz)
+    dist = np.sqrt((coords ** 2).sum(axis=1))
+    split = ~((dist < radius - buffer_dist) | (dist > radius + buffer_dist))
+    g = np.reshape(np.mgrid[0:n_side, 0:n_side, 0:n_side].T, (n_side ** 3, 3)).astype(float)
+    g = g * np.array([dx / n_side, dy / n_side, dz / n_side])
+    for i in np.nonzero(split)[0]:
+        pts = g + (coords[i] - np.array([dx / 2, dy / 2, dz / 2]))
+        d = np.linalg.norm(pts, axis=1)
+        vols[i] = vol_bin * (np.count_nonzero(d < radius) / float(len(pts)))
+    return vols
+
+
 class UniformDensityField(FieldBase):
     """Rectilinear voxel grid with trilinear density deposition
     (chromo/fields.pyx:324-2316)."""
@@ -131,24 +156,10 @@ class UniformDensityField(FieldBase):
         """Per-voxel accessible volume (chromo/fields.pyx:714-951): the full
         voxel, or for a spherical confinement the fraction of an n_side^3
         point lattice in each voxel near the boundary that lies inside."""
-        vols = np.full(self.n_bins, self.vol_bin)
         if assume_fully_accessible == 1 or self.confine_type != "Spherical":
-            return vols
-        idx = np.arange(self.n_bins)
-        ix, iy, iz = idx % self.nx, (idx // self.nx) % self.ny, idx // (self.nx * self.ny)
-        nxyz = np.array([self.nx, self.ny, self.nz])
-        cen = np.stack([ix, iy, iz], axis=1) - (nxyz - 1) / 2
-        coords = cen @ np.diag([self.dx, self.dy, self.dz])
-        buffer_dist = np.sqrt(2) / 4 * max(self.dx, self.dy, self.dz)
-        dist = np.sqrt((coords ** 2).sum(axis=1))
-        split = ~((dist < self.confine_length - buffer_dist) | (dist > self.confine_length + buffer_dist))
-        g = np.reshape(np.mgrid[0:n_side, 0:n_side, 0:n_side].T, (n_side ** 3, 3)).astype(float)
-        g = g * np.array([self.dx / n_side, self.dy / n_side, self.dz / n_side])
-        for i in np.nonzero(split)[0]:
-            pts = g + (coords[i] - np.array([self.dx / 2, self.dy / 2, self.dz / 2]))
-            d = np.linalg.norm(pts, axis=1)
-            vols[i] = self.vol_bin * (np.count_nonzero(d < self.confine_length) / float(len(pts)))
-        return vols
+            return np.full(self.n_bins, self.vol_bin)
+        return spherical_accessible_volumes(self.nx, self.ny, self.nz, self.dx, self.dy, self.dz,
+                                            self.confine_length, self.vol_bin, n_side)
 
     @property
     def uniform_access(self):

@@ -17,6 +17,23 @@ def gaussian_walk(rng, n_beads, step=16.5):
     return r
 
 
+def confined_walks(rng, n_chains, n_beads, step, radius):
+    """`n_chains` walks of unit steps times `step` from the origin that stay
+    inside a sphere of `radius`: a step that would leave it is drawn again
+    (the rule of confined_gaussian_walk, chromo/util/poly_paths.py:298-336),
+    all chains advanced together.  Returns [n_chains, n_beads, 3]."""
+    r = np.zeros((n_chains, n_beads, 3))
+    for i in range(1, n_beads):
+        todo = np.arange(n_chains)
+        while len(todo):
+            d = rng.standard_normal((len(todo), 3))
+            p = r[todo, i - 1] + d / np.linalg.norm(d, axis=1)[:, None] * step
+            ok = (p * p).sum(axis=1) <= radius * radius
+            r[todo[ok], i] = p[ok]
+            todo = todo[~ok]
+    return r
+
+
 def tangents_from_coordinates(r):
     n = r.shape[0]
     t3 = np.zeros((n, 3))

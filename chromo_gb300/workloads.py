@@ -12,6 +12,10 @@ Sizes follow the benchmark configurations of this path:
               (the batched + differentiation configuration; no exchange).
 * ``profile`` 256 chains of 5,000 beads: the CTA shape of ``batched`` with
               fixed lengths, a bounded case for profilers.
+* ``sphere``  256 chains of 5,000 beads, each confined to a sphere of radius
+              700 nm inside its 40^3 grid (Spherical confinement, per-voxel
+              accessible volumes at the surface), binders and chi ladder as
+              ``batched``.
 * ``large``   32 chains of 100,000 beads, 100^3 grids, chi ladder of 8 rungs
               times a sweep of 4 mu_A values (one grid of 4 x 8 parameter slots:
               chi exchanged along rows, mu_A along columns).
@@ -77,6 +81,7 @@ class Workload:
     seed: int
     steps_per_round: int = 62    # ~1e4 attempted moves per replica per exchange round
     mu_rungs: int = 0            # > 1: grids of mu_rungs x n_rungs, mu_A exchanged along mu rungs
+    sphere_radius: float = 0.0   # > 0: Spherical confinement with accessible volumes
     replicas: int = field(init=False)
 
     def __post_init__(self):
@@ -114,6 +119,13 @@ def make_workload(name: str, seed_offset: int = 0) -> Workload:
         chi = np.tile(np.linspace(0.5, 2.0, 16), R // 16)
         return Workload("profile", np.full(R, 5000), 40, 2, mu, chi, [-4.0, -3.0],
                         [{"PRC1": 1.0}, {}], 50, 16, BASE_SEED + 3 + seed_offset)
+    if name == "sphere":
+        R = 256
+        mu = rng.uniform(-1.0, 0.0, size=(R, 2))
+        chi = np.tile(np.linspace(0.5, 2.0, 16), R // 16)
+        return Workload("sphere", np.full(R, 5000), 40, 2, mu, chi, [-4.0, -3.0],
+                        [{"PRC1": 1.0}, {}], 50, 16, BASE_SEED + 5 + seed_offset,
+                        sphere_radius=700.0)
     if name == "large":
         R, rungs = 32, 8
         mu_a = np.repeat([-1.0, -2.0 / 3.0, -1.0 / 3.0, 0.0], rungs)
@@ -136,9 +148,12 @@ class ChainState:
 def make_chains(w: Workload) -> List[ChainState]:
     rng = np.random.default_rng(w.seed)
     out = []
-    for n in w.lengths:
+    walks = None
+    if w.sphere_radius > 0:  # equal lengths: all chains walked together
+        walks = syn.confined_walks(rng, w.replicas, int(w.lengths[0]), BEAD_SPACING, w.sphere_radius)
+    for j, n in enumerate(w.lengths):
         n = int(n)
-        r = syn.gaussian_walk(rng, n, BEAD_SPACING)
+        r = walks[j] if walks is not None else syn.gaussian_walk(rng, n, BEAD_SPACING)
         t3, t2 = syn.tangents_from_coordinates(r)
         marks = np.stack([syn.markov_marks(rng, n, w.run_length) for _ in range(w.n_binders)], 1)
         out.append(ChainState(r, t3, t2, np.zeros((n, w.n_binders), np.int64), marks))
@@ -152,10 +167,16 @@ def binder_names(nb):
 def build_sim(w: Workload, chains=None, pos_fp64=False, warps_per_block=0, lanes_per_move=0) -> nat.Sim:
     chains = chains if chains is not None else make_chains(w)
     R, nb = w.replicas, w.n_binders
+    confined = w.sphere_radius > 0
     sim = nat.Sim(w.lengths, [[w.nbins] * 3] * R, nb, pos_fp64=pos_fp64, max_segment=152,
                   max_tangent=int(max(w.lengths)), warps_per_block=warps_per_block,
-                  lanes_per_move=lanes_per_move)
+                  lanes_per_move=lanes_per_move, nonuniform_access=confined)
     width = w.nbins * VOXEL
+    access = None
+    if confined:
+        from .fields import spherical_accessible_volumes
+        access = spherical_accessible_volumes(w.nbins, w.nbins, w.nbins, VOXEL, VOXEL, VOXEL,
+                                              w.sphere_radius, width ** 3 / w.nbins ** 3)
     vint = 4.0 / 3.0 * np.pi * R_INT ** 3
     pref, intra, xpref = field_prefactors(w.eps, [vint] * nb, w.cross, binder_names(nb), VOXEL ** 3)
     bead_vol = 4.0 / 3.0 * np.pi * BEAD_RAD ** 3
@@ -167,7 +188,10 @@ def build_sim(w: Workload, chains=None, pos_fp64=False, warps_per_block=0, lanes
                       bonds=bonds_array(eb, g, ep, epp, eta))
         sim.set_field(rep, field_params(field_kind=2, nxyz=(w.nbins,) * 3, widths=(width,) * 3,
                                         n_binders=nb, chi=float(w.chi[rep]), vf_limit=0.5,
-                                        bead_vol=bead_vol, pref=pref, intra=intra, xpref=xpref))
+                                        bead_vol=bead_vol, pref=pref, intra=intra, xpref=xpref,
+                                        confine_kind=1 if confined else 0,
+                                        confine_length=w.sphere_radius),
+                      access_vol=access)
         sim.set_binding(rep, binding_params(sites=[SITES] * nb, e_mod=[HP1_E_MOD] * nb,
                                             e_nomod=[HP1_E_NOMOD] * nb, mu=list(w.mu[rep]),
                                             mu_adjust_factor=1.0))

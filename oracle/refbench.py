@@ -78,8 +78,12 @@ def _build_reference_replica(w, rep, chain):
                   binder_names=np.array(names), chemical_mods=chain.marks.copy(),
                   chemical_mod_names=np.array([f"m{b}" for b in range(len(names))]))
     width = w.nbins * VOXEL
+    confine = {}
+    if getattr(w, "sphere_radius", 0) > 0:  # spherical confinement with accessible volumes
+        confine = dict(confine_type="Spherical", confine_length=float(w.sphere_radius),
+                       assume_fully_accessible=0)
     f = UniformDensityField([p], binders, width, w.nbins, width, w.nbins, width, w.nbins,
-                            chi=float(w.chi[rep]))
+                            chi=float(w.chi[rep]), **confine)
     bab, mab = cmc.get_amplitude_bounds([p])
     ctrls = all_moves("/tmp/chromo_refbench_logs", bab.bounds, mab.bounds, SimpleControl)
     return p, binders, f, ctrls

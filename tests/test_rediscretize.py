@@ -138,7 +138,7 @@ def test_refinement_re_equilibrates_binding_on_the_gpu(g):
     """Binding re-equilibration of the refined chain runs binding moves through
     mc_sim on the GPU: states stay within 0..sites, some beads get bound (the
     binders' chemical potential favours binding on marked beads), and the
-    positions are untouched."""
+    positions are untouched (up to their FP32 storage on the device)."""
     p, binders = _chromatin(g)
     pcg = rd.get_cg_chromatin(p, 6, name_cg="cg")
     udf = UniformDensityField([p], binders, 800.0, 20, 800.0, 20, 800.0, 20, chi=1.0)
@@ -149,7 +149,7 @@ def test_refinement_re_equilibrates_binding_on_the_gpu(g):
     np.random.seed(21)
     ref1, _ = quiet(rd.refine_chromatin, pcg, 64, 16.5, mods, ucg, binding_equilibration=400,
                     random_seed=3)
-    np.testing.assert_array_equal(ref1.r, ref0.r)
+    np.testing.assert_array_equal(ref1.r, ref0.r.astype(np.float32))
     sites = [cb.get_by_name(nm).sites_per_bead for nm in ("HP1", "PRC1")]
     assert np.all(ref1.states >= 0) and np.all(ref1.states <= np.array(sites))
     assert ref1.states.sum() > 0

@@ -138,54 +138,6 @@ __device__ __forceinline__ void deposit_bead(const RepDev& rd, int ncol, int* ke
   }
 }
 
-// Add the signed fixed-point contributions q[l] (bead weight; times the packed
-// binder states `st` for the binder columns) to the eight voxels v[l] of a
-// move's voxel table; contributions of zero claim nothing.  The home-slot
-// claims are issued back to back; only a claim that meets another key probes
-// on.  A table that cannot take a new voxel, or whose count of voxels passes
-// `cap`, sets `full_bit` in err (E_OVF for an optimistic shared table, after
-// which the caller starts the move again in its global table; E_SPIN where
-// the table was sized for the worst case).
-__device__ __forceinline__ void claim_add8(const RepDev& rd, int hcol, int* keys, int* used, int* nused,
-                                           long long* vals, int logH, const int v[8], const long long q[8],
-                                           unsigned st, unsigned& err, bool split, int cap,
-                                           unsigned full_bit) {
-  int slot[8], prev[8];
-#pragma unroll
-  for (int l = 0; l < 8; l++) {
-    slot[l] = (int)(((unsigned)v[l] * 0x9E3779B1u) >> (32 - logH));
-    prev[l] = q[l] != 0 ? atomicCAS(&keys[slot[l]], -1, v[l]) : v[l];
-  }
-  unsigned fresh = 0;
-#pragma unroll
-  for (int l = 0; l < 8; l++) {
-    if (prev[l] == -1) {
-      fresh |= 1u << l;
-    } else if (prev[l] != v[l]) {
-      bool inserted = false;
-      unsigned e = 0;
-      slot[l] = hash_probe(keys, logH, v[l], slot[l], inserted, e);
-      if (slot[l] < 0) { err |= full_bit; break; }
-      if (inserted) fresh |= 1u << l;
-    }
-  }
-  if (fresh) {
-    int at = atomicAdd(nused, __popc(fresh));
-#pragma unroll
-    for (int l = 0; l < 8; l++)
-      if ((fresh >> l) & 1u) used[at++] = slot[l];
-    if (at > cap) err |= full_bit;
-  }
-  if (err & full_bit) return;
-#pragma unroll
-  for (int l = 0; l < 8; l++) {
-    if (q[l] == 0) continue;
-    add_delta(vals, hcol, slot[l], 0, q[l], split);
-    for (int b = 0; b < rd.nb; b++)
-      add_delta(vals, hcol, slot[l], 1 + b, q[l] * (long long)((st >> (8 * b)) & 0xFF), split);
-  }
-}
-
 // Claim (or find) the slots of up to NQ voxels per lane (v[j] where
 // want[j]) in a table shared by the lanes `peers` (this lane's bit set); the
 // peers append their new slots to the used list with one counter update.
@@ -252,29 +204,6 @@ __device__ __forceinline__ void add_corner(long long* vals, int hcol, int slot, 
                                            bool split) {
   add_delta(vals, hcol, slot, 0, q, split);
   for (int b = 0; b < nb; b++) add_delta(vals, hcol, slot, 1 + b, q * (long long)((sw >> (8 * b)) & 0xFF), split);
-}
-
-// Remove one bead's old trilinear weights (w0 at voxels v0) and add its new
-// ones (w1 at v1).  When both lie in the same eight voxels (the same lower
-// corner) each voxel gets one contribution q(w1) - q(w0) and the second set
-// is empty: fewer claims and atomics than two separate deposits, the same
-// integer sums.  Both sets go through the same two calls whatever the case,
-// so lanes of a warp do not diverge on it.
-template <typename Real>
-__device__ __forceinline__ void deposit_pair(const RepDev& rd, int hcol, int* keys, int* used, int* nused,
-                                             long long* vals, int logH, const Real w0[8], const int v0[8],
-                                             const Real w1[8], const int v1[8], unsigned st, unsigned& err,
-                                             bool split, int cap, unsigned full_bit) {
-  const bool same = v0[0] == v1[0];
-  long long qa[8], qb[8];
-#pragma unroll
-  for (int l = 0; l < 8; l++) {
-    const long long q0 = q40(w0[l]), q1 = q40(w1[l]);
-    qa[l] = same ? q1 - q0 : -q0;
-    qb[l] = same ? 0 : q1;
-  }
-  claim_add8(rd, hcol, keys, used, nused, vals, logH, v0, qa, st, err, split, cap, full_bit);
-  claim_add8(rd, hcol, keys, used, nused, vals, logH, v1, qb, st, err, split, cap, full_bit);
 }
 
 // One voxel's grid row -- bead weight, then one column per binder -- with

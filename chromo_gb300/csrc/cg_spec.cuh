@@ -650,8 +650,9 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     int* idx = S.idx;
     Acc part = acc_zero<Acc>();
     int dbl = 0;
-    // eight lanes per bead as for the position moves: corner lane 0 takes the
-    // binding free energy, each lane the change of its corner's binder column
+    // eight lanes per bead, one trilinear corner each: corner lane 0 takes
+    // the binding free energy, each lane the change of its corner's binder
+    // column
     constexpr int BP = G / 8;
     const int kc = gl >> 3, cl = gl & 7;
     for (long long kb = 0; __any_sync(kFull, kb < m); kb += BP) {

@@ -112,7 +112,7 @@ def _tune_child(workload, rank, local):
     chains = wl.make_chains(w)
     autotune.tune(lambda W, G: wl.build_sim(w, chains, warps_per_block=W, lanes_per_move=G),
                   w.lengths, [[w.nbins] * 3] * w.replicas, w.n_binders, steps=TUNE_STEPS,
-                  warmup=TUNE_WARMUP)
+                  warmup=TUNE_WARMUP, extra_key=workload)
 
 
 def derivatives_leg(sim, w, stream):
@@ -316,9 +316,12 @@ def main():
     child = mp.get_context("spawn").Process(target=_tune_child, args=(args.workload, rank, local))
     child.start()
     child.join()
+    if child.exitcode != 0:
+        print(f"autotune child exited with {child.exitcode}; tuning in this process", file=sys.stderr)
     shape, tune_table = autotune.tune(
         lambda W, G: wl.build_sim(w, chains, warps_per_block=W, lanes_per_move=G),
-        w.lengths, [[w.nbins] * 3] * w.replicas, w.n_binders, steps=TUNE_STEPS, warmup=TUNE_WARMUP)
+        w.lengths, [[w.nbins] * 3] * w.replicas, w.n_binders, steps=TUNE_STEPS, warmup=TUNE_WARMUP,
+        extra_key=args.workload)
     mark("autotune")
     sim = wl.build_sim(w, chains, warps_per_block=shape[0], lanes_per_move=shape[1])
     if w.mu_rungs:

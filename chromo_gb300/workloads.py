@@ -25,6 +25,7 @@ replica runs all five moves under SimpleControl with the reference's
 amplitude bounds and cycle counts (chromo/mc/__init__.py:295-332,
 chromo/mc/mc_controller.py:216-266).
 """
+import functools
 from dataclasses import dataclass, field
 from typing import List
 
@@ -160,6 +161,18 @@ def make_chains(w: Workload) -> List[ChainState]:
     return out
 
 
+@functools.lru_cache(maxsize=4)
+def _sphere_volumes(nbins, radius):
+    """Accessible volumes of a sphere of `radius` centred in an nbins^3 grid of
+    VOXEL-sized voxels (computed once per grid; every replica shares them)."""
+    from .fields import spherical_accessible_volumes
+    width = nbins * VOXEL
+    v = spherical_accessible_volumes(nbins, nbins, nbins, VOXEL, VOXEL, VOXEL, radius,
+                                     width ** 3 / nbins ** 3)
+    v.setflags(write=False)
+    return v
+
+
 def binder_names(nb):
     return ["HP1", "PRC1", "B3"][:nb]
 
@@ -172,11 +185,7 @@ def build_sim(w: Workload, chains=None, pos_fp64=False, warps_per_block=0, lanes
                   max_tangent=int(max(w.lengths)), warps_per_block=warps_per_block,
                   lanes_per_move=lanes_per_move, nonuniform_access=confined)
     width = w.nbins * VOXEL
-    access = None
-    if confined:
-        from .fields import spherical_accessible_volumes
-        access = spherical_accessible_volumes(w.nbins, w.nbins, w.nbins, VOXEL, VOXEL, VOXEL,
-                                              w.sphere_radius, width ** 3 / w.nbins ** 3)
+    access = _sphere_volumes(w.nbins, w.sphere_radius) if confined else None
     vint = 4.0 / 3.0 * np.pi * R_INT ** 3
     pref, intra, xpref = field_prefactors(w.eps, [vint] * nb, w.cross, binder_names(nb), VOXEL ** 3)
     bead_vol = 4.0 / 3.0 * np.pi * BEAD_RAD ** 3

@@ -11,7 +11,7 @@ from typing import Dict, List, Optional, Tuple
 import numpy as np
 
 from .mc_controller import Controller, SimpleControl, all_moves
-from .mc_sim import mc_sim, mc_sim_audit, set_position_precision
+from .mc_sim import mc_sim, mc_sim_audit, mc_step, set_position_precision
 from .moves import Bounds
 
 

@@ -17,6 +17,8 @@ One polymer per call: the reference's field supports one polymer in
 practice (chromo/fields.pyx:53-54); for many independent chains use
 ``chromo_gb300.batched.ReplicaBatch``.
 """
+import itertools
+
 import numpy as np
 
 from .. import _native as nat
@@ -177,6 +179,38 @@ def mc_sim(polymers, readerproteins, num_mc_steps, mc_move_controllers, field,
         _pull(sim, poly, field, ctrls)
     finally:
         sim.close()
+
+
+_STEP_SEEDS = itertools.count(0x5EED000000000000)
+
+
+def mc_step(adaptible_move, poly, readerproteins, field, active_field=1, update_distances=0,
+            random_seed=None):
+    """One attempted move of ``adaptible_move`` on ``poly`` (chromo/mc/mc_sim.pyx:106-182):
+    proposal at the move's current amplitudes, polymer dE plus the field dE when
+    ``active_field`` is set and ``poly`` is in ``field`` (not for tangent rotations),
+    Metropolis decision and commit, on the GPU; the move's attempt and success counters and
+    acceptance tracker are updated, its amplitudes are not (that is ``mc_sim``'s
+    controller step).
+
+    ``update_distances`` only concerns polymers that track pairwise distances (the steric
+    chromatin model, not on this path) and must be 0.  The random stream is Philox keyed by
+    ``random_seed``; by default each call takes the next seed of a per-process sequence,
+    so that successive calls draw fresh streams (the reference draws from libc ``rand()``).
+    """
+    if update_distances:
+        raise NotImplementedError("pairwise-distance updates (steric chromatin) are not on this path")
+    from .mc_controller import NoControl
+    amp_bead, amp_move = int(adaptible_move.amp_bead), float(adaptible_move.amp_move)
+    ctrl = NoControl(adaptible_move, (amp_bead, amp_bead), (amp_move, amp_move))
+    seed = next(_STEP_SEEDS) if random_seed is None else int(random_seed)
+    saved = adaptible_move.num_per_cycle
+    adaptible_move.num_per_cycle = 1
+    try:
+        mc_sim([poly], readerproteins, 1, [ctrl], field if active_field else None,
+               float(getattr(poly, "mu_adjust_factor", 1.0)), seed)
+    finally:
+        adaptible_move.num_per_cycle = saved
 
 
 def mc_sim_audit(polymers, readerproteins, num_mc_steps, mc_move_controllers, field,

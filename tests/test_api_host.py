@@ -114,3 +114,37 @@ def test_null_field_membership():
     assert Chromatin.straight_line_in_x("q", np.full(9, 16.5), binder_names=np.array(["HP1"])) not in f
     with pytest.raises(ValueError):
         NullField([p], confine_type="Tetrahedral")
+
+
+def test_mc_step_runs_one_move_at_current_amplitudes(monkeypatch):
+    """mc_step (chromo/mc/mc_sim.pyx:106-182) hands mc_sim one step of one
+    uncontrolled move at the adapter's current amplitudes, drops the field
+    when it is not active, restores num_per_cycle, and draws a fresh random
+    stream on every call unless given a seed (the GPU run itself is mc_sim's)."""
+    import importlib
+    ms = importlib.import_module("chromo_gb300.mc.mc_sim")  # the package re-exports the function
+    p = Chromatin.straight_line_in_x("p", np.full(99, 16.5), binder_names=np.array(["HP1"]))
+    binders = cb.make_binder_collection([cb.get_by_name("HP1")])
+    field = UniformDensityField([p], binders, 400, 10, 400, 10, 400, 10)
+    bab, mab = get_amplitude_bounds([p])
+    move = all_moves("/tmp", bab.bounds, mab.bounds, SimpleControl)[2].move  # slide
+    move.amp_bead, move.amp_move = 7, 2.5
+    calls = []
+
+    def fake_mc_sim(polymers, readerproteins, n_steps, ctrls, fld, maf, seed):
+        (c,) = ctrls
+        calls.append(dict(polys=list(polymers), n=n_steps, kind=c.kind, bead=c.bead_amp_bounds,
+                          amp=c.move_amp_bounds, npc=c.move.num_per_cycle, field=fld, seed=seed))
+
+    monkeypatch.setattr(ms, "mc_sim", fake_mc_sim)
+    ms.mc_step(move, p, binders, field, 1, 0)
+    ms.mc_step(move, p, binders, field, 0, 0)
+    ms.mc_step(move, p, binders, field, 1, 0, random_seed=42)
+    assert [c["n"] for c in calls] == [1, 1, 1] and all(c["polys"] == [p] for c in calls)
+    assert all(c["kind"] == 0 and c["npc"] == 1 for c in calls)
+    assert calls[0]["bead"] == (7, 7) and calls[0]["amp"] == (2.5, 2.5)
+    assert calls[0]["field"] is field and calls[1]["field"] is None
+    assert calls[0]["seed"] != calls[1]["seed"] and calls[2]["seed"] == 42
+    assert move.num_per_cycle == 60
+    with pytest.raises(NotImplementedError):
+        ms.mc_step(move, p, binders, field, 1, 1)

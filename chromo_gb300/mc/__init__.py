@@ -36,18 +36,21 @@ def get_amplitude_bounds(polymers) -> Tuple[Bounds, Bounds]:
 
 def polymer_in_field(polymers, binders, field, num_save_mc, num_saves, bead_amp_bounds,
                      move_amp_bounds, mc_move_controllers: Optional[List[Controller]] = None,
-                     random_seed: Optional[int] = 0, mu_schedule=None, output_dir=None, **kwargs):
+                     random_seed: Optional[int] = 0, mu_schedule=None, output_dir=None,
+                     start_index: int = 0, **kwargs):
     """Run ``num_saves`` rounds of ``num_save_mc`` MC steps, keeping a snapshot of
     every polymer after each round (chromo/mc/__init__.py:36-161).  With an
     ``output_dir`` each snapshot is also written as ``<name>-<i>.csv`` in the
-    reference's polymer CSV format (``PolymerBase.to_csv``)."""
+    reference's polymer CSV format (``PolymerBase.to_csv``), i counting from
+    ``start_index`` (a resumed run continues the numbering)."""
     np.random.seed(random_seed)
     if mc_move_controllers is None:
         mc_move_controllers = all_moves(str(output_dir or "."), bead_amp_bounds.bounds,
                                         move_amp_bounds.bounds, SimpleControl)
     snapshots = []
-    for mc_count in range(num_saves):
-        mu_adjust_factor = mu_schedule.function(mc_count, num_saves) if mu_schedule is not None else 1
+    for mc_count in range(start_index, start_index + num_saves):
+        mu_adjust_factor = (mu_schedule.function(mc_count - start_index, num_saves)
+                            if mu_schedule is not None else 1)
         inner_seed = np.random.randint(0, 1E9)
         mc_sim(polymers, binders, num_save_mc, mc_move_controllers, field, mu_adjust_factor,
                inner_seed)
@@ -58,3 +61,43 @@ def polymer_in_field(polymers, binders, field, num_save_mc, num_saves, bead_amp_
             for p in polymers:
                 p.to_csv(str(Path(output_dir) / f"{p.name}-{mc_count}.csv"))
     return snapshots
+
+
+def latest_snapshots(output_dir) -> Dict[str, Tuple[int, Path]]:
+    """The latest ``<name>-<i>.csv`` snapshot of every polymer in ``output_dir``:
+    {name: (i, path)} (the role of get_latest_configuration and
+    find_polymers_in_output_dir, chromo/util/poly_stat.py:184-259, for the flat
+    layout ``polymer_in_field`` writes)."""
+    out: Dict[str, Tuple[int, Path]] = {}
+    for path in Path(output_dir).glob("*-*.csv"):
+        name, _, idx = path.stem.rpartition("-")
+        if not name or not idx.isdigit():
+            continue
+        i = int(idx)
+        if name not in out or i > out[name][0]:
+            out[name] = (i, path)
+    return out
+
+
+def continue_polymer_in_field_simulation(polymer_class, binders, field, output_dir, num_save_mc,
+                                         num_saves, mc_move_controllers: Optional[List[Controller]] = None,
+                                         random_seed: Optional[int] = 0):
+    """Continue a ``polymer_in_field`` run from the latest snapshot of each
+    polymer in ``output_dir`` (chromo/mc/__init__.py:167-227): the polymers are
+    read back with ``polymer_class.from_file``, placed in ``field``, and run for
+    ``num_saves`` more snapshots, numbered after the latest.  Returns the new
+    snapshots, as ``polymer_in_field``."""
+    latest = latest_snapshots(output_dir)
+    if not latest:
+        raise FileNotFoundError(f"no <name>-<i>.csv snapshot in {output_dir}")
+    names = sorted(latest)
+    polymers = [polymer_class.from_file(str(latest[n][1]), n) for n in names]
+    field.polymers = polymers
+    field.n_polymers = len(polymers)
+    if hasattr(field, "_density_fx"):
+        field._density_fx = None  # the density of the loaded polymers is deposited anew
+    bead_amp_bounds, move_amp_bounds = get_amplitude_bounds(polymers)
+    return polymer_in_field(polymers, binders, field, num_save_mc, num_saves, bead_amp_bounds,
+                            move_amp_bounds, mc_move_controllers, random_seed=random_seed,
+                            output_dir=output_dir,
+                            start_index=max(latest[n][0] for n in names) + 1)

@@ -148,3 +148,37 @@ def test_mc_step_runs_one_move_at_current_amplitudes(monkeypatch):
     assert move.num_per_cycle == 60
     with pytest.raises(NotImplementedError):
         ms.mc_step(move, p, binders, field, 1, 1)
+
+
+def test_continue_polymer_in_field_from_latest_snapshot(monkeypatch, tmp_path):
+    """continue_polymer_in_field_simulation (chromo/mc/__init__.py:167-227)
+    reads each polymer's latest <name>-<i>.csv, puts it in the field, and
+    continues the snapshot numbering (the MC steps are mc_sim's, faked here)."""
+    import chromo_gb300.mc as mc
+    binders = cb.make_binder_collection([cb.get_by_name("HP1")])
+    p = Chromatin.straight_line_in_x("chr", np.full(49, 16.5), binder_names=np.array(["HP1"]))
+    p.to_csv(str(tmp_path / "chr-0.csv"))
+    p.r[:, 1] += 3.0
+    p.states[::2, 0] = 1
+    p.to_csv(str(tmp_path / "chr-1.csv"))
+    (tmp_path / "notes-x.csv").write_text("not a snapshot")
+    field = UniformDensityField([p], binders, 400, 10, 400, 10, 400, 10)
+    seen = []
+
+    def fake_mc_sim(polymers, readerproteins, n_steps, ctrls, fld, maf, seed):
+        (q,) = polymers
+        seen.append((q.r.copy(), q.states.copy(), fld is field and q in fld, n_steps))
+        q.r[:, 2] += 1.0
+
+    monkeypatch.setattr(mc, "mc_sim", fake_mc_sim)
+    assert {k: v[0] for k, v in mc.latest_snapshots(tmp_path).items()} == {"chr": 1}
+    snaps = mc.continue_polymer_in_field_simulation(Chromatin, binders, field, str(tmp_path), 5, 2)
+    assert len(snaps) == 2 and len(seen) == 2
+    np.testing.assert_array_equal(seen[0][0], p.r)
+    np.testing.assert_array_equal(seen[0][1], p.states)
+    assert seen[0][2] and seen[0][3] == 5
+    assert (tmp_path / "chr-2.csv").exists() and (tmp_path / "chr-3.csv").exists()
+    q = Chromatin.from_file(str(tmp_path / "chr-3.csv"), "chr")
+    np.testing.assert_allclose(q.r[:, 2], p.r[:, 2] + 2.0)
+    with pytest.raises(FileNotFoundError):
+        mc.continue_polymer_in_field_simulation(Chromatin, binders, field, str(tmp_path / "none"), 5, 1)

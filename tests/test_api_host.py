@@ -182,3 +182,22 @@ def test_continue_polymer_in_field_from_latest_snapshot(monkeypatch, tmp_path):
     np.testing.assert_allclose(q.r[:, 2], p.r[:, 2] + 2.0)
     with pytest.raises(FileNotFoundError):
         mc.continue_polymer_in_field_simulation(Chromatin, binders, field, str(tmp_path / "none"), 5, 1)
+
+
+def test_confined_workload_chains_and_volumes():
+    """The confined benchmark workload: every bead starts inside its sphere,
+    and the accessible volumes it uploads are those UniformDensityField
+    computes for the same grid and confinement (chromo/fields.pyx:714-951)."""
+    from chromo_gb300 import workloads as wl
+    w = wl.make_workload("sphere")
+    chains = wl.make_chains(w)
+    assert len(chains) == w.replicas == 256
+    assert max(np.linalg.norm(c.r, axis=1).max() for c in chains[:16]) <= w.sphere_radius
+    p = Chromatin("p", chains[0].r, bead_length=np.full(len(chains[0].r) - 1, wl.BEAD_SPACING),
+                  binder_names=np.array(["HP1"]))
+    width = w.nbins * wl.VOXEL
+    f = UniformDensityField([p], cb.make_binder_collection([cb.get_by_name("HP1")]), width, w.nbins,
+                            width, w.nbins, width, w.nbins, confine_type="Spherical",
+                            confine_length=w.sphere_radius, assume_fully_accessible=0)
+    np.testing.assert_array_equal(wl._sphere_volumes(w.nbins, w.sphere_radius), f.access_vols)
+    assert f.access_vols.min() > 0

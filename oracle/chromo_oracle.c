@@ -1232,6 +1232,27 @@ int64_t or_mc_sim(or_system *s, or_ctl *ctl, int64_t n_ctl, int64_t n_steps,
 }
 
 /* size helpers for the ctypes wrapper */
+/* Known-answer hooks (test infrastructure): the rotation about axis a through
+ * p (arbitrary_axis_rotation, linalg.pyx:62-143) in the reference's
+ * arithmetic, as the 3 x 4 matrix [R | T] row by row, and the transform of
+ * bead i of s by such a matrix (transform_r_t3_t2, move_funcs.pyx:121-154):
+ * out = r', t3', t2'. */
+void or_kat_axis_rotation(const double a[3], const double p[3], double ang, double out[12])
+{
+    double M[3][4];
+    axis_rotation(a, p, ang, M, 1);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 4; j++) out[4 * i + j] = M[i][j];
+}
+
+void or_kat_transform(const or_system *s, int64_t i, const double M12[12], double out[9])
+{
+    double M[3][4];
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 4; b++) M[a][b] = M12[4 * a + b];
+    transform_bead(s, i, M, out);
+}
+
 int64_t or_sizeof_system(void) { return (int64_t)sizeof(or_system); }
 int64_t or_sizeof_ctl(void) { return (int64_t)sizeof(or_ctl); }
 int64_t or_sizeof_record(void) { return (int64_t)sizeof(or_record); }

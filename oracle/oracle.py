@@ -90,6 +90,8 @@ def lib(tag: str):
         L.or_mc_sim.argtypes = [C.POINTER(_System), C.POINTER(Ctl), _I, _I,
                                 _P, _I, C.POINTER(_I), _P, _I, C.POINTER(_I), _P, _I]
         L.or_mc_sim.restype = _I
+        L.or_kat_axis_rotation.argtypes = [_P, _P, C.c_double, _P]
+        L.or_kat_transform.argtypes = [C.POINTER(_System), _I, _P, _P]
         assert L.or_sizeof_system() == C.sizeof(_System)
         assert L.or_sizeof_ctl() == C.sizeof(Ctl)
         assert L.or_sizeof_record() == RECORD_DTYPE.itemsize
@@ -202,6 +204,13 @@ class OracleSystem:
         s = C.byref(self._s)
         return (self._L.or_elastic_E(s), self._L.or_binding_E(s), self._L.or_field_E(s))
 
+    def transform(self, i, M):
+        """Bead i moved by the 3 x 4 matrix M (transform_r_t3_t2): (r', t3', t2')."""
+        M = np.ascontiguousarray(M, dtype=np.float64).reshape(12)
+        out = np.zeros(9)
+        self._L.or_kat_transform(C.byref(self._s), int(i), M.ctypes.data, out.ctypes.data)
+        return out[:3], out[3:6], out[6:]
+
     def mc_sim(self, ctls, n_steps, draws, bstates, max_records=None):
         """Run ``mc_sim`` (chromo/mc/mc_sim.pyx:26-103); returns the per-move records."""
         arr = (Ctl * len(ctls))(*ctls)
@@ -239,3 +248,13 @@ def make_ctl(move_name, *, amp_move, amp_bead, num_per_cycle=1, simple=True,
     c.move_lo, c.move_hi = move_bounds
     c.acc_rate, c.alpha = 0.0, 2 / (moves_in_average + 1)
     return c
+
+
+def axis_rotation(axis, point, angle, tag="f64"):
+    """The 3 x 4 rotation matrix [R | T] about `axis` through `point`
+    (arbitrary_axis_rotation, chromo/util/linalg.pyx:62-143), from the oracle."""
+    a = np.ascontiguousarray(axis, dtype=np.float64)
+    p = np.ascontiguousarray(point, dtype=np.float64)
+    out = np.zeros(12)
+    lib(tag).or_kat_axis_rotation(a.ctypes.data, p.ctypes.data, float(angle), out.ctypes.data)
+    return out.reshape(3, 4)

@@ -405,10 +405,10 @@ def main():
     # ---- e2e through the C ABI with host buffers
     h2d = d2h = 0
     pos_b = 16
-    # A host-driven loop: every round uploads its input chains from host
+    # A host-driven loop: every step uploads its input chains from host
     # memory (all replicas: positions, tangents, binding states), rebuilds the
     # densities, runs one exchange round and reads the resulting chains back;
-    # the next round's input is that snapshot.  The first round is untimed.
+    # the next step's input is that snapshot.  The first step is untimed.
     e2e_steps = max(2, min(args.steps, 5))
     t_e2e = 0.0
     # start from the state the timed rounds started from (the chains are

@@ -5,13 +5,21 @@ One "step" is one replica-exchange round of the batched workload: every
 replica (256 chains, 2,000-20,000 beads, own 40^3 grid, two binders) runs 62
 MC steps of all five moves (~1e4 attempted moves per replica), then chi is
 exchanged along 16-rung ladders.  The round is a captured CUDA graph replayed
-K times.  ``value`` is whole-job attempted moves/s with the state resident in
-HBM; ``e2e`` is the same through the C ABI with host buffers (state uploaded
-from pinned memory and the snapshot read back every step); ``plain`` is one
-10,000-bead chain on the same kernel (one CTA); ``roofline`` reports the MC
-kernel's algorithmic bytes per launch over its CUDA-event duration against
-the measured HBM peak; ``cpu_baseline`` is the reference's own CPU code on
-this host's cores.
+K times.  Before the W warm-up rounds, SETTLE_ROUNDS rounds bring the move
+controllers to steady state (SimpleControl widens the segments for thousands
+of MC steps; the bead amplitudes of crank shaft, end pivot and slide reach
+their bounds), so every leg measures the steady state.
+
+``value`` is whole-job attempted moves/s over the K timed rounds with the
+state resident in HBM; ``roofline`` is the MC kernel of those same rounds
+(CUDA event-record nodes inside the replayed graph: algorithmic bytes per
+launch over its device duration, against the measured HBM peak); ``e2e`` is
+the same K rounds from the same start state through the C ABI with host
+buffers (state uploaded from pinned memory and the snapshot read back every
+step); ``plain`` is one 10,000-bead chain on the same kernel (one CTA),
+settled the same way; ``cpu_baseline`` is the reference's own CPU code on
+this host's cores, started from a state settled for the same number of MC
+steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
@@ -99,20 +107,61 @@ def profile_case(args):
                       "algorithmic_bytes": wl.algorithmic_bytes(tal, w.n_binders)}), flush=True)
 
 
-TUNE_WARMUP, TUNE_STEPS = 186, 62  # the timed region's state: three rounds of warm-up, one timed
+# Exchange rounds (62 MC steps each) run before the warm-up rounds: after
+# 4,960 MC steps the bead amplitudes of crank shaft, end pivot and slide sit at
+# their bounds (150 beads) and the per-round cost has stopped growing.
+SETTLE_ROUNDS = 80
+TUNE_WARMUP, TUNE_STEPS = 62, 124  # from the settled state: one round of warm-up, two timed
+
+
+def settled_state(w, chains, stream, rounds=SETTLE_ROUNDS, sim=None):
+    """(chains, controllers per replica) after `rounds` exchange rounds of the
+    workload (the default launch shape; untimed)."""
+    from chromo_gb300 import workloads as wl
+    own = sim is None
+    if own:
+        sim = wl.build_sim(w, chains)
+    for _ in range(rounds):
+        sim.run_batched(1, w.steps_per_round, w.n_rungs, 5, stream)
+    sim.sync(stream)
+    snap = ([dict(r=r, t3=t3, t2=t2, states=st) for r, t3, t2, st in sim.get_chains()],
+            [sim.get_controllers(r) for r in range(w.replicas)])
+    if own:
+        sim.close()
+    return snap
+
+
+def build_settled(w, chains, snap, **shape):
+    """A sim of the workload holding a settled state (chains and controllers)."""
+    from chromo_gb300 import workloads as wl
+    sim = wl.build_sim(w, chains, **shape)
+    sim.set_chains(snap[0])
+    for r in range(w.replicas):
+        sim.set_controllers(r, snap[1][r])
+    sim.deposit(-1)
+    return sim
 
 
 def _tune_child(workload, rank, local):
-    """Autotune the launch shape of this rank's workload (fills the cache)."""
+    """Autotune the launch shape of this rank's workload at steady state
+    (fills the cache): every candidate starts from the settled state."""
     import torch
     torch.cuda.set_device(local)
     from chromo_gb300 import autotune
     from chromo_gb300 import workloads as wl
     w = wl.make_workload(workload, seed_offset=rank)
     chains = wl.make_chains(w)
-    autotune.tune(lambda W, G: wl.build_sim(w, chains, warps_per_block=W, lanes_per_move=G),
+    snap = settled_state(w, chains, torch.cuda.current_stream().cuda_stream)
+    autotune.tune(lambda W, G: build_settled(w, chains, snap, warps_per_block=W, lanes_per_move=G),
                   w.lengths, [[w.nbins] * 3] * w.replicas, w.n_binders, steps=TUNE_STEPS,
-                  warmup=TUNE_WARMUP, extra_key=workload)
+                  warmup=TUNE_WARMUP, extra_key=workload + "-settled")
+
+
+def _at_bound(ctls):
+    """Fraction of replicas whose crank-shaft, end-pivot and slide bead
+    amplitudes sit at their upper bounds."""
+    hit = [all(c[k].amp_bead >= int(c[k].bead_hi) for k in (0, 1, 2)) for c in ctls]
+    return sum(hit) / max(1, len(hit))
 
 
 def derivatives_leg(sim, w, stream):
@@ -259,12 +308,12 @@ def reference_arm(args, rank, world):
     w = make_workload(args.workload)
     per_step = 1.0
     res = refbench.run(args.workload, budget=per_step * (args.steps + args.warmup),
-                       n_procs=os.cpu_count())
+                       n_procs=os.cpu_count(), settle_steps=SETTLE_ROUNDS * w.steps_per_round)
     out = {
         "impl": "reference", "metric": METRIC, "value": res["value"], "unit": "moves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD_DESCS[args.workload],
                    "replicas": int(w.replicas)},
         "cpu_baseline": {"value": res["value"], "unit": "moves/s", "cores": res["cores"],
@@ -318,19 +367,36 @@ def main():
     child.join()
     if child.exitcode != 0:
         print(f"autotune child exited with {child.exitcode}; tuning in this process", file=sys.stderr)
+    snap = []
+
+    def build_for_tuning(W, G):  # only when the child left no cached result
+        if not snap:
+            snap.append(settled_state(w, chains, sh))
+        return build_settled(w, chains, snap[0], warps_per_block=W, lanes_per_move=G)
+
     shape, tune_table = autotune.tune(
-        lambda W, G: wl.build_sim(w, chains, warps_per_block=W, lanes_per_move=G),
-        w.lengths, [[w.nbins] * 3] * w.replicas, w.n_binders, steps=TUNE_STEPS, warmup=TUNE_WARMUP,
-        extra_key=args.workload)
+        build_for_tuning, w.lengths, [[w.nbins] * 3] * w.replicas, w.n_binders, steps=TUNE_STEPS,
+        warmup=TUNE_WARMUP, extra_key=args.workload + "-settled")
+    snap.clear()
     mark("autotune")
     sim = wl.build_sim(w, chains, warps_per_block=shape[0], lanes_per_move=shape[1])
     if w.mu_rungs:
         sim.set_mu_ladder(w.mu_rungs, 0)
-    mark("build_sim")
     steps_round = w.steps_per_round
     moves_round = w.replicas * steps_round * w.moves_per_step
-    # ---- warm-up rounds (graph capture happens on the first)
-    for _ in range(max(args.warmup, 3)):
+    warm = max(args.warmup, 3)
+    # the MC kernel of every round is timed on the device (event-record nodes
+    # in the replayed graph), settle and warm-up rounds included
+    sim.set_round_timing(SETTLE_ROUNDS + warm + args.steps)
+    mark("build_sim")
+    # ---- settle: the controllers reach steady state (graph capture on the first round)
+    for _ in range(SETTLE_ROUNDS):
+        sim.run_batched(1, steps_round, w.n_rungs, 11 + rank, sh)
+    sim.sync(sh)
+    settle_ctl = [sim.get_controllers(r) for r in range(w.replicas)]
+    mark("settle")
+    # ---- warm-up rounds
+    for _ in range(warm):
         sim.run_batched(1, steps_round, w.n_rungs, 11 + rank, sh)
     sim.sync(sh)
     sim.reset_tally()
@@ -341,48 +407,39 @@ def main():
     # ---- timed rounds
     barrier(world)
     torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     with ClockSampler(local) as clocks:
-        ev0.record(stream)
-        for _ in range(args.steps):
+        evs[0].record(stream)
+        for k in range(args.steps):
             sim.run_batched(1, steps_round, w.n_rungs, 11 + rank, sh)
-        ev1.record(stream)
+            evs[k + 1].record(stream)
         torch.cuda.synchronize()
     sim.sync(sh)
     barrier(world)
-    ms = ev0.elapsed_time(ev1)
+    round_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    ms = evs[0].elapsed_time(evs[-1])
     ms_max = allreduce_max(ms, world)
     tal = np.stack([sim.tally(r) for r in range(w.replicas)])
     attempts = float(tal[:, :, 0].sum())
     total_attempts = allreduce_sum(attempts, world)
     value = total_attempts / (ms_max / 1000.0)
+    mc_ms_all = sim.round_times()
+    settle_mc_ms = mc_ms_all[:SETTLE_ROUNDS]
+    mc_ms = mc_ms_all[-args.steps:]
     mark("warmup_and_timed")
-    # ---- roofline: MC kernel alone, CUDA events per launch
-    sim.reset_tally()
-    n_launch = 5
-    evs = [torch.cuda.Event(enable_timing=True) for _ in range(n_launch + 1)]
-    evs[0].record(stream)
-    for i in range(n_launch):
-        sim.run(steps_round, 101 + i, sh)
-        evs[i + 1].record(stream)
-    torch.cuda.synchronize()
-    sim.sync(sh)
-    launch_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(n_launch)]
-    avg_launch_s = sum(launch_ms) / n_launch / 1000.0
-    tal2 = np.stack([sim.tally(r) for r in range(w.replicas)])
-    bytes_per_launch = wl.algorithmic_bytes(tal2, w.n_binders) / n_launch
+    # ---- roofline: the MC kernel of the timed rounds themselves
+    avg_launch_s = float(np.mean(mc_ms)) / 1000.0
+    bytes_per_launch = wl.algorithmic_bytes(tal, w.n_binders) / args.steps
     peak, peak_kind = load_peaks()
     achieved = bytes_per_launch / avg_launch_s / 1e9
-    # DRAM bytes per attempted move from the committed ncu capture of the
-    # same kernel (256 x 5,000-bead case), scaled by the moves of one launch
-    traffic = None
-    prof = ROOT / "profiles" / "spec_kernel_256x5000.md"
+    # DRAM bytes per attempted move of one MC launch of this workload at steady
+    # state, from the committed ncu capture, times the moves of one launch
+    traffic, traffic_src = None, None
+    prof = ROOT / "profiles" / f"spec_kernel_{args.workload}_dram.json"
     if prof.exists():
-        import re
-        hit = re.search(r"DRAM bytes per attempted move \| ([0-9.]+)", prof.read_text())
-        if hit:
-            traffic = float(hit.group(1)) * float(tal2[:, :, 0].sum()) / n_launch
-    mark("roofline_launches")
+        d = json.loads(prof.read_text())
+        traffic = float(d["dram_bytes_per_attempted_move"]) * attempts / args.steps
+        traffic_src = f"profiles/{prof.name}"
     # ---- energy drift: FP64 energies recomputed on the device (cg_energies)
     # around three MC launches (~3e4 moves per replica, no exchange) against
     # the running sum of accepted dE.  Includes the reference's tangent-rotation
@@ -402,22 +459,19 @@ def main():
              "how": "FP64 full-energy recompute on the device before and after 3 MC launches "
                     "vs the running sum of accepted dE"}
     mark("energy_drift")
-    # ---- e2e through the C ABI with host buffers
-    h2d = d2h = 0
+    # ---- e2e through the C ABI with host buffers: the same K rounds from the
+    # same start state (chains and controllers).  Every step uploads its input
+    # chains from host memory (all replicas: positions, tangents, binding
+    # states), rebuilds the densities, runs one exchange round and reads the
+    # resulting chains back; the next step's input is that snapshot.
     pos_b = 16
-    # A host-driven loop: every step uploads its input chains from host
-    # memory (all replicas: positions, tangents, binding states), rebuilds the
-    # densities, runs one exchange round and reads the resulting chains back;
-    # the next step's input is that snapshot.  The first step is untimed.
-    e2e_steps = max(2, min(args.steps, 5))
-    t_e2e = 0.0
-    # start from the state the timed rounds started from (the chains are
-    # uploaded by the first, untimed round)
+    spare, other = sim.get_chains(), sim.get_chains()  # host snapshot buffers, allocated untimed
+    sim.set_chains([dict(r=r, t3=t3, t2=t2, states=st) for r, t3, t2, st in start_chains])  # pinned staging
     for r in range(w.replicas):
         sim.set_controllers(r, start_ctl[r])
     inp = start_chains
-    spare, other = sim.get_chains(), sim.get_chains()  # two host snapshot buffers, allocated untimed
-    for k in range(e2e_steps + 1):
+    t_e2e = 0.0
+    for k in range(args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sim.set_chains([dict(r=r, t3=t3, t2=t2, states=st) for r, t3, t2, st in inp])
@@ -425,21 +479,21 @@ def main():
         sim.run_batched(1, steps_round, w.n_rungs, 11 + rank, sh)
         sim.sync(sh)
         out = sim.get_chains(out=spare)
-        dt = time.perf_counter() - t0
-        if k > 0:
-            t_e2e += dt
+        t_e2e += time.perf_counter() - t0
         spare = other if k == 0 else inp  # the start snapshot is never overwritten
         inp = out
     nbeads = int(w.lengths.sum())
     h2d = nbeads * (3 * pos_b + 4)
     d2h = nbeads * (3 * pos_b + 4)
-    e2e_value = allreduce_sum(moves_round * e2e_steps, world) / allreduce_max(t_e2e, world)
+    e2e_value = allreduce_sum(moves_round * args.steps, world) / allreduce_max(t_e2e, world)
     mark("e2e")
-    # ---- plain single chain (one CTA) on the same kernel
+    # ---- plain single chain (one CTA) on the same kernel, settled for the
+    # same number of MC steps as the batched replicas
     wp = wl.make_workload("plain", seed_offset=rank)
     psim = wl.build_sim(wp)
-    psim.run(20, 5, sh)
+    psim.run(SETTLE_ROUNDS * steps_round, 5, sh)
     psim.sync(sh)
+    p_snap = (psim.get_chains(), [psim.get_controllers(0)])
     psim.reset_tally()
     pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     pe0.record(stream)
@@ -453,8 +507,9 @@ def main():
     # the same chain with one move in flight (one warp, no speculative
     # batching): the kernel run strictly one move after the other
     ssim = wl.build_sim(wp, warps_per_block=1)
-    ssim.run(20, 5, sh)
-    ssim.sync(sh)
+    ssim.set_chains([dict(r=r, t3=t3, t2=t2, states=st) for r, t3, t2, st in p_snap[0]])
+    ssim.set_controllers(0, p_snap[1][0])
+    ssim.deposit(-1)
     ssim.reset_tally()
     pe0.record(stream)
     ssim.run(100, 6, sh)
@@ -472,7 +527,8 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         from oracle import refbench
-        cpu = refbench.run(args.workload, budget=args.cpu_budget, n_procs=os.cpu_count())
+        cpu = refbench.run(args.workload, budget=args.cpu_budget, n_procs=os.cpu_count(),
+                           settle_steps=SETTLE_ROUNDS * steps_round)
     mark("cpu_baseline")
     if rank == 0:
         out = {
@@ -486,21 +542,30 @@ def main():
                        "l2": "inputs larger than L2 (%.0f MB of grids and chains > 129 MB)"
                              % ((w.replicas * w.nbins ** 3 * 32 + nbeads * 104) / 1e6),
                        "graph": "one exchange round captured in a CUDA graph, replayed per step",
+                       "settle": {"rounds": SETTLE_ROUNDS, "mc_steps": SETTLE_ROUNDS * steps_round,
+                                  "bead_amplitudes_at_bound": _at_bound(settle_ctl),
+                                  "mc_kernel_ms_every_10th_round":
+                                      [round(float(x), 2) for x in settle_mc_ms[::10]]},
                        "launch_shape": dict(zip(("warps_per_replica", "lanes_per_move", "moves_in_flight",
                                                  "hash_slots"), sim.launch_shape())),
                        "autotune_moves_per_s": {k: round(v) for k, v in tune_table.items()}},
+            "rounds": {"round_ms": [round(x, 3) for x in round_ms],
+                       "mc_kernel_ms": [round(float(x), 3) for x in mc_ms]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "spec_kernel<float>", "peak_source": peak_kind,
-                         "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
-                         "moves_per_launch": float(tal2[:, :, 0].sum()) / n_launch},
+                         "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                         "kernel": "spec_kernel<float,%d>" % sim.launch_shape()[1],
+                         "peak_source": peak_kind, "bytes_per_launch": bytes_per_launch,
+                         "avg_launch_ms": avg_launch_s * 1e3, "moves_per_launch": attempts / args.steps,
+                         "timing": "the MC kernel of the K timed rounds: CUDA event-record nodes "
+                                   "around it inside the replayed graph"},
             "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "path": "C ABI, host-driven rounds: cg_set_chains (the previous round's host "
                             "snapshot, FP64 -> pinned -> HBM, all replicas), cg_deposit, cg_run_batched, "
                             "cg_get_chains (into reused host arrays)"},
             "plain": {"value": plain_value, "unit": "moves/s",
-                      "workload": "one 10,000-bead chain, 60^3 grid, one binder, 300 MC steps",
+                      "workload": "one 10,000-bead chain, 60^3 grid, one binder, 300 MC steps after "
+                                  "%d settle MC steps" % (SETTLE_ROUNDS * steps_round),
                       "batched_over_plain": value / plain_value,
                       "one_move_in_flight": {"value": seq_value, "unit": "moves/s",
                                              "workload": "the same chain, one warp, 100 MC steps",

@@ -84,7 +84,8 @@ EXPORTS = [
     "cg_reset_tally", "cg_exchange", "cg_get_chi", "cg_run_batched", "cg_get_launch_info",
     "cg_field_energy_static", "cg_energies", "cg_set_chains", "cg_get_chains", "cg_gradient",
     "cg_sample_terms", "cg_get_samples", "cg_get_launch_shape", "cg_mc_warps_per_sm",
-    "cg_set_mu_ladder", "cg_get_mu", "cg_get_swap_counts",
+    "cg_set_mu_ladder", "cg_get_mu", "cg_get_swap_counts", "cg_run_logged", "cg_set_round_timing",
+    "cg_get_round_times",
 ]
 N_TERMS = 14
 
@@ -117,6 +118,9 @@ def lib():
             "cg_run": ([P, I64, C.c_uint64, P], C.c_int),
             "cg_sync": ([P, P], C.c_int),
             "cg_run_audit": ([P, I32, I64, P, I64, P, I64, P, I64, P, P, P], C.c_int),
+            "cg_run_logged": ([P, I64, C.c_uint64, P, I64, P], C.c_int),
+            "cg_set_round_timing": ([P, I32], C.c_int),
+            "cg_get_round_times": ([P, P, I32, P], C.c_int),
             "cg_energy": ([P, I32, P], C.c_int),
             "cg_reset_running_energy": ([P], C.c_int),
             "cg_get_tally": ([P, I32, P], C.c_int),
@@ -308,6 +312,16 @@ class Sim:
                                  C.byref(bu)))
         return recs[:min(nrec.value, max_records)], du.value, bu.value
 
+    def run_logged(self, n_steps, seed, max_records):
+        """``run`` with the production kernel's per-move log: a list with one
+        record array per replica (its attempted moves in order, at most
+        ``max_records``)."""
+        recs = np.zeros((self.R, int(max_records)), dtype=RECORD_DTYPE)
+        n = np.zeros(self.R, dtype=np.int64)
+        check(lib().cg_run_logged(self.h, int(n_steps), int(seed) & (2**64 - 1), _ptr(recs),
+                                  int(max_records), _ptr(n)))
+        return [recs[r, :min(int(n[r]), int(max_records))] for r in range(self.R)]
+
     def energy(self, rep):
         out = np.zeros(4)
         check(lib().cg_energy(self.h, rep, _ptr(out)))
@@ -373,6 +387,18 @@ class Sim:
     def run_batched(self, n_rounds, n_steps, n_rungs, seed, stream=None):
         check(lib().cg_run_batched(self.h, int(n_rounds), int(n_steps), int(n_rungs),
                                    int(seed) & (2**64 - 1), stream))
+
+    def set_round_timing(self, capacity):
+        """Time the MC kernel of every ``run_batched`` round on the device
+        (CUDA events inside the graph), keeping the last ``capacity``."""
+        check(lib().cg_set_round_timing(self.h, int(capacity)))
+
+    def round_times(self, max_rounds=1 << 16):
+        """MC-kernel milliseconds of the last timed rounds, oldest first."""
+        out = np.zeros(int(max_rounds), dtype=np.float32)
+        n = C.c_int32()
+        check(lib().cg_get_round_times(self.h, _ptr(out), int(max_rounds), C.byref(n)))
+        return out[:n.value].astype(np.float64)
 
     def launch_shape(self):
         """(warps per replica, lanes per move, moves in flight, shared voxel-table slots)."""

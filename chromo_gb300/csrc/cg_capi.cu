@@ -93,10 +93,37 @@ struct cg_sim {
   size_t spec_bytes = 0;
   // captured batched graph
   cudaGraphExec_t graph = nullptr;
+  cudaGraph_t graph_src = nullptr;  // kept while its timing nodes are re-pointed per launch
   long long graph_rounds = -1, graph_steps = -1;
   int graph_rungs = -1;
   unsigned long long graph_seed = 0;
   cudaStream_t graph_stream = nullptr;
+  // per-round timing of the MC kernel inside the graph (cg_set_round_timing):
+  // ring of timing_cap event pairs; each captured round's two event-record
+  // nodes are pointed at the next pair before every launch
+  int timing_cap = 0;
+  long long timing_count = 0;
+  std::vector<cudaEvent_t> tev_begin, tev_end;
+  std::vector<cudaEvent_t> cap_begin, cap_end;  // events the nodes were captured with
+  std::vector<cudaGraphNode_t> tnode_begin, tnode_end;
+
+  void drop_graph() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (graph_src) cudaGraphDestroy(graph_src);
+    graph = nullptr;
+    graph_src = nullptr;
+    for (cudaEvent_t e : cap_begin) cudaEventDestroy(e);
+    for (cudaEvent_t e : cap_end) cudaEventDestroy(e);
+    cap_begin.clear(); cap_end.clear(); tnode_begin.clear(); tnode_end.clear();
+  }
+  void drop_timing() {
+    drop_graph();
+    for (cudaEvent_t e : tev_begin) cudaEventDestroy(e);
+    for (cudaEvent_t e : tev_end) cudaEventDestroy(e);
+    tev_begin.clear(); tev_end.clear();
+    timing_cap = 0;
+    timing_count = 0;
+  }
   // derivatives: per-bead gradient, per-replica terms, running sums (allocated on first use)
   float* grad = nullptr;
   double* terms = nullptr;
@@ -215,7 +242,7 @@ const char* cg_last_error(void) { return g_err.c_str(); }
 
 void cg_destroy(cg_sim* s) {
   if (!s) return;
-  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->drop_timing();
   if (s->pinned) cudaFreeHost(s->pinned);
   void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
                   s->bonds32, s->grid, s->access_vol, s->access_sc, s->access_vb, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
@@ -753,6 +780,38 @@ int cg_run(cg_sim* s, int64_t n_steps, uint64_t seed, void* stream) {
   return CG_OK;
 }
 
+int cg_run_logged(cg_sim* s, int64_t n_steps, uint64_t seed, cg_move_record* records, int64_t max_records,
+                  int64_t* n_records) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (n_steps < 0 || max_records < 0) return fail(CG_ERR_ARG, "negative size");
+  if (max_records > 0 && !records) return fail(CG_ERR_ARG, "null records");
+  std::vector<RepDev> rd0(s->R), rd1(s->R);
+  CUDA_TRY(cudaDeviceSynchronize());
+  CUDA_TRY(cudaMemcpy(rd0.data(), s->reps, sizeof(RepDev) * s->R, cudaMemcpyDeviceToHost));
+  cg_move_record* d_log = nullptr;
+  const long long cap = std::max<int64_t>(max_records, 1);
+  cudaError_t e = cudaMalloc(&d_log, sizeof(cg_move_record) * cap * s->R);
+  if (e == cudaSuccess && n_steps > 0) {
+    KArgs a = s->args();
+    a.n_steps = n_steps;
+    a.seed = seed;
+    a.mlog = d_log;
+    a.mlog_cap = max_records;
+    cg_launch_spec(a, s->fp64, s->spec_bytes, 0);
+    s->kernels++;
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(rd1.data(), s->reps, sizeof(RepDev) * s->R, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && max_records > 0)
+    e = cudaMemcpy(records, d_log, sizeof(cg_move_record) * max_records * s->R, cudaMemcpyDeviceToHost);
+  cudaFree(d_log);
+  if (e != cudaSuccess) return fail(CG_ERR_CUDA, cudaGetErrorString(e));
+  if (n_records)
+    for (int r = 0; r < s->R; r++) n_records[r] = (int64_t)(rd1[r].draw_pos - rd0[r].draw_pos);
+  return device_errors(s);
+}
+
 int cg_sync(cg_sim* s, void* stream) {
   if (!s) return fail(CG_ERR_ARG, "null sim");
   CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
@@ -910,7 +969,7 @@ int cg_set_mu_ladder(cg_sim* s, int32_t mu_rungs, int32_t binder) {
   if (binder < 0 || binder >= s->nb) return fail(CG_ERR_ARG, "binder index out of range");
   s->mu_rungs = mu_rungs;
   s->mu_binder = binder;
-  if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }  // arguments are baked into it
+  s->drop_graph();  // arguments are baked into it
   return CG_OK;
 }
 
@@ -956,9 +1015,18 @@ int cg_run_batched(cg_sim* s, int64_t n_rounds, int64_t n_steps, int32_t n_rungs
   if (n_rungs)
     if (int rc = check_rungs(s, n_rungs)) return rc;
   cudaStream_t st = (cudaStream_t)stream;
+  const bool timed = s->timing_cap > 0;
   if (!(s->graph && s->graph_rounds == n_rounds && s->graph_steps == n_steps && s->graph_rungs == n_rungs &&
-        s->graph_seed == seed && s->graph_stream == st)) {
-    if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+        s->graph_seed == seed && s->graph_stream == st && (long long)s->tnode_begin.size() == (timed ? n_rounds : 0))) {
+    s->drop_graph();
+    if (timed) {
+      s->cap_begin.assign(n_rounds, nullptr);
+      s->cap_end.assign(n_rounds, nullptr);
+      for (long long k = 0; k < n_rounds; k++) {
+        CUDA_TRY(cudaEventCreate(&s->cap_begin[k]));
+        CUDA_TRY(cudaEventCreate(&s->cap_end[k]));
+      }
+    }
     cudaStream_t cap;
     CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     cudaGraph_t gr;
@@ -967,20 +1035,81 @@ int cg_run_batched(cg_sim* s, int64_t n_rounds, int64_t n_steps, int32_t n_rungs
       KArgs a = s->args();
       a.n_steps = n_steps;
       a.seed = seed;
+      if (timed) cudaEventRecordWithFlags(s->cap_begin[k], cap, cudaEventRecordExternal);
       cg_launch_spec(a, s->fp64, s->spec_bytes, cap);
+      if (timed) cudaEventRecordWithFlags(s->cap_end[k], cap, cudaEventRecordExternal);
       if (n_rungs) enqueue_exchange(s, n_rungs, -1, seed, cap);
     }
     cudaError_t e = cudaStreamEndCapture(cap, &gr);
     cudaStreamDestroy(cap);
     if (e != cudaSuccess) return fail(CG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    if (timed) {  // the event-record nodes of each round, found by the events they were captured with
+      size_t n = 0;
+      cudaGraphGetNodes(gr, nullptr, &n);
+      std::vector<cudaGraphNode_t> nodes(n);
+      if (n) cudaGraphGetNodes(gr, nodes.data(), &n);
+      s->tnode_begin.assign(n_rounds, nullptr);
+      s->tnode_end.assign(n_rounds, nullptr);
+      for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType ty;
+        if (cudaGraphNodeGetType(nd, &ty) != cudaSuccess || ty != cudaGraphNodeTypeEventRecord) continue;
+        cudaEvent_t ev = nullptr;
+        cudaGraphEventRecordNodeGetEvent(nd, &ev);
+        for (long long k = 0; k < n_rounds; k++) {
+          if (ev == s->cap_begin[k]) s->tnode_begin[k] = nd;
+          if (ev == s->cap_end[k]) s->tnode_end[k] = nd;
+        }
+      }
+      for (long long k = 0; k < n_rounds; k++)
+        if (!s->tnode_begin[k] || !s->tnode_end[k]) {
+          cudaGraphDestroy(gr);
+          s->tnode_begin.clear();
+          return fail(CG_ERR_CUDA, "graph capture: round timing nodes not found");
+        }
+    }
     e = cudaGraphInstantiate(&s->graph, gr, 0);
-    cudaGraphDestroy(gr);
-    if (e != cudaSuccess) return fail(CG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    s->graph_src = gr;
+    if (e != cudaSuccess) { s->drop_graph(); return fail(CG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
     s->graph_rounds = n_rounds; s->graph_steps = n_steps; s->graph_rungs = n_rungs;
     s->graph_seed = seed; s->graph_stream = st;
   }
+  if (timed)
+    for (long long k = 0; k < n_rounds; k++) {
+      const long long slot = (s->timing_count + k) % s->timing_cap;
+      CUDA_TRY(cudaGraphExecEventRecordNodeSetEvent(s->graph, s->tnode_begin[k], s->tev_begin[slot]));
+      CUDA_TRY(cudaGraphExecEventRecordNodeSetEvent(s->graph, s->tnode_end[k], s->tev_end[slot]));
+    }
   CUDA_TRY(cudaGraphLaunch(s->graph, st));
+  if (timed) s->timing_count += n_rounds;
   s->kernels += n_rounds;
+  return CG_OK;
+}
+
+int cg_set_round_timing(cg_sim* s, int32_t capacity) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (capacity < 0 || capacity > (1 << 20)) return fail(CG_ERR_ARG, "capacity must be in 0..2^20");
+  CUDA_TRY(cudaDeviceSynchronize());
+  s->drop_timing();
+  s->tev_begin.assign(capacity, nullptr);
+  s->tev_end.assign(capacity, nullptr);
+  for (int k = 0; k < capacity; k++) {
+    CUDA_TRY(cudaEventCreate(&s->tev_begin[k]));
+    CUDA_TRY(cudaEventCreate(&s->tev_end[k]));
+  }
+  s->timing_cap = capacity;
+  return CG_OK;
+}
+
+int cg_get_round_times(cg_sim* s, float* mc_ms, int32_t max, int32_t* count) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (max < 0 || (max > 0 && !mc_ms)) return fail(CG_ERR_ARG, "bad output buffer");
+  long long n = std::min<long long>(std::min<long long>(s->timing_count, s->timing_cap), max);
+  for (long long i = 0; i < n; i++) {
+    const long long slot = (s->timing_count - n + i) % s->timing_cap;
+    CUDA_TRY(cudaEventSynchronize(s->tev_end[slot]));
+    CUDA_TRY(cudaEventElapsedTime(&mc_ms[i], s->tev_begin[slot], s->tev_end[slot]));
+  }
+  if (count) *count = (int32_t)n;
   return CG_OK;
 }
 

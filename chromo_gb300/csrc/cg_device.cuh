@@ -18,6 +18,15 @@ constexpr double kFxInv = 1.0 / 1099511627776.0;
 constexpr double kEHugePoly = 1e25;                     // chromo/polymers.pyx:35
 constexpr double kEHugeField = 1e99;                    // chromo/fields.pyx:32
 constexpr double kRandMax = 2147483647.0;               // glibc RAND_MAX
+// The 1e99 penalties of the field (a voxel above vf_limit, fields.pyx:1832-1840;
+// a bead outside the confinement, fields.pyx:121-202) are summed exactly, in
+// integer units of kHugeUnit = 1e99 * 2^-40: a voxel above the limit holding
+// n fixed-point units of bead weight costs huge_units(n, Vb / V) = n Vb / V
+// rounded once (1e99 vf = kHugeUnit * n Vb / V), a bead outside costs 2^40.
+// A move's penalty is then independent of the order of its voxels and is
+// exactly zero when the weight above the limit does not change, so the
+// decisions in that regime are well defined.
+constexpr double kHugeUnit = kEHugeField * kFxInv;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxIter = 4096;                          // cap on resampling loops
 
@@ -611,6 +620,10 @@ __device__ __forceinline__ void voxel_weights(const RepDev& rd, const GridF& gf,
 }
 
 __device__ __forceinline__ long long q40(double w) { return __double2ll_rn(w * kFxScale); }
+// penalty units of a voxel above vf_limit (see kHugeUnit)
+__device__ __forceinline__ long long huge_units(long long n, double vb_over_v) {
+  return __double2ll_rn((double)n * vb_over_v);
+}
 __device__ __forceinline__ long long q40(float w) { return cgm_q40f(w); }
 
 // ---------------------------------------------------------------- warp helpers

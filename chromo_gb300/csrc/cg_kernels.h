@@ -40,8 +40,9 @@ struct MovePlan {
   int kind, m, ind0, indf;
   int empty, err, regfail, dec;
   unsigned cmask;
-  int nvox, gtab, gstage, bsel, pad;
+  int nvox, gtab, gstage, bsel, ndraw;
   double dE;
+  double dEp;  // polymer part of dE (written only when the move log is on)
   // block-wide deposit of a position move (its beads' corners spread over
   // every thread of the CTA): the proposal's transform and table kind in,
   // the two boundary bond terms, the confinement counts and the error bits out
@@ -60,6 +61,7 @@ struct SpecShared {
   MovePlan plan[kMaxS];
   int nused[kMaxS];
   unsigned long long t0;   // move counter (selects each move's random sub-stream)
+  unsigned long long tlog; // move counter at launch (index origin of the move log)
   double run_dE;
   int cut, stop;
   unsigned accmask;
@@ -116,6 +118,10 @@ struct KArgs {
   cg_move_record* a_recs;
   long long a_max_recs;
   long long* a_out;
+  // production kernel's move log (null: off): records [n_reps x mlog_cap],
+  // move k of the launch (k < mlog_cap) of replica r at r * mlog_cap + k
+  cg_move_record* mlog;
+  long long mlog_cap;
   // replica exchange
   int* rep_of_rung;            // parameter slot -> replica holding that slot's (chi, mu)
   unsigned long long* swaps;

@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
           using Acc = typename AccOf<Real>::type;
           Acc dEp = acc_zero<Acc>(), dEs = acc_zero<Acc>();
           double dEh = 0;
+          long long dEH = 0;  // the exact 1e99 penalties, in kHugeUnit units
           long long nvox = 0;
           bool empty = false;
           int* keys = s_keys; int* used = s_used; long long* vals = s_vals; int logH = a.logH;
@@ -233,15 +234,12 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
               dEp = warp_sum(part);
               if (check_field && rd.confine_kind) {
                 int oo = __reduce_add_sync(kFull, (unsigned)oob);
-                double conf = 0;
-                conf += (double)(oo >> 16) * kEHugeField;
-                conf -= (double)(oo & 0xFFFF) * kEHugeField;
-                dEh = conf;
+                dEH += ((long long)(oo >> 16) - (long long)(oo & 0xFFFF)) << 40;
               }
               __syncwarp();
               if (density) {
                 int nu = ws.nused;
-                field_dE_voxels(ws, a, ncol, keys, used, vals, nu, lane, nvox, dEs, dEh);
+                field_dE_voxels(ws, a, ncol, keys, used, vals, nu, lane, nvox, dEs, dEh, dEH);
               }
             }
           } else if (kind == CG_TANGENT_ROTATION) {
@@ -383,17 +381,18 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
                 ld3(r4, ind0 + k, p);
                 oob += out_of_bounds(rd, p, true);
               }
-              dEh = (double)__reduce_add_sync(kFull, (unsigned)oob) * kEHugeField;
+              dEH += (long long)__reduce_add_sync(kFull, (unsigned)oob) << 40;
             }
             __syncwarp();
             if (density) {
               int nu = ws.nused;
-              field_dE_voxels(ws, a, ncol, keys, used, vals, nu, lane, nvox, dEs, dEh);
+              field_dE_voxels(ws, a, ncol, keys, used, vals, nu, lane, nvox, dEs, dEh, dEH);
               add_intra(ws, bsel, ddb, dEs, dEh);
             }
           }
           if (AUDIT && g.fail) err |= E_STREAM;
           if (err) break;
+          dEh = with_huge(dEh, dEH);
           // ------------------------------------------------ Metropolis + commit
           int accepted = -1;
           if (!empty) {
@@ -600,7 +599,9 @@ __global__ void energy_kernel(KArgs a, double* out) {
         for (int e = 0; e < rd.nb; e++) fe += rd.xpref[b * CG_MAX_BINDERS + e] * rho[b] * rho[e];
       double vf = ((double)grid[v * a.ncol] * kFxInv) / V * rd.bead_vol;
       double sv = (V / rd.bead_vol) * vf * vf;
-      sx += sv;
+      // S: the chi-free sum over the voxels at or below vf_limit (a voxel
+      // above it costs 1e99 vf, which does not depend on chi)
+      if (!(vf > rd.vf_limit)) sx += sv;
       fe += vf > rd.vf_limit ? kEHugeField * vf : rd.chi * sv;
     }
   }
@@ -631,21 +632,26 @@ __global__ void chi_sum_kernel(KArgs a, double* out) {
   double sx = 0;
   if (rd.field_kind == 2 && !rd.has_access) {
     // uniform voxel volume: S = (V / Vb) c^2 sum g0^2 with c = 2^-40 Vb / V the
-    // volume fraction per fixed-point unit (no FP64 division per voxel)
+    // volume fraction per fixed-point unit (no FP64 division per voxel); a
+    // voxel whose volume fraction may be above vf_limit takes the exact test
+    // of energy_kernel and is left out of S when above it
     const long long* grid = a.grid + rd.vox_off * a.ncol;
+    const double c = kFxInv / rd.vol_bin * rd.bead_vol;
+    const double near = rd.vf_limit * (1.0 - 1e-9);
     double s00 = 0;
     for (long long v = threadIdx.x; v < rd.n_vox; v += blockDim.x) {
-      const double g0 = (double)grid[v * a.ncol];
+      const long long n = grid[v * a.ncol];
+      const double g0 = (double)n;
+      if (g0 * c > near && ((double)n * kFxInv) / rd.vol_bin * rd.bead_vol > rd.vf_limit) continue;
       s00 += g0 * g0;
     }
-    const double c = kFxInv / rd.vol_bin * rd.bead_vol;
     sx = (rd.vol_bin / rd.bead_vol) * (c * c) * s00;
   } else if (rd.field_kind == 2) {
     const long long* grid = a.grid + rd.vox_off * a.ncol;
     for (long long v = threadIdx.x; v < rd.n_vox; v += blockDim.x) {
       double V = rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin;
       double vf = ((double)grid[v * a.ncol] * kFxInv) / V * rd.bead_vol;
-      sx += (V / rd.bead_vol) * vf * vf;
+      if (!(vf > rd.vf_limit)) sx += (V / rd.bead_vol) * vf * vf;
     }
   }
   const double t = block_sum(sx, sh);
@@ -662,8 +668,9 @@ __global__ void chi_sum_kernel(KArgs a, double* out) {
 
 // ---------------------------------------------------------------- replica exchange
 // Swap chi between neighbouring rungs of each ladder (n_rungs consecutive
-// rung slots per ladder).  eout[5 r + 4] holds S_r = sum over voxels of
-// (V/Vb) vf^2, the chi-free part of replica r's field energy, so that
+// rung slots per ladder).  eout[5 r + 4] holds S_r = sum over the voxels at
+// or below vf_limit of (V/Vb) vf^2, the chi-free part of replica r's field
+// energy (a voxel above the limit costs 1e99 vf whatever chi is), so that
 // E_r = chi_r S_r + (chi-independent terms).  One block; round < 0 takes the
 // round number from a device counter and advances it (graph replays).
 __global__ void exchange_kernel(KArgs a, const double* eout, int n_rungs, long long round_in,

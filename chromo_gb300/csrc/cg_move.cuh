@@ -220,28 +220,53 @@ __device__ __forceinline__ void load_row(const long long* gv, int ncol, long lon
   }
 }
 
-// chi term of one voxel in FP64 (fields.pyx:1792-1875 with the vf_limit branch)
-static __device__ __noinline__ double chi_term64(const RepDev& rd, double V, long long g0, long long d0) {
+// chi term of one voxel in FP64 (fields.pyx:1792-1875 with the vf_limit
+// branch): `soft` is the FP64 part, `huge` the 1e99 penalty of the voxel
+// above vf_limit in kHugeUnit units (after the move minus before it).
+struct ChiSplit {
+  double soft;
+  long long huge;
+};
+static __device__ __noinline__ ChiSplit chi_term64(const RepDev& rd, double V, long long g0, long long d0) {
   double vf0 = ((double)g0 * kFxInv) / V * rd.bead_vol;
   double vf1 = ((double)(g0 + d0) * kFxInv) / V * rd.bead_vol;
   double k = rd.chi * (V / rd.bead_vol);
-  if (vf1 > rd.vf_limit || vf0 > rd.vf_limit)
-    return (vf1 > rd.vf_limit ? kEHugeField * vf1 : k * vf1 * vf1)
-         - (vf0 > rd.vf_limit ? kEHugeField * vf0 : k * vf0 * vf0);
-  return k * ((vf1 - vf0) * (vf1 + vf0));
+  ChiSplit t{0.0, 0};
+  if (vf1 > rd.vf_limit || vf0 > rd.vf_limit) {
+    const double u = rd.bead_vol / V;
+    if (vf1 > rd.vf_limit) t.huge += huge_units(g0 + d0, u);
+    else t.soft += k * vf1 * vf1;
+    if (vf0 > rd.vf_limit) t.huge -= huge_units(g0, u);
+    else t.soft -= k * vf0 * vf0;
+    return t;
+  }
+  t.soft = k * ((vf1 - vf0) * (vf1 + vf0));
+  return t;
+}
+
+// hard + huge * kHugeUnit: the FP64 part of a move's dE with its exact 1e99
+// penalties added (out of line, the penalties are rare)
+static __device__ __noinline__ double hard_with_huge(double hard, long long huge) {
+  return hard + (double)huge * kHugeUnit;
+}
+__device__ __forceinline__ double with_huge(double hard, long long huge) {
+  return huge != 0 ? hard_with_huge(hard, huge) : hard;
 }
 
 // Field dE over the touched voxels (fixed-point grid), FP64 arithmetic; also
 // stores the post-move grid values into the hash values for the commit.  The
-// sum is added to `hard` (the FP64 part of the move's dE), nothing to `soft`.
+// sum is added to `hard` (the FP64 part of the move's dE), nothing to `soft`;
+// the 1e99 penalties of voxels above vf_limit go to `huge` (kHugeUnit units).
 // Called by the whole warp; lane gl of each group of G lanes takes voxels
 // gl, gl + G, ... of its group's table.
 template <int G = 32>
 static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
-                                  long long& n_vox, double& soft, double& hard, bool split = false) {
+                                  long long& n_vox, double& soft, double& hard, long long& huge,
+                                  bool split = false) {
   const RepDev& rd = ws.rd;
   double part = 0;
+  long long hpart = 0;
   const long long* grid = a.grid + rd.vox_off * a.ncol;
   for (int i = lane; i < nused; i += G) {
     int slot = used[i];
@@ -267,24 +292,30 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
       for (int e = 0; e < CG_MAX_BINDERS; e++)
         if (b < rd.nb && e < rd.nb)
           c += rd.xpref[b * CG_MAX_BINDERS + e] * (rho[b] * dd[e] + dd[b] * rho[e] + dd[b] * dd[e]);
-    c += chi_term64(rd, V, g0, d0);
+    const ChiSplit t = chi_term64(rd, V, g0, d0);
+    c += t.soft;
+    hpart += t.huge;
     d[0] = g0 + d0;
     part += c;
   }
   n_vox = nused;
   (void)soft;
   hard += gsum<G>(part);
+  if (gany<G>(hpart != 0)) huge += gsum<G>(hpart);
 }
 
 // FP32 arithmetic per voxel, fixed-point accumulation into `soft`; voxels at
-// or near the volume-fraction limit take the FP64 branch (into the FP64 side
-// sum), so the 1e99 penalty is decided as in FP64.
+// or near the volume-fraction limit take the FP64 branch (chi terms into the
+// FP64 side sum, the 1e99 penalties exactly into `huge`), so which side of the
+// limit a voxel lies on is decided as in FP64.
 template <int G = 32>
 static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
-                                  long long& n_vox, Fx& soft, double& hard, bool split = false) {
+                                  long long& n_vox, Fx& soft, double& hard, long long& huge,
+                                  bool split = false) {
   const RepDev& rd = ws.rd;
   Fx part = Fx{0, 0.0};
+  long long hpart = 0;
   const long long* grid = a.grid + rd.vox_off * a.ncol;
   (void)hard;
   for (int i = lane; i < nused; i += G) {
@@ -319,7 +350,9 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
     float dvf = (float)d0 * sc * ws.f_vb;
     if (vf0 > ws.f_lim - 1e-3f || vf0 + dvf > ws.f_lim - 1e-3f) {
       acc_add(part, c);
-      part.hard += chi_term64(rd, rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin, g0, d0);
+      const ChiSplit t = chi_term64(rd, rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin, g0, d0);
+      part.hard = add_hard(part.hard, t.soft);
+      hpart += t.huge;
     } else {
       acc_add(part, c + k * (dvf * (2.0f * vf0 + dvf)));
     }
@@ -327,6 +360,7 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
   }
   n_vox = nused;
   acc_add(soft, gsum<G>(part));
+  if (gany<G>(hpart != 0)) huge += gsum<G>(hpart);
 }
 
 __device__ __forceinline__ void commit_grid(const RepDev& rd, const KArgs& a, int hcol, int* keys,

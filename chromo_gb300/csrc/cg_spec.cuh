@@ -307,6 +307,33 @@ __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, in
   }
 }
 
+// Move-log terms of a plan (out of line: the log is off in production runs).
+static __device__ __noinline__ void log_terms_d(MovePlan& P, double dEp, unsigned long long pos) {
+  P.dEp = dEp;
+  P.ndraw = (int)pos;
+}
+__device__ __forceinline__ void log_terms(MovePlan& P, double dEp, unsigned long long pos) {
+  log_terms_d(P, dEp, pos);
+}
+__device__ __forceinline__ void log_terms(MovePlan& P, const Fx& dEp, unsigned long long pos) {
+  log_terms_d(P, acc_d(dEp), pos);
+}
+
+// Record of move t (its plan) in the move log, when t is within the log.
+static __device__ __noinline__ void log_move(const KArgs& a, int rep, unsigned long long k, const MovePlan& P) {
+  if (k >= (unsigned long long)a.mlog_cap) return;
+  cg_move_record rec;
+  rec.kind = P.kind;
+  rec.n_inds = P.empty ? 0 : P.m;
+  rec.ind0 = P.ind0;
+  rec.indf = P.indf;
+  rec.dE_poly = P.empty ? 0.0 : P.dEp;
+  rec.dE_field = P.empty ? 0.0 : P.dE - P.dEp;
+  rec.accepted = P.empty ? -1 : P.dec;
+  rec.n_draws = P.ndraw;
+  a.mlog[(long long)rep * a.mlog_cap + (long long)k] = rec;
+}
+
 // Evaluate move t of the batch in slot s (group lanes gl = 0..G-1); `live`
 // is false for the groups of a partly filled batch and for the warps without
 // a move, which run the collectives and block barriers with empty work.
@@ -342,6 +369,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
   // FP64 part: confinement penalties, and the whole field dE for FP64 storage)
   Acc dEp = acc_zero<Acc>(), dEs = acc_zero<Acc>();
   double dEh = 0;
+  long long dEH = 0;  // the exact 1e99 penalties, in kHugeUnit units
   long long nvox = 0;
   bool empty = !live;
   int gtab = 0, gstage = 0;
@@ -525,14 +553,11 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     dEp = gsum<G>(part);
     if (check_field && rd.confine_kind) {
       int oo = gsum<G>(oob);
-      double conf = 0;
-      conf += (double)(oo >> 16) * kEHugeField;
-      conf -= (double)(oo & 0xFFFF) * kEHugeField;
-      dEh = conf;
+      dEH += ((long long)(oo >> 16) - (long long)(oo & 0xFFFF)) << 40;
     }
     __syncwarp();
     if (density)
-      field_dE_voxels<G>(ws, a, hcol, S.keys, S.used, S.vals, *nused, gl, nvox, dEs, dEh, !gtab);
+      field_dE_voxels<G>(ws, a, hcol, S.keys, S.used, S.vals, *nused, gl, nvox, dEs, dEh, dEH, !gtab);
   } else if (kind == CG_TANGENT_ROTATION) {
     Real ang = 0;
     long long n = 0;
@@ -698,11 +723,11 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
         ld3(r4, ind0 + k, p);
         oob += out_of_bounds(rd, p, true);
       }
-      dEh = (double)gsum<G>(oob) * kEHugeField;
+      dEH += (long long)gsum<G>(oob) << 40;
     }
     __syncwarp();
     if (density) {
-      field_dE_voxels<G>(ws, a, hcol, S.keys, S.used, S.vals, *nused, gl, nvox, dEs, dEh, !gtab);
+      field_dE_voxels<G>(ws, a, hcol, S.keys, S.used, S.vals, *nused, gl, nvox, dEs, dEh, dEH, !gtab);
       if (m > 0) add_intra(ws, bsel, ddb, dEs, dEh);
     }
     if (gl == 0 && live) P.bsel = bsel;
@@ -738,11 +763,12 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     if (gl == 0 && live) atomicOr(&P.cmask, cmb);
   }
   bool dec = false;
-  if (live && !err && !empty) dec = decide(g.next(), dEp, dEs, dEh, gl == 0 ? &P.dE : nullptr);
+  if (live && !err && !empty) dec = decide(g.next(), dEp, dEs, with_huge(dEh, dEH), gl == 0 ? &P.dE : nullptr);
   if (gl == 0 && live) {
     P.kind = kind; P.m = (int)m; P.ind0 = (int)ind0; P.indf = (int)indf;
     P.empty = empty ? 1 : 0; P.err = (int)err; P.regfail = regfail; P.dec = dec ? 1 : 0;
     P.nvox = (int)nvox; P.gtab = gtab; P.gstage = gstage;
+    if (a.mlog) log_terms(P, dEp, g.pos);
   }
 }
 
@@ -945,6 +971,7 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
     const RepDev& rd0 = sh.ws.rd;
     setup_f32(sh.ws);
     sh.t0 = rd0.draw_pos;
+    sh.tlog = rd0.draw_pos;
     sh.run_dE = rd0.run_dE;
     sh.stop = 0;
     sh.cut = 0;
@@ -1010,6 +1037,7 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
               const double alpha = c.alpha, beta = 1 - c.alpha;
               for (int w = 0; w < cut; w++) {
                 const MovePlan& P = sh.plan[w];
+                if (a.mlog) log_move(a, rep, sh.t0 + (unsigned long long)w - sh.tlog, P);
                 if (P.empty) continue;
                 if (P.dec) run += P.dE;
                 rate = (P.dec ? alpha : 0.0) + beta * rate;

@@ -15,6 +15,11 @@
 // threads) race on it and give wrong results.  Calls on one stream are
 // ordered and safe.  The scratch does not need to start at zero: each call
 // clears the cells it uses on its stream before depositing.
+//
+// The first call on a device may load this library's device code there (with
+// CUDA's lazy module loading the module, and with it the 8 MiB array, is
+// created on first use): that call belongs in the caller's set-up phase, and
+// from the second call on nothing is created.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -28,11 +33,13 @@ namespace {
 using cg::GridF;
 using cg::RepDev;
 
-// 2^20 int64 cells (8 MiB) of grid, then the doubly-bound counters.  Enough
-// for a 64^3 grid with three binders (262,144 voxels x 4 columns) or 80^3
-// with one binder (512,000 voxels x 2 columns).
+// 2^20 int64 cells (8 MiB) of grid, then the doubly-bound counters and a
+// flag word set when a position is not finite.  Enough for a 64^3 grid with
+// three binders (262,144 voxels x 4 columns) or 80^3 with one binder
+// (512,000 voxels x 2 columns).
 constexpr long long kStaticCells = 1LL << 20;
-constexpr long long kStaticTotal = kStaticCells + CG_MAX_BINDERS;
+constexpr long long kStaticFlags = CG_MAX_BINDERS + 1;
+constexpr long long kStaticTotal = kStaticCells + kStaticFlags;
 __device__ __align__(256) long long g_static_scratch[kStaticTotal];
 
 // Device address of g_static_scratch, looked up once per device by the first
@@ -57,6 +64,9 @@ int scratch_on_device(long long** out) {
   return CG_OK;
 }
 
+// Device memory of the current device, or managed memory.  Memory of another
+// device is refused: the kernels run on the current device and would fault
+// on it without peer access.
 int device_pointer(const void* p, const char* name) {
   cudaPointerAttributes at;
   cudaError_t e = cudaPointerGetAttributes(&at, p);
@@ -66,12 +76,21 @@ int device_pointer(const void* p, const char* name) {
   }
   if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
     return cg::record_error(CG_ERR_ARG, std::string(name) + " must point to device memory");
+  if (at.type == cudaMemoryTypeDevice) {
+    int dev = -1;
+    e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cg::record_error(CG_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (at.device != dev)
+      return cg::record_error(CG_ERR_ARG, std::string(name) + " is memory of device " + std::to_string(at.device) +
+                                              ", not of the current device " + std::to_string(dev));
+  }
   return CG_OK;
 }
 
 // Every bead adds its eight fixed-point trilinear weights to the total-density
 // column and, times its bound count, to each binder's column
-// (update_all_densities_for_all_polymers, chromo/fields.pyx:2041-2106).
+// (update_all_densities_for_all_polymers, chromo/fields.pyx:2041-2106).  A bead
+// whose position is not finite deposits nothing and sets doubly[CG_MAX_BINDERS].
 __global__ void static_deposit_kernel(RepDev rd, const double* r, const long long* states,
                                       long long* grid, unsigned long long* doubly) {
   const int ncol = rd.nb + 1;
@@ -81,6 +100,10 @@ __global__ void static_deposit_kernel(RepDev rd, const double* r, const long lon
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < rd.n_beads;
        i += (long long)gridDim.x * blockDim.x) {
     const double p[3] = {r[3 * i], r[3 * i + 1], r[3 * i + 2]};
+    if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]))) {
+      atomicOr(doubly + CG_MAX_BINDERS, 1ull);
+      continue;
+    }
     double w[8];
     int v[8];
     cg::voxel_weights(rd, gf, p, w, v);
@@ -120,7 +143,7 @@ __device__ double static_block_sum(double v, double* sh) {
 // One block: the field energy of the grid in the consistent form
 // (chromo/fields.pyx:1939-2316 with the per-voxel terms of :1675-1875), plus
 // the intra-bead term of doubly bound beads; out[1] is the chi-free sum
-// S = sum_v (V / V_bead) vf^2.
+// S = sum_v (V / V_bead) vf^2 over the voxels at or below vf_limit.
 __global__ void static_energy_kernel(RepDev rd, const long long* grid, const unsigned long long* doubly,
                                      const double* access_vol, double* out) {
   __shared__ double sh[32];
@@ -135,7 +158,7 @@ __global__ void static_energy_kernel(RepDev rd, const long long* grid, const uns
       for (int e = 0; e < rd.nb; e++) fe += rd.xpref[b * CG_MAX_BINDERS + e] * rho[b] * rho[e];
     const double vf = ((double)grid[v * ncol] * cg::kFxInv) / V * rd.bead_vol;
     const double sv = (V / rd.bead_vol) * vf * vf;
-    sx += sv;
+    if (!(vf > rd.vf_limit)) sx += sv;  // above vf_limit the term is 1e99 vf, free of chi
     fe += vf > rd.vf_limit ? cg::kEHugeField * vf : rd.chi * sv;
   }
   const double t_fe = static_block_sum(fe, sh);
@@ -143,8 +166,9 @@ __global__ void static_energy_kernel(RepDev rd, const long long* grid, const uns
   if (threadIdx.x == 0) {
     double intra = 0;
     for (int b = 0; b < rd.nb; b++) intra += rd.intra[b] * (double)doubly[b];
-    out[0] = t_fe + intra;
-    out[1] = t_sx;
+    const bool bad = doubly[CG_MAX_BINDERS] != 0;  // a position was not finite
+    out[0] = bad ? __longlong_as_double(0x7FF8000000000000LL) : t_fe + intra;
+    out[1] = bad ? __longlong_as_double(0x7FF8000000000000LL) : t_sx;
   }
 }
 
@@ -199,7 +223,7 @@ extern "C" int cg_field_energy_static(const cg_field_params* f, int64_t n_beads,
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemsetAsync(grid, 0, sizeof(long long) * cells, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(doubly, 0, sizeof(unsigned long long) * CG_MAX_BINDERS, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(doubly, 0, sizeof(unsigned long long) * kStaticFlags, s);
   if (e != cudaSuccess) return cg::record_error(CG_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
   if (n_beads > 0) {
     long long blocks = (n_beads + 255) / 256;

@@ -245,11 +245,15 @@ class Chromatin(SSWLC):
 # ---- initial paths (chromo/util/poly_paths.py) ----
 
 def gaussian_walk(num_steps: int, step_sizes: np.ndarray) -> np.ndarray:
-    steps = np.random.standard_normal((num_steps, 3))
-    magnitude_steps = np.linalg.norm(steps, axis=1)
-    positions = np.cumsum(np.divide(steps, magnitude_steps[:, None]) * step_sizes[:, np.newaxis],
-                          axis=0)
-    return np.vstack((np.zeros(3), positions))
+    """Random walk of ``num_steps`` steps from the origin (num_steps + 1 points):
+    step k points along a direction drawn isotropically (a normalised
+    standard-normal 3-vector from numpy's global generator, all drawn as one
+    block) and has length ``step_sizes[k]`` (chromo/util/poly_paths.py:269-295)."""
+    dirs = np.random.standard_normal((num_steps, 3))
+    dirs = dirs / np.linalg.norm(dirs, axis=1)[:, None]
+    out = np.zeros((num_steps + 1, 3))
+    out[1:] = np.cumsum(dirs * np.asarray(step_sizes)[:, None], axis=0)
+    return out
 
 
 def in_confinement(point, confine_type, confine_length):
@@ -276,23 +280,7 @@ def confined_gaussian_walk(num_points, step_sizes, confine_type, confine_length)
 
 
 def estimate_tangents_from_coordinates(coordinates: np.ndarray):
-    """t3 from neighbouring coordinates, t2 orthogonal to it
-    (chromo/util/poly_paths.py:506-545)."""
-    n = coordinates.shape[0]
-    t3 = np.zeros((n, 3))
-    t2 = np.zeros((n, 3))
-    first = coordinates[1, :] - coordinates[0, :]
-    last = coordinates[n - 1, :] - coordinates[n - 2, :]
-    t3[0, :] = first / np.linalg.norm(first)
-    t3[n - 1, :] = last / np.linalg.norm(last)
-    for i in range(1, n - 1):
-        d = coordinates[i + 1, :] - coordinates[i - 1, :]
-        t3[i, :] = d / np.linalg.norm(d)
-    a1 = np.array([1, 0, 0])
-    a2 = np.array([0, 1, 0])
-    for i in range(n):
-        trial = np.cross(t3[i, :], a1)
-        if np.all(trial == 0):
-            trial = np.cross(t3[i, :], a2)
-        t2[i, :] = trial / np.linalg.norm(trial)
-    return t3, t2
+    """t3 from the neighbouring coordinates (one-sided at the two ends) and a
+    unit t2 perpendicular to it (chromo/util/poly_paths.py:506-545)."""
+    from .synthetic import tangents_from_coordinates
+    return tangents_from_coordinates(np.asarray(coordinates, dtype=float))

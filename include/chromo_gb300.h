@@ -170,6 +170,21 @@ int cg_run_audit(cg_sim *sim, int32_t rep, int64_t n_steps,
                  cg_move_record *records, int64_t max_records, int64_t *n_records,
                  int64_t *draws_used, int64_t *bstates_used);
 
+/* cg_run with a per-move log (blocking): the production kernel, at the sim's
+ * launch shape, runs n_steps MC steps of every replica from the state and
+ * move counters it holds, as cg_run does, and writes each attempted move's
+ * record, in move order, to records[rep * max_records + k] for the first
+ * max_records moves of each replica; n_records[rep] (R entries) receives the
+ * number of moves the replica attempted.  dE_poly and dE_field are the move's
+ * polymer and field dE, n_draws the number of draws it took from its own
+ * random sub-stream, accepted = -1 marks an empty move.  This is the device
+ * counterpart of the reference's per-move log (MCAdapter.accept / reject with
+ * log_move, chromo/mc/moves.pyx:156-300, into AcceptanceTracker.log_move,
+ * chromo/util/mc_stat.py:116-145); the parity tests replay the same moves on
+ * the CPU from it. */
+int cg_run_logged(cg_sim *sim, int64_t n_steps, uint64_t seed, cg_move_record *records,
+                  int64_t max_records, int64_t *n_records);
+
 /* FP64 energies of one replica, recomputed from the resident state:
  * out[0] elastic (SSWLC.compute_E, chromo/polymers.pyx:1348-1381),
  * out[1] binding free energy (sum of the single-site terms whose differences
@@ -182,8 +197,9 @@ int cg_reset_running_energy(cg_sim *sim);
 
 /* cg_energy for every replica at once: out [n_replicas x 5] = elastic,
  * binding, field (as cg_energy), running sum of accepted dE, and the chi-free
- * part S = sum_v (V / V_bead) vf^2 of the field energy (field = chi * S +
- * terms that do not depend on chi).  Work is enqueued on `stream`; the call
+ * part S = sum_v (V / V_bead) vf^2 of the field energy, over the voxels at or
+ * below vf_limit (field = chi * S + terms that do not depend on chi; a voxel
+ * above the limit costs 1e99 vf whatever chi is).  Work is enqueued on `stream`; the call
  * returns once out is filled. */
 int cg_energies(cg_sim *sim, double *out, void *stream);
 
@@ -258,6 +274,17 @@ int cg_get_launch_info(cg_sim *sim, int32_t *warps_per_block, int32_t *hash_slot
 int cg_get_launch_shape(cg_sim *sim, int32_t *warps_per_block, int32_t *lanes_per_move,
                         int32_t *moves_in_flight, int32_t *hash_slots);
 
+/* Per-round timing of cg_run_batched (no counterpart in the reference, which
+ * has no device): with capacity > 0 every captured round brackets its MC
+ * kernel with two CUDA event-record nodes, pointed before each launch at the
+ * next of `capacity` event pairs (a ring), so the kernel's duration is
+ * measured on the device inside the replayed graph.  0 turns it off.  Either
+ * way the next cg_run_batched captures its graph again. */
+int cg_set_round_timing(cg_sim *sim, int32_t capacity);
+/* Durations (ms) of the MC kernel of the last min(rounds run, capacity, max)
+ * timed rounds, oldest first; *count receives how many.  Waits for them. */
+int cg_get_round_times(cg_sim *sim, float *mc_ms, int32_t max, int32_t *count);
+
 /* Warps of the MC kernel for (storage precision, lanes per move) that fit one
  * SM's register file, or -1 for a shape that is not built.  No counterpart in
  * the reference; the autotuner derives its candidate shapes from it. */
@@ -267,7 +294,8 @@ int cg_mc_warps_per_sm(int32_t pos_fp64, int32_t lanes_per_move);
  * reference).  Deposits the chain into a fixed-point density grid and writes
  * out[0] = the field energy in the form cg_energy reports in its out[2]
  * (chromo/fields.pyx:1939-2316, :1675-1875, re-deposit of :2041-2106) and
- * out[1] = the chi-free sum S = sum_v (V / V_bead) vf^2.  For callers that
+ * out[1] = the chi-free sum S = sum_v (V / V_bead) vf^2 over the voxels at or
+ * below vf_limit; both are NaN when a position is not finite.  For callers that
  * must not allocate device memory (a server whose device memory belongs to its
  * own pool; code in which a cudaMalloc would stall work in flight).
  *
@@ -280,8 +308,12 @@ int cg_mc_warps_per_sm(int32_t pos_fp64, int32_t lanes_per_move);
  * The grid lives in a static device array of 1,048,576 int64 cells (8 MiB):
  * nx*ny*nz*(n_binders+1) above that is rejected with CG_ERR_ARG.  Each call
  * zeroes the cells it uses on `stream` first, so nothing needs to start at
- * zero.  The first call on each device looks up the array's address
- * (cudaGetSymbolAddress) and should come before any stream capture.  There is
+ * zero.  The first call on each device may load the library's device code
+ * there (under CUDA's lazy module loading the module, with its 8 MiB array, is
+ * created on first use) and looks up the array's address
+ * (cudaGetSymbolAddress): make it in the set-up phase, before any stream
+ * capture; from the second call on nothing is created.  Device pointers must
+ * belong to the current device (or be managed memory).  There is
  * one array per device: calls that overlap in time on one device (different
  * streams or host threads) race on it; calls on one stream are ordered. */
 int cg_field_energy_static(const cg_field_params *field, int64_t n_beads, const double *r,

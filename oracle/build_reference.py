@@ -12,6 +12,10 @@ reference is untouched.  ``oracle/ref_stubs`` supplies pandas / numba /
 matplotlib / pyximport stand-ins at import time.
 
 Usage:  python oracle/build_reference.py [--src /path/to/reference]
+
+The checkout is taken from ``--src``, else from the ``CHROMO_REFERENCE``
+environment variable, else from the mount point of this build container
+(``reference_source()``).
 """
 import argparse
 import os
@@ -84,6 +88,15 @@ def build(src: Path) -> Path:
     return OUT
 
 
+def reference_source():
+    """The reference checkout to build from: $CHROMO_REFERENCE, else the
+    container's read-only mount; None when neither holds chromo/."""
+    for cand in (os.environ.get("CHROMO_REFERENCE"), "/root/reference"):
+        if cand and (Path(cand) / "chromo").is_dir():
+            return Path(cand)
+    return None
+
+
 def sys_path_entries() -> list:
     """Paths to prepend to ``sys.path`` to import the built reference."""
     return [str(HERE / "ref_stubs"), str(OUT)]
@@ -91,6 +104,9 @@ def sys_path_entries() -> list:
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default="/root/reference")
+    ap.add_argument("--src", default=None)
     a = ap.parse_args()
-    print(build(Path(a.src)))
+    src = Path(a.src) if a.src else reference_source()
+    if src is None:
+        sys.exit("no reference checkout: pass --src or set CHROMO_REFERENCE")
+    print(build(src))

@@ -56,6 +56,12 @@
 #define OR_E_HUGE_POLY 1e25 /* chromo/polymers.pyx:35 */
 #define OR_E_HUGE_FIELD 1e99 /* chromo/fields.pyx:32 */
 #define OR_FX_SCALE 1099511627776.0 /* 2^40 */
+/* fixed_density = 1 (the GPU's formula): the 1e99 penalties are summed exactly
+ * in integer units of OR_HUGE_UNIT = 1e99 * 2^-40 -- a voxel above vf_limit
+ * holding n fixed-point units costs llrint(n * Vb / V) units (1e99 vf rounded
+ * once), a bead outside the confinement 2^40 units -- so a move's penalty does
+ * not depend on the order of its voxels. */
+#define OR_HUGE_UNIT (OR_E_HUGE_FIELD / OR_FX_SCALE)
 #define OR_MAXB 8
 
 enum { MV_CRANK = 0, MV_END_PIVOT = 1, MV_SLIDE = 2, MV_TANGENT = 3, MV_BINDING = 4 };
@@ -128,13 +134,50 @@ typedef struct {
     const int64_t *b;
     int64_t nb_, bpos;
     int err;
+    /* Philox mode (philox != 0): the GPU production kernel's random numbers.
+     * Every attempted move t has its own sub-streams: draw j is word j & 3 of
+     * Philox4x32-10 at counter (j >> 2, t_lo, t_hi, 0x2545F491) under `key`,
+     * shifted right by one (31 bits, the role of rand()); binding state k is
+     * umulhi(word k & 3 at counter (k >> 2, t_lo, t_hi, 0x7F4A7C15) under
+     * `keyb`, sites + 1).  pos / bpos restart at 0 for every move. */
+    int philox;
+    uint32_t key[2], keyb[2];
+    uint64_t t;
+    int64_t ties;   /* decisions taken from the followed run in the tie band */
 } or_rng;
 
 /* ---------------- random stream ---------------------------------------- */
 
+/* Philox4x32-10 (Salmon, Moraes, Dror and Shaw, SC'11): ten rounds of two
+ * 32 x 32 -> 64-bit multiplies with the published multipliers and Weyl key
+ * increments. */
+static void or_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3], k0 = key[0], k1 = key[1];
+    for (int i = 0; i < 10; i++) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c1 = (uint32_t)p1;
+        c3 = (uint32_t)p0;
+        c0 = n0;
+        c2 = n2;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+static uint32_t philox_word(const or_rng *g, const uint32_t key[2], uint32_t tag, uint64_t j)
+{
+    uint32_t ctr[4] = {(uint32_t)(j >> 2), (uint32_t)g->t, (uint32_t)(g->t >> 32), tag}, out[4];
+    or_philox(ctr, key, out);
+    return out[j & 3];
+}
+
 /* draws == NULL: take libc rand() itself, as the reference does (timing runs) */
 static int64_t rnd(or_rng *g)
 {
+    if (g->philox) return (int64_t)(philox_word(g, g->key, 0x2545F491u, (uint64_t)g->pos++) >> 1);
     if (!g->a) { g->pos++; return (int64_t)rand(); }
     if (g->pos >= g->n) { g->err = OR_ERR_DRAWS; return 0; }
     return (int64_t)g->a[g->pos++];
@@ -144,6 +187,10 @@ static double rndu(or_rng *g) { return (double)rnd(g) / OR_RAND_MAX; }
 
 static int64_t rnd_state(or_rng *g, int64_t n_tails)
 {
+    if (g->philox) {
+        uint32_t w = philox_word(g, g->keyb, 0x7F4A7C15u, (uint64_t)g->bpos++);
+        return (int64_t)(((uint64_t)w * (uint64_t)(n_tails + 1)) >> 32);
+    }
     if (!g->b) { g->bpos++; return (int64_t)(rand() % (int)(n_tails + 1)); }
     if (g->bpos >= g->nb_) { g->err = OR_ERR_BSTATES; return 0; }
     return g->b[g->bpos++];
@@ -602,9 +649,9 @@ void or_deposit_all(or_system *s)
  * trial positions.  The cubical branch for trial = 0 is nested under
  * "if trial == 1" in the reference and therefore always counts zero; that is
  * kept. */
-static double confinement_E(const or_system *s, int64_t n, int trial)
+static int64_t confinement_count(const or_system *s, int64_t n, int trial)
 {
-    if (s->confine_kind == 0) return 0.;
+    if (s->confine_kind == 0) return 0;
     int64_t out = 0;
     for (int64_t k = 0; k < n; k++) {
         double p[3];
@@ -617,7 +664,12 @@ static double confinement_E(const or_system *s, int64_t n, int trial)
                 if (fabs(p[j]) > s->confine_length / 2) out++;
         }
     }
-    return (double)out * OR_E_HUGE_FIELD;
+    return out;
+}
+
+static double confinement_E(const or_system *s, int64_t n, int trial)
+{
+    return (double)confinement_count(s, n, trial) * OR_E_HUGE_FIELD;
 }
 
 static void touch(or_system *s, int64_t v, int *is_new)
@@ -750,7 +802,8 @@ static int64_t doubly_bound(const or_system *s, int64_t n, int64_t b, int trial,
 }
 
 /* get_dE_binders_and_beads + nonspecific_interact_dE, fields.pyx:1675-1875 */
-static double dE_binders_and_beads(or_system *s, int64_t n, int state_change, int64_t bsel)
+static double dE_binders_and_beads(or_system *s, int64_t n, int state_change, int64_t bsel,
+                                   int64_t *huge)
 {
     int64_t nb = s->n_binders, nc = nb + 1;
     double dE = 0;
@@ -814,8 +867,12 @@ static double dE_binders_and_beads(or_system *s, int64_t n, int state_change, in
         double vf1 = ((double)(s->density_fx[v * nc] + s->dfx[v * nc]) / OR_FX_SCALE) / V * s->bead_vol;
         double k = s->chi * (V / s->bead_vol);
         if (vf1 > s->vf_limit || vf0 > s->vf_limit) {
-            c += (vf1 > s->vf_limit ? OR_E_HUGE_FIELD * vf1 : k * vf1 * vf1)
-               - (vf0 > s->vf_limit ? OR_E_HUGE_FIELD * vf0 : k * vf0 * vf0);
+            double u = s->bead_vol / V;
+            if (vf1 > s->vf_limit)
+                *huge += llrint((double)(s->density_fx[v * nc] + s->dfx[v * nc]) * u);
+            else c += k * vf1 * vf1;
+            if (vf0 > s->vf_limit) *huge -= llrint((double)s->density_fx[v * nc] * u);
+            else c -= k * vf0 * vf0;
         } else {
             c += k * ((vf1 - vf0) * (vf1 + vf0));
         }
@@ -833,6 +890,20 @@ static double dE_binders_and_beads(or_system *s, int64_t n, int state_change, in
 static double field_dE(or_system *s, int64_t n, int state_change, int64_t bsel)
 {
     double dE = 0;
+    if (s->fixed_density) {
+        /* the GPU's formula: exact penalty units (OR_HUGE_UNIT) */
+        int64_t huge = 0;
+        if (s->field_kind == 1) {
+            huge = (confinement_count(s, n, 1) - confinement_count(s, n, 0)) * (int64_t)OR_FX_SCALE;
+            return (double)huge * OR_HUGE_UNIT;
+        }
+        if (!state_change)
+            huge += (confinement_count(s, n, 1) - confinement_count(s, n, 0)) * (int64_t)OR_FX_SCALE;
+        change_in_density(s, n, state_change, bsel);
+        dE += dE_binders_and_beads(s, n, state_change, bsel, &huge);
+        if (huge) dE += (double)huge * OR_HUGE_UNIT;
+        return dE;
+    }
     if (s->field_kind == 1) {
         /* NullField.compute_dE evaluates confinement for every move type */
         dE = confinement_E(s, n, 1);
@@ -844,8 +915,8 @@ static double field_dE(or_system *s, int64_t n, int state_change, int64_t bsel)
         dE -= confinement_E(s, n, 0);
     }
     change_in_density(s, n, state_change, bsel);
-    if (!s->fixed_density) pyset_order(s);
-    dE += dE_binders_and_beads(s, n, state_change, bsel);
+    pyset_order(s);
+    dE += dE_binders_and_beads(s, n, state_change, bsel, NULL);
     return dE;
 }
 
@@ -983,7 +1054,11 @@ static void end_pivot_fulcrum(const or_system *s, int64_t ind0, int64_t indf, in
 /* Propose (move_funcs.pyx), evaluate dE (mc_sim.pyx:153-162), Metropolis
  * (:163-171), accept / reject (moves.pyx:156-286, fields.pyx:1968).
  * Returns n_inds (0: empty move, returned before dE as in mc_sim.pyx:150-151). */
-static int64_t mc_step(or_system *s, or_ctl *c, or_rng *g, or_record *rec)
+/* One attempted move.  forced (0 / 1, or -1 for none) is the decision of a
+ * run being followed: it replaces this move's own decision when the two
+ * differ and dE lies in the tie band |dE + ln u| <= 1e-5 max(1, |dE|), where
+ * the FP32 arithmetic of the followed run may legitimately decide otherwise. */
+static int64_t mc_step(or_system *s, or_ctl *c, or_rng *g, or_record *rec, int forced)
 {
     int64_t N = s->n_beads, nb = s->n_binders, n = 0, ind0 = 0, indf = 0, bsel = -1;
     int64_t draw0 = g->pos;
@@ -1141,8 +1216,13 @@ static int64_t mc_step(or_system *s, or_ctl *c, or_rng *g, or_record *rec)
         dE += dEp;
         dE += dEf;
         double ex = exp(-dE);
-        int acc = rndu(g) < ex;
+        double u = rndu(g);
+        int acc = u < ex;
         if (g->err) return g->err;
+        if (forced >= 0 && forced != acc && fabs(dE + log(u)) <= 1e-5 * fmax(1.0, fabs(dE))) {
+            acc = forced;
+            g->ties++;
+        }
         if (acc) {
             if (kind == MV_BINDING) {
                 for (int64_t k = 0; k < n; k++) s->states[s->inds[k] * nb + bsel] = s->new_states[k];
@@ -1203,14 +1283,11 @@ static void update_amplitudes(or_ctl *c)
     }
 }
 
-/* mc_sim, mc_sim.pyx:26-103 (one polymer).  Returns the number of records
- * written (attempted moves) or a negative error code. */
-int64_t or_mc_sim(or_system *s, or_ctl *ctl, int64_t n_ctl, int64_t n_steps,
-                  const uint32_t *draws, int64_t n_draws, int64_t *draw_pos,
-                  const int64_t *bstates, int64_t n_bstates, int64_t *bstate_pos,
-                  or_record *recs, int64_t max_recs)
+/* The step loop of mc_sim, mc_sim.pyx:88-103 (one polymer); follow as in
+ * mc_step, indexed by record. */
+static int64_t mc_loop(or_system *s, or_ctl *ctl, int64_t n_ctl, int64_t n_steps, or_rng *g,
+                       const int8_t *follow, int64_t n_follow, or_record *recs, int64_t max_recs)
 {
-    or_rng g = {draws, n_draws, *draw_pos, bstates, n_bstates, *bstate_pos, 0};
     int64_t nrec = 0;
     for (int64_t k = 0; k < n_steps; k++) {
         for (int64_t ci = 0; ci < n_ctl; ci++) {
@@ -1218,17 +1295,64 @@ int64_t or_mc_sim(or_system *s, or_ctl *ctl, int64_t n_ctl, int64_t n_steps,
             if (c->move_on == 1) {
                 for (int64_t j = 0; j < c->num_per_cycle; j++) {
                     or_record *rec = (recs && nrec < max_recs) ? &recs[nrec] : NULL;
-                    int64_t r = mc_step(s, c, &g, rec);
-                    if (r < 0) { *draw_pos = g.pos; *bstate_pos = g.bpos; return r; }
+                    int forced = (follow && nrec < n_follow) ? follow[nrec] : -1;
+                    if (g->philox) { g->pos = 0; g->bpos = 0; }
+                    int64_t r = mc_step(s, c, g, rec, forced);
+                    if (r < 0) return r;
                     nrec++;
+                    if (g->philox) g->t++;
                 }
             }
             update_amplitudes(c);
         }
     }
+    return nrec;
+}
+
+/* mc_sim, mc_sim.pyx:26-103 (one polymer).  Returns the number of records
+ * written (attempted moves) or a negative error code. */
+int64_t or_mc_sim(or_system *s, or_ctl *ctl, int64_t n_ctl, int64_t n_steps,
+                  const uint32_t *draws, int64_t n_draws, int64_t *draw_pos,
+                  const int64_t *bstates, int64_t n_bstates, int64_t *bstate_pos,
+                  or_record *recs, int64_t max_recs)
+{
+    or_rng g;
+    memset(&g, 0, sizeof g);
+    g.a = draws; g.n = n_draws; g.pos = *draw_pos;
+    g.b = bstates; g.nb_ = n_bstates; g.bpos = *bstate_pos;
+    int64_t r = mc_loop(s, ctl, n_ctl, n_steps, &g, NULL, 0, recs, max_recs);
     *draw_pos = g.pos;
     *bstate_pos = g.bpos;
-    return nrec;
+    return r;
+}
+
+/* mc_sim driven by the GPU production kernel's random numbers (see or_rng):
+ * replica `rep` of a run seeded with `seed`, starting at move counter
+ * *move_pos (advanced by the attempted moves).  follow (n_follow entries, or
+ * NULL) holds the followed run's decisions per attempted move (1, 0, -1 for an
+ * empty move); *ties receives how many tie-band decisions were taken from it. */
+int64_t or_mc_sim_philox(or_system *s, or_ctl *ctl, int64_t n_ctl, int64_t n_steps, uint64_t seed,
+                         int32_t rep, int64_t *move_pos, const int8_t *follow, int64_t n_follow,
+                         int64_t *ties, or_record *recs, int64_t max_recs)
+{
+    or_rng g;
+    memset(&g, 0, sizeof g);
+    g.philox = 1;
+    g.key[0] = (uint32_t)seed ^ ((uint32_t)rep * 0x85EBCA6Bu);
+    g.key[1] = (uint32_t)(seed >> 32) ^ 0x1B873593u;
+    g.keyb[0] = g.key[0] ^ 0x68E31DA4u;
+    g.keyb[1] = g.key[1] ^ 0xB5297A4Du;
+    g.t = (uint64_t)*move_pos;
+    int64_t r = mc_loop(s, ctl, n_ctl, n_steps, &g, follow, n_follow, recs, max_recs);
+    *move_pos = (int64_t)g.t;
+    if (ties) *ties = g.ties;
+    return r;
+}
+
+/* Known-answer hook: one Philox4x32-10 block (test infrastructure). */
+void or_kat_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    or_philox(ctr, key, out);
 }
 
 /* size helpers for the ctypes wrapper */

@@ -90,7 +90,11 @@ def lib(tag: str):
         L.or_mc_sim.argtypes = [C.POINTER(_System), C.POINTER(Ctl), _I, _I,
                                 _P, _I, C.POINTER(_I), _P, _I, C.POINTER(_I), _P, _I]
         L.or_mc_sim.restype = _I
+        L.or_mc_sim_philox.argtypes = [C.POINTER(_System), C.POINTER(Ctl), _I, _I, C.c_uint64, C.c_int32,
+                                       C.POINTER(_I), _P, _I, C.POINTER(_I), _P, _I]
+        L.or_mc_sim_philox.restype = _I
         L.or_kat_axis_rotation.argtypes = [_P, _P, C.c_double, _P]
+        L.or_kat_philox.argtypes = [_P, _P, _P]
         L.or_kat_transform.argtypes = [C.POINTER(_System), _I, _P, _P]
         assert L.or_sizeof_system() == C.sizeof(_System)
         assert L.or_sizeof_ctl() == C.sizeof(Ctl)
@@ -236,6 +240,35 @@ class OracleSystem:
         return recs[:n]
 
 
+def _mc_sim_philox(self, ctls, n_steps, seed, rep, move_pos=0, follow=None, max_records=None):
+    """``mc_sim`` driven by the GPU production kernel's random numbers: replica
+    ``rep`` of a run seeded with ``seed``, from move counter ``move_pos``.
+    ``follow`` (the GPU's ``accepted`` per attempted move) settles decisions in
+    the tie band |dE + ln u| <= 1e-5 max(1, |dE|).  Returns (records, move
+    counter after the run, tie-band decisions taken from ``follow``)."""
+    arr = (Ctl * len(ctls))(*ctls)
+    if max_records is None:
+        max_records = n_steps * sum(int(c.num_per_cycle) for c in ctls if c.move_on)
+    recs = np.zeros(max_records, dtype=RECORD_DTYPE)
+    fol = None if follow is None else np.ascontiguousarray(follow, dtype=np.int8)
+    mp, ties = _I(int(move_pos)), _I(0)
+    n = self._L.or_mc_sim_philox(C.byref(self._s), arr, len(ctls), int(n_steps), int(seed) & (2**64 - 1),
+                                 int(rep), C.byref(mp), None if fol is None else fol.ctypes.data,
+                                 0 if fol is None else len(fol), C.byref(ties),
+                                 recs.ctypes.data if max_records else None, max_records)
+    for i, c in enumerate(ctls):
+        C.memmove(C.byref(c), C.byref(arr[i]), C.sizeof(Ctl))
+    if n == -3:
+        raise ValueError("bead selection window larger than the polymer "
+                         "(chromo/util/bead_selection.pyx:86-89)")
+    if n < 0:
+        raise RuntimeError(f"oracle mc_sim error {n}")
+    return recs[:n], mp.value, ties.value
+
+
+OracleSystem.mc_sim_philox = _mc_sim_philox
+
+
 def make_ctl(move_name, *, amp_move, amp_bead, num_per_cycle=1, simple=True,
              bead_bounds=(0, 0), move_bounds=(0.0, 0.0), move_on=1, moves_in_average=20.0):
     c = Ctl()
@@ -248,6 +281,16 @@ def make_ctl(move_name, *, amp_move, amp_bead, num_per_cycle=1, simple=True,
     c.move_lo, c.move_hi = move_bounds
     c.acc_rate, c.alpha = 0.0, 2 / (moves_in_average + 1)
     return c
+
+
+def philox4x32_10(ctr, key, tag="f64"):
+    """One Philox4x32-10 block from the oracle (the generator of its Philox
+    mode), as four 32-bit words."""
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.zeros(4, dtype=np.uint32)
+    lib(tag).or_kat_philox(c.ctypes.data, k.ctypes.data, out.ctypes.data)
+    return [int(x) for x in out]
 
 
 def axis_rotation(axis, point, angle, tag="f64"):

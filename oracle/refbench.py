@@ -10,6 +10,12 @@ replicas of the benchmark workload through the reference's ``mc_sim`` for a
 time budget, and the aggregate rate is sum(attempted moves) / wall time.
 If the reference cannot be built, the C restatement (``chromo_oracle.c``)
 is timed instead and reported as kind "port".
+
+The timed window is matched to the GPU's: before timing, every sampled
+replica is brought to the state after ``settle_steps`` MC steps (the GPU
+benchmark's settle phase, after which the move controllers' bead amplitudes
+sit at their bounds) by the C restatement, and the reference then starts from
+that chain and those controller amplitudes and acceptance rates.
 """
 import multiprocessing as mp
 import os
@@ -57,7 +63,52 @@ def _ref_path():
             sys.path.insert(0, p)
 
 
-def _build_reference_replica(w, rep, chain):
+def _settled(w, rep, chain, settle_steps, seed):
+    """Replica `rep` after `settle_steps` MC steps of the C restatement (its
+    own libc rand() draws): (chain with the settled r, t3, t2, states;
+    [(amp_move, amp_bead, acc_rate) per controller]; the oracle system and its
+    controllers, for the port worker)."""
+    import copy
+    import ctypes
+    import numpy as np
+    from oracle.oracle import OracleSystem, make_ctl
+    from chromo_gb300.energetics import dss_parameters, field_prefactors
+    from chromo_gb300.workloads import (BEAD_RAD, BEAD_SPACING, HP1_E_MOD, HP1_E_NOMOD, LP,
+                                        NUM_PER_CYCLE, R_INT, SITES, VOXEL, amplitude_bounds,
+                                        binder_names)
+    n = len(chain.r)
+    _, eb, g, ep, epp, eta = dss_parameters(np.full(n - 1, BEAD_SPACING), LP)
+    nb = w.n_binders
+    vint = 4.0 / 3.0 * np.pi * R_INT ** 3
+    pref, intra, xpref = field_prefactors(w.eps, [vint] * nb, w.cross, binder_names(nb), VOXEL ** 3)
+    width = w.nbins * VOXEL
+    confine = {}
+    if getattr(w, "sphere_radius", 0) > 0:  # spherical confinement with accessible volumes
+        from chromo_gb300.workloads import _sphere_volumes
+        confine = dict(confine_kind=1, confine_length=float(w.sphere_radius),
+                       access_vol=_sphere_volumes(w.nbins, float(w.sphere_radius)))
+    o = OracleSystem(r=chain.r, t3=chain.t3, t2=chain.t2, states=chain.states, marks=chain.marks,
+                     eps_bend=eb, gamma=g, eps_par=ep, eps_perp=epp, eta=eta, sites=[SITES] * nb,
+                     e_mod=[HP1_E_MOD] * nb, e_nomod=[HP1_E_NOMOD] * nb, mu=w.mu[rep],
+                     nxyz=(w.nbins,) * 3, widths=(width,) * 3, chi=float(w.chi[rep]),
+                     bead_vol=4.0 / 3.0 * np.pi * BEAD_RAD ** 3, pref=pref, intra=intra,
+                     xpref=xpref, pos="f64", fixed_density=0, **confine)
+    o.deposit_all()
+    bead, move = amplitude_bounds(n)
+    ctls = [make_ctl(m, amp_move=move[m][0], amp_bead=int(bead[m][0]),
+                     num_per_cycle=NUM_PER_CYCLE[m], bead_bounds=bead[m], move_bounds=move[m])
+            for m in ["crank_shaft", "end_pivot", "slide", "tangent_rotation", "change_binding_state"]]
+    if settle_steps:
+        ctypes.CDLL(None).srand(seed)
+        o.mc_sim(ctls, settle_steps, None, None, max_records=0)
+    c = copy.copy(chain)
+    c.r, c.t3, c.t2 = o.r.copy(), o.t3.copy(), o.t2.copy()
+    c.states = o.states.copy()
+    amps = [(float(k.amp_move), int(k.amp_bead), float(k.acc_rate)) for k in ctls]
+    return c, amps, (o, ctls)
+
+
+def _build_reference_replica(w, rep, chain, amps=None):
     import numpy as np
     import chromo.binders as cb
     import chromo.mc as cmc
@@ -86,19 +137,25 @@ def _build_reference_replica(w, rep, chain):
                             chi=float(w.chi[rep]), **confine)
     bab, mab = cmc.get_amplitude_bounds([p])
     ctrls = all_moves("/tmp/chromo_refbench_logs", bab.bounds, mab.bounds, SimpleControl)
+    for c, a in zip(ctrls, amps or []):  # the settled amplitudes and acceptance rates
+        c.move.amp_move, c.move.amp_bead = a[0], a[1]
+        c.move.acceptance_tracker.acceptance_rate = a[2]
     return p, binders, f, ctrls
 
 
 def _ref_worker(args):
-    wname, reps, budget, seed = args
+    wname, reps, budget, seed, settle_steps = args
     _ref_path()
     import ctypes
     from chromo.mc.mc_sim import mc_sim
     from chromo_gb300.workloads import make_chains, make_workload
     w = make_workload(wname)
     chains = make_chains(w)
+    built = []
+    for r in reps:
+        c, amps, _ = _settled(w, r, chains[r], settle_steps, seed + r)
+        built.append(_build_reference_replica(w, r, c, amps))
     ctypes.CDLL(None).srand(seed)
-    built = [_build_reference_replica(w, r, chains[r]) for r in reps]
     attempts, t0 = 0, time.perf_counter()
     i = 0
     while time.perf_counter() - t0 < budget:
@@ -111,42 +168,14 @@ def _ref_worker(args):
 
 
 def _port_worker(args):
-    wname, reps, budget, seed = args
+    wname, reps, budget, seed, settle_steps = args
     for p in (str(ROOT), str(HERE)):
         if p not in sys.path:
             sys.path.insert(0, p)
-    import ctypes
-    import numpy as np
-    from oracle.oracle import OracleSystem, make_ctl
-    from chromo_gb300.energetics import dss_parameters, field_prefactors
-    from chromo_gb300.workloads import (BEAD_RAD, BEAD_SPACING, HP1_E_MOD, HP1_E_NOMOD, LP,
-                                        NUM_PER_CYCLE, R_INT, SITES, VOXEL, amplitude_bounds,
-                                        binder_names, make_chains, make_workload)
+    from chromo_gb300.workloads import make_chains, make_workload
     w = make_workload(wname)
     chains = make_chains(w)
-    ctypes.CDLL(None).srand(seed)
-    systems = []
-    for rep in reps:
-        c = chains[rep]
-        n = len(c.r)
-        _, eb, g, ep, epp, eta = dss_parameters(np.full(n - 1, BEAD_SPACING), LP)
-        nb = w.n_binders
-        vint = 4.0 / 3.0 * np.pi * R_INT ** 3
-        pref, intra, xpref = field_prefactors(w.eps, [vint] * nb, w.cross, binder_names(nb), VOXEL ** 3)
-        width = w.nbins * VOXEL
-        o = OracleSystem(r=c.r, t3=c.t3, t2=c.t2, states=c.states, marks=c.marks, eps_bend=eb,
-                         gamma=g, eps_par=ep, eps_perp=epp, eta=eta, sites=[SITES] * nb,
-                         e_mod=[HP1_E_MOD] * nb, e_nomod=[HP1_E_NOMOD] * nb, mu=w.mu[rep],
-                         nxyz=(w.nbins,) * 3, widths=(width,) * 3, chi=float(w.chi[rep]),
-                         bead_vol=4.0 / 3.0 * np.pi * BEAD_RAD ** 3, pref=pref, intra=intra,
-                         xpref=xpref, pos="f64", fixed_density=0)
-        o.deposit_all()
-        bead, move = amplitude_bounds(n)
-        ctls = [make_ctl(m, amp_move=move[m][0], amp_bead=int(bead[m][0]),
-                         num_per_cycle=NUM_PER_CYCLE[m], bead_bounds=bead[m], move_bounds=move[m])
-                for m in ["crank_shaft", "end_pivot", "slide", "tangent_rotation",
-                          "change_binding_state"]]
-        systems.append((o, ctls))
+    systems = [_settled(w, rep, chains[rep], settle_steps, seed + rep)[2] for rep in reps]
     attempts, t0, i = 0, time.perf_counter(), 0
     while time.perf_counter() - t0 < budget:
         o, ctls = systems[i % len(systems)]
@@ -157,8 +186,9 @@ def _port_worker(args):
     return attempts, time.perf_counter() - t0
 
 
-def run(workload="batched", budget=2.0, n_procs=None, prefer="reference"):
-    """Aggregate attempted moves/s of the CPU implementation on this host."""
+def run(workload="batched", budget=2.0, n_procs=None, prefer="reference", settle_steps=0):
+    """Aggregate attempted moves/s of the CPU implementation on this host, from
+    the state after `settle_steps` MC steps of every sampled replica."""
     if str(ROOT) not in sys.path:
         sys.path.insert(0, str(ROOT))
     from chromo_gb300.workloads import make_workload
@@ -177,13 +207,14 @@ def run(workload="batched", budget=2.0, n_procs=None, prefer="reference"):
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(n_procs) as pool:
-        res = pool.map(worker, [(workload, reps[i][:2], budget, 1234 + i) for i in range(n_procs)])
+        res = pool.map(worker, [(workload, reps[i][:2], budget, 1234 + i, settle_steps)
+                                for i in range(n_procs)])
     wall = max(r[1] for r in res)
     attempts = sum(r[0] for r in res)
     return {"value": attempts / wall, "unit": "moves/s", "cores": n_procs, "kind": kind,
             "sample": (f"{workload} workload: {n_procs} spawn workers x {budget:.1f} s, each cycling "
-                       f"{min(2, len(reps[0]))} of its replicas through mc_sim one step at a time; "
-                       f"{attempts} attempted moves"),
+                       f"{min(2, len(reps[0]))} of its replicas through mc_sim one step at a time "
+                       f"from the state after {settle_steps} settle MC steps; {attempts} attempted moves"),
             "fallback_reason": reason, "elapsed_s": time.perf_counter() - t0}
 
 

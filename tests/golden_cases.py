@@ -42,8 +42,9 @@ def oracle_ctls(g):
     return out
 
 
-def gpu_sim(g, pos_fp64, state="0"):
-    """A one-replica ``chromo_gb300._native.Sim`` holding a golden case."""
+def gpu_sim(g, pos_fp64, state="0", warps_per_block=0, lanes_per_move=0):
+    """A one-replica ``chromo_gb300._native.Sim`` holding a golden case (at the
+    library's default launch shape unless one is given)."""
     from chromo_gb300 import _native as nat
     from chromo_gb300.device import binding_params, bonds_array, field_params, move_ctl
     n, nb = g["states0"].shape
@@ -53,7 +54,8 @@ def gpu_sim(g, pos_fp64, state="0"):
     max_tan = int(max(ctl0[3][1], ctl0[3][5]))
     access = g.get("access_vols")
     sim = nat.Sim([n], [list(g["nxyz"])], nb, pos_fp64=pos_fp64, max_segment=max_seg,
-                  max_tangent=max_tan, nonuniform_access=access is not None)
+                  max_tangent=max_tan, nonuniform_access=access is not None,
+                  warps_per_block=warps_per_block, lanes_per_move=lanes_per_move)
     sim.set_chain(0, r=g["r" + state], t3=g["t3" + state], t2=g["t2" + state],
                   states=g["states" + state], marks=g["marks"],
                   bonds=bonds_array(g["eps_bend"], g["gamma"], g["eps_par"], g["eps_perp"], g["eta"]))

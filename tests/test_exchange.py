@@ -40,9 +40,13 @@ def exchange_uniform(seed, round_, rung):
     return (o[0] >> 1) / 2147483647.0
 
 
-def chi_free_sum(grid, vol_bin, bead_vol):
+def chi_free_sum(grid, vol_bin, bead_vol, vf_limit=0.5):
+    """S = sum of (V / Vb) vf^2 over the voxels at or below vf_limit: the part of
+    the field energy that chi multiplies (a voxel above the limit costs 1e99 vf,
+    chromo/fields.pyx:1832-1840, whatever chi is)."""
     vf = (grid[:, 0].astype(np.float64) * 2.0 ** -40) / vol_bin * bead_vol
-    return float(np.sum((vol_bin / bead_vol) * vf * vf))
+    keep = ~(vf > vf_limit)
+    return float(np.sum((vol_bin / bead_vol) * vf[keep] * vf[keep]))
 
 
 def expected_exchange(chi, S, rep_of_rung, n_rungs, round_, seed, tie=1e-9):
@@ -216,5 +220,47 @@ def test_mu_ladder_rounds_match_host_rule():
         counts = sim.swap_counts()
         assert int(counts["mu_swaps"].sum()) == mu_total
         assert 0 < mu_total < int(counts["mu_attempts"].sum())
+    finally:
+        sim.close()
+
+
+@pytest.mark.gpu
+def test_exchange_with_voxel_above_vf_limit():
+    """One replica holds a voxel above vf_limit (half its chain packed into one
+    voxel).  That voxel's 1e99 vf does not depend on chi, so the true energy
+    change of a chi swap is -(chi_a - chi_b)(S_a - S_b) with S over the voxels
+    at or below the limit only: the device's S equals that host sum, differs
+    from the sum over all voxels, and every swap decision follows it."""
+    pytest.importorskip("torch")
+    from chromo_gb300 import workloads as wl
+    w, sim = _small_ladder_sim()
+    S0 = _chi_sums(sim, w)
+    sim.close()
+    chi = np.tile(np.arange(4) / max(float(np.std(S0)), 1e-12), 2)
+    w, sim = _small_ladder_sim(chi)
+    try:
+        r, t3, t2, st = sim.get_chain(0)
+        rng = np.random.default_rng(3)
+        r[:200] = 20.0 + rng.uniform(-2.0, 2.0, size=(200, 3))  # 200 beads inside one 40 nm voxel
+        sim.set_chain(0, r=r)
+        sim.deposit(-1)
+        vol_bin, bead_vol = wl.VOXEL ** 3, 4.0 / 3.0 * np.pi * wl.BEAD_RAD ** 3
+        g0 = sim.density(0)
+        vf = (g0[:, 0].astype(np.float64) * 2.0 ** -40) / vol_bin * bead_vol
+        assert vf.max() > 0.5
+        S = _chi_sums(sim, w)
+        S_all0 = float(np.sum((vol_bin / bead_vol) * vf * vf))
+        assert S_all0 > S[0] * 1.5, "the over-limit voxel must matter to the test"
+        dev = sim.energies()[:, 4]
+        np.testing.assert_allclose(dev, S, rtol=1e-12)
+        seed, ror, cur = 4242, np.arange(w.replicas), sim.chi()
+        for rnd in range(6):
+            S = _chi_sums(sim, w)
+            want, ror, _, ties = expected_exchange(cur, S, ror, 4, rnd, seed)
+            sim.exchange(4, rnd, seed)
+            got = sim.chi()
+            if not ties:
+                np.testing.assert_array_equal(got, want)
+            cur = got
     finally:
         sim.close()

@@ -88,6 +88,57 @@ def test_static_field_energy_matches_sim_on_10k_chain():
     assert second[0] == first[0] and second[1] == first[1]
 
 
+def _plain_field():
+    from chromo_gb300 import workloads as wl
+    from chromo_gb300.device import field_params
+    from chromo_gb300.energetics import field_prefactors
+    w = wl.make_workload("plain")
+    vint = 4.0 / 3.0 * np.pi * wl.R_INT ** 3
+    pref, intra, xpref = field_prefactors(w.eps, [vint], w.cross, wl.binder_names(1), wl.VOXEL ** 3)
+    return w, field_params(field_kind=2, nxyz=(w.nbins,) * 3, widths=(w.nbins * wl.VOXEL,) * 3,
+                           n_binders=1, chi=1.0, vf_limit=0.5,
+                           bead_vol=4.0 / 3.0 * np.pi * wl.BEAD_RAD ** 3, pref=pref, intra=intra,
+                           xpref=xpref)
+
+
+@pytest.mark.gpu
+def test_static_field_energy_reports_nonfinite_position():
+    """A position that is not finite makes both outputs NaN (the call itself
+    succeeds: the check runs on the device), and the next call with finite
+    positions is correct again."""
+    pytest.importorskip("torch")
+    from chromo_gb300 import workloads as wl
+    w, fp = _plain_field()
+    c = wl.make_chains(w)[0]
+    r = c.r.copy()
+    r[17, 1] = np.nan
+    bad = _static_energies(fp, r, c.states, calls=1)[0]
+    assert np.isnan(bad).all()
+    good = _static_energies(fp, c.r, c.states, calls=1)[0]
+    assert np.isfinite(good).all()
+
+
+@pytest.mark.gpu
+def test_static_field_energy_second_call_allocates_nothing():
+    """After the first call on the device (which may load the module), a call
+    leaves the device's free memory exactly as it found it."""
+    torch = pytest.importorskip("torch")
+    from chromo_gb300 import workloads as wl
+    w, fp = _plain_field()
+    c = wl.make_chains(w)[0]
+    r = torch.tensor(np.ascontiguousarray(c.r), device="cuda")
+    st = torch.tensor(np.ascontiguousarray(c.states), device="cuda")
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    _call(fp, int(r.shape[0]), r.data_ptr(), st.data_ptr(), out.data_ptr(), stream)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        _call(fp, int(r.shape[0]), r.data_ptr(), st.data_ptr(), out.data_ptr(), stream)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
 def test_static_field_energy_rejects_grid_beyond_scratch():
     """Checked before any CUDA call, so it runs without a GPU."""
     from chromo_gb300 import _native as nat

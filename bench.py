@@ -112,6 +112,7 @@ def profile_case(args):
 # their bounds (150 beads) and the per-round cost has stopped growing.
 SETTLE_ROUNDS = 80
 TUNE_WARMUP, TUNE_STEPS = 62, 124  # from the settled state: one round of warm-up, two timed
+GUARD_TOL_ABS, GUARD_TOL_REL = 20.0, 1e-3  # drift guard bound per check (kT, relative to |E|)
 
 
 def settled_state(w, chains, stream, rounds=SETTLE_ROUNDS, sim=None):
@@ -155,6 +156,18 @@ def _tune_child(workload, rank, local):
     autotune.tune(lambda W, G: build_settled(w, chains, snap, warps_per_block=W, lanes_per_move=G),
                   w.lengths, [[w.nbins] * 3] * w.replicas, w.n_binders, steps=TUNE_STEPS,
                   warmup=TUNE_WARMUP, extra_key=workload + "-settled")
+
+
+def _guard_report(sim, every, moves_per_round):
+    """The on-device drift guard's checks (large workload), or None."""
+    if not every:
+        return None
+    import numpy as np
+    d, checks = sim.drift()
+    return {"every_rounds": every, "moves_per_replica_between_checks": every * moves_per_round,
+            "checks": checks, "max_abs_drift_kT": float(np.abs(d).max()),
+            "median_abs_drift_kT": float(np.median(np.abs(d))),
+            "bound": "%g kT + %g |E|" % (GUARD_TOL_ABS, GUARD_TOL_REL)}
 
 
 def _at_bound(ctls):
@@ -384,6 +397,14 @@ def main():
         sim.set_mu_ladder(w.mu_rungs, 0)
     steps_round = w.steps_per_round
     moves_round = w.replicas * steps_round * w.moves_per_step
+    guard_every, guard = 0, None
+    if args.workload == "large":
+        # the on-device FP64 full-energy recompute every ~1e5 moves per replica,
+        # inside the captured round; the tolerance covers the reference's
+        # tangent-rotation rule for adjacent beads (its summed dE is not the
+        # energy change) and FP32 rounding
+        guard_every = int(np.ceil(1e5 / (steps_round * w.moves_per_step)))
+        sim.set_drift_guard(guard_every, tol_abs=GUARD_TOL_ABS, tol_rel=GUARD_TOL_REL)
     warm = max(args.warmup, 3)
     # the MC kernel of every round is timed on the device (event-record nodes
     # in the replayed graph), settle and warm-up rounds included
@@ -469,6 +490,9 @@ def main():
     sim.set_chains([dict(r=r, t3=t3, t2=t2, states=st) for r, t3, t2, st in start_chains])  # pinned staging
     for r in range(w.replicas):
         sim.set_controllers(r, start_ctl[r])
+    if guard_every:  # the guard's reference energies belong to the state just uploaded
+        guard = _guard_report(sim, guard_every, steps_round * w.moves_per_step)
+        sim.set_drift_guard(guard_every, tol_abs=GUARD_TOL_ABS, tol_rel=GUARD_TOL_REL)
     inp = start_chains
     t_e2e = 0.0
     for k in range(args.steps):
@@ -571,6 +595,7 @@ def main():
                                              "workload": "the same chain, one warp, 100 MC steps",
                                              "batched_over": value / seq_value}},
             "energy_drift": drift,
+            "drift_guard": guard,
             "gpu_launches": launches,
             "clocks": clocks.summary(),
             "phase_seconds": phases,

@@ -15,7 +15,7 @@ MAX_MARK = 3
 MOVE_NAMES = ["crank_shaft", "end_pivot", "slide", "tangent_rotation", "change_binding_state"]
 
 STATUS = {0: "ok", -1: "argument", -2: "cuda", -3: "window", -4: "stream", -5: "nonfinite",
-          -6: "spin", -7: "nomem"}
+          -6: "spin", -7: "nomem", -8: "drift"}
 
 
 class CgError(RuntimeError):
@@ -55,6 +55,7 @@ class FieldParams(C.Structure):
         ("chi", C.c_double), ("vf_limit", C.c_double), ("bead_vol", C.c_double),
         ("pref", C.c_double * MAX_BINDERS), ("intra", C.c_double * MAX_BINDERS),
         ("xpref", C.c_double * (MAX_BINDERS * MAX_BINDERS)),
+        ("fast_field", C.c_int32), ("n_points", C.c_int32),
     ]
 
 
@@ -85,7 +86,7 @@ EXPORTS = [
     "cg_field_energy_static", "cg_energies", "cg_set_chains", "cg_get_chains", "cg_gradient",
     "cg_sample_terms", "cg_get_samples", "cg_get_launch_shape", "cg_mc_warps_per_sm",
     "cg_set_mu_ladder", "cg_get_mu", "cg_get_swap_counts", "cg_run_logged", "cg_set_round_timing",
-    "cg_get_round_times",
+    "cg_get_round_times", "cg_set_drift_guard", "cg_get_drift",
 ]
 N_TERMS = 14
 
@@ -121,6 +122,8 @@ def lib():
             "cg_run_logged": ([P, I64, C.c_uint64, P, I64, P], C.c_int),
             "cg_set_round_timing": ([P, I32], C.c_int),
             "cg_get_round_times": ([P, P, I32, P], C.c_int),
+            "cg_set_drift_guard": ([P, I32, D, D], C.c_int),
+            "cg_get_drift": ([P, P, P], C.c_int),
             "cg_energy": ([P, I32, P], C.c_int),
             "cg_reset_running_energy": ([P], C.c_int),
             "cg_get_tally": ([P, I32, P], C.c_int),
@@ -387,6 +390,18 @@ class Sim:
     def run_batched(self, n_rounds, n_steps, n_rungs, seed, stream=None):
         check(lib().cg_run_batched(self.h, int(n_rounds), int(n_steps), int(n_rungs),
                                    int(seed) & (2**64 - 1), stream))
+
+    def set_drift_guard(self, every_rounds, tol_abs=0.0, tol_rel=0.0):
+        """Check every ``every_rounds``-th ``run_batched`` round's recomputed
+        FP64 energies against the running sums on the device (0: off)."""
+        check(lib().cg_set_drift_guard(self.h, int(every_rounds), float(tol_abs), float(tol_rel)))
+
+    def drift(self):
+        """(drift at each replica's last check [R], checks made)."""
+        out = np.zeros(self.R)
+        n = C.c_int64()
+        check(lib().cg_get_drift(self.h, _ptr(out), C.byref(n)))
+        return out, n.value
 
     def set_round_timing(self, capacity):
         """Time the MC kernel of every ``run_batched`` round on the device

@@ -124,6 +124,28 @@ struct cg_sim {
     timing_cap = 0;
     timing_count = 0;
   }
+  // drift guard of the batched rounds (cg_set_drift_guard)
+  int guard_every = 0, guard_chunks = 1;
+  double guard_tol_abs = 0, guard_tol_rel = 0;
+  double *guard_partial = nullptr, *guard_e_ref = nullptr, *guard_run_ref = nullptr, *guard_drift = nullptr;
+  int* guard_init = nullptr;
+  unsigned long long* guard_counter = nullptr;
+  cg::GuardArgs guard_args() const {
+    cg::GuardArgs g{};
+    g.every = guard_every; g.chunks = guard_chunks; g.tol_abs = guard_tol_abs; g.tol_rel = guard_tol_rel;
+    g.partial = guard_partial; g.e_ref = guard_e_ref; g.run_ref = guard_run_ref; g.drift = guard_drift;
+    g.init = guard_init; g.counter = guard_counter;
+    return g;
+  }
+  void free_guard() {
+    void* ptrs[] = {guard_partial, guard_e_ref, guard_run_ref, guard_drift, guard_init, guard_counter};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+    guard_partial = guard_e_ref = guard_run_ref = guard_drift = nullptr;
+    guard_init = nullptr;
+    guard_counter = nullptr;
+    guard_every = 0;
+  }
   // derivatives: per-bead gradient, per-replica terms, running sums (allocated on first use)
   float* grad = nullptr;
   double* terms = nullptr;
@@ -243,6 +265,7 @@ const char* cg_last_error(void) { return g_err.c_str(); }
 void cg_destroy(cg_sim* s) {
   if (!s) return;
   s->drop_timing();
+  s->free_guard();
   if (s->pinned) cudaFreeHost(s->pinned);
   void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
                   s->bonds32, s->grid, s->access_vol, s->access_sc, s->access_vb, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
@@ -657,6 +680,12 @@ int cg_set_field(cg_sim* s, int rep, const cg_field_params* f, const double* acc
   for (int b = 0; b < CG_MAX_BINDERS; b++) { d.pref[b] = f->pref[b]; d.intra[b] = f->intra[b]; }
   for (int b = 0; b < CG_MAX_BINDERS * CG_MAX_BINDERS; b++) d.xpref[b] = f->xpref[b];
   d.has_access = access_vol ? 1 : 0;
+  if (f->fast_field && f->field_kind == 2) {
+    if (f->n_points < 1 || f->n_points > (1 << 20)) return fail(CG_ERR_ARG, "n_points must be in 1..2^20");
+    d.fast_n = f->n_points + (f->n_points % 2);  // init_fast_field rounds up to even
+  } else {
+    d.fast_n = 0;
+  }
   if (access_vol) {
     // the factors the MC kernel's FP32 field terms need per voxel, in the
     // same FP64 arithmetic the kernel would do per touched voxel
@@ -764,6 +793,9 @@ static int device_errors(cg_sim* s) {
   if (any & cg::E_WINDOW) return fail(CG_ERR_WINDOW, std::string(msg) + ": bead selection window must be less than polymer length");
   if (any & cg::E_STREAM) return fail(CG_ERR_STREAM, std::string(msg) + ": supplied random stream exhausted");
   if (any & cg::E_NONFINITE) return fail(CG_ERR_NONFINITE, std::string(msg) + ": non-finite position");
+  if (any & cg::E_DRIFT)
+    return fail(CG_ERR_DRIFT, std::string(msg) + ": recomputed energy left the running sum of dE by more than "
+                              "the drift guard's bound (cg_get_drift)");
   return fail(CG_ERR_SPIN, std::string(msg) + ": iteration cap reached");
 }
 
@@ -1039,6 +1071,7 @@ int cg_run_batched(cg_sim* s, int64_t n_rounds, int64_t n_steps, int32_t n_rungs
       cg_launch_spec(a, s->fp64, s->spec_bytes, cap);
       if (timed) cudaEventRecordWithFlags(s->cap_end[k], cap, cudaEventRecordExternal);
       if (n_rungs) enqueue_exchange(s, n_rungs, -1, seed, cap);
+      if (s->guard_every) cg_launch_guard(a, s->guard_args(), s->fp64, cap);
     }
     cudaError_t e = cudaStreamEndCapture(cap, &gr);
     cudaStreamDestroy(cap);
@@ -1082,6 +1115,50 @@ int cg_run_batched(cg_sim* s, int64_t n_rounds, int64_t n_steps, int32_t n_rungs
   CUDA_TRY(cudaGraphLaunch(s->graph, st));
   if (timed) s->timing_count += n_rounds;
   s->kernels += n_rounds;
+  return CG_OK;
+}
+
+int cg_set_drift_guard(cg_sim* s, int32_t every_rounds, double tol_abs, double tol_rel) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (every_rounds < 0) return fail(CG_ERR_ARG, "every_rounds must be >= 0");
+  if (!(tol_abs >= 0) || !(tol_rel >= 0)) return fail(CG_ERR_ARG, "tolerances must be >= 0");
+  CUDA_TRY(cudaDeviceSynchronize());
+  s->drop_graph();  // the guard's launches are part of the captured round
+  s->free_guard();
+  if (every_rounds == 0) return CG_OK;
+  // enough chunk x replica blocks to spread one recompute over the GPU
+  const int chunks = (int)std::max<long long>(1, std::min<long long>(64, (4LL * std::max(s->n_sm, 1) + s->R - 1) / s->R));
+  const size_t R = (size_t)s->R;
+  cudaError_t e = cudaMalloc(&s->guard_partial, sizeof(double) * R * chunks * 6);
+  if (e == cudaSuccess) e = cudaMalloc(&s->guard_e_ref, sizeof(double) * R);
+  if (e == cudaSuccess) e = cudaMalloc(&s->guard_run_ref, sizeof(double) * R);
+  if (e == cudaSuccess) e = cudaMalloc(&s->guard_drift, sizeof(double) * R);
+  if (e == cudaSuccess) e = cudaMalloc(&s->guard_init, sizeof(int) * R);
+  if (e == cudaSuccess) e = cudaMalloc(&s->guard_counter, sizeof(unsigned long long) * 2);
+  if (e == cudaSuccess) e = cudaMemset(s->guard_drift, 0, sizeof(double) * R);
+  if (e == cudaSuccess) e = cudaMemset(s->guard_init, 0, sizeof(int) * R);
+  if (e == cudaSuccess) e = cudaMemset(s->guard_counter, 0, sizeof(unsigned long long) * 2);
+  if (e != cudaSuccess) {
+    s->free_guard();
+    return fail(CG_ERR_NOMEM, std::string("drift guard buffers: ") + cudaGetErrorString(e));
+  }
+  s->guard_every = every_rounds;
+  s->guard_chunks = chunks;
+  s->guard_tol_abs = tol_abs;
+  s->guard_tol_rel = tol_rel;
+  return CG_OK;
+}
+
+int cg_get_drift(cg_sim* s, double* drift, int64_t* checks) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (!s->guard_every) return fail(CG_ERR_ARG, "the drift guard is off (cg_set_drift_guard)");
+  CUDA_TRY(cudaDeviceSynchronize());
+  if (drift) CUDA_TRY(cudaMemcpy(drift, s->guard_drift, sizeof(double) * s->R, cudaMemcpyDeviceToHost));
+  if (checks) {
+    unsigned long long c[2];
+    CUDA_TRY(cudaMemcpy(c, s->guard_counter, sizeof c, cudaMemcpyDeviceToHost));
+    *checks = (int64_t)c[1];
+  }
   return CG_OK;
 }
 

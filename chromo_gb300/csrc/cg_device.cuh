@@ -31,7 +31,7 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxIter = 4096;                          // cap on resampling loops
 
 // device-side error bits (mapped to cg_status on the host)
-enum : unsigned { E_WINDOW = 1u, E_STREAM = 2u, E_NONFINITE = 4u, E_SPIN = 8u };
+enum : unsigned { E_WINDOW = 1u, E_STREAM = 2u, E_NONFINITE = 4u, E_SPIN = 8u, E_DRIFT = 32u };
 // internal: a move's shared-memory voxel table filled up (the move is then
 // evaluated again with its global-memory table; never reported)
 constexpr unsigned E_OVF = 16u;
@@ -46,11 +46,12 @@ struct RepDev {
   int field_kind, confine_kind, max_binders, has_access;
   double confine_length, chi, vf_limit, bead_vol;
   double pref[CG_MAX_BINDERS], intra[CG_MAX_BINDERS], xpref[CG_MAX_BINDERS * CG_MAX_BINDERS];
-  int sites[CG_MAX_BINDERS], pad0;
+  int sites[CG_MAX_BINDERS], fast_n;  // fast_n: sub-bins per voxel of the move deposits (0: exact)
   double mu[CG_MAX_BINDERS], mu_adjust;
   double bind_f[CG_MAX_BINDERS * (CG_MAX_MARK + 1) * (CG_MAX_MARK + 1)];
   unsigned long long draw_pos, bstate_pos;
   double run_dE;
+  double xch_dE;  // energy change of this replica's accepted chi / mu swaps
   unsigned err, pad1;
 };
 
@@ -544,6 +545,7 @@ __device__ __forceinline__ float pymodf(float a, float b) {
 // FP32 copies of the grid geometry, derived once per launch
 struct GridF {
   float w[3], half_w[3], half_d[3], inv_d[3];
+  float sw[3], inv_sw[3], nsub[3], half_np;  // fast_field sub-bins (FP32 storage)
   int n[3], nx, nxy;
 };
 
@@ -557,7 +559,12 @@ __device__ __forceinline__ void make_gridf(const RepDev& rd, GridF& gf) {
     gf.half_d[j] = (float)(0.5 * d);
     gf.inv_d[j] = (float)(1.0 / d);
     gf.n[j] = n[j];
+    const int np = rd.fast_n > 0 ? rd.fast_n : 1;
+    gf.sw[j] = (float)(d / (double)np);
+    gf.inv_sw[j] = (float)((double)np / d);
+    gf.nsub[j] = (float)((double)np * n[j]);
   }
+  gf.half_np = (float)(0.5 * (rd.fast_n > 0 ? rd.fast_n : 1));
   gf.nx = rd.nx;
   gf.nxy = rd.nx * rd.ny;
 }
@@ -596,6 +603,61 @@ __device__ __forceinline__ void voxel_axes(const RepDev&, const GridF& gf, const
   }
 }
 
+// The sub-bin version of voxel_axes for per-move density changes with
+// fast_field (get_change_in_density_quickly, fields.pyx:1235-1368, with the
+// tables of init_fast_field, :577-671): each coordinate is moved to the lower
+// edge of its sub-bin, floor((x + L/2) / w_sub) mod (n_points n), w_sub =
+// d / n_points, and the voxel and weight are those of that edge, shifted by
+// half a voxel.  FP64: the reference's arithmetic.
+__device__ __forceinline__ void fast_axes(const RepDev& rd, const GridF&, const double pos[3],
+                                          double wl[3], int lo[3], int hi[3]) {
+  const double width[3] = {rd.wx, rd.wy, rd.wz};
+  const int n[3] = {rd.nx, rd.ny, rd.nz};
+  const double np = (double)rd.fast_n;
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const double d = width[j] / (double)n[j];
+    const double sw = d / np;
+    const double sb = pymod(floor((pos[j] + 0.5 * width[j]) / sw), np * (double)n[j]);
+    const double q = ((sb - np / 2) * sw) / d;
+    const double ind = floor(q);
+    const int li = ind == -1.0 ? n[j] - 1 : (int)ind;
+    lo[j] = li < 0 ? 0 : (li >= n[j] ? n[j] - 1 : li);
+    hi[j] = lo[j] + 1 == n[j] ? 0 : lo[j] + 1;
+    wl[j] = 1 - (q - ind);
+  }
+}
+// FP32 storage: the same construction in binary32.
+__device__ __forceinline__ void fast_axes(const RepDev&, const GridF& gf, const float pos[3], float wl[3],
+                                          int lo[3], int hi[3]) {
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const float sb = pymodf(floorf((pos[j] + gf.half_w[j]) * gf.inv_sw[j]), gf.nsub[j]);
+    const float q = ((sb - gf.half_np) * gf.sw[j]) * gf.inv_d[j];
+    const float fl = floorf(q);
+    const int ind = (int)fl;
+    const int li = ind == -1 ? gf.n[j] - 1 : ind;
+    lo[j] = li < 0 ? 0 : (li >= gf.n[j] ? gf.n[j] - 1 : li);
+    hi[j] = lo[j] + 1 == gf.n[j] ? 0 : lo[j] + 1;
+    wl[j] = 1 - (q - fl);
+  }
+}
+// Per-axis voxels and weights of a move's density change: the sub-bin ones
+// with fast_field, else the exact ones (full deposits always use the exact
+// ones, as the reference's update_all_densities does).  Out of line for
+// fast_field, which production runs leave off.
+template <typename Real>
+static __device__ __noinline__ void fast_axes_ool(const RepDev& rd, const GridF& gf, const Real pos[3],
+                                                  Real wl[3], int lo[3], int hi[3]) {
+  fast_axes(rd, gf, pos, wl, lo, hi);
+}
+template <typename Real>
+__device__ __forceinline__ void move_axes(const RepDev& rd, const GridF& gf, const Real pos[3], Real wl[3],
+                                          int lo[3], int hi[3]) {
+  if (rd.fast_n > 0) fast_axes_ool(rd, gf, pos, wl, lo, hi);
+  else voxel_axes(rd, gf, pos, wl, lo, hi);
+}
+
 // Corner l (bit 0: x, bit 1: y, bit 2: z upper) of the eight trilinear
 // weights and its voxel index.
 template <typename Real>
@@ -615,6 +677,16 @@ __device__ __forceinline__ void voxel_weights(const RepDev& rd, const GridF& gf,
   Real wl[3];
   int lo[3], hi[3];
   voxel_axes(rd, gf, pos, wl, lo, hi);
+#pragma unroll
+  for (int l = 0; l < 8; l++) voxel_corner(gf, wl, lo, hi, l, w[l], v[l]);
+}
+
+template <typename Real>
+__device__ __forceinline__ void move_weights(const RepDev& rd, const GridF& gf, const Real pos[3],
+                                             Real w[8], int v[8]) {
+  Real wl[3];
+  int lo[3], hi[3];
+  move_axes(rd, gf, pos, wl, lo, hi);
 #pragma unroll
   for (int l = 0; l < 8; l++) voxel_corner(gf, wl, lo, hi, l, w[l], v[l]);
 }

@@ -135,8 +135,21 @@ struct KArgs {
   unsigned long long* mu_swap_attempts;
 };
 
+// Drift guard of the batched rounds (cg_guard.cu): every `every`-th round the
+// full FP64 energies are recomputed in chunks x replicas blocks and checked
+// against the running sums.
+struct GuardArgs {
+  int every, chunks;
+  double tol_abs, tol_rel;
+  double* partial;                // [n_reps x chunks x 6]
+  double *e_ref, *run_ref, *drift;  // [n_reps]
+  int* init;                      // [n_reps]: a reference energy is held
+  unsigned long long* counter;    // [0] rounds seen, [1] checks made
+};
+
 }  // namespace cg
 
+void cg_launch_guard(const cg::KArgs& a, const cg::GuardArgs& g, bool fp64, cudaStream_t s);
 void cg_launch_mc(const cg::KArgs& a, bool fp64, bool audit, cudaStream_t s);
 void cg_launch_spec(const cg::KArgs& a, bool fp64, size_t smem_bytes, cudaStream_t s);
 cudaError_t cg_set_spec_smem(bool fp64, int lanes_per_move, int bytes);

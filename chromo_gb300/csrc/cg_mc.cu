@@ -22,6 +22,7 @@
 #include "cg_device.cuh"
 #include "cg_kernels.h"
 #include "cg_move.cuh"
+#include "cg_energy.cuh"
 
 namespace cg {
 
@@ -223,8 +224,8 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
                 if (density && fin) {
                   Real w0[8], w1[8];
                   int v0[8], v1[8];
-                  voxel_weights(rd, gf, r, w0, v0);
-                  voxel_weights(rd, gf, tr, w1, v1);
+                  move_weights(rd, gf, r, w0, v0);
+                  move_weights(rd, gf, tr, w1, v1);
                   unsigned s = st[i];
                   deposit_bead(rd, ncol, keys, used, &ws.nused, vals, logH, w0, v0, s, true, err);
                   deposit_bead(rd, ncol, keys, used, &ws.nused, vals, logH, w1, v1, s, false, err);
@@ -360,7 +361,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
                 Real p[3], w[8];
                 int v[8];
                 ld3(r4, i, p);
-                voxel_weights(rd, gf, p, w, v);
+                move_weights(rd, gf, p, w, v);
 #pragma unroll
                 for (int l = 0; l < 8; l++) {
                   int slot = hash_slot(keys, used, &ws.nused, logH, v[l], err);
@@ -559,52 +560,12 @@ __global__ void energy_kernel(KArgs a, double* out) {
   __shared__ double sh[32];
   const int rep = blockIdx.x;
   const RepDev& rd = a.reps[rep];
-  const V4<Pos>* r4 = reinterpret_cast<const V4<Pos>*>(a.r4) + rd.bead_off;
-  const V4<Pos>* t34 = reinterpret_cast<const V4<Pos>*>(a.t34) + rd.bead_off;
-  const double* bonds = a.bonds + rd.bead_off * 6;
-  const unsigned* st = a.states + rd.bead_off;
-  const unsigned* mk = a.marks + rd.bead_off;
-  double el = 0, bi = 0, fe = 0, sx = 0;
-  long long dbl[CG_MAX_BINDERS] = {0, 0, 0};
-  for (long long i = threadIdx.x; i < rd.n_beads; i += blockDim.x) {
-    if (i > 0) {  // SSWLC.compute_E, polymers.pyx:1348-1381
-      double r0[3], r1[3], a0[3], a1[3], dr[3], dp[3], bend[3];
-      ld3(r4, i - 1, r0); ld3(r4, i, r1); ld3(t34, i - 1, a0); ld3(t34, i, a1);
-      Bond<double> b = load_bond<double>(bonds, i - 1);
-      for (int j = 0; j < 3; j++) dr[j] = r1[j] - r0[j];
-      double par = a0[0] * dr[0] + a0[1] * dr[1] + a0[2] * dr[2];
-      for (int j = 0; j < 3; j++) dp[j] = dr[j] - a0[j] * par;
-      for (int j = 0; j < 3; j++) bend[j] = a1[j] + (-a0[j] - b.eta * dp[j]);
-      el += e_pair(b, bend, par, dp);
-    }
-    unsigned sw = st[i], mw = mk[i];
-    int tot = 0;
-    for (int b = 0; b < rd.nb; b++) {
-      int s = (int)((sw >> (8 * b)) & 0xFF), nm = (int)((mw >> (8 * b)) & 0xFF);
-      double me = rd.mu[b] > 0 ? rd.mu[b] * (-rd.mu_adjust + 2) : rd.mu[b] * rd.mu_adjust;
-      bi += bind_f(rd, b, nm, s) - (double)s * me;
-      tot += s;
-      dbl[b] += s == 2;
-    }
-    if (rd.max_binders != -1 && tot > rd.max_binders) bi += kEHugePoly * (double)(tot - rd.max_binders);
-  }
-  if (rd.field_kind == 2) {
-    const long long* grid = a.grid + rd.vox_off * a.ncol;
-    for (long long v = threadIdx.x; v < rd.n_vox; v += blockDim.x) {
-      double V = rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin;
-      double rho[CG_MAX_BINDERS];
-      for (int b = 0; b < rd.nb; b++) rho[b] = ((double)grid[v * a.ncol + 1 + b] * kFxInv) / V;
-      for (int b = 0; b < rd.nb; b++) fe += rd.pref[b] * rho[b] * rho[b];
-      for (int b = 0; b < rd.nb; b++)
-        for (int e = 0; e < rd.nb; e++) fe += rd.xpref[b * CG_MAX_BINDERS + e] * rho[b] * rho[e];
-      double vf = ((double)grid[v * a.ncol] * kFxInv) / V * rd.bead_vol;
-      double sv = (V / rd.bead_vol) * vf * vf;
-      // S: the chi-free sum over the voxels at or below vf_limit (a voxel
-      // above it costs 1e99 vf, which does not depend on chi)
-      if (!(vf > rd.vf_limit)) sx += sv;
-      fe += vf > rd.vf_limit ? kEHugeField * vf : rd.chi * sv;
-    }
-  }
+  EnergyParts p{0.0, 0.0, 0.0, 0.0, {0, 0, 0}};
+  for (long long i = threadIdx.x; i < rd.n_beads; i += blockDim.x) bead_energy<Pos>(a, rd, i, p);
+  if (rd.field_kind == 2)
+    for (long long v = threadIdx.x; v < rd.n_vox; v += blockDim.x) voxel_energy(a, rd, v, p);
+  const double el = p.el, bi = p.bi, fe = p.fe, sx = p.sx;
+  const long long* dbl = p.dbl;
   double t_el = block_sum(el, sh);
   double t_bi = block_sum(bi, sh);
   double t_fe = block_sum(fe, sh);
@@ -693,6 +654,9 @@ __global__ void exchange_kernel(KArgs a, const double* eout, int n_rungs, long l
                      make_uint2((unsigned)seed ^ 0xA4093822u, (unsigned)(seed >> 32)));
     const double u = (double)(o.x >> 1) / kRandMax;
     if (u < exp(x)) {
+      // E_r = chi_r S_r + (chi-free terms): the swap's energy change of each replica
+      a.reps[ia].xch_dE += (cb - ca) * eout[5 * ia + 4];
+      a.reps[ib].xch_dE += (ca - cb) * eout[5 * ib + 4];
       a.reps[ia].chi = cb;
       a.reps[ib].chi = ca;
       a.rep_of_rung[ra] = ib;
@@ -728,6 +692,8 @@ __global__ void exchange_kernel(KArgs a, const double* eout, int n_rungs, long l
                        make_uint2((unsigned)seed ^ 0xA4093822u, (unsigned)(seed >> 32)));
       const double u = (double)(o.x >> 1) / kRandMax;
       if (u < exp(-dE)) {
+        a.reps[ia].xch_dE += (eff(mua, fa) - eff(mub, fa)) * na;
+        a.reps[ib].xch_dE += (eff(mub, fb) - eff(mua, fb)) * nb;
         a.reps[ia].mu[b] = mub;
         a.reps[ib].mu[b] = mua;
         a.rep_of_rung[sa] = ib;

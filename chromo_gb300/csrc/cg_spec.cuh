@@ -202,8 +202,8 @@ __device__ __forceinline__ void bead_task(const RepDev& rd, const GridF& gf, con
   if (density && fin) {
     Real wl0[3], wl1[3];
     int lo0[3], hi0[3], lo1[3], hi1[3];
-    voxel_axes(rd, gf, r, wl0, lo0, hi0);
-    voxel_axes(rd, gf, tr, wl1, lo1, hi1);
+    move_axes(rd, gf, r, wl0, lo0, hi0);
+    move_axes(rd, gf, tr, wl1, lo1, hi1);
     const bool same = lo0[0] == lo1[0] && lo0[1] == lo1[1] && lo0[2] == lo1[2];
 #pragma unroll
     for (int j = 0; j < kCornersPerLane; j++) {
@@ -700,7 +700,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
           Real p[3], wl[3], w;
           int lo[3], hi[3];
           ld3(r4, i, p);
-          voxel_axes(rd, gf, p, wl, lo, hi);
+          move_axes(rd, gf, p, wl, lo, hi);
           voxel_corner(gf, wl, lo, hi, cl, w, vq[0]);
           q = q40(w) * (long long)(s_new - s_old);
           want[0] = true;

@@ -9,8 +9,9 @@ MOVE_KIND = {n: i for i, n in enumerate(nat.MOVE_NAMES)}
 
 def field_params(*, field_kind, confine_kind=0, confine_length=0.0, nxyz=(1, 1, 1),
                  widths=(1.0, 1.0, 1.0), n_binders=1, chi=0.0, vf_limit=0.5, bead_vol=1.0,
-                 pref=(), intra=(), xpref=None):
+                 pref=(), intra=(), xpref=None, fast_field=0, n_points=1000):
     fp = nat.FieldParams()
+    fp.fast_field, fp.n_points = int(bool(fast_field)), int(n_points)
     fp.field_kind, fp.confine_kind, fp.confine_length = int(field_kind), int(confine_kind), float(confine_length)
     fp.nx, fp.ny, fp.nz = (int(v) for v in nxyz)
     fp.n_binders = int(n_binders)

@@ -13,7 +13,6 @@ speed approximation for CPUs; the GPU always evaluates exact trilinear
 weights, so the flag is accepted and recorded but does not change the
 arithmetic.
 """
-import warnings
 
 import numpy as np
 
@@ -101,10 +100,9 @@ class UniformDensityField(FieldBase):
         self.chi = float(chi)
         self.vf_limit = float(vf_limit)
         self.fast_field = int(fast_field)
-        self.n_points = int(n_points)
-        if self.fast_field:
-            warnings.warn("fast_field: the GPU evaluates exact trilinear weights; the "
-                          "sub-bin approximation is not used", stacklevel=2)
+        # init_fast_field (chromo/fields.pyx:577-671) rounds n_points up to even;
+        # the sub-bin weights are evaluated on the device from that count
+        self.n_points = int(n_points) + int(n_points) % 2 if self.fast_field else int(n_points)
         self.init_field_energy_prefactors()
         self.binder_dict = self.binders.to_dict(orient="records")
         self.access_vols = self.get_accessible_volumes(20, assume_fully_accessible)

@@ -100,7 +100,7 @@ def _field_struct(poly, field):
             confine_length=field.confine_length, nxyz=(field.nx, field.ny, field.nz),
             widths=(field.x_width, field.y_width, field.z_width), n_binders=nb, chi=field.chi,
             vf_limit=field.vf_limit, bead_vol=poly.beads[0].vol, pref=pref, intra=intra,
-            xpref=xpref)
+            xpref=xpref, fast_field=field.fast_field, n_points=field.n_points)
     if kind == 1:
         return field_params(field_kind=1, confine_kind=_CONFINE[field.confine_type],
                             confine_length=field.confine_length, n_binders=nb)

@@ -35,7 +35,9 @@ typedef enum {
     CG_ERR_NONFINITE = -5,    /* NaN / Inf position produced by a move */
     CG_ERR_SPIN = -6,         /* an iteration cap was hit (bead-selection resampling,
                                  tangent-index redraws, hash probing) */
-    CG_ERR_NOMEM = -7
+    CG_ERR_NOMEM = -7,
+    CG_ERR_DRIFT = -8         /* the drift guard found the recomputed energy off the running
+                                 sum of dE (cg_set_drift_guard) */
 } cg_status;
 
 /* Move kinds, in the order of chromo/mc/mc_controller.py:255-258. */
@@ -79,6 +81,9 @@ typedef struct {
     double pref[CG_MAX_BINDERS];    /* field_energy_prefactor */
     double intra[CG_MAX_BINDERS];   /* interaction_energy_intranucleosome */
     double xpref[CG_MAX_BINDERS * CG_MAX_BINDERS]; /* cross_talk_field_energy_prefactor[b][c] */
+    int32_t fast_field;    /* 1: per-move density changes from sub-bin weights (init_fast_field,
+                              chromo/fields.pyx:577-671, 1235-1368); full deposits stay exact */
+    int32_t n_points;      /* sub-bins per voxel and axis when fast_field (rounded up to even) */
 } cg_field_params;
 
 /* Binding energetics of the polymer's beads (chromo/polymers.pyx:1408-1538). */
@@ -273,6 +278,24 @@ int cg_get_launch_info(cg_sim *sim, int32_t *warps_per_block, int32_t *hash_slot
  * the autotuner (chromo_gb300.autotune) reads it. */
 int cg_get_launch_shape(cg_sim *sim, int32_t *warps_per_block, int32_t *lanes_per_move,
                         int32_t *moves_in_flight, int32_t *hash_slots);
+
+/* On-device drift guard of cg_run_batched (no counterpart in the reference,
+ * whose running energy is an exact-order FP64 sum on one CPU core): with
+ * every_rounds > 0, every every_rounds-th captured round ends with every
+ * replica's full FP64 energy (the cg_energy sum: elastic + binding + field)
+ * recomputed from the resident state, and its change since the previous
+ * check compared with the change, over the same rounds, of the running sum of
+ * accepted dE plus the energy change of the replica's accepted chi / mu swaps.
+ * A difference above tol_abs + tol_rel * max(1, |E|), or a non-finite one,
+ * makes the next cg_sync return CG_ERR_DRIFT.  The first check takes the
+ * reference energies.  0 turns the guard off.  Drift has two sources: FP32
+ * rounding of the per-move dE, and the reference's tangent-rotation rule for
+ * adjacent beads (chromo/polymers.pyx:1074-1080), whose summed dE is not the
+ * energy change; the tolerances must cover both. */
+int cg_set_drift_guard(cg_sim *sim, int32_t every_rounds, double tol_abs, double tol_rel);
+/* drift[rep] (R entries) = the difference measured at the last check of each
+ * replica; *checks = the number of checks made.  Waits for the device. */
+int cg_get_drift(cg_sim *sim, double *drift, int64_t *checks);
 
 /* Per-round timing of cg_run_batched (no counterpart in the reference, which
  * has no device): with capacity > 0 every captured round brackets its MC

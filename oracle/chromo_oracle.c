@@ -111,6 +111,7 @@ typedef struct {
     double *trial;              /* N x 9 : r, t3, t2 of the moved beads (as OR_POS, widened) */
     int64_t *new_states;        /* N */
     unsigned char *picked;      /* N */
+    int64_t fast_n;             /* fast_field: sub-bins per voxel and axis (0: exact weights) */
 } or_system;
 
 typedef struct {
@@ -582,6 +583,74 @@ static void voxel_weights_f32(const or_system *s, const double pos[3], double w[
     }
 }
 
+/* Eight weights and voxels from per-axis lower voxels and lower weights. */
+static void corners(const or_system *s, const double wl[3], const int64_t lo[3], const int64_t hi[3],
+                    double w[8], int64_t v[8])
+{
+    for (int l = 0; l < 8; l++) {
+        int bx = l & 1, by = (l >> 1) & 1, bz = (l >> 2) & 1;
+        double fx = bx ? (1 - wl[0]) : wl[0];
+        double fy = by ? (1 - wl[1]) : wl[1];
+        double fz = bz ? (1 - wl[2]) : wl[2];
+        w[l] = fx * fy * fz;
+        int64_t ix = bx ? hi[0] : lo[0], iy = by ? hi[1] : lo[1], iz = bz ? hi[2] : lo[2];
+        v[l] = ix + s->nx * iy + s->nx * s->ny * iz;
+    }
+}
+
+/* fast_field: the weights of a move's density change from sub-bins
+ * (get_change_in_density_quickly, fields.pyx:1235-1368, with the tables of
+ * init_fast_field, :577-671): a coordinate's sub-bin is
+ * floor((x + L/2) / w_sub) mod (n_points n), w_sub = dx / n_points, and the
+ * voxel and lower weight are those of the sub-bin's lower edge shifted by
+ * half a voxel: q = ((i - n_points/2) w_sub) / dx, voxel floor(q) (-1 -> n-1),
+ * lower weight 1 - (q - floor(q)).  Full deposits keep exact weights. */
+static void fast_weights(const or_system *s, const double pos[3], double w[8], int64_t v[8])
+{
+    const double width[3] = {s->x_width, s->y_width, s->z_width};
+    const int64_t n[3] = {s->nx, s->ny, s->nz};
+    const double np = (double)s->fast_n;
+    int64_t lo[3], hi[3];
+    if (emu32(s)) {  /* the GPU's binary32 construction */
+        float wl[3];
+        for (int j = 0; j < 3; j++) {
+            double d = width[j] / (double)n[j];
+            float hw = (float)(0.5 * width[j]), inv_sw = (float)(np / d), sw = (float)(d / np);
+            float nsub = (float)(np * (double)n[j]), inv_d = (float)(1.0 / d), hnp = (float)(0.5 * np);
+            float sb = pymodf_(floorf(((float)pos[j] + hw) * inv_sw), nsub);
+            float q = ((sb - hnp) * sw) * inv_d;
+            float fl = floorf(q);
+            int ind = (int)fl;
+            int64_t li = ind == -1 ? n[j] - 1 : ind;
+            lo[j] = li < 0 ? 0 : (li >= n[j] ? n[j] - 1 : li);
+            hi[j] = (lo[j] + 1) % n[j];
+            wl[j] = 1 - (q - fl);
+        }
+        for (int l = 0; l < 8; l++) {
+            int bx = l & 1, by = (l >> 1) & 1, bz = (l >> 2) & 1;
+            float fx = bx ? (1 - wl[0]) : wl[0];
+            float fy = by ? (1 - wl[1]) : wl[1];
+            float fz = bz ? (1 - wl[2]) : wl[2];
+            w[l] = (double)(fx * fy * fz);
+            int64_t ix = bx ? hi[0] : lo[0], iy = by ? hi[1] : lo[1], iz = bz ? hi[2] : lo[2];
+            v[l] = ix + s->nx * iy + s->nx * s->ny * iz;
+        }
+        return;
+    }
+    double wl[3];
+    for (int j = 0; j < 3; j++) {
+        double d = width[j] / (double)n[j];
+        double sw = d / np;
+        double sb = pymod(floor((pos[j] + 0.5 * width[j]) / sw), np * (double)n[j]);
+        double q = ((sb - np / 2) * sw) / d;
+        double ind = floor(q);
+        lo[j] = ind == -1.0 ? n[j] - 1 : (int64_t)ind;
+        hi[j] = (lo[j] + 1) % n[j];
+        wl[j] = 1 - (q - ind);
+    }
+    corners(s, wl, lo, hi, w, v);
+}
+
 static void voxel_weights(const or_system *s, const double pos[3], double w[8], int64_t v[8])
 {
     if (emu32(s)) { voxel_weights_f32(s, pos, w, v); return; }
@@ -757,8 +826,13 @@ static void change_in_density(or_system *s, int64_t n, int state_change, int64_t
         ld3(s->r, i, p0);
         if (state_change) { p1[0] = p0[0]; p1[1] = p0[1]; p1[2] = p0[2]; }
         else { p1[0] = s->trial[9 * k]; p1[1] = s->trial[9 * k + 1]; p1[2] = s->trial[9 * k + 2]; }
-        voxel_weights(s, p0, w[0], v[0]);
-        voxel_weights(s, p1, w[1], v[1]);
+        if (s->fast_n > 0) {
+            fast_weights(s, p0, w[0], v[0]);
+            fast_weights(s, p1, w[1], v[1]);
+        } else {
+            voxel_weights(s, p0, w[0], v[0]);
+            voxel_weights(s, p1, w[1], v[1]);
+        }
         for (int c = 0; c < 2; c++) {
             for (int l = 0; l < 8; l++) {
                 int is_new;

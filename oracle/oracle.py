@@ -41,7 +41,7 @@ class _System(C.Structure):
         ("fixed_density", _I), ("density", _P), ("density_fx", _P),
         ("density_trial", _P), ("dfx", _P), ("slot_of", _P), ("found", _P),
         ("n_found", _I), ("found_cap", _I), ("inds", _P), ("trial", _P),
-        ("new_states", _P), ("picked", _P),
+        ("new_states", _P), ("picked", _P), ("fast_n", _I),
     ]
 
 
@@ -126,6 +126,8 @@ class OracleSystem:
 
     pos: "f64" (positions stored as FP64) or "f32" (FP32 storage, as on GPU).
     fixed_density: 0 for the reference's FP64 density, 1 for int64 fixed point.
+    fast_n: fast_field sub-bins per voxel and axis for the per-move density
+    changes (0: exact weights).
     """
 
     def __init__(self, *, r, t3, t2, states, marks, eps_bend, gamma, eps_par, eps_perp,
@@ -133,7 +135,7 @@ class OracleSystem:
                  field_kind=2, confine_kind=0, confine_length=0.0,
                  nxyz=(1, 1, 1), widths=(1.0, 1.0, 1.0), access_vol=None, chi=1.0,
                  vf_limit=0.5, bead_vol=4 / 3 * np.pi * 125, pref=(), intra=(), xpref=None,
-                 pos="f64", fixed_density=0):
+                 pos="f64", fixed_density=0, fast_n=0):
         self.pos = pos
         fdt = np.float64 if pos == "f64" else np.float32
         # private copies: the oracle mutates its state in place
@@ -177,6 +179,7 @@ class OracleSystem:
         s.chi, s.vf_limit, s.bead_vol = chi, vf_limit, bead_vol
         s.pref, s.intra, s.xpref = self.pref.ctypes.data, self.intra.ctypes.data, self.xpref.ctypes.data
         s.fixed_density = fixed_density
+        s.fast_n = int(fast_n) + int(fast_n) % 2
         s.density, s.density_fx = self.density.ctypes.data, self.density_fx.ctypes.data
         self._s = s
         self._L = lib(pos)

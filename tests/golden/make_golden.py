@@ -94,6 +94,11 @@ CASES = {
     "sphere_access": dict(n=120, nbins=16, vox=40.0, binders=[("HP1", -0.4, -4.0, {})], chi=1.0,
                           confine=("Spherical", 300.0), access=True, steps=4, moves="all", seed=17,
                           run=20),
+    # fast_field: per-move density changes from 64 sub-bins per voxel and axis
+    # (the reference's tables), full deposits exact; two binders with cross talk
+    "fast_field": dict(n=200, nbins=8, vox=40.0, binders=[("HP1", -0.5, -4.0, {"PRC1": 1.0}),
+                                                          ("PRC1", -0.3, -3.0, {})],
+                       chi=1.2, fast=64, steps=4, moves="all", seed=18, run=30),
     # large amplitudes without adaptation: long segments, many tangent beads
     "big_amps": dict(n=160, nbins=8, vox=40.0, binders=[("HP1", -0.4, -4.0, {})], chi=1.0,
                      steps=30, moves="big", seed=16, run=20),
@@ -131,7 +136,9 @@ def make_field(cfg, p, binders):
     return UniformDensityField([p], binders, w, cfg["nbins"], w, cfg["nbins"], w, cfg["nbins"],
                                confine_type=ct, confine_length=cl, chi=cfg["chi"],
                                assume_fully_accessible=0 if cfg.get("access") else 1,
-                               vf_limit=cfg.get("vf_limit", 0.5))
+                               vf_limit=cfg.get("vf_limit", 0.5),
+                               fast_field=1 if cfg.get("fast") else 0,
+                               n_points=cfg.get("fast", 1000))
 
 
 def make_controllers(cfg, p):
@@ -293,6 +300,7 @@ def run_case(name, cfg):
         E_elastic1=p.compute_E(),
         access_vols=(np.array([field.access_vols[i] for i in range(field.n_bins)])
                      if uniform and cfg.get("access") else None),
+        fast_n=field.n_points if uniform and cfg.get("fast") else None,
     )
     out = {k: v for k, v in out.items() if v is not None}
     np.savez_compressed(OUT / f"{name}.npz", **out)

@@ -28,7 +28,7 @@ def oracle_system(g, pos="f64", fixed_density=0, state="0"):
         access_vol=g.get("access_vols"), chi=float(g["chi"]), vf_limit=float(g["vf_limit"]),
         bead_vol=4.0 / 3.0 * np.pi * float(g["bead_rad"]) ** 3,
         pref=g["pref"], intra=g["intra"], xpref=g["xpref"], pos=pos,
-        fixed_density=fixed_density)
+        fixed_density=fixed_density, fast_n=int(g.get("fast_n", 0)))
 
 
 def oracle_ctls(g):
@@ -64,7 +64,8 @@ def gpu_sim(g, pos_fp64, state="0", warps_per_block=0, lanes_per_move=0):
         confine_length=float(g["confine_length"]), nxyz=g["nxyz"], widths=g["widths"],
         n_binders=nb, chi=float(g["chi"]), vf_limit=float(g["vf_limit"]),
         bead_vol=4.0 / 3.0 * np.pi * float(g["bead_rad"]) ** 3, pref=g["pref"], intra=g["intra"],
-        xpref=g["xpref"]), access_vol=access)
+        xpref=g["xpref"], fast_field=int(g.get("fast_n", 0)) > 0,
+        n_points=int(g.get("fast_n", 0)) or 1000), access_vol=access)
     sim.set_binding(0, binding_params(sites=g["sites"], e_mod=g["e_mod"], e_nomod=g["e_nomod"],
                                       mu=g["mu"], mu_adjust_factor=float(g["mu_adjust_factor"]),
                                       max_binders=int(g["max_binders"])))

@@ -27,7 +27,9 @@ def _setup(g):
         f = UniformDensityField([p], binders, w[0], n[0], w[1], n[1], w[2], n[2],
                                 confine_type=ct, confine_length=float(g["confine_length"]),
                                 chi=float(g["chi"]), vf_limit=float(g["vf_limit"]),
-                                assume_fully_accessible=0 if "access_vols" in g else 1)
+                                assume_fully_accessible=0 if "access_vols" in g else 1,
+                                fast_field=1 if "fast_n" in g else 0,
+                                n_points=int(g.get("fast_n", 1000)))
     else:
         ct = {1: "Spherical", 2: "Cubical"}[int(g["confine_kind"])]
         f = NullField([p], confine_type=ct, confine_length=float(g["confine_length"]))

@@ -86,7 +86,9 @@ EXPORTS = [
     "cg_field_energy_static", "cg_energies", "cg_set_chains", "cg_get_chains", "cg_gradient",
     "cg_sample_terms", "cg_get_samples", "cg_get_launch_shape", "cg_mc_warps_per_sm",
     "cg_set_mu_ladder", "cg_get_mu", "cg_get_swap_counts", "cg_run_logged", "cg_set_round_timing",
-    "cg_get_round_times", "cg_set_drift_guard", "cg_get_drift",
+    "cg_get_round_times", "cg_set_drift_guard", "cg_get_drift", "cg_set_chains_device",
+    "cg_deposit_async", "cg_energies_device", "cg_gradient_device", "cg_state_bytes", "cg_save_state",
+    "cg_load_state", "cg_set_twist",
 ]
 N_TERMS = 14
 
@@ -123,6 +125,14 @@ def lib():
             "cg_set_round_timing": ([P, I32], C.c_int),
             "cg_get_round_times": ([P, P, I32, P], C.c_int),
             "cg_set_drift_guard": ([P, I32, D, D], C.c_int),
+            "cg_set_chains_device": ([P, P, P, P], C.c_int),
+            "cg_deposit_async": ([P, P], C.c_int),
+            "cg_energies_device": ([P, P, P], C.c_int),
+            "cg_gradient_device": ([P, P, P, P], C.c_int),
+            "cg_state_bytes": ([P], C.c_int64),
+            "cg_save_state": ([P, P, I64], C.c_int),
+            "cg_load_state": ([P, P, I64], C.c_int),
+            "cg_set_twist": ([P, I32, P, P], C.c_int),
             "cg_get_drift": ([P, P, P], C.c_int),
             "cg_energy": ([P, I32, P], C.c_int),
             "cg_reset_running_energy": ([P], C.c_int),
@@ -270,6 +280,18 @@ class Sim:
         check(lib().cg_get_chains(self.h, *tabs))
         return out
 
+    def set_twist(self, rep, eps_twist, omega0):
+        """SSTWLC twist of replica ``rep`` (per-bond modulus and natural twist;
+        None turns it off)."""
+        if eps_twist is None:
+            check(lib().cg_set_twist(self.h, rep, None, None))
+            return
+        e = np.ascontiguousarray(eps_twist, dtype=np.float64)
+        w = np.ascontiguousarray(omega0, dtype=np.float64)
+        if e.size != int(self.n_beads[rep]) - 1 or w.size != e.size:
+            raise ValueError("one twist modulus and natural twist per bond")
+        check(lib().cg_set_twist(self.h, rep, _ptr(e), _ptr(w)))
+
     def set_field(self, rep, fp: FieldParams, access_vol=None):
         av = None if access_vol is None else np.ascontiguousarray(access_vol, dtype=np.float64)
         check(lib().cg_set_field(self.h, rep, C.byref(fp), _ptr(av)))
@@ -390,6 +412,20 @@ class Sim:
     def run_batched(self, n_rounds, n_steps, n_rungs, seed, stream=None):
         check(lib().cg_run_batched(self.h, int(n_rounds), int(n_steps), int(n_rungs),
                                    int(seed) & (2**64 - 1), stream))
+
+    def save_state(self) -> np.ndarray:
+        """The whole resident state as a byte image (cg_save_state)."""
+        n = lib().cg_state_bytes(self.h)
+        if n < 0:
+            check(int(n))
+        buf = np.empty(int(n), dtype=np.uint8)
+        check(lib().cg_save_state(self.h, _ptr(buf), int(n)))
+        return buf
+
+    def load_state(self, image: np.ndarray):
+        """Restore an image from ``save_state`` of a sim with the same layout."""
+        image = np.ascontiguousarray(image, dtype=np.uint8)
+        check(lib().cg_load_state(self.h, _ptr(image), int(image.size)))
 
     def set_drift_guard(self, every_rounds, tol_abs=0.0, tol_rel=0.0):
         """Check every ``every_rounds``-th ``run_batched`` round's recomputed

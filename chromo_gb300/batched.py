@@ -102,6 +102,8 @@ class ReplicaBatch:
         for r, (p, f, ctrls) in enumerate(zip(self.polymers, self.fields, self.controllers)):
             sim.set_chain(r, r=p.r, t3=p.t3, t2=p.t2, states=p.states, marks=p.chemical_mods,
                           bonds=p.bond_parameters())
+            if hasattr(p, "twist_parameters"):  # SSTWLC
+                sim.set_twist(r, *p.twist_parameters())
             uni = isinstance(f, UniformDensityField)
             sim.set_field(r, _field_struct(p, f), access_vol=f.access_vols if (self._nonuni and uni) else None)
             sim.set_binding(r, _binding_struct(p))
@@ -258,6 +260,22 @@ class ReplicaBatch:
                 mv.num_attempt = int(c.num_attempt)
                 mv.num_success = int(c.num_success)
                 mv.acceptance_tracker.acceptance_rate = c.acc_rate
+
+    # ------------------------------------------------------------ checkpoint
+    def save_checkpoint(self, path):
+        """Write the batch's whole device state (chains, grids, controllers,
+        chi / mu slots, every replica's move counter and running dE, exchange
+        round and swap counts) to ``path`` (a .npy byte image).  A batch built
+        from the same polymers, fields and controllers that loads it continues
+        bit for bit as this one would, given the same seeds."""
+        np.save(path, self.sim.save_state(), allow_pickle=False)
+
+    def load_checkpoint(self, path):
+        """Restore a ``save_checkpoint`` image and refresh the host objects."""
+        self.sim.load_state(np.load(path, allow_pickle=False))
+        self.pull()
+        e = self.sim.energies()
+        self._E0 = e[:, 0] + e[:, 1] + e[:, 2] - e[:, 3]  # the baseline the saved running sum had
 
     def close(self):
         self.sim.close()

@@ -124,6 +124,7 @@ struct cg_sim {
     timing_cap = 0;
     timing_count = 0;
   }
+  double* twist = nullptr;  // SSTWLC bond parameters (cg_set_twist), allocated on first use
   // drift guard of the batched rounds (cg_set_drift_guard)
   int guard_every = 0, guard_chunks = 1;
   double guard_tol_abs = 0, guard_tol_rel = 0;
@@ -173,6 +174,7 @@ struct cg_sim {
     a.reps = reps; a.ctl = ctl; a.n_ctl = n_ctl; a.n_reps = R; a.tally = tally;
     a.r4 = r4; a.t34 = t34; a.t24 = t24; a.states = states; a.marks = marks; a.bonds = bonds;
     a.bonds32 = bonds32;
+    a.twist = twist;
     a.grid = grid; a.access_vol = access_vol; a.access_sc = access_sc; a.access_vb = access_vb;
     a.ncol = ncol; a.hcol = nb + 1;
     a.g_keys = g_keys; a.g_used = g_used; a.g_bslot = g_bslot; a.g_vals = g_vals; a.g_logH = g_logH;
@@ -267,6 +269,7 @@ void cg_destroy(cg_sim* s) {
   s->drop_timing();
   s->free_guard();
   if (s->pinned) cudaFreeHost(s->pinned);
+  if (s->twist) cudaFree(s->twist);
   void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
                   s->bonds32, s->grid, s->access_vol, s->access_sc, s->access_vb, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
                   s->picked, s->d_picked_off, s->eout, s->aout, s->rep_of_rung, s->swaps,
@@ -537,6 +540,31 @@ int cg_set_chain(cg_sim* s, int rep, const double* r, const double* t3, const do
     CUDA_TRY(cudaMemcpy(s->bonds32 + 8 * off, bf.data(), 4 * 8 * n, cudaMemcpyHostToDevice));
   }
   return CG_OK;
+}
+
+int cg_set_twist(cg_sim* s, int rep, const double* eps_twist, const double* omega0) {
+  if (int rc = check_rep(s, rep)) return rc;
+  RepDev d;
+  if (int rc = get_rep(s, rep, &d)) return rc;
+  if (!eps_twist) {
+    d.twist = 0;
+    return put_rep(s, rep, &d);
+  }
+  if (!omega0) return fail(CG_ERR_ARG, "omega0 is required with eps_twist");
+  const long long n = s->n_beads[rep], off = s->bead_off[rep];
+  for (long long i = 0; i + 1 < n; i++)
+    if (!(eps_twist[i] > 0) || !std::isfinite(omega0[i]))
+      return fail(CG_ERR_ARG, "twist moduli must be positive and natural twists finite");
+  if (!s->twist) {
+    CUDA_TRY(cudaMalloc(&s->twist, 16 * std::max(1LL, s->total_beads)));
+    CUDA_TRY(cudaMemset(s->twist, 0, 16 * std::max(1LL, s->total_beads)));
+    s->drop_graph();  // the kernels' arguments changed
+  }
+  std::vector<double> tw(2 * n, 0.0);
+  for (long long i = 0; i + 1 < n; i++) { tw[2 * i] = eps_twist[i]; tw[2 * i + 1] = omega0[i]; }
+  CUDA_TRY(cudaMemcpy(s->twist + 2 * off, tw.data(), 16 * n, cudaMemcpyHostToDevice));
+  d.twist = 1;
+  return put_rep(s, rep, &d);
 }
 
 int cg_get_chain(cg_sim* s, int rep, double* r, double* t3, double* t2, int64_t* states) {
@@ -939,6 +967,39 @@ int cg_gradient(cg_sim* s, float* dEdr, double* terms) {
   return CG_OK;
 }
 
+int cg_set_chains_device(cg_sim* s, const double* r, const double* t3, void* stream) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (!r && !t3) return CG_OK;
+  cg_launch_store_chains(s->args(), s->fp64 != 0, s->total_beads, r, t3, (cudaStream_t)stream);
+  CUDA_TRY(cudaGetLastError());
+  return CG_OK;
+}
+
+int cg_deposit_async(cg_sim* s, void* stream) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(cudaMemsetAsync(s->grid, 0, 8 * s->ncol * s->total_vox, st));
+  cg_launch_deposit(s->args(), s->fp64, -1, s->R, s->max_beads, st);
+  CUDA_TRY(cudaGetLastError());
+  return CG_OK;
+}
+
+int cg_energies_device(cg_sim* s, double* out, void* stream) {
+  if (!s || !out) return fail(CG_ERR_ARG, "null argument");
+  cg_launch_energy(s->args(), s->fp64, out, (cudaStream_t)stream);
+  CUDA_TRY(cudaGetLastError());
+  return CG_OK;
+}
+
+int cg_gradient_device(cg_sim* s, double* dEdr, double* dEdt3, void* stream) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (!dEdr) return fail(CG_ERR_ARG, "dEdr is required");
+  if (dEdt3 && s->twist) return fail(CG_ERR_ARG, "dE/dt3 does not include SSTWLC twist terms");
+  cg_launch_gradient64(s->args(), s->fp64 != 0, dEdr, dEdt3, s->max_beads, (cudaStream_t)stream);
+  CUDA_TRY(cudaGetLastError());
+  return CG_OK;
+}
+
 int cg_sample_terms(cg_sim* s, void* stream) {
   if (!s) return fail(CG_ERR_ARG, "null sim");
   if (int rc = ensure_derivative_buffers(s)) return rc;
@@ -1159,6 +1220,93 @@ int cg_get_drift(cg_sim* s, double* drift, int64_t* checks) {
     CUDA_TRY(cudaMemcpy(c, s->guard_counter, sizeof c, cudaMemcpyDeviceToHost));
     *checks = (int64_t)c[1];
   }
+  return CG_OK;
+}
+
+// ---------------------------------------------------------------- checkpoint
+// The whole resident state of a sim, as one byte image: a header naming the
+// layout, then every device buffer whose contents carry over between calls.
+namespace {
+struct StateHeader {
+  unsigned long long magic, version;
+  long long R, nb, ncol, fp64, total_beads, total_vox, n_ctl, mu_rungs, mu_binder, twist;
+};
+constexpr unsigned long long kStateMagic = 0x31534D4F52484343ULL;  // "CCHROMS1"
+
+struct StatePart {
+  void* dev;
+  size_t bytes;
+};
+
+std::vector<StatePart> state_parts(cg_sim* s) {
+  const size_t R = (size_t)s->R, B = (size_t)s->total_beads;
+  std::vector<StatePart> p = {
+      {s->reps, sizeof(RepDev) * R},        {s->ctl, sizeof(cg_move_ctl) * 5 * R},
+      {s->tally, 8 * 30 * R},               {s->r4, s->pos_bytes() * B},
+      {s->t34, s->pos_bytes() * B},         {s->t24, s->pos_bytes() * B},
+      {s->states, 4 * B},                   {s->marks, 4 * B},
+      {s->bonds, 48 * B},                   {s->bonds32, 32 * B},
+      {s->grid, 8 * (size_t)s->ncol * (size_t)s->total_vox},
+      {s->rep_of_rung, 4 * R},              {s->swaps, 8 * R},
+      {s->swap_attempts, 8 * R},            {s->xround, 8},
+      {s->mu_swaps, 8 * R},                 {s->mu_swap_attempts, 8 * R}};
+  if (s->twist) p.push_back({s->twist, 16 * B});
+  if (s->nonuniform) {
+    p.push_back({s->access_vol, 8 * (size_t)s->total_vox});
+    p.push_back({s->access_sc, 4 * (size_t)s->total_vox});
+    p.push_back({s->access_vb, 8 * (size_t)s->total_vox});
+  }
+  return p;
+}
+
+StateHeader state_header(const cg_sim* s) {
+  StateHeader h{kStateMagic, 1, s->R, s->nb, s->ncol, s->fp64, s->total_beads, s->total_vox, s->n_ctl,
+                s->mu_rungs, s->mu_binder, s->twist ? 1 : 0};
+  return h;
+}
+}  // namespace
+
+int64_t cg_state_bytes(cg_sim* s) {
+  if (!s) return fail(CG_ERR_ARG, "null sim");
+  size_t n = sizeof(StateHeader);
+  for (const StatePart& p : state_parts(s)) n += p.bytes;
+  return (int64_t)n;
+}
+
+int cg_save_state(cg_sim* s, void* buf, int64_t bytes) {
+  if (!s || !buf) return fail(CG_ERR_ARG, "null argument");
+  if (bytes < cg_state_bytes(s)) return fail(CG_ERR_ARG, "buffer smaller than cg_state_bytes()");
+  CUDA_TRY(cudaDeviceSynchronize());
+  unsigned char* out = static_cast<unsigned char*>(buf);
+  const StateHeader h = state_header(s);
+  memcpy(out, &h, sizeof h);
+  size_t off = sizeof h;
+  for (const StatePart& p : state_parts(s)) {
+    CUDA_TRY(cudaMemcpy(out + off, p.dev, p.bytes, cudaMemcpyDeviceToHost));
+    off += p.bytes;
+  }
+  return CG_OK;
+}
+
+int cg_load_state(cg_sim* s, const void* buf, int64_t bytes) {
+  if (!s || !buf) return fail(CG_ERR_ARG, "null argument");
+  if (bytes < (int64_t)sizeof(StateHeader)) return fail(CG_ERR_ARG, "state image too short");
+  StateHeader h, want = state_header(s);
+  memcpy(&h, buf, sizeof h);
+  if (h.magic != kStateMagic || h.version != want.version)
+    return fail(CG_ERR_ARG, "not a state image of this library");
+  if (memcmp(&h, &want, sizeof h) != 0)
+    return fail(CG_ERR_ARG, "state image of a simulation with another layout (replicas, beads, grids, "
+                            "binders, precision, controllers or mu ladder differ)");
+  if (bytes < cg_state_bytes(s)) return fail(CG_ERR_ARG, "state image truncated");
+  CUDA_TRY(cudaDeviceSynchronize());
+  const unsigned char* in = static_cast<const unsigned char*>(buf);
+  size_t off = sizeof h;
+  for (const StatePart& p : state_parts(s)) {
+    CUDA_TRY(cudaMemcpy(p.dev, in + off, p.bytes, cudaMemcpyHostToDevice));
+    off += p.bytes;
+  }
+  if (s->guard_every) CUDA_TRY(cudaMemset(s->guard_init, 0, sizeof(int) * s->R));  // new reference energies
   return CG_OK;
 }
 

@@ -52,6 +52,7 @@ struct RepDev {
   unsigned long long draw_pos, bstate_pos;
   double run_dE;
   double xch_dE;  // energy change of this replica's accepted chi / mu swaps
+  int twist, pad2;  // twist: SSTWLC bond energy (KArgs::twist holds the bond parameters)
   unsigned err, pad1;
 };
 
@@ -254,6 +255,11 @@ __device__ __forceinline__ void acc_add(Fx& s, const Fx& v) {
   s.q += v.q;
   if (!is_zero64(v.hard)) s.hard = add_hard(s.hard, v.hard);
 }
+// An FP64 term (the twist part of a bond's dE): added as FP64 for FP64
+// storage, rounded to FP32 and added in fixed point for FP32 storage (its
+// relative error 6e-8 is far inside the path's 1e-5 bound).
+__device__ __forceinline__ void acc_add_d(double& s, double v) { s += v; }
+__device__ __forceinline__ void acc_add_d(Fx& s, double v) { acc_add(s, (float)v); }
 __device__ __forceinline__ double acc_d(double v) { return v; }
 __device__ __forceinline__ double acc_d(const Fx& v) { return (double)v.q * kFxEInv + v.hard; }
 template <typename A> __device__ __forceinline__ A acc_zero();
@@ -466,6 +472,48 @@ __device__ __forceinline__ double pair_dE_rev(const Bond<Real>& b, const Real r0
     bc[i] = t31[i] - t30[i] - dp[i] * b.eta;
   }
   return (double)e_pair(b, bt, pt, dpt) - (double)e_pair(b, bc, pc, dp);
+}
+
+// ---------------------------------------------------------------- SSTWLC twist
+// E_pair_with_twist (chromo/polymers.pyx:2050-2102) adds 0.5 eps_twist dw^2 to
+// the bond energy, dw = omega - omega0 wrapped into [-pi, pi), omega the
+// twist angle of the two beads' (t2, t3) frames
+// (compute_twist_angle_omega, :3427-3461): with t1 = t2 x t3,
+// omega = atan2(t2_0 . t1_1 - t1_0 . t2_1, t1_0 . t1_1 + t2_0 . t2_1).
+// Evaluated in FP64 for both storage types (a few bonds per move, twist
+// chains only).
+struct Frame {
+  double t2[3], t3[3];
+};
+template <typename Real>
+__device__ __forceinline__ Frame frame_of(const Real t2[3], const Real t3[3]) {
+  return Frame{{(double)t2[0], (double)t2[1], (double)t2[2]}, {(double)t3[0], (double)t3[1], (double)t3[2]}};
+}
+template <typename Pos>
+__device__ __forceinline__ Frame frame_of(const V4<Pos>& t2, const V4<Pos>& t3) {
+  return Frame{{(double)t2.x, (double)t2.y, (double)t2.z}, {(double)t3.x, (double)t3.y, (double)t3.z}};
+}
+__device__ __forceinline__ double twist_energy(const double* tw, const Frame& a, const Frame& b) {
+  const double t1a[3] = {a.t2[1] * a.t3[2] - a.t2[2] * a.t3[1], a.t2[2] * a.t3[0] - a.t2[0] * a.t3[2],
+                         a.t2[0] * a.t3[1] - a.t2[1] * a.t3[0]};
+  const double t1b[3] = {b.t2[1] * b.t3[2] - b.t2[2] * b.t3[1], b.t2[2] * b.t3[0] - b.t2[0] * b.t3[2],
+                         b.t2[0] * b.t3[1] - b.t2[1] * b.t3[0]};
+  const double y = (a.t2[0] * t1b[0] + a.t2[1] * t1b[1] + a.t2[2] * t1b[2]) -
+                   (t1a[0] * b.t2[0] + t1a[1] * b.t2[1] + t1a[2] * b.t2[2]);
+  const double x = (t1a[0] * t1b[0] + t1a[1] * t1b[1] + t1a[2] * t1b[2]) +
+                   (a.t2[0] * b.t2[0] + a.t2[1] * b.t2[1] + a.t2[2] * b.t2[2]);
+  const double kPi = 3.141592653589793;
+  double dw = atan2(y, x) - tw[1];
+  dw -= 2 * kPi * floor((dw + kPi) / (2 * kPi));
+  return 0.5 * tw[0] * (dw * dw);
+}
+// twist part of a bond's dE: E(a_new, b_new) - E(a_cur, b_cur); tw = (eps_twist, omega0)
+static __device__ __noinline__ double twist_pair_dE(const double* tw, Frame a_cur, Frame b_cur, Frame a_new,
+                                                    Frame b_new) {
+  return twist_energy(tw, a_new, b_new) - twist_energy(tw, a_cur, b_cur);
+}
+static __device__ __noinline__ double twist_bond_energy(const double* tw, Frame a, Frame b) {
+  return twist_energy(tw, a, b);
 }
 
 // (x + y + z) / 2 as FF

@@ -34,6 +34,11 @@ __device__ __forceinline__ void bead_energy(const KArgs& a, const RepDev& rd, lo
     for (int j = 0; j < 3; j++) dp[j] = dr[j] - a0[j] * par;
     for (int j = 0; j < 3; j++) bend[j] = a1[j] + (-a0[j] - b.eta * dp[j]);
     p.el += e_pair(b, bend, par, dp);
+    if (rd.twist) {  // SSTWLC.compute_E, chromo/polymers.pyx:2250-2285
+      const V4<Pos>* t24 = reinterpret_cast<const V4<Pos>*>(a.t24) + rd.bead_off;
+      p.el += twist_bond_energy(a.twist + 2 * (rd.bead_off + i - 1), frame_of(t24[i - 1], t34[i - 1]),
+                                frame_of(t24[i], t34[i]));
+    }
   }
   const unsigned sw = a.states[rd.bead_off + i], mw = a.marks[rd.bead_off + i];
   int tot = 0;

@@ -69,8 +69,28 @@ __device__ __forceinline__ void weights_and_slopes(const RepDev& rd, const doubl
   }
 }
 
-template <typename Pos>
-__global__ void gradient_kernel(KArgs a, float* out) {
+// d E_pair / d a0 and d E_pair / d a1 of bond (j -> j+1) (the t3 tangents at
+// j and j+1 taken as free vectors, as the energy's formula reads them):
+//   dE/da1 = eb bend,
+//   dE/da0 = eb (eta (par bend + (a0.bend) dr) - bend) + ep (par - gamma) dr
+//            - epp (par dp + (a0.dp) dr).
+__device__ __forceinline__ void bond_tangent_grad(const Bond<double>& b, const double a0[3], const double a1[3],
+                                                  const double dr[3], double g0[3], double g1[3]) {
+  const double par = a0[0] * dr[0] + a0[1] * dr[1] + a0[2] * dr[2];
+  double dp[3], bend[3];
+  for (int j = 0; j < 3; j++) dp[j] = dr[j] - a0[j] * par;
+  for (int j = 0; j < 3; j++) bend[j] = a1[j] + (-a0[j] - b.eta * dp[j]);
+  const double ab = a0[0] * bend[0] + a0[1] * bend[1] + a0[2] * bend[2];
+  const double ad = a0[0] * dp[0] + a0[1] * dp[1] + a0[2] * dp[2];
+  for (int j = 0; j < 3; j++) {
+    g1[j] = b.eb * bend[j];
+    g0[j] = b.eb * (b.eta * (par * bend[j] + ab * dr[j]) - bend[j]) + b.ep * (par - b.g) * dr[j] -
+            b.epp * (par * dp[j] + ad * dr[j]);
+  }
+}
+
+template <typename Pos, typename Out>
+__global__ void gradient_kernel(KArgs a, Out* out, Out* out_t3) {
   const int rep = blockIdx.y;
   const RepDev& rd = a.reps[rep];
   const V4<Pos>* r4 = reinterpret_cast<const V4<Pos>*>(a.r4) + rd.bead_off;
@@ -81,24 +101,36 @@ __global__ void gradient_kernel(KArgs a, float* out) {
   const long long N = rd.n_beads;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
        i += (long long)gridDim.x * blockDim.x) {
-    double ri[3], ai[3], gr[3] = {0, 0, 0};
+    double ri[3], ai[3], gr[3] = {0, 0, 0}, gt[3] = {0, 0, 0};
     ld3(r4, i, ri);
     ld3(t34, i, ai);
-    if (i > 0) {  // bond (i-1 -> i): + dE/ddr
+    if (i > 0) {  // bond (i-1 -> i): + dE/ddr; dE/da1 for the tangent
       double rp[3], ap[3], dr[3], g[3];
       ld3(r4, i - 1, rp);
       ld3(t34, i - 1, ap);
       for (int j = 0; j < 3; j++) dr[j] = ri[j] - rp[j];
-      bond_grad(load_bond<double>(bonds, i - 1), ap, ai, dr, g);
+      const Bond<double> b = load_bond<double>(bonds, i - 1);
+      bond_grad(b, ap, ai, dr, g);
       for (int j = 0; j < 3; j++) gr[j] += g[j];
+      if (out_t3) {
+        double g0[3], g1[3];
+        bond_tangent_grad(b, ap, ai, dr, g0, g1);
+        for (int j = 0; j < 3; j++) gt[j] += g1[j];
+      }
     }
-    if (i + 1 < N) {  // bond (i -> i+1): - dE/ddr
+    if (i + 1 < N) {  // bond (i -> i+1): - dE/ddr; dE/da0 for the tangent
       double rn[3], an[3], dr[3], g[3];
       ld3(r4, i + 1, rn);
       ld3(t34, i + 1, an);
       for (int j = 0; j < 3; j++) dr[j] = rn[j] - ri[j];
-      bond_grad(load_bond<double>(bonds, i), ai, an, dr, g);
+      const Bond<double> b = load_bond<double>(bonds, i);
+      bond_grad(b, ai, an, dr, g);
       for (int j = 0; j < 3; j++) gr[j] -= g[j];
+      if (out_t3) {
+        double g0[3], g1[3];
+        bond_tangent_grad(b, ai, an, dr, g0, g1);
+        for (int j = 0; j < 3; j++) gt[j] += g0[j];
+      }
     }
     if (rd.field_kind == 2) {
       double w[8], dw[8][3];
@@ -123,10 +155,16 @@ __global__ void gradient_kernel(KArgs a, float* out) {
         for (int j = 0; j < 3; j++) gr[j] += phi * dw[l][j];
       }
     }
-    float* o = out + 3 * (rd.bead_off + i);
-    o[0] = (float)gr[0];
-    o[1] = (float)gr[1];
-    o[2] = (float)gr[2];
+    Out* o = out + 3 * (rd.bead_off + i);
+    o[0] = (Out)gr[0];
+    o[1] = (Out)gr[1];
+    o[2] = (Out)gr[2];
+    if (out_t3) {
+      Out* ot = out_t3 + 3 * (rd.bead_off + i);
+      ot[0] = (Out)gt[0];
+      ot[1] = (Out)gt[1];
+      ot[2] = (Out)gt[2];
+    }
   }
 }
 
@@ -224,13 +262,48 @@ __global__ void terms_kernel(KArgs a, double* terms, double* acc) {
 
 }  // namespace cg
 
-void cg_launch_gradient(const cg::KArgs& a, bool fp64, float* out, long long max_beads, cudaStream_t s) {
+static dim3 gradient_grid(const cg::KArgs& a, long long max_beads) {
   long long bx = (max_beads + 127) / 128;
   if (bx > 64) bx = 64;
   if (bx < 1) bx = 1;
-  dim3 grid((unsigned)bx, (unsigned)a.n_reps);
-  if (fp64) cg::gradient_kernel<double><<<grid, 128, 0, s>>>(a, out);
-  else cg::gradient_kernel<float><<<grid, 128, 0, s>>>(a, out);
+  return dim3((unsigned)bx, (unsigned)a.n_reps);
+}
+
+void cg_launch_gradient(const cg::KArgs& a, bool fp64, float* out, long long max_beads, cudaStream_t s) {
+  const dim3 grid = gradient_grid(a, max_beads);
+  if (fp64) cg::gradient_kernel<double, float><<<grid, 128, 0, s>>>(a, out, nullptr);
+  else cg::gradient_kernel<float, float><<<grid, 128, 0, s>>>(a, out, nullptr);
+}
+
+void cg_launch_gradient64(const cg::KArgs& a, bool fp64, double* out, double* out_t3, long long max_beads,
+                          cudaStream_t s) {
+  const dim3 grid = gradient_grid(a, max_beads);
+  if (fp64) cg::gradient_kernel<double, double><<<grid, 128, 0, s>>>(a, out, out_t3);
+  else cg::gradient_kernel<float, double><<<grid, 128, 0, s>>>(a, out, out_t3);
+}
+
+namespace cg {
+// Global bead b (replicas concatenated) of FP64 [total_beads x 3] arrays into
+// the resident 4-vector storage.
+template <typename Pos>
+__global__ void store_chains_kernel(KArgs a, long long total, const double* r, const double* t3) {
+  V4<Pos>* r4 = reinterpret_cast<V4<Pos>*>(a.r4);
+  V4<Pos>* t34 = reinterpret_cast<V4<Pos>*>(a.t34);
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < total;
+       b += (long long)gridDim.x * blockDim.x) {
+    if (r) r4[b] = V4<Pos>{(Pos)r[3 * b], (Pos)r[3 * b + 1], (Pos)r[3 * b + 2], (Pos)0};
+    if (t3) t34[b] = V4<Pos>{(Pos)t3[3 * b], (Pos)t3[3 * b + 1], (Pos)t3[3 * b + 2], (Pos)0};
+  }
+}
+}  // namespace cg
+
+void cg_launch_store_chains(const cg::KArgs& a, bool fp64, long long total, const double* r, const double* t3,
+                            cudaStream_t s) {
+  long long blocks = (total + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  if (fp64) cg::store_chains_kernel<double><<<(unsigned)blocks, 256, 0, s>>>(a, total, r, t3);
+  else cg::store_chains_kernel<float><<<(unsigned)blocks, 256, 0, s>>>(a, total, r, t3);
 }
 
 void cg_launch_terms(const cg::KArgs& a, double* terms, double* acc, cudaStream_t s) {

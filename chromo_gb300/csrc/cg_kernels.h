@@ -82,6 +82,7 @@ struct KArgs {
   unsigned* marks;            // packed int8 chemical_mods per bead
   const double* bonds;        // 6 doubles per bead (bond i -> i+1)
   const float* bonds32;       // the same in FP32, 8 floats per bead (16-byte aligned rows)
+  const double* twist;        // per bead: eps_twist, omega0 of bond i -> i+1 (null: no SSTWLC replica)
   long long* grid;            // ncol int64 per voxel
   const double* access_vol;   // per voxel, or null
   const float* access_sc;     // per voxel: (float)(2^-40 / V), with access_vol
@@ -168,6 +169,10 @@ constexpr int kTerms = 14;                                // energy terms per re
 constexpr int kAccPerRep = kTerms + kTerms * kTerms + 1;  // running sums of T, T T^T, count
 }
 void cg_launch_gradient(const cg::KArgs& a, bool fp64, float* out, long long max_beads, cudaStream_t s);
+void cg_launch_gradient64(const cg::KArgs& a, bool fp64, double* out, double* out_t3, long long max_beads,
+                          cudaStream_t s);
+void cg_launch_store_chains(const cg::KArgs& a, bool fp64, long long total, const double* r, const double* t3,
+                            cudaStream_t s);
 void cg_launch_terms(const cg::KArgs& a, double* terms, double* acc, cudaStream_t s);
 void cg_launch_exchange(const cg::KArgs& a, const double* eout, int n_rungs, long long round,
                         unsigned long long seed, cudaStream_t s);

@@ -212,11 +212,21 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
                   Real r0[3], t30[3];
                   ld3(r4, i - 1, r0); ld3(t34, i - 1, t30);
                   acc_add(part, pair_dE_fwd(bond_at(bonds, bonds32, i - 1, (Real)0), r0, r, tr, t30, t3, tt3));
+                  if (rd.twist) {  // SSTWLC twist term, polymers.pyx:2104-2175
+                    const Frame l = frame_of(t24[i - 1], t34[i - 1]);
+                    acc_add_d(part, twist_pair_dE(a.twist + 2 * (rd.bead_off + i - 1), l, frame_of(t2, t3), l,
+                                                  frame_of(tt2, tt3)));
+                  }
                 }
                 if (k == m - 1 && indf != N) {  // reverse bond, polymers.pyx:1132-1142
                   Real r1[3], t31[3];
                   ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
                   acc_add(part, pair_dE_rev(bond_at(bonds, bonds32, i, (Real)0), r, tr, r1, t3, tt3, t31));
+                  if (rd.twist) {  // :2177-2248
+                    const Frame rr = frame_of(t24[i + 1], t34[i + 1]);
+                    acc_add_d(part, twist_pair_dE(a.twist + 2 * (rd.bead_off + i), frame_of(t2, t3), rr,
+                                                  frame_of(tt2, tt3), rr));
+                  }
                 }
                 if (check_field && rd.confine_kind) {
                   oob += out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
@@ -325,6 +335,20 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
                 Real r1[3], t31[3];
                 ld3(r4, i + 1, r1); ld3(t34, i + 1, t31);
                 acc_add(de, pair_dE_rev(bond_at(bonds, bonds32, i, (Real)0), r, r, r1, t3, tt3, t31));
+              }
+              if (rd.twist) {  // SSTWLC twist terms of both bonds
+                const double* tw = a.twist + 2 * rd.bead_off;
+                const Frame cur = frame_of(t2, t3), nw = frame_of(tt2, tt3);
+                double dt = 0;
+                if (i != 0) {
+                  const Frame l = frame_of(t24[i - 1], t34[i - 1]);
+                  dt += twist_pair_dE(tw + 2 * (i - 1), l, cur, l, nw);
+                }
+                if (i + 1 != N) {
+                  const Frame rr = frame_of(t24[i + 1], t34[i + 1]);
+                  dt += twist_pair_dE(tw + 2 * i, cur, rr, nw, rr);
+                }
+                acc_add_d(de, dt);
               }
               acc_add(part, de);
             }

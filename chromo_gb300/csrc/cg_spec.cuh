@@ -136,11 +136,13 @@ struct ChainView {
   const unsigned* st;
   const double* bonds;
   const float* bonds32;
+  const double* twist;  // (eps_twist, omega0) per bond, SSTWLC replicas only
   __device__ ChainView(const KArgs& a, const RepDev& rd)
       : r4(reinterpret_cast<const V4<Pos>*>(a.r4) + rd.bead_off),
         t34(reinterpret_cast<const V4<Pos>*>(a.t34) + rd.bead_off),
         t24(reinterpret_cast<const V4<Pos>*>(a.t24) + rd.bead_off),
-        st(a.states + rd.bead_off), bonds(a.bonds + rd.bead_off * 6), bonds32(a.bonds32 + rd.bead_off * 8) {}
+        st(a.states + rd.bead_off), bonds(a.bonds + rd.bead_off * 6), bonds32(a.bonds32 + rd.bead_off * 8),
+        twist(rd.twist ? a.twist + rd.bead_off * 2 : nullptr) {}
 };
 
 // Lanes per bead of the position-move deposit; each lane takes 8 / kLanesPerBead
@@ -197,6 +199,11 @@ __device__ __forceinline__ void bead_task(const RepDev& rd, const GridF& gf, con
   pterm = acc_zero<Acc>();
   if (left) acc_add(pterm, pair_dE_fwd(bn, rn, r, tr, tn, t3, tt3));
   if (right) acc_add(pterm, pair_dE_rev(bn, r, tr, rn, t3, tt3, tn));
+  if (cv.twist && (left || right)) {  // SSTWLC: the bond's twist term
+    const Frame nb = frame_of(cv.t24[in], TN), cur = frame_of(t2, t3), nw = frame_of(tt2, tt3);
+    const double* tw = cv.twist + 2 * (left ? in : i);
+    acc_add_d(pterm, left ? twist_pair_dE(tw, nb, cur, nb, nw) : twist_pair_dE(tw, cur, nb, nw, nb));
+  }
   oob = 0;
   if (cl == 0 && conf) oob = out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
   if (density && fin) {
@@ -646,6 +653,20 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       Acc de = acc_zero<Acc>();
       if (hl) acc_add(de, pair_dE_fwd(bl, r0, r, r, t30, t3, tt3));
       if (hr) acc_add(de, pair_dE_rev(br, r, r, r1, t3, tt3, t31));
+      if (rd.twist) {  // SSTWLC: twist terms of both bonds
+        const double* tw = a.twist + rd.bead_off * 2;
+        const Frame cur = frame_of(t2, t3), nw = frame_of(tt2, tt3);
+        double dt = 0;
+        if (hl) {
+          const Frame l = frame_of(t24[il], t34[il]);
+          dt += twist_pair_dE(tw + 2 * il, l, cur, l, nw);
+        }
+        if (hr) {
+          const Frame rr = frame_of(t24[ir], t34[ir]);
+          dt += twist_pair_dE(tw + 2 * i, cur, rr, nw, rr);
+        }
+        acc_add_d(de, dt);
+      }
       acc_add(part, de);
     }
     g.pos = axis_base + 2 * (unsigned long long)m;

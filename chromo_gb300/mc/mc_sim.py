@@ -119,6 +119,8 @@ def _device(poly, field, ctrls=(), precision=None):
                   nonuniform_access=nonuni)
     sim.set_chain(0, r=poly.r, t3=poly.t3, t2=poly.t2, states=poly.states,
                   marks=poly.chemical_mods, bonds=poly.bond_parameters())
+    if hasattr(poly, "twist_parameters"):  # SSTWLC
+        sim.set_twist(0, *poly.twist_parameters())
     sim.set_field(0, _field_struct(poly, field),
                   access_vol=field.access_vols if nonuni else None)
     sim.set_binding(0, _binding_struct(poly))

@@ -224,6 +224,47 @@ class SSWLC(PolymerBase):
         return cls(name, r, t3=t3, t2=t2, bead_length=step_lengths, **kwargs)
 
 
+# natural twist of bare DNA per nm: 2 pi / 10.5 bp, 0.332 nm per bp
+# (NATURAL_TWIST_BARE / LENGTH_BP, chromo/polymers.pyx:38-40)
+NATURAL_TWIST_BARE = 2 * np.pi / 10.5
+LENGTH_BP = 0.332
+
+
+class SSTWLC(SSWLC):
+    """Stretchable, shearable wormlike chain with twist (chromo/polymers.pyx:1889-2320).
+
+    ``lt`` is the twist persistence length (nm).  Each bond's energy gains
+    0.5 eps_twist dw^2 with eps_twist = lt / (delta lp) = lt / bead_length and
+    dw the twist angle of the two beads' (t2, t3) frames minus the natural
+    twist bead_length * (2 pi / 10.5) / 0.332, wrapped into [-pi, pi).  The MC
+    kernels evaluate the twist terms in FP64."""
+
+    def __init__(self, name, r, *, bead_length, lp, lt, bead_rad=5, t3=_empty_2d, t2=_empty_2d,
+                 states=_mty_2d_int, binder_names=_empty_1d, chemical_mods=_mty_2d_int,
+                 chemical_mod_names=_empty_1d, log_path="", max_binders=-1):
+        self.lt = float(lt)
+        super().__init__(name, r, bead_length=bead_length, lp=lp, bead_rad=bead_rad, t3=t3, t2=t2,
+                         states=states, binder_names=binder_names, chemical_mods=chemical_mods,
+                         chemical_mod_names=chemical_mod_names, log_path=log_path,
+                         max_binders=max_binders)
+
+    def _find_parameters(self, bead_length):
+        super()._find_parameters(bead_length)
+        # eps_twist = lt / (delta lp), delta = bead_length / lp (polymers.pyx:1957-2001)
+        self.eps_twist = self.lt / (self.delta * self.lp)
+
+    def natural_twist(self):
+        """omega0 per bond: bead_length * (2 pi / 10.5) / 0.332 (polymers.pyx:2088-2090)."""
+        return np.asarray(self.bead_length, dtype=np.float64) * NATURAL_TWIST_BARE / LENGTH_BP
+
+    def twist_parameters(self):
+        """(eps_twist, omega0) per bond, as the device takes them."""
+        return np.asarray(self.eps_twist, dtype=np.float64), self.natural_twist()
+
+    def __str__(self):
+        return f"Polymer_Class<SSTWLC>, {PolymerBase.__str__(self)}"
+
+
 class Chromatin(SSWLC):
     """SSWLC model of chromatin, lp = 53 nm (chromo/polymers.pyx:1821-1887)."""
 

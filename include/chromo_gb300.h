@@ -137,6 +137,16 @@ int cg_set_chains(cg_sim *sim, const double *const *r, const double *const *t3,
 int cg_get_chains(cg_sim *sim, double *const *r, double *const *t3, double *const *t2,
                   int64_t *const *states);
 
+/* SSTWLC twist for replica rep (chromo/polymers.pyx:1889-2320): per bond
+ * i -> i+1 (N - 1 each) the twist modulus eps_twist = lt / bead_length and the
+ * natural twist omega0 = bead_length * (2 pi / 10.5) / 0.332.  The bond
+ * energy gains 0.5 eps_twist dw^2, dw = omega - omega0 wrapped into
+ * [-pi, pi), omega the twist angle of the two beads' (t2, t3) frames
+ * (compute_twist_angle_omega, :3427-3461), in every move's dE and in the
+ * energies; FP64 arithmetic for both storage types.  eps_twist = NULL turns
+ * it off.  cg_gradient_device refuses dE/dt3 while a replica has twist. */
+int cg_set_twist(cg_sim *sim, int32_t rep, const double *eps_twist, const double *omega0);
+
 /* Field of one replica; access_vol [G] or NULL when every voxel is fully
  * accessible (get_accessible_volumes, chromo/fields.pyx:714-768). */
 int cg_set_field(cg_sim *sim, int32_t rep, const cg_field_params *field, const double *access_vol);
@@ -221,6 +231,22 @@ int cg_energies(cg_sim *sim, double *out, void *stream);
  * cross-talk prefactors are linear in eps, chromo/fields.pyx:687-712).
  * Synchronous. */
 int cg_gradient(cg_sim *sim, float *dEdr, double *terms);
+/* Device-resident counterparts for callers whose data already lives on the
+ * GPU (a torch.autograd.Function on CUDA tensors; no counterpart in the
+ * reference, which has no device).  All arrays are DEVICE pointers with the
+ * replicas' beads concatenated in replica order; all work is enqueued on
+ * `stream` and nothing is copied to the host.
+ * cg_set_chains_device: positions r and/or tangents t3 [total_beads x 3] FP64
+ *   (either may be NULL) into the resident chains (rounded to the storage type);
+ * cg_deposit_async: cg_deposit of every replica, on `stream`;
+ * cg_energies_device: out [n_replicas x 5] as cg_energies;
+ * cg_gradient_device: dE/dr and (dEdt3 != NULL) dE/dt3 [total_beads x 3] FP64
+ *   of the cg_energy sum; t3 enters only the elastic energy, through the two
+ *   bonds at each bead (chromo/polymers.pyx:1348-1381), taken as free vectors. */
+int cg_set_chains_device(cg_sim *sim, const double *r, const double *t3, void *stream);
+int cg_deposit_async(cg_sim *sim, void *stream);
+int cg_energies_device(cg_sim *sim, double *out, void *stream);
+int cg_gradient_device(cg_sim *sim, double *dEdr, double *dEdt3, void *stream);
 /* Add every replica's 14 terms T and their products T T^T to running sums on
  * the device (enqueued on `stream`), for reweighting: the covariance of any
  * two linear combinations of the terms follows from the sums. */
@@ -296,6 +322,21 @@ int cg_set_drift_guard(cg_sim *sim, int32_t every_rounds, double tol_abs, double
 /* drift[rep] (R entries) = the difference measured at the last check of each
  * replica; *checks = the number of checks made.  Waits for the device. */
 int cg_get_drift(cg_sim *sim, double *drift, int64_t *checks);
+
+/* Checkpoint of the whole resident state (no counterpart in the reference,
+ * whose resume restarts from a polymer CSV snapshot with fresh random streams,
+ * chromo/mc/__init__.py:167-227): chains, binding states, bond parameters,
+ * density grids, accessible volumes, controllers, tallies, every replica's
+ * parameters (chi, mu), move counter (which selects each move's Philox
+ * sub-stream) and running dE, the exchange slot map, round counter and swap
+ * counts.  cg_load_state into a sim created with the same layout (checked)
+ * continues the run exactly as if it had not stopped, given the same seeds.
+ * cg_state_bytes: the image size; cg_save_state / cg_load_state: host buffer
+ * of at least that size.  The drift guard takes new reference energies after
+ * a load. */
+int64_t cg_state_bytes(cg_sim *sim);
+int cg_save_state(cg_sim *sim, void *buf, int64_t bytes);
+int cg_load_state(cg_sim *sim, const void *buf, int64_t bytes);
 
 /* Per-round timing of cg_run_batched (no counterpart in the reference, which
  * has no device): with capacity > 0 every captured round brackets its MC

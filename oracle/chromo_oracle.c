@@ -112,6 +112,9 @@ typedef struct {
     int64_t *new_states;        /* N */
     unsigned char *picked;      /* N */
     int64_t fast_n;             /* fast_field: sub-bins per voxel and axis (0: exact weights) */
+    /* SSTWLC twist (NULL: SSWLC): eps_twist = lt / bead_length and the natural
+     * twist omega0 = bead_length * (2 pi / 10.5) / 0.332 per bond */
+    const double *eps_twist, *omega0;
 } or_system;
 
 typedef struct {
@@ -399,10 +402,37 @@ static double e_pair(const or_system *s, const double bend[3], double dr_par,
                                    + dr_perp[2] * dr_perp[2]);
 }
 
-/* bead_pair_dE_poly_forward, polymers.pyx:1177-1277 (bead 1 moved) */
+/* compute_twist_angle_omega, polymers.pyx:3427-3461: with t1 = t2 x t3,
+ * omega = atan2(t2_0 . t1_1 - t1_0 . t2_1, t1_0 . t1_1 + t2_0 . t2_1) */
+static double twist_omega(const double t2a[3], const double t3a[3], const double t2b[3], const double t3b[3])
+{
+    double t1a[3] = {t2a[1] * t3a[2] - t2a[2] * t3a[1], t2a[2] * t3a[0] - t2a[0] * t3a[2],
+                     t2a[0] * t3a[1] - t2a[1] * t3a[0]};
+    double t1b[3] = {t2b[1] * t3b[2] - t2b[2] * t3b[1], t2b[2] * t3b[0] - t2b[0] * t3b[2],
+                     t2b[0] * t3b[1] - t2b[1] * t3b[0]};
+    double y = (t2a[0] * t1b[0] + t2a[1] * t1b[1] + t2a[2] * t1b[2])
+             - (t1a[0] * t2b[0] + t1a[1] * t2b[1] + t1a[2] * t2b[2]);
+    double x = (t1a[0] * t1b[0] + t1a[1] * t1b[1] + t1a[2] * t1b[2])
+             + (t2a[0] * t2b[0] + t2a[1] * t2b[1] + t2a[2] * t2b[2]);
+    return atan2(y, x);
+}
+
+/* E_pair_with_twist, polymers.pyx:2050-2102: the SSWLC bond energy plus
+ * 0.5 eps_twist dw^2, dw = omega - omega0 wrapped into [-pi, pi) */
+static double e_pair_twist(const or_system *s, const double bend[3], double dr_par, const double dr_perp[3],
+                           double omega, int64_t b)
+{
+    double dw = omega - s->omega0[b];
+    dw -= 2 * M_PI * floor((dw + M_PI) / (2 * M_PI));
+    return e_pair(s, bend, dr_par, dr_perp, b) + 0.5 * s->eps_twist[b] * sq(dw, !s->fixed_density);
+}
+
+/* bead_pair_dE_poly_forward, polymers.pyx:1177-1277 (bead 1 moved); with
+ * twist bead_pair_dE_poly_forward_with_twist, :2104-2175 (t2 of both beads) */
 static double pair_dE_fwd(const or_system *s, const double r0[3], const double r1[3],
                           const double tr1[3], const double t30[3], const double t31[3],
-                          const double tt31[3], int64_t b)
+                          const double tt31[3], int64_t b, const double t20[3], const double t21[3],
+                          const double tt21[3])
 {
     double drt[3], dr[3], dpt[3], dp[3], bt[3], bc[3];
     for (int i = 0; i < 3; i++) { drt[i] = tr1[i] - r0[i]; dr[i] = r1[i] - r0[i]; }
@@ -414,13 +444,18 @@ static double pair_dE_fwd(const or_system *s, const double r0[3], const double r
         bt[i] = tt31[i] - t30[i] - dpt[i] * s->eta[b];
         bc[i] = t31[i] - t30[i] - dp[i] * s->eta[b];
     }
+    if (s->eps_twist)
+        return e_pair_twist(s, bt, pt, dpt, twist_omega(t20, t30, tt21, tt31), b)
+             - e_pair_twist(s, bc, pc, dp, twist_omega(t20, t30, t21, t31), b);
     return e_pair(s, bt, pt, dpt, b) - e_pair(s, bc, pc, dp, b);
 }
 
-/* bead_pair_dE_poly_reverse, polymers.pyx:1279-1346 (bead 0 moved) */
+/* bead_pair_dE_poly_reverse, polymers.pyx:1279-1346 (bead 0 moved); with
+ * twist bead_pair_dE_poly_reverse_with_twist, :2177-2248 */
 static double pair_dE_rev(const or_system *s, const double r0[3], const double tr0[3],
                           const double r1[3], const double t30[3], const double tt30[3],
-                          const double t31[3], int64_t b)
+                          const double t31[3], int64_t b, const double t20[3], const double tt20[3],
+                          const double t21[3])
 {
     double drt[3], dr[3], dpt[3], dp[3], bt[3], bc[3];
     for (int i = 0; i < 3; i++) { drt[i] = r1[i] - tr0[i]; dr[i] = r1[i] - r0[i]; }
@@ -432,6 +467,9 @@ static double pair_dE_rev(const or_system *s, const double r0[3], const double t
         bt[i] = t31[i] - tt30[i] - dpt[i] * s->eta[b];
         bc[i] = t31[i] - t30[i] - dp[i] * s->eta[b];
     }
+    if (s->eps_twist)
+        return e_pair_twist(s, bt, pt, dpt, twist_omega(tt20, tt30, t21, t31), b)
+             - e_pair_twist(s, bc, pc, dp, twist_omega(t20, t30, t21, t31), b);
     return e_pair(s, bt, pt, dpt, b) - e_pair(s, bc, pc, dp, b);
 }
 
@@ -440,14 +478,16 @@ static double pair_dE_rev(const or_system *s, const double r0[3], const double t
 static double continuous_dE(const or_system *s, int64_t ind0, int64_t indf,
                             const double *trial_first, const double *trial_last)
 {
-    double dE = 0, a[3], b[3], c[3], d[3];
+    double dE = 0, a[3], b[3], c[3], d[3], e[3], f[3];
     if (ind0 != 0) {
         ld3(s->r, ind0 - 1, a); ld3(s->r, ind0, b); ld3(s->t3, ind0 - 1, c); ld3(s->t3, ind0, d);
-        dE += pair_dE_fwd(s, a, b, trial_first, c, d, trial_first + 3, ind0 - 1);
+        ld3(s->t2, ind0 - 1, e); ld3(s->t2, ind0, f);
+        dE += pair_dE_fwd(s, a, b, trial_first, c, d, trial_first + 3, ind0 - 1, e, f, trial_first + 6);
     }
     if (indf != s->n_beads) {
         ld3(s->r, indf - 1, a); ld3(s->r, indf, b); ld3(s->t3, indf - 1, c); ld3(s->t3, indf, d);
-        dE += pair_dE_rev(s, a, trial_last, b, c, trial_last + 3, d, indf - 1);
+        ld3(s->t2, indf - 1, e); ld3(s->t2, indf, f);
+        dE += pair_dE_rev(s, a, trial_last, b, c, trial_last + 3, d, indf - 1, e, trial_last + 6, f);
     }
     return dE;
 }
@@ -463,7 +503,13 @@ double or_elastic_E(const or_system *s)
         double par = a[0] * dr[0] + a[1] * dr[1] + a[2] * dr[2];
         for (int j = 0; j < 3; j++) dp[j] = dr[j] - a[j] * par;
         for (int j = 0; j < 3; j++) bend[j] = b[j] + (-a[j] - s->eta[i - 1] * dp[j]);
-        E += e_pair(s, bend, par, dp, i - 1);
+        if (s->eps_twist) {  /* SSTWLC.compute_E, polymers.pyx:2250-2285 */
+            double c2[3], d2[3];
+            ld3(s->t2, i - 1, c2); ld3(s->t2, i, d2);
+            E += e_pair_twist(s, bend, par, dp, twist_omega(c2, a, d2, b), i - 1);
+        } else {
+            E += e_pair(s, bend, par, dp, i - 1);
+        }
     }
     return E;
 }

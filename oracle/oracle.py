@@ -41,7 +41,7 @@ class _System(C.Structure):
         ("fixed_density", _I), ("density", _P), ("density_fx", _P),
         ("density_trial", _P), ("dfx", _P), ("slot_of", _P), ("found", _P),
         ("n_found", _I), ("found_cap", _I), ("inds", _P), ("trial", _P),
-        ("new_states", _P), ("picked", _P), ("fast_n", _I),
+        ("new_states", _P), ("picked", _P), ("fast_n", _I), ("eps_twist", _P), ("omega0", _P),
     ]
 
 
@@ -128,6 +128,8 @@ class OracleSystem:
     fixed_density: 0 for the reference's FP64 density, 1 for int64 fixed point.
     fast_n: fast_field sub-bins per voxel and axis for the per-move density
     changes (0: exact weights).
+    eps_twist, omega0: per-bond twist modulus and natural twist of an SSTWLC
+    chain (None: SSWLC).
     """
 
     def __init__(self, *, r, t3, t2, states, marks, eps_bend, gamma, eps_par, eps_perp,
@@ -135,7 +137,7 @@ class OracleSystem:
                  field_kind=2, confine_kind=0, confine_length=0.0,
                  nxyz=(1, 1, 1), widths=(1.0, 1.0, 1.0), access_vol=None, chi=1.0,
                  vf_limit=0.5, bead_vol=4 / 3 * np.pi * 125, pref=(), intra=(), xpref=None,
-                 pos="f64", fixed_density=0, fast_n=0):
+                 pos="f64", fixed_density=0, fast_n=0, eps_twist=None, omega0=None):
         self.pos = pos
         fdt = np.float64 if pos == "f64" else np.float32
         # private copies: the oracle mutates its state in place
@@ -180,6 +182,11 @@ class OracleSystem:
         s.pref, s.intra, s.xpref = self.pref.ctypes.data, self.intra.ctypes.data, self.xpref.ctypes.data
         s.fixed_density = fixed_density
         s.fast_n = int(fast_n) + int(fast_n) % 2
+        self.twist = None
+        if eps_twist is not None:  # SSTWLC: twist modulus and natural twist per bond
+            self.twist = [np.ascontiguousarray(eps_twist, dtype=np.float64),
+                          np.ascontiguousarray(omega0, dtype=np.float64)]
+            s.eps_twist, s.omega0 = self.twist[0].ctypes.data, self.twist[1].ctypes.data
         s.density, s.density_fx = self.density.ctypes.data, self.density_fx.ctypes.data
         self._s = s
         self._L = lib(pos)

@@ -4,11 +4,14 @@ statistical check of the GPU path (tests/test_gpu_equilibrium.py).
 Run here (the container that mounts the reference), after
 ``python oracle/build_reference.py``::
 
-    python tests/golden/make_equilibrium.py
+    python tests/golden/make_equilibrium.py [one_binder|two_binders]
 
-One small system -- a 100-bead Chromatin chain (16.5 nm spacing, lp 53 nm)
-with one binder (HP1 preset, mu = -0.4, eps = -4) in a periodic 240 nm box of
-6^3 voxels, chi = 1, all five moves under SimpleControl -- is run RUNS times
+Each case is one small system run RUNS times.  one_binder: a 100-bead
+Chromatin chain (16.5 nm spacing, lp 53 nm) with one binder (HP1 preset,
+mu = -0.4, eps = -4) in a periodic 240 nm box of 6^3 voxels, chi = 1, all
+five moves under SimpleControl.  two_binders: the same chain with two binders
+(HP1: mu = -0.5, eps = -4, cross talk +1 with PRC1; PRC1: mu = -0.3,
+eps = -3), chi = 1.5.  Each system is run RUNS times
 from the same seeded start with independent random streams (libc ``srand``
 and numpy seeds per run; ``mc_sim`` reseeds numpy on every call, so every call
 gets its own seed).  After BURN MC steps, SAMPLES snapshots are taken every
@@ -16,7 +19,7 @@ EVERY steps and the per-run time averages of these observables are stored:
 
 * R2: squared end-to-end distance (unwrapped positions), nm^2;
 * Rg2: squared radius of gyration, nm^2;
-* occupancy: mean binding state / sites per bead;
+* occupancy: mean binding state / sites per bead, per binder;
 * five fractions of voxels whose bead count (density times voxel volume) is
   below 0.05, in [0.05, 0.25), [0.25, 0.5), [0.5, 1), or 1 and above (the
   first bin is open below: the reference's FP64 density of an emptied voxel
@@ -36,24 +39,33 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
-OUT = HERE / "stats" / "eq_one_binder.npz"
 
-CFG = dict(n=100, nbins=6, vox=40.0, binders=[("HP1", -0.4, -4.0, {})], chi=1.0, moves="all",
-           seed=21, run=20)
+CASES = {
+    "one_binder": dict(n=100, nbins=6, vox=40.0, binders=[("HP1", -0.4, -4.0, {})], chi=1.0,
+                       moves="all", seed=21, run=20),
+    "two_binders": dict(n=100, nbins=6, vox=40.0, binders=[("HP1", -0.5, -4.0, {"PRC1": 1.0}),
+                                                           ("PRC1", -0.3, -3.0, {})],
+                        chi=1.5, moves="all", seed=22, run=20),
+}
 RUNS, BURN, SAMPLES, EVERY = 16, 1500, 300, 20
 BINS = np.array([-np.inf, 0.05, 0.25, 0.5, 1.0, np.inf])
-OBS = ["R2", "Rg2", "occupancy", "vox_0_0.05", "vox_0.05_0.25", "vox_0.25_0.5", "vox_0.5_1",
-       "vox_1_inf", "count2"]
+VOX = ["vox_0_0.05", "vox_0.05_0.25", "vox_0.25_0.5", "vox_0.5_1", "vox_1_inf"]
+
+
+def obs_names(binder_names):
+    occ = ["occupancy"] if len(binder_names) == 1 else [f"occupancy_{b}" for b in binder_names]
+    return ["R2", "Rg2"] + occ + VOX + ["count2"]
 
 
 def observables(r, states, counts, sites):
-    """The observables of one snapshot (shared with the GPU test)."""
+    """The observables of one snapshot (shared with the GPU test): R2, Rg2, the
+    occupancy of each binder, the voxel bead-count histogram, its second moment."""
     r = np.asarray(r, dtype=np.float64)
     d = r[-1] - r[0]
     rc = r - r.mean(axis=0)
     hist = np.histogram(counts, bins=BINS)[0] / len(counts)
-    return np.concatenate([[d @ d, (rc * rc).sum(axis=1).mean(), np.mean(states[:, 0]) / sites],
-                           hist, [np.mean(counts ** 2)]])
+    occ = [np.mean(states[:, b]) / sites[b] for b in range(states.shape[1])]
+    return np.concatenate([[d @ d, (rc * rc).sum(axis=1).mean()], occ, hist, [np.mean(counts ** 2)]])
 
 
 def _setup():
@@ -62,12 +74,15 @@ def _setup():
     return mg
 
 
-def one_run(k):
+def one_run(args):
+    name, k = args
+    cfg = CASES[name]
     mg = _setup()
     from chromo.mc.mc_sim import mc_sim
-    p, binders, marks, _ = mg.build_case(CFG)
-    field = mg.make_field(CFG, p, binders)
-    ctrls = mg.make_controllers(CFG, p)
+    p, binders, marks, _ = mg.build_case(cfg)
+    field = mg.make_field(cfg, p, binders)
+    ctrls = mg.make_controllers(cfg, p)
+    sites = [mg.cb.get_by_name(b[0]).sites_per_bead for b in cfg["binders"]]
     libc = ctypes.CDLL(None)
     libc.srand(7919 * (k + 1))
     seed = 100000 * (k + 1)
@@ -77,42 +92,47 @@ def one_run(k):
     for s in range(SAMPLES):
         mc_sim([p], binders, EVERY, ctrls, field, 1.0, seed + 1 + s)
         counts = np.asarray(field.density)[:, 0] * vol
-        obs.append(observables(p.r, np.asarray(p.states), counts, 2))
+        obs.append(observables(p.r, np.asarray(p.states), counts, sites))
     return np.mean(obs, axis=0)
 
 
-def main():
+def main(name):
+    cfg = CASES[name]
+    out = HERE / "stats" / f"eq_{name}.npz"
     mg = _setup()
-    p, binders, marks, states0 = mg.build_case(CFG)
-    field = mg.make_field(CFG, p, binders)
-    ctrls = mg.make_controllers(CFG, p)
+    p, binders, marks, states0 = mg.build_case(cfg)
+    field = mg.make_field(cfg, p, binders)
+    ctrls = mg.make_controllers(cfg, p)
     ctl0 = [(c.move.amp_move, c.move.amp_bead, c.move.num_per_cycle, 1,
              c.bead_amp_bounds[0], c.bead_amp_bounds[1], c.move_amp_bounds[0], c.move_amp_bounds[1])
             for c in ctrls]
-    row = field.binder_dict[0]
-    hp1 = mg.cb.get_by_name("HP1")
+    rows = field.binder_dict
+    objs = [mg.cb.get_by_name(b[0]) for b in cfg["binders"]]
+    names = [b[0] for b in cfg["binders"]]
     with mp.get_context("spawn").Pool(min(RUNS, mp.cpu_count())) as pool:
-        runs = np.array(pool.map(one_run, range(RUNS)))
-    OUT.parent.mkdir(exist_ok=True)
+        runs = np.array(pool.map(one_run, [(name, k) for k in range(RUNS)]))
+    out.parent.mkdir(exist_ok=True)
     np.savez_compressed(
-        OUT, obs_names=np.array(OBS), runs=runs, burn=BURN, samples=SAMPLES, every=EVERY,
+        out, obs_names=np.array(obs_names(names)), runs=runs, burn=BURN, samples=SAMPLES, every=EVERY,
         r0=np.asarray(p.r).copy(), t30=np.asarray(p.t3).copy(), t20=np.asarray(p.t2).copy(),
         states0=np.asarray(p.states).copy(), marks=np.asarray(p.chemical_mods).copy(),
         eps_bend=np.asarray(p.eps_bend), gamma=np.asarray(p.gamma), eps_par=np.asarray(p.eps_par),
         eps_perp=np.asarray(p.eps_perp), eta=np.asarray(p.eta),
-        sites=np.array([hp1.sites_per_bead]), e_mod=np.array([hp1.bind_energy_mod]),
-        e_nomod=np.array([hp1.bind_energy_no_mod]), mu=np.array([hp1.chemical_potential]),
+        sites=np.array([o.sites_per_bead for o in objs]), e_mod=np.array([o.bind_energy_mod for o in objs]),
+        e_nomod=np.array([o.bind_energy_no_mod for o in objs]),
+        mu=np.array([o.chemical_potential for o in objs]),
         nxyz=np.array([field.nx, field.ny, field.nz]),
         widths=np.array([field.x_width, field.y_width, field.z_width]), chi=field.chi,
         vf_limit=field.vf_limit, bead_rad=5.0,
-        pref=np.array([row["field_energy_prefactor"]]),
-        intra=np.array([row["interaction_energy_intranucleosome"]]),
-        xpref=np.array([[row["cross_talk_field_energy_prefactor"][row["name"]]]]),
+        pref=np.array([r["field_energy_prefactor"] for r in rows]),
+        intra=np.array([r["interaction_energy_intranucleosome"] for r in rows]),
+        xpref=np.array([[r["cross_talk_field_energy_prefactor"][o["name"]] for o in rows] for r in rows]),
         ctl0=np.array(ctl0, dtype=np.float64))
     m, se = runs.mean(axis=0), runs.std(axis=0, ddof=1) / np.sqrt(RUNS)
-    for name, a, b_ in zip(OBS, m, se):
-        print(f"{name:>14}: {a:.6g} +- {b_:.3g}")
+    for nm, a, b_ in zip(obs_names(names), m, se):
+        print(f"{nm:>20}: {a:.6g} +- {b_:.3g}")
 
 
 if __name__ == "__main__":
-    main()
+    for nm in sys.argv[1:] or list(CASES):
+        main(nm)

@@ -40,7 +40,7 @@ import chromo.mc.mc_controller as ctl  # noqa: E402
 import chromo.mc.move_funcs as mf  # noqa: E402
 from chromo.fields import NullField, UniformDensityField  # noqa: E402
 from chromo.mc.mc_sim import mc_sim  # noqa: E402
-from chromo.polymers import Chromatin  # noqa: E402
+from chromo.polymers import SSTWLC, Chromatin  # noqa: E402
 import ref_shim  # noqa: E402
 
 LIBC = ctypes.CDLL(None)
@@ -99,6 +99,10 @@ CASES = {
     "fast_field": dict(n=200, nbins=8, vox=40.0, binders=[("HP1", -0.5, -4.0, {"PRC1": 1.0}),
                                                           ("PRC1", -0.3, -3.0, {})],
                        chi=1.2, fast=64, steps=4, moves="all", seed=18, run=30),
+    # twist: an SSTWLC chain (twist persistence length 100 nm), whose bond energy
+    # adds the twist term of the t2 / t3 frames (chromo/polymers.pyx:1889-2320)
+    "twist": dict(n=200, nbins=8, vox=40.0, binders=[("HP1", -0.4, -4.0, {})], chi=1.0, lt=100.0,
+                  steps=4, moves="all", seed=19, run=20),
     # large amplitudes without adaptation: long segments, many tangent beads
     "big_amps": dict(n=160, nbins=8, vox=40.0, binders=[("HP1", -0.4, -4.0, {})], chi=1.0,
                      steps=30, moves="big", seed=16, run=20),
@@ -120,10 +124,13 @@ def build_case(cfg):
     states = rng.integers(0, 3, size=marks.shape).astype(np.int64) if cfg.get("random_states") \
         else np.zeros_like(marks)
     np.random.seed(cfg["seed"])
-    p = Chromatin.gaussian_walk_polymer(
-        "p", n, np.full(n - 1, 16.5), states=states, binder_names=np.array(names),
-        chemical_mods=marks, chemical_mod_names=np.array([f"m{i}" for i in range(len(names))]),
-        max_binders=cfg.get("max_binders", -1))
+    kw = dict(states=states, binder_names=np.array(names), chemical_mods=marks,
+              chemical_mod_names=np.array([f"m{i}" for i in range(len(names))]),
+              max_binders=cfg.get("max_binders", -1))
+    if cfg.get("lt"):
+        p = SSTWLC.gaussian_walk_polymer("p", n, np.full(n - 1, 16.5), lp=53.0, lt=cfg["lt"], **kw)
+    else:
+        p = Chromatin.gaussian_walk_polymer("p", n, np.full(n - 1, 16.5), **kw)
     return p, binders, marks, states
 
 
@@ -157,12 +164,13 @@ def make_controllers(cfg, p):
 
 def clone(p, cfg):
     names = list(np.asarray(p.binder_names))
-    return Chromatin("p", np.asarray(p.r).copy(), bead_length=np.asarray(p.bead_length).copy(),
-                     t3=np.asarray(p.t3).copy(), t2=np.asarray(p.t2).copy(),
-                     states=np.asarray(p.states).copy(), binder_names=np.array(names),
-                     chemical_mods=np.asarray(p.chemical_mods).copy(),
-                     chemical_mod_names=np.asarray(p.chemical_mod_names),
-                     max_binders=cfg.get("max_binders", -1))
+    kw = dict(bead_length=np.asarray(p.bead_length).copy(), t3=np.asarray(p.t3).copy(),
+              t2=np.asarray(p.t2).copy(), states=np.asarray(p.states).copy(),
+              binder_names=np.array(names), chemical_mods=np.asarray(p.chemical_mods).copy(),
+              chemical_mod_names=np.asarray(p.chemical_mod_names), max_binders=cfg.get("max_binders", -1))
+    if cfg.get("lt"):
+        return SSTWLC("p", np.asarray(p.r).copy(), lp=53.0, lt=cfg["lt"], **kw)
+    return Chromatin("p", np.asarray(p.r).copy(), **kw)
 
 
 def audit_loop(p, field, ctrls, steps, mu_adjust_factor):
@@ -301,6 +309,8 @@ def run_case(name, cfg):
         access_vols=(np.array([field.access_vols[i] for i in range(field.n_bins)])
                      if uniform and cfg.get("access") else None),
         fast_n=field.n_points if uniform and cfg.get("fast") else None,
+        lt=cfg.get("lt"), eps_twist=np.asarray(p.eps_twist).copy() if cfg.get("lt") else None,
+        omega0=(np.asarray(p.bead_length) * (2 * np.pi / 10.5) / 0.332) if cfg.get("lt") else None,
     )
     out = {k: v for k, v in out.items() if v is not None}
     np.savez_compressed(OUT / f"{name}.npz", **out)

@@ -28,7 +28,8 @@ def oracle_system(g, pos="f64", fixed_density=0, state="0"):
         access_vol=g.get("access_vols"), chi=float(g["chi"]), vf_limit=float(g["vf_limit"]),
         bead_vol=4.0 / 3.0 * np.pi * float(g["bead_rad"]) ** 3,
         pref=g["pref"], intra=g["intra"], xpref=g["xpref"], pos=pos,
-        fixed_density=fixed_density, fast_n=int(g.get("fast_n", 0)))
+        fixed_density=fixed_density, fast_n=int(g.get("fast_n", 0)),
+        eps_twist=g.get("eps_twist"), omega0=g.get("omega0"))
 
 
 def oracle_ctls(g):
@@ -76,6 +77,8 @@ def gpu_sim(g, pos_fp64, state="0", warps_per_block=0, lanes_per_move=0):
                              num_per_cycle=int(npc), simple=bool(simple), bead_bounds=(blo, bhi),
                              move_bounds=(mlo, mhi)))
     sim.set_controllers(0, ctls)
+    if "eps_twist" in g:
+        sim.set_twist(0, g["eps_twist"], g["omega0"])
     if uniform:
         sim.deposit(0)
     return sim

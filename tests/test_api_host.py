@@ -7,7 +7,7 @@ import chromo_gb300.binders as cb
 from chromo_gb300.fields import NullField, UniformDensityField
 from chromo_gb300.mc import get_amplitude_bounds
 from chromo_gb300.mc.mc_controller import SimpleControl, all_moves
-from chromo_gb300.polymers import Chromatin
+from chromo_gb300.polymers import SSTWLC, Chromatin
 from golden_cases import CASES, load
 
 
@@ -20,10 +20,13 @@ def _poly_from_golden(g, state="0"):
         b.cross_talk_interaction_energy = {
             str(o): float(g["cross"][i, j]) for j, o in enumerate(names)
             if not np.isnan(g["cross"][i, j])}
-    p = Chromatin("p", g["r" + state], bead_length=g["bead_length"], t3=g["t3" + state],
-                  t2=g["t2" + state], states=g["states" + state], binder_names=np.array(names),
-                  chemical_mods=g["marks"], chemical_mod_names=np.array(names),
-                  max_binders=int(g["max_binders"]))
+    kw = dict(bead_length=g["bead_length"], t3=g["t3" + state], t2=g["t2" + state],
+              states=g["states" + state], binder_names=np.array(names), chemical_mods=g["marks"],
+              chemical_mod_names=np.array(names), max_binders=int(g["max_binders"]))
+    if "lt" in g:  # an SSTWLC chain
+        p = SSTWLC("p", g["r" + state], lp=float(g["lp"]), lt=float(g["lt"]), **kw)
+    else:
+        p = Chromatin("p", g["r" + state], **kw)
     binders = cb.make_binder_collection([cb.get_by_name(n) for n in names])
     return p, binders
 
@@ -34,6 +37,10 @@ def test_sswlc_parameters_match_reference(name):
     p, _ = _poly_from_golden(g)
     for k in ("eps_bend", "gamma", "eps_par", "eps_perp", "eta"):
         np.testing.assert_array_equal(getattr(p, k), g[k])
+    if "lt" in g:  # SSTWLC: twist modulus (polymers.pyx:1957-2001) and natural twist
+        eps, w0 = p.twist_parameters()
+        np.testing.assert_array_equal(eps, g["eps_twist"])
+        np.testing.assert_array_equal(w0, g["omega0"])
 
 
 @pytest.mark.parametrize("name", [c for c in CASES if c != "null_spherical"])

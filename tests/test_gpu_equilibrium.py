@@ -1,18 +1,20 @@
 """Long runs reproduce the reference's equilibrium statistics.
 
-The fixture ``tests/golden/stats/eq_one_binder.npz`` (written by
+The fixtures ``tests/golden/stats/eq_<case>.npz`` (written by
 ``tests/golden/make_equilibrium.py`` from the reference's own ``mc_sim``)
-holds the per-run time averages of independent reference runs from one
-seeded start: a 100-bead chain with one binder in a periodic 6^3-voxel box.
-Here 64 replicas of the same start run on the GPU (FP32 storage, independent
-Philox streams) for the same burn-in and sampling schedule, and every
-observable -- squared end-to-end distance and radius of gyration, binder
-occupancy, the histogram of bead counts per voxel and its second moment --
-must agree with the reference's mean within 3 combined standard errors (the
-per-run and per-replica time averages are independent samples).  The Markov
-chains differ only in their random streams (libc rand() against Philox), so
-this is the distributional check of the whole move set, the field and the
-controllers over ~1e8 moves.
+hold the per-run time averages of independent reference runs from one seeded
+start: a 100-bead chain in a periodic 6^3-voxel box with one binder
+(one_binder) or with two binders and cross talk (two_binders).  Here 64
+replicas of the same start run on the GPU (FP32 storage, independent Philox
+streams) for the same burn-in and sampling schedule -- the two-binder case at
+the launch shape of the batched benchmark, 6 warps x 32 lanes per replica --
+and every observable (squared end-to-end distance and radius of gyration,
+each binder's occupancy, the histogram of bead counts per voxel and its
+second moment) must agree with the reference's mean within 3 combined
+standard errors (the per-run and per-replica time averages are independent
+samples).  The Markov chains differ only in their random streams (libc
+rand() against Philox), so this is the distributional check of the whole
+move set, the field, cross talk and the controllers over ~1e8 moves.
 """
 from pathlib import Path
 
@@ -20,7 +22,7 @@ import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
-FIXTURE = Path(__file__).resolve().parent / "golden" / "stats" / "eq_one_binder.npz"
+STATS = Path(__file__).resolve().parent / "golden" / "stats"
 BINS = np.array([-np.inf, 0.05, 0.25, 0.5, 1.0, np.inf])
 MOVE_NAMES = ["crank_shaft", "end_pivot", "slide", "tangent_rotation", "change_binding_state"]
 
@@ -30,20 +32,22 @@ def observables(r, states, counts, sites):
     d = r[-1] - r[0]
     rc = r - r.mean(axis=0)
     hist = np.histogram(counts, bins=BINS)[0] / len(counts)
-    return np.concatenate([[d @ d, (rc * rc).sum(axis=1).mean(), np.mean(states[:, 0]) / sites],
-                           hist, [np.mean(counts ** 2)]])
+    occ = [np.mean(states[:, b]) / sites[b] for b in range(states.shape[1])]
+    return np.concatenate([[d @ d, (rc * rc).sum(axis=1).mean()], occ, hist, [np.mean(counts ** 2)]])
 
 
-def _replicas(g, R):
+def _replicas(g, R, shape=(0, 0)):
     from chromo_gb300 import _native as nat
     from chromo_gb300.device import binding_params, bonds_array, field_params, move_ctl
     n = len(g["r0"])
+    nb = len(g["sites"])
     ctl0 = g["ctl0"]
     max_seg = int(max(max(row[1], row[5]) for k, row in enumerate(ctl0) if k != 3)) + 2
-    sim = nat.Sim([n] * R, [list(g["nxyz"])] * R, 1, max_segment=max_seg,
-                  max_tangent=int(max(ctl0[3][1], ctl0[3][5])))
+    sim = nat.Sim([n] * R, [list(g["nxyz"])] * R, nb, max_segment=max_seg,
+                  max_tangent=int(max(ctl0[3][1], ctl0[3][5])), warps_per_block=shape[0],
+                  lanes_per_move=shape[1])
     bonds = bonds_array(g["eps_bend"], g["gamma"], g["eps_par"], g["eps_perp"], g["eta"])
-    fp = field_params(field_kind=2, nxyz=g["nxyz"], widths=g["widths"], n_binders=1,
+    fp = field_params(field_kind=2, nxyz=g["nxyz"], widths=g["widths"], n_binders=nb,
                       chi=float(g["chi"]), vf_limit=float(g["vf_limit"]),
                       bead_vol=4.0 / 3.0 * np.pi * float(g["bead_rad"]) ** 3, pref=g["pref"],
                       intra=g["intra"], xpref=g["xpref"])
@@ -62,14 +66,16 @@ def _replicas(g, R):
     return sim
 
 
-def test_equilibrium_statistics_match_reference():
-    if not FIXTURE.exists():
+@pytest.mark.parametrize("case,shape", [("one_binder", (0, 0)), ("two_binders", (6, 32))])
+def test_equilibrium_statistics_match_reference(case, shape):
+    fixture = STATS / f"eq_{case}.npz"
+    if not fixture.exists():
         pytest.skip("equilibrium fixture not generated")
-    with np.load(FIXTURE, allow_pickle=False) as z:
+    with np.load(fixture, allow_pickle=False) as z:
         g = {k: z[k] for k in z.files}
     R, seed = 64, 20261203
-    sim = _replicas(g, R)
-    sites = int(g["sites"][0])
+    sim = _replicas(g, R, shape)
+    sites = [int(x) for x in g["sites"]]
     sim.run(int(g["burn"]), seed)
     acc = np.zeros((R, len(g["obs_names"])))
     for _ in range(int(g["samples"])):

@@ -139,12 +139,18 @@ def test_sampled_sensitivities_are_finite_and_counted():
 
 
 @pytest.mark.gpu
-def test_autograd_bridge_returns_the_kernel_gradient():
+def test_autograd_bridge_on_device_tensors():
+    """replica_energy on CUDA tensors: energies equal cg_energies, dE/dr equals
+    the gradient kernel's (FP32 output of cg_gradient, so within FP32
+    rounding), dE/dt3 equals FP64 central differences of the NumPy energy
+    (h = 1e-6; the energy is quadratic in t3), and every tensor stays on the
+    device."""
     torch = pytest.importorskip("torch")
     from chromo_gb300.autograd import replica_energy
     from chromo_gb300.batched import ReplicaBatch
     from golden_cases import load
     from test_gpu_api import _setup as api_setup
+    from energy_model import elastic
     polys, fields, ctrls = [], [], []
     for _ in range(3):
         p, _, f, c = api_setup(load("two_binders"))
@@ -152,11 +158,63 @@ def test_autograd_bridge_returns_the_kernel_gradient():
         fields.append(f)
         ctrls.append(c)
     with ReplicaBatch(polys, fields, ctrls, precision="fp64") as b:
-        pos = torch.tensor(np.concatenate([p.r for p in polys]), dtype=torch.float64, requires_grad=True)
-        E = replica_energy(pos, b)
-        np.testing.assert_allclose(E.detach().numpy(), b.energies()[:, :3].sum(1), rtol=1e-12)
-        weights = torch.tensor([1.0, -2.0, 0.5], dtype=torch.float64)
-        (E * weights).sum().backward()
+        dev = torch.device("cuda")
+        pos = torch.tensor(np.concatenate([p.r for p in polys]), dtype=torch.float64, device=dev,
+                           requires_grad=True)
+        t3 = torch.tensor(np.concatenate([p.t3 for p in polys]), dtype=torch.float64, device=dev,
+                          requires_grad=True)
+        E = replica_energy(pos, b, tangents=t3)
+        assert E.is_cuda
+        np.testing.assert_allclose(E.detach().cpu().numpy(), b.energies()[:, :3].sum(1), rtol=1e-12)
+        weights = torch.tensor([1.0, -2.0, 0.5], dtype=torch.float64, device=dev)
+        gr, gt = torch.autograd.grad((E * weights).sum(), (pos, t3))
+        assert gr.is_cuda and gt.is_cuda
         per, _ = b.gradient()
         want = np.concatenate([w * g.astype(np.float64) for w, g in zip([1.0, -2.0, 0.5], per)])
-        np.testing.assert_allclose(pos.grad.numpy(), want, rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(gr.cpu().numpy(), want, rtol=2e-6, atol=1e-6)
+        # dE/dt3 of replica 0 against central differences of the elastic energy
+        p0 = polys[0]
+        n = p0.num_beads
+        bonds = np.stack([p0.eps_bend, p0.gamma, p0.eps_par, p0.eps_perp, p0.eta], axis=1)
+        r0, a0 = np.asarray(p0.r, dtype=np.float64), np.asarray(p0.t3, dtype=np.float64)
+        h = 1e-6
+        got = gt.cpu().numpy()[:n]
+        for i in (0, 1, n // 2, n - 1):
+            for j in range(3):
+                up, dn = a0.copy(), a0.copy()
+                up[i, j] += h
+                dn[i, j] -= h
+                fd = (elastic(r0, up, bonds) - elastic(r0, dn, bonds)) / (2 * h)
+                assert got[i, j] == pytest.approx(fd, rel=1e-6, abs=1e-6), (i, j)
+
+
+@pytest.mark.gpu
+def test_device_sums_of_sampled_terms_equal_host_sums():
+    """cg_sample_terms adds every replica's 14 terms T and T T^T to running sums
+    on the device; after each of 12 sampled configurations the host reads the
+    same terms (cg_gradient), and the device sums equal the host sums."""
+    pytest.importorskip("torch")
+    from chromo_gb300.batched import ReplicaBatch
+    from golden_cases import load
+    from test_gpu_api import _setup as api_setup
+    polys, fields, ctrls = [], [], []
+    for _ in range(2):
+        p, _, f, c = api_setup(load("two_binders"))
+        polys.append(p)
+        fields.append(f)
+        ctrls.append(c)
+    with ReplicaBatch(polys, fields, ctrls) as b:
+        b.sim.samples(reset=True)
+        host_t, host_tt = 0.0, 0.0
+        for k in range(12):
+            b.sim.run(1, 500 + k)
+            b.sim.sync()
+            _, T = b.sim.gradient(positions=False, terms=True)
+            host_t = host_t + T
+            host_tt = host_tt + np.einsum("ri,rj->rij", T, T)
+            b.sim.sample_terms()
+        b.sim.sync()
+        sum_t, sum_tt, count = b.sim.samples()
+        assert np.all(count == 12)
+        np.testing.assert_allclose(sum_t, host_t, rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(sum_tt, host_tt, rtol=1e-12, atol=1e-12)

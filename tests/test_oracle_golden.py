@@ -25,7 +25,12 @@ def test_oracle_reproduces_reference(name):
     assert len(recs) == len(ref)
     for f in ("kind", "n_inds", "accepted"):
         np.testing.assert_array_equal(recs[f], ref[f])
-    np.testing.assert_array_equal(recs["dE_poly"], ref["dE_poly"])
+    if "eps_twist" in g:
+        # the twist angle's dot products go through numpy's BLAS in the
+        # reference, whose summation order is unspecified: last-bit differences
+        np.testing.assert_allclose(recs["dE_poly"], ref["dE_poly"], rtol=1e-9, atol=1e-12)
+    else:
+        np.testing.assert_array_equal(recs["dE_poly"], ref["dE_poly"])
     np.testing.assert_array_equal(recs["dE_field"], ref["dE_field"])
     np.testing.assert_array_equal(s.r, g["r1"])
     np.testing.assert_array_equal(s.t3, g["t31"])

@@ -72,23 +72,28 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-budget", type=float, default=2.0)
     ap.add_argument("--profile", action="store_true",
-                    help="case for ncu: 256 x 5000-bead replicas, 1 warm-up + 2 MC launches")
+                    help="case for ncu: 256 x 5000-bead replicas settled for %d MC launches, then "
+                         "1 warm-up + 2 MC launches" % 80)
     return ap.parse_args()
 
 
 def profile_case(args):
     """A bounded case for profilers: 256 replicas of 5,000 beads each (the
     batched workload's CTA shape), 40^3 grids of 3 int64 columns (393 MB of
-    grids: larger than L2, under 1 GB on the device), one warm-up launch and
-    two launches of the MC kernel of 62 steps each."""
+    grids: larger than L2, under 1 GB on the device), brought to steady state
+    by SETTLE_ROUNDS launches of the MC kernel (62 steps each), then one
+    warm-up launch and two launches: a profiler captures MC launch number
+    SETTLE_ROUNDS + 2 (-k regex:spec_kernel -s SETTLE_ROUNDS+1 -c 1)."""
     import numpy as np
     import torch
     from chromo_gb300.build import build
     build()
     from chromo_gb300 import workloads as wl
     w = wl.make_workload("profile")
-    sim = wl.build_sim(w)
+    sim = wl.build_sim(w, warps_per_block=6, lanes_per_move=32)
     sh = torch.cuda.current_stream().cuda_stream
+    for k in range(SETTLE_ROUNDS):
+        sim.run(w.steps_per_round, 1000 + k, sh)
     sim.run(w.steps_per_round, 1, sh)
     sim.sync(sh)
     sim.reset_tally()

@@ -88,7 +88,7 @@ EXPORTS = [
     "cg_set_mu_ladder", "cg_get_mu", "cg_get_swap_counts", "cg_run_logged", "cg_set_round_timing",
     "cg_get_round_times", "cg_set_drift_guard", "cg_get_drift", "cg_set_chains_device",
     "cg_deposit_async", "cg_energies_device", "cg_gradient_device", "cg_state_bytes", "cg_save_state",
-    "cg_load_state", "cg_set_twist",
+    "cg_load_state", "cg_set_twist", "cg_steric_energy", "cg_steric_delta",
 ]
 N_TERMS = 14
 
@@ -133,6 +133,8 @@ def lib():
             "cg_save_state": ([P, P, I64], C.c_int),
             "cg_load_state": ([P, P, I64], C.c_int),
             "cg_set_twist": ([P, I32, P, P], C.c_int),
+            "cg_steric_energy": ([P, I32, D, D, P], C.c_int),
+            "cg_steric_delta": ([P, I32, I64, I64, P, D, D, P], C.c_int),
             "cg_get_drift": ([P, P, P], C.c_int),
             "cg_energy": ([P, I32, P], C.c_int),
             "cg_reset_running_energy": ([P], C.c_int),
@@ -279,6 +281,20 @@ class Sim:
             tabs.append(t)
         check(lib().cg_get_chains(self.h, *tabs))
         return out
+
+    def steric_energy(self, rep, excluded_distance, V0=1.0):
+        """Clash energy of replica ``rep``'s resident chain (cg_steric_energy)."""
+        out = C.c_double()
+        check(lib().cg_steric_energy(self.h, rep, float(excluded_distance), float(V0), C.byref(out)))
+        return out.value
+
+    def steric_delta(self, rep, ind0, indf, r_trial, excluded_distance, V0=1.0):
+        """Clash-energy change of moving beads [ind0, indf) to ``r_trial``."""
+        t = np.ascontiguousarray(r_trial, dtype=np.float64).reshape(-1, 3)
+        out = C.c_double()
+        check(lib().cg_steric_delta(self.h, rep, int(ind0), int(indf), _ptr(t), float(excluded_distance),
+                                    float(V0), C.byref(out)))
+        return out.value
 
     def set_twist(self, rep, eps_twist, omega0):
         """SSTWLC twist of replica ``rep`` (per-bond modulus and natural twist;

@@ -125,6 +125,8 @@ struct cg_sim {
     timing_count = 0;
   }
   double* twist = nullptr;  // SSTWLC bond parameters (cg_set_twist), allocated on first use
+  double* steric_work = nullptr;  // steric clash rows, trial segment and total (allocated on first use)
+  long long steric_cap = 0;
   // drift guard of the batched rounds (cg_set_drift_guard)
   int guard_every = 0, guard_chunks = 1;
   double guard_tol_abs = 0, guard_tol_rel = 0;
@@ -270,6 +272,7 @@ void cg_destroy(cg_sim* s) {
   s->free_guard();
   if (s->pinned) cudaFreeHost(s->pinned);
   if (s->twist) cudaFree(s->twist);
+  if (s->steric_work) cudaFree(s->steric_work);
   void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
                   s->bonds32, s->grid, s->access_vol, s->access_sc, s->access_vb, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
                   s->picked, s->d_picked_off, s->eout, s->aout, s->rep_of_rung, s->swaps,
@@ -565,6 +568,42 @@ int cg_set_twist(cg_sim* s, int rep, const double* eps_twist, const double* omeg
   CUDA_TRY(cudaMemcpy(s->twist + 2 * off, tw.data(), 16 * n, cudaMemcpyHostToDevice));
   d.twist = 1;
   return put_rep(s, rep, &d);
+}
+
+static int steric_run(cg_sim* s, int rep, long long ind0, long long indf, const double* r_trial, double e,
+                      double V0, double* out) {
+  if (int rc = check_rep(s, rep)) return rc;
+  if (!out) return fail(CG_ERR_ARG, "null out");
+  if (!(e > 0) || !std::isfinite(V0)) return fail(CG_ERR_ARG, "excluded distance must be > 0, V0 finite");
+  const long long n = s->n_beads[rep];
+  const long long m = r_trial ? indf - ind0 : 0;
+  if (r_trial && (ind0 < 0 || indf > n || m < 1)) return fail(CG_ERR_ARG, "need 0 <= ind0 < indf <= n_beads");
+  const long long need = n + 3 * m + 1;
+  if (need > s->steric_cap) {
+    if (s->steric_work) cudaFree(s->steric_work);
+    s->steric_work = nullptr;
+    s->steric_cap = 0;
+    CUDA_TRY(cudaMalloc(&s->steric_work, 8 * need));
+    s->steric_cap = need;
+  }
+  double* rows = s->steric_work;
+  double* trial = r_trial ? rows + n : nullptr;
+  double* total = rows + n + 3 * m;
+  if (trial) CUDA_TRY(cudaMemcpy(trial, r_trial, 8 * 3 * m, cudaMemcpyHostToDevice));
+  cg_launch_steric(s->args(), s->fp64 != 0, rep, r_trial ? m : n, ind0, indf, trial, e, V0, rows, total, 0);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpy(out, total, 8, cudaMemcpyDeviceToHost));
+  return CG_OK;
+}
+
+int cg_steric_energy(cg_sim* s, int32_t rep, double excluded_distance, double V0, double* out) {
+  return steric_run(s, rep, 0, 0, nullptr, excluded_distance, V0, out);
+}
+
+int cg_steric_delta(cg_sim* s, int32_t rep, int64_t ind0, int64_t indf, const double* r_trial,
+                    double excluded_distance, double V0, double* out) {
+  if (!r_trial) return fail(CG_ERR_ARG, "null r_trial");
+  return steric_run(s, rep, ind0, indf, r_trial, excluded_distance, V0, out);
 }
 
 int cg_get_chain(cg_sim* s, int rep, double* r, double* t3, double* t2, int64_t* states) {

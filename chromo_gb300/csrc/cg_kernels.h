@@ -151,6 +151,8 @@ struct GuardArgs {
 }  // namespace cg
 
 void cg_launch_guard(const cg::KArgs& a, const cg::GuardArgs& g, bool fp64, cudaStream_t s);
+void cg_launch_steric(const cg::KArgs& a, bool fp64, int rep, long long n_rows, long long ind0, long long indf,
+                      const double* trial, double e, double V0, double* rows, double* out, cudaStream_t s);
 void cg_launch_mc(const cg::KArgs& a, bool fp64, bool audit, cudaStream_t s);
 void cg_launch_spec(const cg::KArgs& a, bool fp64, size_t smem_bytes, cudaStream_t s);
 cudaError_t cg_set_spec_smem(bool fp64, int lanes_per_move, int bytes);

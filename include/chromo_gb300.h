@@ -147,6 +147,18 @@ int cg_get_chains(cg_sim *sim, double *const *r, double *const *t3, double *cons
  * it off.  cg_gradient_device refuses dE/dt3 while a replica has twist. */
 int cg_set_twist(cg_sim *sim, int32_t rep, const double *eps_twist, const double *omega0);
 
+/* Steric clashes of the detailed chromatin model (DetailedChromatinWithSterics,
+ * chromo/polymers.pyx:2738-2938): every pair of beads of replica rep closer
+ * than excluded_distance costs V0 ((e/d)^12 - 2 (e/d)^6 + 1).
+ * cg_steric_energy: the clash energy of the resident chain
+ * (eval_E_steric_clashes, :2900-2920).  cg_steric_delta: its change when
+ * beads [ind0, indf) move to r_trial ((indf - ind0) x 3, host FP64)
+ * (get_delta_distances + eval_delta_steric_clashes, :2827-2898), an O(m N)
+ * pass over the chain.  Both blocking, deterministic (rows added in order). */
+int cg_steric_energy(cg_sim *sim, int32_t rep, double excluded_distance, double V0, double *out);
+int cg_steric_delta(cg_sim *sim, int32_t rep, int64_t ind0, int64_t indf, const double *r_trial,
+                    double excluded_distance, double V0, double *out);
+
 /* Field of one replica; access_vol [G] or NULL when every voxel is fully
  * accessible (get_accessible_volumes, chromo/fields.pyx:714-768). */
 int cg_set_field(cg_sim *sim, int32_t rep, const cg_field_params *field, const double *access_vol);

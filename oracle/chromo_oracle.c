@@ -1501,3 +1501,50 @@ int64_t or_sizeof_system(void) { return (int64_t)sizeof(or_system); }
 int64_t or_sizeof_ctl(void) { return (int64_t)sizeof(or_ctl); }
 int64_t or_sizeof_record(void) { return (int64_t)sizeof(or_record); }
 int64_t or_pos_bytes(void) { return (int64_t)sizeof(OR_POS); }
+
+/* ---------------- steric clashes: chromo/polymers.pyx:2738-2938 ----------- */
+
+/* Clash energy of one pair at distance d: V0 ((e/d)^12 - 2 (e/d)^6 + 1)
+ * when d < e (the excluded distance, twice the bead radius), else 0
+ * (eval_delta_steric_clashes / eval_E_steric_clashes; Cython pow for **). */
+static double clash(double d, double e, double V0)
+{
+    if (!(d < e)) return 0.0;
+    double f = e / d;
+    return V0 * (pow(f, 12.0) - 2 * pow(f, 6.0) + 1);
+}
+
+static double pair_dist(const double *a, const double *b)
+{
+    return sqrt(pow(a[0] - b[0], 2.0) + pow(a[1] - b[1], 2.0) + pow(a[2] - b[2], 2.0));
+}
+
+/* eval_E_steric_clashes, polymers.pyx:2900-2920: every pair i < j. r: N x 3. */
+double or_steric_E(const double *r, int64_t n, double e, double V0)
+{
+    double E = 0;
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t j = i + 1; j < n; j++) E += clash(pair_dist(r + 3 * i, r + 3 * j), e, V0);
+    return E;
+}
+
+/* get_delta_distances + eval_delta_steric_clashes, polymers.pyx:2827-2898:
+ * beads [ind0, indf) move to rt (m x 3); pairs (i moved, j any) counted once
+ * (j >= i inside the moved range skipped); trial minus current. */
+double or_steric_dE(const double *r, const double *rt, int64_t n, int64_t ind0, int64_t indf, double e,
+                    double V0)
+{
+    double dE = 0;
+    for (int64_t i = ind0; i < indf; i++) {
+        const double *pi_t = rt + 3 * (i - ind0), *pi = r + 3 * i;
+        for (int64_t j = 0; j < n; j++) {
+            if (j >= i && j >= ind0 && j < indf) continue;
+            const double *pj_t = (j >= ind0 && j < indf) ? rt + 3 * (j - ind0) : r + 3 * j;
+            double dt = (i == j) ? 0.0 : pair_dist(pi_t, pj_t);
+            double dc = (i == j) ? 0.0 : pair_dist(pi, r + 3 * j);
+            dE += clash(dt, e, V0);
+            dE -= clash(dc, e, V0);
+        }
+    }
+    return dE;
+}

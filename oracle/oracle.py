@@ -95,6 +95,10 @@ def lib(tag: str):
         L.or_mc_sim_philox.restype = _I
         L.or_kat_axis_rotation.argtypes = [_P, _P, C.c_double, _P]
         L.or_kat_philox.argtypes = [_P, _P, _P]
+        L.or_steric_E.argtypes = [_P, _I, C.c_double, C.c_double]
+        L.or_steric_E.restype = C.c_double
+        L.or_steric_dE.argtypes = [_P, _P, _I, _I, _I, C.c_double, C.c_double]
+        L.or_steric_dE.restype = C.c_double
         L.or_kat_transform.argtypes = [C.POINTER(_System), _I, _P, _P]
         assert L.or_sizeof_system() == C.sizeof(_System)
         assert L.or_sizeof_ctl() == C.sizeof(Ctl)
@@ -311,3 +315,19 @@ def axis_rotation(axis, point, angle, tag="f64"):
     out = np.zeros(12)
     lib(tag).or_kat_axis_rotation(a.ctypes.data, p.ctypes.data, float(angle), out.ctypes.data)
     return out.reshape(3, 4)
+
+
+def steric_energy(r, excluded_distance, V0=1.0):
+    """Clash energy of every bead pair (eval_E_steric_clashes,
+    chromo/polymers.pyx:2900-2920), from the oracle."""
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    return lib("f64").or_steric_E(r.ctypes.data, len(r), float(excluded_distance), float(V0))
+
+
+def steric_delta(r, r_trial_segment, ind0, indf, excluded_distance, V0=1.0):
+    """Clash-energy change of moving beads [ind0, indf) to ``r_trial_segment``
+    (get_delta_distances + eval_delta_steric_clashes, :2827-2898)."""
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    t = np.ascontiguousarray(r_trial_segment, dtype=np.float64)
+    return lib("f64").or_steric_dE(r.ctypes.data, t.ctypes.data, len(r), int(ind0), int(indf),
+                                   float(excluded_distance), float(V0))

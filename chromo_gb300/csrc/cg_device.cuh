@@ -783,10 +783,13 @@ template <int G> __device__ __forceinline__ unsigned gballot(bool p) {
 }
 template <int G> __device__ __forceinline__ bool gany(bool p) { return gballot<G>(p) != 0u; }
 // Fixed-point sums are exact; the FP64 side sum is reduced only when some
-// lane of the group holds one.
+// lane of the warp holds one.  The test is a warp vote, not a group vote: the
+// reduction's shuffles name all 32 lanes, so with G < 32 every group of the
+// warp must take the branch together (a group that holds only zeros adds
+// zeros).
 template <int G> __device__ __forceinline__ Fx gsum(Fx v) {
   v.q = gsum<G>(v.q);
-  if (gany<G>(!is_zero64(v.hard))) v.hard = gsum<G>(v.hard);
+  if (__any_sync(kFull, !is_zero64(v.hard))) v.hard = gsum<G>(v.hard);
   return v;
 }
 __device__ __forceinline__ Fx warp_sum(Fx v) { return gsum<32>(v); }

@@ -301,7 +301,7 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
   n_vox = nused;
   (void)soft;
   hard += gsum<G>(part);
-  if (gany<G>(hpart != 0)) huge += gsum<G>(hpart);
+  if (__any_sync(kFull, hpart != 0)) huge += gsum<G>(hpart);  // warp vote: see gsum(Fx)
 }
 
 // FP32 arithmetic per voxel, fixed-point accumulation into `soft`; voxels at
@@ -360,7 +360,7 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
   }
   n_vox = nused;
   acc_add(soft, gsum<G>(part));
-  if (gany<G>(hpart != 0)) huge += gsum<G>(hpart);
+  if (__any_sync(kFull, hpart != 0)) huge += gsum<G>(hpart);  // warp vote: see gsum(Fx)
 }
 
 __device__ __forceinline__ void commit_grid(const RepDev& rd, const KArgs& a, int hcol, int* keys,

@@ -1006,8 +1006,16 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
       cg_move_ctl& c = sh.ws.ctl[ci];
       const int kind = (int)c.move_kind;
       if (c.move_on == 1) {
-        long long done = 0;
+        long long done = 0, batches = 0;
         while (done < c.num_per_cycle) {
+          // every batch attempts at least one move or stops the run, so there
+          // are at most num_per_cycle batches; the cap turns a stalled loop
+          // into an error status instead of a spin
+          if (++batches > c.num_per_cycle + 64) {
+            if (tid == 0) sh.stop = E_SPIN;
+            __syncthreads();
+            break;
+          }
           const int B = (int)(c.num_per_cycle - done < Sn ? c.num_per_cycle - done : Sn);
           const bool wlive = warp * GPW < B;  // the warp has a move of this batch
           const bool live = slot < B;

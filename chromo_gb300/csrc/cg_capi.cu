@@ -53,7 +53,7 @@ struct cg_sim {
   std::vector<long long> n_beads, bead_off, n_vox, vox_off, picked_off;
   std::vector<int> dims;
   long long total_beads = 0, total_vox = 0, total_picked = 0;
-  long long max_segment = 0, max_tangent = 0, max_beads = 0;
+  long long max_segment = 0, max_tangent = 0, max_beads = 0, max_vox = 0;
   int n_ctl = 5;
   long long kernels = 0;
   // device buffers
@@ -89,6 +89,7 @@ struct cg_sim {
   int logH = 0, warp_smem = 0, off_draws = 0, off_keys = 0, off_used = 0, off_bslot = 0, off_vals = 0, off_stage = 0,
       off_idx = 0;
   int spec_w = 1, spec_g = 32, spec_s = 1, spec_logHB = 11, spec_off_bkeys = 0, spec_off_bmask = 0, spec_off_warps = 0;
+  int pool_on = 0, pool_logH = 0, off_pkeys = 0, off_pused = 0, off_pvals = 0;
   long long stage_cap = 0;
   size_t spec_bytes = 0;
   // captured batched graph
@@ -187,6 +188,8 @@ struct cg_sim {
     a.off_idx = off_idx; a.off_bslot = off_bslot;
     a.spec_w = spec_w; a.spec_g = spec_g; a.spec_s = spec_s; a.spec_logHB = spec_logHB; a.spec_off_bkeys = spec_off_bkeys;
     a.spec_off_bmask = spec_off_bmask; a.spec_off_warps = spec_off_warps;
+    a.pool_on = pool_on; a.pool_logH = pool_logH; a.off_pkeys = off_pkeys; a.off_pused = off_pused;
+    a.off_pvals = off_pvals;
     a.rep_of_rung = rep_of_rung; a.swaps = swaps; a.swap_attempts = swap_attempts;
     a.xround = xround;
     a.mu_rungs = mu_rungs; a.mu_binder = mu_binder; a.nbound = nbound;
@@ -215,13 +218,25 @@ struct cg_sim {
     logH = lh; stage_cap = sc; warp_smem = (int)o;
     return warp_smem;
   }
-  // CTA layout: header, block voxel table (2^lhb entries), one region per
-  // move slot (W warps of 32 / G slots).
-  size_t cta_layout(int lhb, int W, int G) {
+  // CTA layout: header, block voxel table (2^lhb entries), the pooled voxel
+  // table (2^lhp entries: keys, used list, nb + 1 split int64 values; none
+  // for lhp = 0), one region per move slot (W warps of 32 / G slots).
+  size_t cta_layout(int lhb, int W, int G, int lhp = 0) {
     size_t o = align16(sizeof(cg::SpecShared));
     spec_off_bkeys = (int)o; o += 4 * (size_t(1) << lhb);
     spec_off_bmask = (int)o; o += 4 * (size_t(1) << lhb);
     o = align32(o);
+    pool_on = lhp > 0 ? 1 : 0;
+    pool_logH = lhp;
+    off_pkeys = off_pused = off_pvals = 0;
+    if (lhp > 0) {
+      const size_t HP = size_t(1) << lhp;
+      off_pkeys = (int)o; o += 4 * HP;
+      off_pused = (int)o; o += 4 * HP;
+      o = align16(o);
+      off_pvals = (int)o; o += 8 * HP * (nb + 1);
+      o = align32(o);
+    }
     spec_off_warps = (int)o;
     spec_logHB = lhb;
     spec_w = W;
@@ -319,13 +334,25 @@ static int choose_shape(cg_sim* s, int w_req, int g_req) {
   const size_t budget = std::min<size_t>(smem_per_sm / ctas_per_sm - 1024, 220 * 1024);
   const int lhb = 10;
   const long long sc = G == 32 ? 48 : 32;
-  int lh = 10;  // at most 1,024 slots: the 32-bit split counters of a shared table cannot overflow
-  for (; lh > 6; lh--) {
-    s->layout(lh, sc);
-    if (s->cta_layout(lhb, W, G) <= budget) break;
+  // FP32 storage: the position moves of a batch share one pooled voxel table
+  // (keys voxel * 32 + slot: grids below 2^26 voxels), as large as fits (up
+  // to 4,096 entries); the slots keep 64-entry tables for binding moves
+  int lhp = 0;
+  if (!s->fp64 && s->max_vox < (1LL << 26)) {
+    s->layout(6, sc);
+    for (int t = 12; t >= 8 && lhp == 0; t--)
+      if (s->cta_layout(lhb, W, G, t) <= budget) lhp = t;
+  }
+  int lh = 6;
+  if (lhp == 0) {
+    lh = 10;  // at most 1,024 slots: the 32-bit split counters of a shared table cannot overflow
+    for (; lh > 6; lh--) {
+      s->layout(lh, sc);
+      if (s->cta_layout(lhb, W, G) <= budget) break;
+    }
   }
   s->layout(lh, sc);
-  s->spec_bytes = s->cta_layout(lhb, W, G);
+  s->spec_bytes = s->cta_layout(lhb, W, G, lhp);
   s->wpb = 1;
   cudaError_t e = cg_set_spec_smem(s->fp64 != 0, G, (int)s->spec_bytes);
   if (e == cudaSuccess) e = cg_set_mc_smem(s->fp64 != 0, (int)(s->spec_off_warps + s->warp_smem));
@@ -366,6 +393,7 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
     s->picked_off.push_back(s->total_picked);
     s->total_picked += (n + 31) / 32;
     s->max_beads = std::max(s->max_beads, n);
+    s->max_vox = std::max(s->max_vox, (long long)nx * ny * nz);
   }
   s->g_logH = next_log2(32 * s->max_segment);
   s->g_stage_cap = std::max(s->max_segment, s->max_tangent);
@@ -1382,7 +1410,7 @@ int cg_get_launch_shape(cg_sim* s, int32_t* wpb, int32_t* lanes, int32_t* in_fli
   if (wpb) *wpb = s->spec_w;
   if (lanes) *lanes = s->spec_g;
   if (in_flight) *in_flight = s->spec_s;
-  if (hash_slots) *hash_slots = 1 << s->logH;
+  if (hash_slots) *hash_slots = s->pool_on ? 1 << s->pool_logH : 1 << s->logH;
   return CG_OK;
 }
 

@@ -51,6 +51,12 @@ struct MovePlan {
   long long pq[2];
   double ph[2];
   double M[12];  // the 3 x 4 transform, stored in the position type
+  // the CTA's pass over the pooled voxel table (FP32 position moves): the
+  // move's field dE in fixed point, its FP64 side sum, its exact 1e99 units,
+  // its touched voxels and a failed registration
+  long long fq, fH;
+  double fh;
+  int fn, freg;
 };
 
 // Shared-memory header of one replica's CTA.
@@ -65,7 +71,7 @@ struct SpecShared {
   double run_dE;
   int cut, stop;
   unsigned accmask;
-  int pad;
+  int npool;  // entries of the pooled voxel table in use
 };
 
 static_assert(sizeof(unsigned) * kDrawCache % 16 == 0, "the draw buffers are written with 16-byte stores");
@@ -109,6 +115,9 @@ struct KArgs {
   // CTA layout: header, block voxel table, then one region per move slot;
   // spec_w warps of 32 / spec_g groups, spec_s = spec_w * 32 / spec_g slots
   int spec_w, spec_g, spec_s, spec_logHB, spec_off_bkeys, spec_off_bmask, spec_off_warps;
+  // pooled voxel table of the CTA (FP32 storage): 2^pool_logH entries keyed by
+  // voxel * 32 + move slot, shared by the position moves of a batch
+  int pool_on, pool_logH, off_pkeys, off_pused, off_pvals;
   unsigned long long seed;
   // audit mode
   int audit_rep;

@@ -304,10 +304,62 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
   if (__any_sync(kFull, hpart != 0)) huge += gsum<G>(hpart);  // warp vote: see gsum(Fx)
 }
 
-// FP32 arithmetic per voxel, fixed-point accumulation into `soft`; voxels at
-// or near the volume-fraction limit take the FP64 branch (chi terms into the
-// FP64 side sum, the 1e99 penalties exactly into `huge`), so which side of the
-// limit a voxel lies on is decided as in FP64.
+// An FP64 term of the FP32 path: in fixed point like the FP32 terms when it
+// is below 2^20 kT (so that the sum stays independent of the order of the
+// terms), else into the FP64 side sum.
+__device__ __forceinline__ void acc_add_wide(Fx& s, double x) {
+  if (fabs(x) < 1048576.0) s.q += __double2ll_rn(x * 1073741824.0);
+  else s.hard = add_hard(s.hard, x);
+}
+
+// Field dE of one touched voxel v of the FP32 path (row `d` of a voxel table:
+// the move's density deltas in, the voxel's post-move row out): FP32
+// arithmetic, fixed-point accumulation into `part`; a voxel at or near the
+// volume-fraction limit takes the FP64 branch (its chi term in fixed point or
+// the side sum, the 1e99 penalties exactly into `huge`), so which side of the
+// limit it lies on is decided as in FP64.
+__device__ __forceinline__ void voxel_dE_f32(const WarpShared& ws, const KArgs& a, const long long* grid, int v,
+                                             long long* d, bool split, Fx& part, long long& huge) {
+  const RepDev& rd = ws.rd;
+  long long row[4];
+  load_row(grid + (long long)v * a.ncol, a.ncol, row);
+  const long long g0 = row[0], d0 = hash_delta(d, split);
+  float sc = ws.f_scale, k = ws.f_k;
+  if (rd.has_access) {  // per-voxel factors precomputed from V (no FP64 division here)
+    sc = a.access_sc[rd.vox_off + v];
+    k = (float)(rd.chi * a.access_vb[rd.vox_off + v]);
+  }
+  float c = 0, rho[CG_MAX_BINDERS], dd[CG_MAX_BINDERS];
+#pragma unroll
+  for (int b = 0; b < CG_MAX_BINDERS; b++) {
+    if (b >= rd.nb) break;
+    long long gb = row[1 + b], db = hash_delta(d + 1 + b, split);
+    rho[b] = (float)gb * sc;
+    dd[b] = (float)db * sc;
+    c += ws.f_pref[b] * (dd[b] * (2.0f * rho[b] + dd[b]));
+    d[1 + b] = gb + db;
+  }
+#pragma unroll
+  for (int b = 0; b < CG_MAX_BINDERS; b++)
+#pragma unroll
+    for (int e = 0; e < CG_MAX_BINDERS; e++)
+      if (b < rd.nb && e < rd.nb)
+        c += ws.f_xpref[b * CG_MAX_BINDERS + e] * (rho[b] * dd[e] + dd[b] * rho[e] + dd[b] * dd[e]);
+  const float vf0 = (float)g0 * sc * ws.f_vb;
+  const float dvf = (float)d0 * sc * ws.f_vb;
+  if (vf0 > ws.f_lim - 1e-3f || vf0 + dvf > ws.f_lim - 1e-3f) {
+    acc_add(part, c);
+    const ChiSplit t = chi_term64(rd, rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin, g0, d0);
+    acc_add_wide(part, t.soft);
+    huge += t.huge;
+  } else {
+    acc_add(part, c + k * (dvf * (2.0f * vf0 + dvf)));
+  }
+  d[0] = g0 + d0;
+}
+
+// FP32 arithmetic per voxel, fixed-point accumulation into `soft` (see
+// voxel_dE_f32), over the voxels of one move's table by its G lanes.
 template <int G = 32>
 static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int hcol, const int* keys,
                                   const int* used, long long* vals, int nused, int lane,
@@ -319,44 +371,8 @@ static __device__ void field_dE_voxels(const WarpShared& ws, const KArgs& a, int
   const long long* grid = a.grid + rd.vox_off * a.ncol;
   (void)hard;
   for (int i = lane; i < nused; i += G) {
-    int slot = used[i];
-    int v = keys[slot];
-    long long* d = vals + (long long)slot * hcol;
-    long long row[4];
-    load_row(grid + (long long)v * a.ncol, a.ncol, row);
-    long long g0 = row[0], d0 = hash_delta(d, split);
-    float sc = ws.f_scale, k = ws.f_k;
-    if (rd.has_access) {  // per-voxel factors precomputed from V (no FP64 division here)
-      sc = a.access_sc[rd.vox_off + v];
-      k = (float)(rd.chi * a.access_vb[rd.vox_off + v]);
-    }
-    float c = 0, rho[CG_MAX_BINDERS], dd[CG_MAX_BINDERS];
-#pragma unroll
-    for (int b = 0; b < CG_MAX_BINDERS; b++) {
-      if (b >= rd.nb) break;
-      long long gb = row[1 + b], db = hash_delta(d + 1 + b, split);
-      rho[b] = (float)gb * sc;
-      dd[b] = (float)db * sc;
-      c += ws.f_pref[b] * (dd[b] * (2.0f * rho[b] + dd[b]));
-      d[1 + b] = gb + db;
-    }
-#pragma unroll
-    for (int b = 0; b < CG_MAX_BINDERS; b++)
-#pragma unroll
-      for (int e = 0; e < CG_MAX_BINDERS; e++)
-        if (b < rd.nb && e < rd.nb)
-          c += ws.f_xpref[b * CG_MAX_BINDERS + e] * (rho[b] * dd[e] + dd[b] * rho[e] + dd[b] * dd[e]);
-    float vf0 = (float)g0 * sc * ws.f_vb;
-    float dvf = (float)d0 * sc * ws.f_vb;
-    if (vf0 > ws.f_lim - 1e-3f || vf0 + dvf > ws.f_lim - 1e-3f) {
-      acc_add(part, c);
-      const ChiSplit t = chi_term64(rd, rd.has_access ? a.access_vol[rd.vox_off + v] : rd.vol_bin, g0, d0);
-      part.hard = add_hard(part.hard, t.soft);
-      hpart += t.huge;
-    } else {
-      acc_add(part, c + k * (dvf * (2.0f * vf0 + dvf)));
-    }
-    d[0] = g0 + d0;
+    const int slot = used[i];
+    voxel_dE_f32(ws, a, grid, keys[slot], vals + (long long)slot * hcol, split, part, hpart);
   }
   n_vox = nused;
   acc_add(soft, gsum<G>(part));

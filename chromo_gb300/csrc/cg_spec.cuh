@@ -147,6 +147,11 @@ struct ChainView {
 
 // Lanes per bead of the position-move deposit; each lane takes 8 / kLanesPerBead
 // of the bead's trilinear corners.
+// Largest position move of the pooled voxel table: an entry gets at most 2 m
+// contributions of |d| < 2^42, which its two 32-bit split counters hold for
+// m < 512.
+constexpr int kPoolMaxBeads = 256;
+
 constexpr int kLanesPerBead = 4;
 constexpr int kCornersPerLane = 8 / kLanesPerBead;
 
@@ -233,14 +238,16 @@ template <typename Acc> __device__ __forceinline__ Acc load_acc(long long q, dou
 template <> __device__ __forceinline__ Fx load_acc<Fx>(long long q, double h) { return Fx{q, h}; }
 template <> __device__ __forceinline__ double load_acc<double>(long long, double h) { return h; }
 
-// Deposit of the batch's position moves that use their slot's shared voxel
-// table (plan.blk), by every thread of the CTA: the moves' bead corners, in
-// move order, are dealt out to the threads (eight per bead), so a move of
-// many beads no longer holds the batch back while the other warps wait.
-// Claims append to each move's used list once per warp and move; the bond
-// terms, confinement counts and error bits go to the move's plan.  A move
-// whose optimistic table overflows (E_OVF) is skipped from then on; its warp
-// deposits it again in its global table.  Called by every thread.
+// Deposit of the batch's position moves that use a shared voxel table
+// (plan.blk), by every thread of the CTA: the moves' bead corners, in move
+// order, are dealt out to the threads (eight per bead), so a move of many
+// beads no longer holds the batch back while the other warps wait.  The
+// table is the CTA's pooled table (FP32 storage: keys voxel * 32 + slot, one
+// used list, claims appended once per warp) or the slot's own table (claims
+// appended once per warp and move).  The bond terms, confinement counts and
+// error bits go to the move's plan.  A move whose optimistic table overflows
+// (E_OVF: a pool or a table past 3/4 load) is skipped from then on; its
+// group deposits it again in its global table.  Called by every thread.
 template <typename Pos>
 __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, int kind) {
   using Acc = typename AccOf<Pos>::type;
@@ -251,6 +258,7 @@ __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, in
   const long long N = rd.n_beads;
   const bool conf = rd.field_kind != 0 && rd.confine_kind;
   const int Hs = 1 << a.logH, hcol = a.hcol;
+  const bool pool = a.pool_on != 0;
   // lane j of every warp holds the end of move j's tasks in the batch's
   // task list (kLanesPerBead per bead of the moves with plan.blk)
   const int lane = (int)(threadIdx.x & 31u);
@@ -294,23 +302,133 @@ __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, in
       if (right) store_acc(P.pq[1], P.ph[1], pterm);
       if (oob) atomicAdd(&P.oob, oob);
     }
-    const unsigned peers = __match_any_sync(kFull, t < total ? s : -1);
-    int* keys = reinterpret_cast<int*>(wb + a.off_keys);
-    int* used = reinterpret_cast<int*>(wb + a.off_used);
-    long long* vals = reinterpret_cast<long long*>(wb + a.off_vals);
+    // the pooled table (one used list for the whole CTA, keys voxel * 32 +
+    // slot), or the move's own table (one used list per move)
+    const unsigned peers = pool ? kFull : __match_any_sync(kFull, t < total ? s : -1);
+    int* keys = reinterpret_cast<int*>(pool ? smem + a.off_pkeys : wb + a.off_keys);
+    int* used = reinterpret_cast<int*>(pool ? smem + a.off_pused : wb + a.off_used);
+    long long* vals = reinterpret_cast<long long*>(pool ? smem + a.off_pvals : wb + a.off_vals);
     bool want[2 * kCornersPerLane];
 #pragma unroll
-    for (int j = 0; j < 2 * kCornersPerLane; j++) want[j] = q[j] != 0;
-    const unsigned full_bit = P.sure ? E_SPIN : E_OVF;
+    for (int j = 0; j < 2 * kCornersPerLane; j++) {
+      want[j] = q[j] != 0;
+      if (pool) vq[j] = vq[j] * 32 + s;
+    }
+    const bool sure = P.sure && !pool;
+    const unsigned full_bit = sure ? E_SPIN : E_OVF;
+    const int lh = pool ? a.pool_logH : a.logH;
     int slot[2 * kCornersPerLane];
-    claim_slots<2 * kCornersPerLane>(keys, used, &sh.nused[s], a.logH, vq, want, slot, e,
-                                     P.sure ? Hs : (3 * Hs) / 4, full_bit, peers);
+    claim_slots<2 * kCornersPerLane>(keys, used, pool ? &sh.npool : &sh.nused[s], lh, vq, want, slot, e,
+                                     sure ? Hs : (3 << lh) / 4, full_bit, peers);
     if (!(e & full_bit)) {
 #pragma unroll
       for (int j = 0; j < 2 * kCornersPerLane; j++)
         if (want[j]) add_corner(vals, hcol, slot[j], q[j], sw, rd.nb, true);
     }
     if (e) atomicOr(&P.derr, e);
+  }
+}
+
+// Field dE and conflict registration of the batch's pooled voxel entries, by
+// every thread of the CTA (FP32 storage): entry -> (voxel, move slot s);
+// the voxel's FP32 field term (voxel_dE_f32, which also leaves the voxel's
+// post-move row in the entry for the commit); its registration in the block
+// voxel table, whose atomicOr returns the moves that registered the voxel
+// first (an earlier one is a conflict of s, a later one learns of s through
+// its plan's mask).  Per move, the fixed-point terms are summed exactly (a
+// warp reduces each move's terms in three 21-bit limbs, one 64-bit atomic
+// per warp and move), so the sum does not depend on which thread took which
+// voxel.  Entries of moves that overflowed the pool are skipped (their
+// groups redo them in their global tables).  Called by every thread.
+static __device__ void block_field_pool(const KArgs& a, SpecShared& sh, unsigned char* smem, int* bkeys,
+                                 unsigned* bmask) {
+  const WarpShared& ws = sh.ws;
+  const RepDev& rd = ws.rd;
+  const int* pkeys = reinterpret_cast<const int*>(smem + a.off_pkeys);
+  const int* pused = reinterpret_cast<const int*>(smem + a.off_pused);
+  long long* pvals = reinterpret_cast<long long*>(smem + a.off_pvals);
+  const long long* grid = a.grid + rd.vox_off * a.ncol;
+  const int n = sh.npool;
+  const int lane = (int)(threadIdx.x & 31u);
+  for (int e0 = (int)(threadIdx.x & ~31u); e0 < n; e0 += (int)blockDim.x) {
+    const int e = e0 + lane;
+    int s = -1;
+    Fx part = Fx{0, 0.0};
+    long long hp = 0;
+    if (e < n) {
+      const int slot = pused[e];
+      const int key = pkeys[slot];
+      s = key & 31;
+      const int v = key >> 5;
+      MovePlan& P = sh.plan[s];
+      if (P.derr & E_OVF) {
+        s = -1;
+      } else {
+        voxel_dE_f32(ws, a, grid, v, pvals + (long long)slot * a.hcol, true, part, hp);
+        const int b = block_insert(bkeys, a.spec_logHB, v);
+        if (b < 0) {
+          atomicOr(&P.freg, 1);
+        } else {
+          const unsigned prior = atomicOr(&bmask[b], 1u << s);
+          const unsigned below = (1u << s) - 1u, above = ~((2u << s) - 1u);
+          if (prior & below) atomicOr(&P.cmask, prior & below);
+          for (unsigned later = prior & above; later; later &= later - 1)
+            atomicOr(&sh.plan[__ffs((int)later) - 1].cmask, 1u << s);
+        }
+        if (!is_zero64(part.hard)) atomicAdd(&P.fh, part.hard);
+        if (hp) atomicAdd(reinterpret_cast<unsigned long long*>(&P.fH), (unsigned long long)hp);
+      }
+    }
+    // q = l2 2^42 + l1 2^21 + l0 with l0, l1 in [0, 2^21) (|q| < 2^50): each
+    // limb's sum over a warp fits 32 bits
+    unsigned todo = __ballot_sync(kFull, s >= 0);
+    while (todo) {
+      const int leader = __ffs((int)todo) - 1;
+      const int sl = __shfl_sync(kFull, s, leader);
+      const bool mine = s == sl;
+      const long long q = mine ? part.q : 0;
+      const unsigned l0 = __reduce_add_sync(kFull, (unsigned)(q & 0x1FFFFF));
+      const unsigned l1 = __reduce_add_sync(kFull, (unsigned)((q >> 21) & 0x1FFFFF));
+      const int l2 = __reduce_add_sync(kFull, (int)(q >> 42));
+      const unsigned who = __ballot_sync(kFull, mine);
+      if (lane == leader) {
+        const long long sum = (long long)l2 * 4398046511104LL + (long long)l1 * 2097152LL + (long long)l0;
+        atomicAdd(reinterpret_cast<unsigned long long*>(&sh.plan[sl].fq), (unsigned long long)sum);
+        atomicAdd(&sh.plan[sl].fn, __popc(who));
+      }
+      todo &= ~who;
+    }
+  }
+}
+
+// Commit of the pooled entries after the batch is resolved, by every thread:
+// the post-move rows of the standing accepted moves (the first `cut`, bits of
+// `acc`) go to the grid with 16-byte stores; every entry is cleared, and so
+// is the block voxel table.
+static __device__ void block_commit_pool(const KArgs& a, SpecShared& sh, unsigned char* smem, int cut, unsigned acc,
+                                  int* bkeys, unsigned* bmask) {
+  const RepDev& rd = sh.ws.rd;
+  int* pkeys = reinterpret_cast<int*>(smem + a.off_pkeys);
+  const int* pused = reinterpret_cast<const int*>(smem + a.off_pused);
+  long long* pvals = reinterpret_cast<long long*>(smem + a.off_pvals);
+  long long* grid = a.grid + rd.vox_off * a.ncol;
+  const int n = sh.npool, hcol = a.hcol, ncol = a.ncol;
+  for (int e = (int)threadIdx.x; e < n; e += (int)blockDim.x) {
+    const int slot = pused[e];
+    const int key = pkeys[slot];
+    const int s = key & 31;
+    long long* src = pvals + (long long)slot * hcol;
+    if (s < cut && ((acc >> s) & 1u) && !(sh.plan[s].derr & E_OVF)) {
+      longlong2* dst = reinterpret_cast<longlong2*>(grid + (long long)(key >> 5) * ncol);
+      dst[0] = make_longlong2(src[0], src[1]);
+      if (ncol == 4) dst[1] = make_longlong2(hcol > 2 ? src[2] : 0, hcol > 3 ? src[3] : 0);
+    }
+    pkeys[slot] = -1;
+    for (int cc = 0; cc < hcol; cc++) src[cc] = 0;
+  }
+  for (int i = (int)threadIdx.x; i < (1 << a.spec_logHB); i += (int)blockDim.x) {
+    bkeys[i] = -1;
+    bmask[i] = 0u;
   }
 }
 
@@ -339,6 +457,15 @@ static __device__ __noinline__ void log_move(const KArgs& a, int rep, unsigned l
   rec.accepted = P.empty ? -1 : P.dec;
   rec.n_draws = P.ndraw;
   a.mlog[(long long)rep * a.mlog_cap + (long long)k] = rec;
+}
+
+// The pooled pass's field terms of a move, added to its field dE.
+__device__ __forceinline__ void add_pool_terms(Fx& s, const MovePlan& P) {
+  s.q += P.fq;
+  if (!is_zero64(P.fh)) s.hard = add_hard(s.hard, P.fh);
+}
+__device__ __forceinline__ void add_pool_terms(double& s, const MovePlan& P) {
+  s += (double)P.fq * kFxEInv + P.fh;
 }
 
 // Evaluate move t of the batch in slot s (group lanes gl = 0..G-1); `live`
@@ -384,6 +511,9 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
   SlotScratch S = sm;
   int* nused = &sh.nused[s];
   const int Hs = 1 << sm.logH;
+  const bool pool = a.pool_on != 0;
+  bool pooled = false;  // a position move whose voxels the CTA's pooled pass evaluates
+  if (threadIdx.x == 0) sh.npool = 0;  // every reader of the last batch's pool passed a barrier since
 
   if (kind <= CG_SLIDE) {
     const ChainView<Pos> cv(a, rd);
@@ -447,14 +577,22 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     m = (!live || err) ? 0 : indf - ind0;
     if (live && !err && m == 0) empty = true;
     if (m > a.stage_cap) { S.stage = gm.stage; gstage = 1; }
-    // voxel table: shared when the move's at most 16 m voxels surely fit, or
-    // optimistically (a few distinct voxels per bead in practice) up to m <=
-    // slots / 4 with a fallback to the global table on overflow; global beyond
-    const bool sure = 16 * m <= Hs;
-    if (!sure && 4 * m > Hs) { use_table(S, gm); gtab = 1; }
+    // voxel table: with the CTA's pooled table (FP32 storage), every move of
+    // up to kPoolMaxBeads beads, optimistically (a pool past 3/4 load sends
+    // the move to its global table); else the slot's own table when the
+    // move's at most 16 m voxels surely fit, or optimistically up to m <=
+    // slots / 4 with the same fallback; global beyond
+    bool sure, blk;
+    if (pool) {
+      sure = false;
+      blk = density && m > 0 && m <= kPoolMaxBeads;
+      if (density && m > 0 && !blk) { use_table(S, gm); gtab = 1; }
+    } else {
+      sure = 16 * m <= Hs;
+      if (!sure && 4 * m > Hs) { use_table(S, gm); gtab = 1; }
+      blk = density && m > 0 && !gtab;  // moves with a shared table are deposited by the whole CTA
+    }
     V4<Pos>* stage = reinterpret_cast<V4<Pos>*>(S.stage);  // r, t3, t2 of each moved bead
-    // moves with a shared table are deposited by the whole CTA
-    const bool blk = density && m > 0 && !gtab;
     if (gl == 0 && live) {
       P.blk = blk ? 1 : 0;
       P.sure = sure ? 1 : 0;
@@ -467,6 +605,9 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       P.cmask = 0;
       P.pq[0] = P.pq[1] = 0;
       P.ph[0] = P.ph[1] = 0;
+      P.fq = P.fH = 0;
+      P.fh = 0;
+      P.fn = P.freg = 0;
       Pos* Mp = reinterpret_cast<Pos*>(P.M);  // in the position type: no conversions
       for (int i = 0; i < 3; i++)
         for (int j = 0; j < 4; j++) Mp[4 * i + j] = M[i][j];
@@ -486,12 +627,14 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       cmb |= gballot<G>(hit) << u0;
     }
     __syncthreads();
+    if (pool && density) block_field_pool(a, sh, reinterpret_cast<unsigned char*>(&sh), bkeys, bmask);
     Acc part = acc_zero<Acc>();
     int oob = 0;
     bool ovf = false;
     if (blk) {
       const unsigned eb = P.derr;
       ovf = (eb & E_OVF) != 0;
+      pooled = pool && !ovf;
       err |= eb & ~E_OVF;
       if (gl == 0) {
         acc_add(part, load_acc<Acc>(P.pq[0], P.ph[0]));
@@ -783,6 +926,15 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     cmb = gor<G>(cmb);
     if (gl == 0 && live) atomicOr(&P.cmask, cmb);
   }
+  if (kind <= CG_SLIDE && pool && density) {
+    __syncthreads();  // the pooled field pass is complete
+    if (pooled) {
+      add_pool_terms(dEs, P);
+      dEH += P.fH;
+      nvox = P.fn;
+      regfail |= P.freg;
+    }
+  }
   bool dec = false;
   if (live && !err && !empty) dec = decide(g.next(), dEp, dEs, with_huge(dEh, dEH), gl == 0 ? &P.dE : nullptr);
   if (gl == 0 && live) {
@@ -986,6 +1138,12 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
     for (int i = gl; i < (1 << a.logH); i += G) { sm.keys[i] = -1; sm.bslot[i] = -1; }
     for (int i = gl; i < (1 << a.logH) * hcol; i += G) sm.vals[i] = 0;
     if (gl == 0) sh.nused[slot] = 0;
+    if (a.pool_on) {
+      int* pk = reinterpret_cast<int*>(smem + a.off_pkeys);
+      long long* pv = reinterpret_cast<long long*>(smem + a.off_pvals);
+      for (int i = tid; i < (1 << a.pool_logH); i += blockDim.x) pk[i] = -1;
+      for (int i = tid; i < (1 << a.pool_logH) * hcol; i += blockDim.x) pv[i] = 0;
+    }
   }
   __syncthreads();
   if (tid == 0) {
@@ -996,6 +1154,7 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
     sh.run_dE = rd0.run_dE;
     sh.stop = 0;
     sh.cut = 0;
+    sh.npool = 0;
   }
   __syncthreads();
   const long long words = (sh.ws.rd.n_beads + 31) / 32;
@@ -1081,6 +1240,8 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
             commit_and_clear<Pos, G>(a, sh, slot, gl, slot < cut && ((acc >> slot) & 1u), sm, gm, bkeys, bmask);
           __syncwarp();
           if (live && gl == 0) sh.nused[slot] = 0;
+          if (kind <= CG_SLIDE && a.pool_on && sh.ws.rd.field_kind == 2)
+            block_commit_pool(a, sh, smem, cut, acc, bkeys, bmask);
           __syncthreads();
           done += cut;
           if (sh.stop) break;

@@ -109,7 +109,8 @@ def profile_case(args):
     ms = e0.elapsed_time(e1)
     print(json.dumps({"case": "profile", "replicas": int(w.replicas), "moves": moves, "ms": ms,
                       "moves_per_s": moves / (ms / 1000.0),
-                      "algorithmic_bytes": wl.algorithmic_bytes(tal, w.n_binders)}), flush=True)
+                      "algorithmic_bytes": wl.algorithmic_bytes(tal, w.n_binders),
+                      "move_stats": wl.move_stats(tal)}), flush=True)
 
 
 # Exchange rounds (62 MC steps each) run before the warm-up rounds: after
@@ -580,6 +581,7 @@ def main():
                        "autotune_moves_per_s": {k: round(v) for k, v in tune_table.items()}},
             "rounds": {"round_ms": [round(x, 3) for x in round_ms],
                        "mc_kernel_ms": [round(float(x), 3) for x in mc_ms]},
+            "move_stats": wl.move_stats(tal),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
                          "kernel": "spec_kernel<float,%d>" % sim.launch_shape()[1],

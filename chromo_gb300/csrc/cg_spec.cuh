@@ -155,6 +155,25 @@ constexpr int kPoolMaxBeads = 256;
 constexpr int kLanesPerBead = 4;
 constexpr int kCornersPerLane = 8 / kLanesPerBead;
 
+// The bond to the fixed right neighbour of moved bead i (old r, t3, t2 and
+// new tr, tt3, tt2), with its twist term: the second bond of a one-bead move
+// when one lane takes the whole bead.
+template <typename Pos, typename Acc>
+static __device__ __noinline__ Acc right_bond_term(const ChainView<Pos>& cv, long long i, const Pos (&r)[3],
+                                                   const Pos (&tr)[3], const Pos (&t3)[3], const Pos (&tt3)[3],
+                                                   const Pos (&t2)[3], const Pos (&tt2)[3]) {
+  const V4<Pos> RN = cv.r4[i + 1], TN = cv.t34[i + 1];
+  const Bond<Pos> bn = bond_at(cv.bonds, cv.bonds32, i, (Pos)0);
+  const Pos rn[3] = {RN.x, RN.y, RN.z}, tn[3] = {TN.x, TN.y, TN.z};
+  Acc out = acc_zero<Acc>();
+  acc_add(out, pair_dE_rev(bn, r, tr, rn, t3, tt3, tn));
+  if (cv.twist) {
+    const Frame nb = frame_of(cv.t24[i + 1], TN), cur = frame_of(t2, t3), nw = frame_of(tt2, tt3);
+    acc_add_d(out, twist_pair_dE(cv.twist + 2 * i, cur, nb, nw, nb));
+  }
+  return out;
+}
+
 // Lane cl (0..kLanesPerBead-1) of bead k of a position move (transform M;
 // segment [ind0, indf) of m beads of a chain of N): transforms the bead,
 // stages its r, t3, t2 (lanes 0-2), takes the bond to a fixed left neighbour
@@ -175,11 +194,15 @@ __device__ __forceinline__ void bead_task(const RepDev& rd, const GridF& gf, con
                                           bool& left, bool& right, Acc& pterm, int& oob) {
   using Real = Pos;
   const long long i = ind0 + k;
+  constexpr int kRightLane = kLanesPerBead > 1 ? 1 : 0;
   left = cl == 0 && k == 0 && ind0 != 0;
-  right = cl == 1 && k == m - 1 && indf != N;
+  right = cl == kRightLane && k == m - 1 && indf != N;
+  // with one lane per bead, a one-bead move's lane takes both bonds; else a
+  // lane takes at most one, and loads one neighbour
+  const bool two = kLanesPerBead == 1 && left && right;
   const long long in = left ? i - 1 : (right ? i + 1 : i);
   const V4<Pos> RN = cv.r4[in], TN = cv.t34[in];
-  const Bond<Real> bn = bond_at(cv.bonds, cv.bonds32, right ? i : in, (Real)0);
+  const Bond<Real> bn = bond_at(cv.bonds, cv.bonds32, (right && !left) ? i : in, (Real)0);
   const V4<Pos> R = cv.r4[i], T3 = cv.t34[i], T2 = cv.t24[i];
   const unsigned swi = density ? cv.st[i] : 0u;
   const Real r[3] = {R.x, R.y, R.z}, t3[3] = {T3.x, T3.y, T3.z}, t2[3] = {T2.x, T2.y, T2.z};
@@ -195,19 +218,27 @@ __device__ __forceinline__ void bead_task(const RepDev& rd, const GridF& gf, con
   }
   const bool fin = isfinite(tr[0]) && isfinite(tr[1]) && isfinite(tr[2]);
   if (!fin) e |= E_NONFINITE;
-  if (cl < 3) {
+#pragma unroll
+  for (int w = cl; w < 3; w += kLanesPerBead) {  // lanes 0-2 stage r, t3, t2 (all three with fewer lanes)
     Real o[3];
-    for (int j = 0; j < 3; j++) o[j] = cl == 0 ? tr[j] : (cl == 1 ? tt3[j] : tt2[j]);
-    stage[3 * k + cl] = V4<Pos>{(Pos)o[0], (Pos)o[1], (Pos)o[2], (Pos)0};
+    for (int j = 0; j < 3; j++) o[j] = w == 0 ? tr[j] : (w == 1 ? tt3[j] : tt2[j]);
+    stage[3 * k + w] = V4<Pos>{(Pos)o[0], (Pos)o[1], (Pos)o[2], (Pos)0};
   }
   const Real rn[3] = {(Real)RN.x, (Real)RN.y, (Real)RN.z}, tn[3] = {(Real)TN.x, (Real)TN.y, (Real)TN.z};
   pterm = acc_zero<Acc>();
   if (left) acc_add(pterm, pair_dE_fwd(bn, rn, r, tr, tn, t3, tt3));
-  if (right) acc_add(pterm, pair_dE_rev(bn, r, tr, rn, t3, tt3, tn));
-  if (cv.twist && (left || right)) {  // SSTWLC: the bond's twist term
+  if (right && !two) acc_add(pterm, pair_dE_rev(bn, r, tr, rn, t3, tt3, tn));
+  if (cv.twist && (left || right) && !two) {  // SSTWLC: the bond's twist term
     const Frame nb = frame_of(cv.t24[in], TN), cur = frame_of(t2, t3), nw = frame_of(tt2, tt3);
     const double* tw = cv.twist + 2 * (left ? in : i);
     acc_add_d(pterm, left ? twist_pair_dE(tw, nb, cur, nb, nw) : twist_pair_dE(tw, cur, nb, nw, nb));
+  }
+  if (two) {  // the right bond of a one-bead move (one lane per bead), out of line
+    acc_add(pterm, right_bond_term<Pos, Acc>(cv, i, r, tr, t3, tt3, t2, tt2));
+    if (cv.twist) {
+      const Frame nb = frame_of(cv.t24[in], TN), cur = frame_of(t2, t3), nw = frame_of(tt2, tt3);
+      acc_add_d(pterm, twist_pair_dE(cv.twist + 2 * in, nb, cur, nb, nw));
+    }
   }
   oob = 0;
   if (cl == 0 && conf) oob = out_of_bounds(rd, tr, true) * 65536 + out_of_bounds(rd, r, false);
@@ -298,8 +329,8 @@ __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, in
       int oob;
       bead_task<Pos, Acc>(rd, gf, cv, kind, M, N, P.ind0, P.indf, P.m, k, cl, stage, true, conf, vq, q, sw, e,
                           left, right, pterm, oob);
-      if (left) store_acc(P.pq[0], P.ph[0], pterm);
-      if (right) store_acc(P.pq[1], P.ph[1], pterm);
+      if (left) store_acc(P.pq[0], P.ph[0], pterm);  // both bonds of a one-lane bead: in pq[0]
+      if (right && !left) store_acc(P.pq[1], P.ph[1], pterm);
       if (oob) atomicAdd(&P.oob, oob);
     }
     // the pooled table (one used list for the whole CTA, keys voxel * 32 +

@@ -244,3 +244,17 @@ def algorithmic_bytes(tally: np.ndarray, n_binders: int, pos_bytes: int = 12) ->
             b += m_acc * nb
         total += b
     return total
+
+
+def move_stats(tally: np.ndarray) -> dict:
+    """Per move kind, from a tally [R, 5, 6]: the share of the attempted
+    moves, the acceptance rate, and the mean beads and touched voxels of an
+    attempted move."""
+    t = tally.reshape(-1, 5, 6).sum(0).astype(np.float64)
+    total = max(1.0, float(t[:, 0].sum()))
+    out = {}
+    for k, name in enumerate(nat.MOVE_NAMES):
+        att = max(1.0, t[k, 0])
+        out[name] = {"share": round(t[k, 0] / total, 4), "acceptance": round(t[k, 1] / att, 4),
+                     "mean_beads": round(t[k, 2] / att, 2), "mean_voxels": round(t[k, 3] / att, 2)}
+    return out

@@ -52,6 +52,14 @@ WORKLOAD_DESCS = {
     "diff": ("batched + differentiation: 64 chains of 5,000 beads, 40^3 grids (40 nm voxels), two "
              "binders, no exchange; dE/dr and dE/d(chi, mu_A, mu_B, eps_AA, eps_BB, eps_AB) kernels "
              "and 1e6 on-device reweighting samples reported under 'derivatives'"),
+    "plain": ("plain single chain: one 10,000-bead chain in a periodic 2400 nm box with a 60^3 grid "
+              "of 40 nm voxels, FP32 positions, int64 fixed-point density; one binder (mu = -0.4, "
+              "eps = -4, chi = 1), marks with mean run length 50; all five moves with SimpleControl; "
+              "1e6 attempted moves per step (10 steps = 1e7 moves)"),
+    "small": ("plain CPU-runnable chain: one 1,000-bead chain in a periodic 1200 nm box with a 30^3 grid "
+              "of 40 nm voxels, FP64 positions; one binder (mu = -0.4, eps = -4, chi = 1), marks with "
+              "mean run length 20; specific_moves (one attempt of each of the five moves per MC "
+              "step) with SimpleControl; 1e4 MC steps per step (10 steps = 1e5 attempts per move kind)"),
     "sphere": ("confined batched: 256 chains of 5,000 beads, each confined to a sphere of radius "
                "700 nm inside its 1600 nm box with a 40^3 grid of 40 nm voxels (Spherical "
                "confinement; per-voxel accessible volumes at the surface); two binders; chi ladder "
@@ -65,10 +73,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "large", "diff", "sphere"],
+    ap.add_argument("--workload", default="batched",
+                    choices=["batched", "large", "diff", "sphere", "plain", "small"],
                     help="batched: 256 replicas (the headline); large: 32 x 100,000 beads with a "
                          "chi x mu ladder; diff: 64 x 5,000 beads plus the derivative kernels and 1e6 "
-                         "reweighting samples")
+                         "reweighting samples; sphere: 256 confined chains; plain: one 10,000-bead "
+                         "chain, 1e7 moves; small: one 1,000-bead FP64 chain, 1e5 attempts per move kind")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-budget", type=float, default=2.0)
     ap.add_argument("--profile", action="store_true",
@@ -233,6 +243,119 @@ def derivatives_leg(sim, w, stream):
             "mean_sensitivities_over_replicas": mean}
 
 
+# MC steps per bench step of the single-chain workloads: ~1e6 attempted moves
+# on the 10,000-bead chain (10 steps = the 1e7 moves of that configuration);
+# 1e4 MC steps of one attempt per move kind on the 1,000-bead chain (10 steps
+# = 1e5 attempts of every move kind)
+SINGLE_STEP_MC = {"plain": 6200, "small": 10000}
+
+
+def single_chain_bench(args, rank, world):
+    """One chain on the production kernel (one CTA): the plain configurations.
+    W warm-up steps from the seeded start, K timed steps (one MC launch each,
+    CUDA events on the launching stream), then the same K steps from the same
+    start state through the C ABI with host buffers (upload, re-deposit, run,
+    read back every step), and the reference's mc_sim on one host core from
+    the state after the same warm-up MC steps (the C restatement advances the
+    chain there; the reference then times itself)."""
+    import numpy as np
+    import torch
+    from chromo_gb300.build import build
+    build()
+    from chromo_gb300 import workloads as wl
+    torch.cuda.set_device(0 if world == 1 else rank % max(1, torch.cuda.device_count()))
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    w = wl.make_workload(args.workload, seed_offset=rank)
+    step_mc = SINGLE_STEP_MC[args.workload]
+    sim = wl.build_sim(w)
+    warm = max(args.warmup, 3)
+    for k in range(warm):
+        sim.run(step_mc, 100 + k, sh)
+    sim.sync(sh)
+    start_chains = sim.get_chains()
+    start_ctl = sim.get_controllers(0)
+    sim.reset_tally()
+    barrier(world)
+    torch.cuda.synchronize()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(torch.cuda.current_device()) as clocks:
+        evs[0].record(stream)
+        for k in range(args.steps):
+            sim.run(step_mc, 200 + k, sh)
+            evs[k + 1].record(stream)
+        torch.cuda.synchronize()
+    sim.sync(sh)
+    barrier(world)
+    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    ms = evs[0].elapsed_time(evs[-1])
+    ms_max = allreduce_max(ms, world)
+    tal = sim.tally(0)[None]
+    attempts = float(tal[:, :, 0].sum())
+    value = allreduce_sum(attempts, world) / (ms_max / 1000.0)
+    pos_bytes = 24 if w.pos_fp64 else 12
+    peak, peak_kind = load_peaks()
+    achieved = wl.algorithmic_bytes(tal, w.n_binders, pos_bytes) / (ms / 1000.0) / 1e9
+    # e2e: the same K steps from the same start through the C ABI with host buffers
+    sim.set_chains([dict(r=r, t3=t3, t2=t2, states=st) for r, t3, t2, st in start_chains])
+    sim.set_controllers(0, start_ctl)
+    spare, other = sim.get_chains(), sim.get_chains()
+    inp, t_e2e = start_chains, 0.0
+    for k in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.set_chains([dict(r=r, t3=t3, t2=t2, states=st) for r, t3, t2, st in inp])
+        sim.deposit(-1)
+        sim.run(step_mc, 200 + k, sh)
+        sim.sync(sh)
+        out = sim.get_chains(out=spare)
+        t_e2e += time.perf_counter() - t0
+        spare = other if k == 0 else inp
+        inp = out
+    n = int(w.lengths[0])
+    io_bytes = n * (3 * (32 if w.pos_fp64 else 16) + 4)
+    e2e_value = allreduce_sum(attempts, world) / allreduce_max(t_e2e, world)
+    shape = sim.launch_shape()
+    sim.close()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import refbench
+        cpu = refbench.run(args.workload, budget=max(args.cpu_budget, 10.0), n_procs=1,
+                           settle_steps=warm * step_mc)
+    if rank != 0:
+        return
+    out = {
+        "metric": METRIC, "value": value, "unit": "moves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if w.pos_fp64 else "f32",
+        "data": "synthetic (seeded Gaussian-walk chain, Markov mark track)",
+        "config": {"workload": WORKLOAD_DESCS[args.workload], "replicas": 1, "beads_total": n,
+                   "mc_steps_per_step": step_mc, "attempted_moves_per_step": int(attempts / args.steps),
+                   "warmup_mc_steps": warm * step_mc,
+                   "l2": "single chain: its state (%.1f MB) is L2-resident; nothing is flushed"
+                         % ((w.nbins ** 3 * 16 + n * 104) / 1e6),
+                   "launch_shape": dict(zip(("warps_per_replica", "lanes_per_move", "moves_in_flight",
+                                             "hash_slots"), shape))},
+        "rounds": {"step_ms": [round(x, 3) for x in step_ms]},
+        "move_stats": wl.move_stats(tal),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "traffic_note": "not captured for the single-chain workloads",
+                     "kernel": "spec_kernel<%s,32>" % ("double" if w.pos_fp64 else "float"),
+                     "peak_source": peak_kind, "avg_launch_ms": ms / args.steps,
+                     "timing": "one MC launch per step, CUDA events on the launching stream"},
+        "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": io_bytes,
+                "d2h_bytes_per_step": io_bytes,
+                "path": "C ABI, host-driven steps: cg_set_chains, cg_deposit, cg_run, cg_get_chains"},
+        "gpu_launches": args.steps,
+        "clocks": clocks.summary(),
+    }
+    if cpu is not None:
+        out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(out), flush=True)
+
+
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -326,8 +449,10 @@ def reference_arm(args, rank, world):
     from chromo_gb300.workloads import make_workload
     w = make_workload(args.workload)
     per_step = 1.0
+    settle = (max(args.warmup, 3) * SINGLE_STEP_MC[args.workload] if args.workload in SINGLE_STEP_MC
+              else SETTLE_ROUNDS * w.steps_per_round)
     res = refbench.run(args.workload, budget=per_step * (args.steps + args.warmup),
-                       n_procs=os.cpu_count(), settle_steps=SETTLE_ROUNDS * w.steps_per_round)
+                       n_procs=os.cpu_count(), settle_steps=settle)
     out = {
         "impl": "reference", "metric": METRIC, "value": res["value"], "unit": "moves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -353,6 +478,9 @@ def main():
     rank, world, local = dist_init(args)
     if args.impl == "reference":
         reference_arm(args, rank, world)
+        return
+    if args.workload in SINGLE_STEP_MC:
+        single_chain_bench(args, rank, world)
         return
     # wall seconds of each untimed setup phase and timed leg, reported with the line
     phases, t_last = {}, [time.perf_counter()]

@@ -2,6 +2,11 @@
 
 Sizes follow the benchmark configurations of this path:
 
+* ``small``   one chain of 1,000 beads in a 1,200 nm box, 30^3 grid of 40 nm
+              voxels, one binder (mu = -0.4, eps = -4, chi = 1), marks with
+              mean run length 20, FP64 positions; the five moves as
+              ``specific_moves`` (one attempt of each kind per MC step,
+              chromo/mc/mc_controller.py:374-421) under SimpleControl.
 * ``plain``   one chain of 10,000 beads, 60^3 grid of 40 nm voxels, one binder
               (mu = -0.4, eps = -4, chi = 1), marks with mean run length 50.
 * ``batched`` 256 chains with lengths log-uniform in [2,000, 20,000], each with
@@ -59,11 +64,17 @@ def amplitude_bounds(n_beads, min_spacing=BEAD_SPACING):
     return bead, move
 
 
-def all_moves_ctl(n_beads):
-    """all_moves(..., SimpleControl) as device controllers."""
+ONE_PER_CYCLE = {m: 1 for m in NUM_PER_CYCLE}  # specific_moves: num_per_cycle = 1
+
+
+def all_moves_ctl(n_beads, cycle=None):
+    """all_moves(..., SimpleControl) as device controllers (``cycle``: the
+    attempts per controller cycle, NUM_PER_CYCLE by default; ONE_PER_CYCLE
+    gives specific_moves(all five moves, ..., SimpleControl))."""
+    cycle = cycle or NUM_PER_CYCLE
     bead, move = amplitude_bounds(n_beads)
     return [move_ctl(m, amp_move=move[m][0], amp_bead=int(bead[m][0]),
-                     num_per_cycle=NUM_PER_CYCLE[m], simple=True, bead_bounds=bead[m],
+                     num_per_cycle=cycle[m], simple=True, bead_bounds=bead[m],
                      move_bounds=move[m]) for m in nat.MOVE_NAMES]
 
 
@@ -83,6 +94,8 @@ class Workload:
     steps_per_round: int = 62    # ~1e4 attempted moves per replica per exchange round
     mu_rungs: int = 0            # > 1: grids of mu_rungs x n_rungs, mu_A exchanged along mu rungs
     sphere_radius: float = 0.0   # > 0: Spherical confinement with accessible volumes
+    cycle: dict = None           # attempts per controller cycle (None: NUM_PER_CYCLE)
+    pos_fp64: bool = False       # FP64 positions (the CPU-runnable configuration)
     replicas: int = field(init=False)
 
     def __post_init__(self):
@@ -90,7 +103,7 @@ class Workload:
 
     @property
     def moves_per_step(self):
-        return int(sum(NUM_PER_CYCLE.values()))
+        return int(sum((self.cycle or NUM_PER_CYCLE).values()))
 
 
 def make_workload(name: str, seed_offset: int = 0) -> Workload:
@@ -99,7 +112,8 @@ def make_workload(name: str, seed_offset: int = 0) -> Workload:
                         [-4.0], [{}], 50, 0, BASE_SEED + 1 + seed_offset)
     if name == "small":  # the CPU-runnable plain configuration
         return Workload("small", np.array([1000]), 30, 1, np.array([[-0.4]]), np.array([1.0]),
-                        [-4.0], [{}], 20, 0, BASE_SEED + seed_offset)
+                        [-4.0], [{}], 20, 0, BASE_SEED + seed_offset, cycle=dict(ONE_PER_CYCLE),
+                        pos_fp64=True)
     rng = np.random.default_rng(BASE_SEED + 2 + seed_offset)
     if name == "batched":
         R, rungs = 256, 16
@@ -177,8 +191,9 @@ def binder_names(nb):
     return ["HP1", "PRC1", "B3"][:nb]
 
 
-def build_sim(w: Workload, chains=None, pos_fp64=False, warps_per_block=0, lanes_per_move=0) -> nat.Sim:
+def build_sim(w: Workload, chains=None, pos_fp64=None, warps_per_block=0, lanes_per_move=0) -> nat.Sim:
     chains = chains if chains is not None else make_chains(w)
+    pos_fp64 = w.pos_fp64 if pos_fp64 is None else pos_fp64
     R, nb = w.replicas, w.n_binders
     confined = w.sphere_radius > 0
     sim = nat.Sim(w.lengths, [[w.nbins] * 3] * R, nb, pos_fp64=pos_fp64, max_segment=152,
@@ -204,7 +219,7 @@ def build_sim(w: Workload, chains=None, pos_fp64=False, warps_per_block=0, lanes
         sim.set_binding(rep, binding_params(sites=[SITES] * nb, e_mod=[HP1_E_MOD] * nb,
                                             e_nomod=[HP1_E_NOMOD] * nb, mu=list(w.mu[rep]),
                                             mu_adjust_factor=1.0))
-        sim.set_controllers(rep, all_moves_ctl(n))
+        sim.set_controllers(rep, all_moves_ctl(n, w.cycle))
     sim.deposit(-1)
     return sim
 

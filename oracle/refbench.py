@@ -95,8 +95,9 @@ def _settled(w, rep, chain, settle_steps, seed):
                      xpref=xpref, pos="f64", fixed_density=0, **confine)
     o.deposit_all()
     bead, move = amplitude_bounds(n)
+    cycle = w.cycle or NUM_PER_CYCLE
     ctls = [make_ctl(m, amp_move=move[m][0], amp_bead=int(bead[m][0]),
-                     num_per_cycle=NUM_PER_CYCLE[m], bead_bounds=bead[m], move_bounds=move[m])
+                     num_per_cycle=cycle[m], bead_bounds=bead[m], move_bounds=move[m])
             for m in ["crank_shaft", "end_pivot", "slide", "tangent_rotation", "change_binding_state"]]
     if settle_steps:
         ctypes.CDLL(None).srand(seed)
@@ -136,7 +137,14 @@ def _build_reference_replica(w, rep, chain, amps=None):
     f = UniformDensityField([p], binders, width, w.nbins, width, w.nbins, width, w.nbins,
                             chi=float(w.chi[rep]), **confine)
     bab, mab = cmc.get_amplitude_bounds([p])
-    ctrls = all_moves("/tmp/chromo_refbench_logs", bab.bounds, mab.bounds, SimpleControl)
+    if w.cycle:  # one attempt of each move per MC step: the reference's specific_moves
+        import chromo.mc.moves as mv
+        from chromo.mc.mc_controller import specific_moves
+        ctrls = specific_moves([mv.crank_shaft, mv.end_pivot, mv.slide, mv.tangent_rotation,
+                                mv.change_binding_state], "/tmp/chromo_refbench_logs", bab.bounds,
+                               mab.bounds, SimpleControl)
+    else:
+        ctrls = all_moves("/tmp/chromo_refbench_logs", bab.bounds, mab.bounds, SimpleControl)
     for c, a in zip(ctrls, amps or []):  # the settled amplitudes and acceptance rates
         c.move.amp_move, c.move.amp_bead = a[0], a[1]
         c.move.acceptance_tracker.acceptance_rate = a[2]
@@ -188,13 +196,15 @@ def _port_worker(args):
 
 def run(workload="batched", budget=2.0, n_procs=None, prefer="reference", settle_steps=0):
     """Aggregate attempted moves/s of the CPU implementation on this host, from
-    the state after `settle_steps` MC steps of every sampled replica."""
+    the state after `settle_steps` MC steps of every sampled replica.  A
+    single-chain workload runs in one process (the reference's mc_sim is
+    serial; more processes would run other chains, not this one faster)."""
     if str(ROOT) not in sys.path:
         sys.path.insert(0, str(ROOT))
     from chromo_gb300.workloads import make_workload
     w = make_workload(workload)
     n_procs = n_procs or os.cpu_count() or 1
-    n_procs = max(1, min(n_procs, w.replicas if w.replicas > 1 else n_procs))
+    n_procs = max(1, min(n_procs, w.replicas))
     kind, reason = "port", ""
     if prefer == "reference":
         ok, reason = ensure_reference_built()

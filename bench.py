@@ -605,12 +605,18 @@ def main():
         sim.run(steps_round, 301 + i, sh)
     sim.sync(sh)
     en1 = sim.energies(sh)
-    d_true = en1[:, :3].sum(1) - en0[:, :3].sum(1)
+    E0, E1 = en0[:, :3].sum(1), en1[:, :3].sum(1)
+    d_true = E1 - E0
     d_run = en1[:, 3] - en0[:, 3]
-    drift_abs = np.abs(d_true - d_run)
+    # a replica whose energy still carries a 1e99 penalty (a voxel above the
+    # volume-fraction limit, or a bead outside the confinement) at either end
+    # has no drift measurable in FP64
+    soft = (np.abs(E0) < 1e20) & (np.abs(E1) < 1e20)
+    drift_abs = np.abs(d_true - d_run)[soft]
     drift = {"max_abs_kT": float(drift_abs.max()), "median_abs_kT": float(np.median(drift_abs)),
-             "max_rel_to_energy": float((drift_abs / np.maximum(1.0, np.abs(en1[:, :3].sum(1)))).max()),
+             "max_rel_to_energy": float((drift_abs / np.maximum(1.0, np.abs(E1[soft]))).max()),
              "moves_per_replica": int(3 * steps_round * w.moves_per_step),
+             "replicas_with_penalised_energy": int((~soft).sum()),
              "how": "FP64 full-energy recompute on the device before and after 3 MC launches "
                     "vs the running sum of accepted dE"}
     mark("energy_drift")

@@ -15,7 +15,10 @@ state with the running sum of accepted dE.  Away from rounding it is zero,
 except for one reference rule kept for parity: tangent_rotation evaluates
 each rotated bead with its neighbours' current tangents
 (chromo/polymers.pyx:1074-1080), so when two adjacent beads rotate in the
-same move the summed dE is not the energy change.
+same move the summed dE is not the energy change.  Moves whose dE carries a
+1e25 / 1e99 penalty are left out of the running sum (one would absorb every
+later dE in FP64); a replica whose baseline or current energy carries a
+penalty has no measurable drift and reports NaN.
 """
 from typing import List, Optional, Sequence
 
@@ -28,6 +31,16 @@ from .mc import get_amplitude_bounds
 from .mc.mc_controller import SimpleControl, all_moves
 from .mc.mc_sim import (_binding_struct, _bounds, _ctl_struct, _field_kind, _field_struct,
                         _grid_dims)
+
+
+# energies at or above this carry the 1e25 max_binders or 1e99 field penalty
+PENALTY_FLOOR = 1e20
+
+
+def _drift(E, E0, run):
+    """(E - E0) - run, NaN where E or E0 carries a penalty."""
+    d = (E - E0) - run
+    return np.where((np.abs(E) < PENALTY_FLOOR) & (np.abs(E0) < PENALTY_FLOOR), d, np.nan)
 
 
 class EnergyDriftError(RuntimeError):
@@ -158,15 +171,17 @@ class ReplicaBatch:
         self.sim.reset_running_energy()
 
     def energy_drift(self) -> np.ndarray:
-        """Per replica: (E_now - E_baseline) - (sum of accepted dE since then)."""
+        """Per replica: (E_now - E_baseline) - (sum of accepted dE since then);
+        NaN where either energy carries a penalty (|E| >= PENALTY_FLOOR)."""
         e = self.sim.energies()
-        return (e[:, 0] + e[:, 1] + e[:, 2] - self._E0) - e[:, 3]
+        return _drift(e[:, 0] + e[:, 1] + e[:, 2], self._E0, e[:, 3])
 
     def check_drift(self, rel_tol: float = 1e-6):
-        """Raise EnergyDriftError if |drift| > rel_tol * max(1, |E|) for any replica."""
+        """Raise EnergyDriftError if |drift| > rel_tol * max(1, |E|) for any
+        replica whose energies carry no penalty."""
         e = self.sim.energies()
         E = e[:, 0] + e[:, 1] + e[:, 2]
-        drift = (E - self._E0) - e[:, 3]
+        drift = _drift(E, self._E0, e[:, 3])
         bad = np.nonzero(np.abs(drift) > rel_tol * np.maximum(1.0, np.abs(E)))[0]
         if len(bad):
             raise EnergyDriftError(f"energy drift above {rel_tol:g} on replicas {bad.tolist()[:8]}: "

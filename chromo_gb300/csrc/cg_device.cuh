@@ -27,6 +27,15 @@ constexpr double kRandMax = 2147483647.0;               // glibc RAND_MAX
 // exactly zero when the weight above the limit does not change, so the
 // decisions in that regime are well defined.
 constexpr double kHugeUnit = kEHugeField * kFxInv;
+// The running sum of accepted dE (RepDev::run_dE) leaves out moves whose dE
+// carries a penalty (|dE| >= kPenaltyFloor: the 1e25 max_binders term or the
+// 1e99 field terms; soft energies of a chain are many orders below): one such
+// term in an FP64 sum would absorb every later dE.  Such moves only leave a
+// penalised state (a move into one is never accepted), so the energy at one
+// end of their interval carries the penalty itself, and differences of the
+// running sum over intervals whose energies carry none stay exact.
+constexpr double kPenaltyFloor = 1e20;
+__device__ __forceinline__ bool soft_dE(double dE) { return fabs(dE) < kPenaltyFloor; }
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxIter = 4096;                          // cap on resampling loops
 

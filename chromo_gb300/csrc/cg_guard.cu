@@ -8,7 +8,9 @@
 // change since the previous check is compared with the change of
 // run_dE + xch_dE over the same rounds.  A difference beyond
 // tol_abs + tol_rel * max(1, |E|) (or a non-finite one) sets the replica's
-// E_DRIFT error bit, which the next cg_sync reports.  The recompute is split
+// E_DRIFT error bit, which the next cg_sync reports.  An interval whose end
+// energies carry a 1e25 / 1e99 penalty is not compared (FP64 cannot resolve
+// the soft energy next to it); its end becomes the next reference.  The recompute is split
 // over chunk x replica blocks whose partial sums are added in chunk order, so
 // it is deterministic and spreads over the GPU even for a few large replicas.
 //
@@ -68,7 +70,9 @@ __global__ void guard_check_kernel(KArgs a, GuardArgs g) {
       E += t[2] + intra;
     }
     const double run = rd.run_dE + rd.xch_dE;
-    if (g.init[rep]) {
+    // an interval whose end energies carry a penalty (|E| >= kPenaltyFloor)
+    // cannot be checked in FP64: the guard takes new references there
+    if (g.init[rep] && fabs(E) < kPenaltyFloor && fabs(g.e_ref[rep]) < kPenaltyFloor) {
       const double d = (E - g.e_ref[rep]) - (run - g.run_ref[rep]);
       g.drift[rep] = d;
       const double bound = g.tol_abs + g.tol_rel * (fabs(E) > 1.0 ? fabs(E) : 1.0);

@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
                   st[i] = sw;
                 }
               }
-              if (lane == 0) { c.num_success += 1; run_dE += dE; }
+              if (lane == 0) { c.num_success += 1; if (soft_dE(dE)) run_dE += dE; }
             }
             if (density && check_field) commit_grid(rd, a, ncol, keys, used, vals, ws.nused, lane, acc);
             if (kind == CG_TANGENT_ROTATION) {

@@ -1258,7 +1258,7 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
                 const MovePlan& P = sh.plan[w];
                 if (a.mlog) log_move(a, rep, sh.t0 + (unsigned long long)w - sh.tlog, P);
                 if (P.empty) continue;
-                if (P.dec) run += P.dE;
+                if (P.dec && soft_dE(P.dE)) run += P.dE;
                 rate = (P.dec ? alpha : 0.0) + beta * rate;
               }
               sh.run_dE = run;

@@ -218,7 +218,12 @@ int cg_run_logged(cg_sim *sim, int64_t n_steps, uint64_t seed, cg_move_record *r
  *        are binding_dE, chromo/polymers.pyx:1383-1538),
  * out[2] field energy in the form whose differences are the per-move field dE
  *        (chromo/fields.pyx:1675-1875),
- * out[3] running sum of accepted dE since the last cg_reset_running_energy. */
+ * out[3] running sum of accepted dE since the last cg_reset_running_energy,
+ *        leaving out the moves whose dE carries a penalty (|dE| >= 1e20: the
+ *        1e25 max_binders term, the 1e99 volume-fraction and confinement
+ *        terms), which would absorb every later dE in an FP64 sum; such moves
+ *        only leave a penalised state, so the running sum's changes equal the
+ *        energy's over every interval whose end energies carry no penalty. */
 int cg_energy(cg_sim *sim, int32_t rep, double *out);
 int cg_reset_running_energy(cg_sim *sim);
 
@@ -326,7 +331,9 @@ int cg_get_launch_shape(cg_sim *sim, int32_t *warps_per_block, int32_t *lanes_pe
  * accepted dE plus the energy change of the replica's accepted chi / mu swaps.
  * A difference above tol_abs + tol_rel * max(1, |E|), or a non-finite one,
  * makes the next cg_sync return CG_ERR_DRIFT.  The first check takes the
- * reference energies.  0 turns the guard off.  Drift has two sources: FP32
+ * reference energies; an interval with a penalised energy (|E| >= 1e20) at
+ * either end is not compared, and its end becomes the next reference.  0
+ * turns the guard off.  Drift has two sources: FP32
  * rounding of the per-move dE, and the reference's tangent-rotation rule for
  * adjacent beads (chromo/polymers.pyx:1074-1080), whose summed dE is not the
  * energy change; the tolerances must cover both. */

@@ -89,3 +89,46 @@ def test_guard_trips_on_corrupted_replica():
         assert np.all(others < 5.0)
     finally:
         sim.close()
+
+
+def test_running_sum_and_guard_through_penalised_start():
+    """Three replicas of the confined workload (5,000 beads in 700 nm spheres)
+    whose seeded start puts bead weight into surface voxels of tiny accessible
+    volume: their first energies carry 1e99 penalties, and the moves that
+    leave those voxels have dE of that size.  Those moves stay out of the
+    running sum of dE (in an FP64 sum they would absorb every later dE), so
+    once the penalties are gone the running sum follows the energy exactly
+    again (FP64 storage, tangent rotation off), and the guard, which skips
+    the penalised interval, checks the later ones and never trips."""
+    from chromo_gb300 import workloads as wl
+    w = wl.make_workload("sphere")
+    chains = wl.make_chains(w)
+    pick = [196, 211, 214]
+    sub = wl.Workload("sphere-subset", w.lengths[pick], w.nbins, w.n_binders, w.mu[pick], w.chi[pick],
+                      w.eps, w.cross, w.run_length, 1, w.seed, steps_per_round=20,
+                      sphere_radius=w.sphere_radius)
+    sim = wl.build_sim(sub, [chains[i] for i in pick], pos_fp64=True)
+    try:
+        _no_tangent(sim, sub)
+        E0 = sim.energies()[:, :3].sum(1)
+        assert np.all(np.abs(E0) >= 1e20), "the start must carry the 1e99 penalty"
+        sim.set_drift_guard(2, tol_abs=1e-6, tol_rel=1e-9)
+        for _ in range(12):
+            sim.run_batched(1, sub.steps_per_round, sub.n_rungs, 9)
+        sim.sync()
+        e1 = sim.energies()
+        E1 = e1[:, :3].sum(1)
+        assert np.all(np.abs(E1) < 1e20), "the penalties are left within 240 MC steps"
+        drift, checks = sim.drift()
+        assert checks == 6
+        assert np.all(np.abs(drift) <= 1e-9 * np.maximum(1.0, np.abs(E1)))
+        # a window without penalties: running-sum change == energy change
+        for _ in range(2):
+            sim.run_batched(1, sub.steps_per_round, sub.n_rungs, 9)
+        sim.sync()
+        e2 = sim.energies()
+        d = (e2[:, :3].sum(1) - E1) - (e2[:, 3] - e1[:, 3])
+        assert np.all(np.abs(d) <= 1e-9 * np.maximum(1.0, np.abs(E1))), d
+        assert np.abs(e2[:, 3]).max() < 1e20
+    finally:
+        sim.close()

@@ -275,6 +275,23 @@ def single_chain_bench(args, rank, world):
     sim.sync(sh)
     start_chains = sim.get_chains()
     start_ctl = sim.get_controllers(0)
+    sim.close()
+    # launch shape from the autotuner, every candidate started from the
+    # warmed-up state (untimed; cached per problem)
+    from chromo_gb300 import autotune
+
+    def build_at_start(W, G):
+        s = wl.build_sim(w, warps_per_block=W, lanes_per_move=G)
+        s.set_chains([dict(r=r, t3=t3, t2=t2, states=st) for r, t3, t2, st in start_chains])
+        s.set_controllers(0, start_ctl)
+        s.deposit(-1)
+        return s
+
+    tune_steps = max(50, step_mc // 20)
+    shape, tune_table = autotune.tune(build_at_start, w.lengths, [[w.nbins] * 3], w.n_binders,
+                                      pos_fp64=w.pos_fp64, steps=tune_steps, warmup=tune_steps // 5,
+                                      extra_key=args.workload + "-warm")
+    sim = build_at_start(*shape)
     sim.reset_tally()
     barrier(world)
     torch.cuda.synchronize()
@@ -315,7 +332,7 @@ def single_chain_bench(args, rank, world):
     n = int(w.lengths[0])
     io_bytes = n * (3 * (32 if w.pos_fp64 else 16) + 4)
     e2e_value = allreduce_sum(attempts, world) / allreduce_max(t_e2e, world)
-    shape = sim.launch_shape()
+    launch = sim.launch_shape()
     sim.close()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -336,7 +353,8 @@ def single_chain_bench(args, rank, world):
                    "l2": "single chain: its state (%.1f MB) is L2-resident; nothing is flushed"
                          % ((w.nbins ** 3 * 16 + n * 104) / 1e6),
                    "launch_shape": dict(zip(("warps_per_replica", "lanes_per_move", "moves_in_flight",
-                                             "hash_slots"), shape))},
+                                             "hash_slots"), launch)),
+                   "autotune_moves_per_s": {k: round(v) for k, v in tune_table.items()}},
         "rounds": {"step_ms": [round(x, 3) for x in step_ms]},
         "move_stats": wl.move_stats(tal),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -635,15 +653,21 @@ def main():
         sim.set_drift_guard(guard_every, tol_abs=GUARD_TOL_ABS, tol_rel=GUARD_TOL_REL)
     inp = start_chains
     t_e2e = 0.0
+    e2e_parts = np.zeros(4)  # seconds in upload, re-deposit, round, read-back
     for k in range(args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sim.set_chains([dict(r=r, t3=t3, t2=t2, states=st) for r, t3, t2, st in inp])
+        t1 = time.perf_counter()
         sim.deposit(-1)  # the densities of the uploaded chains
+        t2 = time.perf_counter()
         sim.run_batched(1, steps_round, w.n_rungs, 11 + rank, sh)
         sim.sync(sh)
+        t3 = time.perf_counter()
         out = sim.get_chains(out=spare)
-        t_e2e += time.perf_counter() - t0
+        t4 = time.perf_counter()
+        t_e2e += t4 - t0
+        e2e_parts += (t1 - t0, t2 - t1, t3 - t2, t4 - t3)
         spare = other if k == 0 else inp  # the start snapshot is never overwritten
         inp = out
     nbeads = int(w.lengths.sum())
@@ -727,7 +751,9 @@ def main():
                     "d2h_bytes_per_step": d2h,
                     "path": "C ABI, host-driven rounds: cg_set_chains (the previous round's host "
                             "snapshot, FP64 -> pinned -> HBM, all replicas), cg_deposit, cg_run_batched, "
-                            "cg_get_chains (into reused host arrays)"},
+                            "cg_get_chains (into reused host arrays)",
+                    "ms_per_step": dict(zip(("set_chains", "deposit", "round", "get_chains"),
+                                            (round(float(x) * 1e3 / args.steps, 3) for x in e2e_parts)))},
             "plain": {"value": plain_value, "unit": "moves/s",
                       "workload": "one 10,000-bead chain, 60^3 grid, one binder, 300 MC steps after "
                                   "%d settle MC steps" % (SETTLE_ROUNDS * steps_round),

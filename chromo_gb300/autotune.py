@@ -56,13 +56,19 @@ def problem_key(n_beads: Sequence[int], grid_dims: Sequence, n_binders: int, pos
 def candidates(n_replicas: int, n_sm: int, pos_fp64: bool, warps_per_sm: Dict[int, int]) -> List[Shape]:
     """Shapes worth timing: for each G, the W that keep every replica's CTA
     resident at once (ceil(R / SMs) CTAs per SM within the register file) --
-    the largest such W and a few below it -- with at most 32 moves in flight."""
+    the largest such W and a few below it -- with at most 32 moves in flight.
+    When every replica has an SM to itself, a few small W at 32 lanes too: a
+    chain whose controller cycles hold few moves (one with specific_moves)
+    has few moves to put in flight, and fewer warps then shorten each
+    batch's barriers."""
     ctas = max(1, math.ceil(n_replicas / max(1, n_sm)))
     out = []
     for G in ((32,) if pos_fp64 else (32, 16, 8)):
         wmax = min(MAX_WARPS, MAX_IN_FLIGHT * G // 32, max(1, warps_per_sm[G] // ctas))
-        ws = sorted({wmax, wmax - 1, wmax - 2, (wmax + 1) // 2} - {0}, reverse=True)
-        out += [(w, G) for w in ws if w >= 1]
+        ws = {wmax, wmax - 1, wmax - 2, (wmax + 1) // 2}
+        if G == 32 and n_replicas <= n_sm:
+            ws |= {w for w in (1, 2, 4) if w <= wmax}
+        out += [(w, G) for w in sorted(ws - {0}, reverse=True) if w >= 1]
     return out
 
 

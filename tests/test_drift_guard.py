@@ -105,7 +105,7 @@ def test_running_sum_and_guard_through_penalised_start():
     chains = wl.make_chains(w)
     pick = [196, 211, 214]
     sub = wl.Workload("sphere-subset", w.lengths[pick], w.nbins, w.n_binders, w.mu[pick], w.chi[pick],
-                      w.eps, w.cross, w.run_length, 1, w.seed, steps_per_round=20,
+                      w.eps, w.cross, w.run_length, 3, w.seed, steps_per_round=20,
                       sphere_radius=w.sphere_radius)
     sim = wl.build_sim(sub, [chains[i] for i in pick], pos_fp64=True)
     try:
@@ -122,9 +122,9 @@ def test_running_sum_and_guard_through_penalised_start():
         drift, checks = sim.drift()
         assert checks == 6
         assert np.all(np.abs(drift) <= 1e-9 * np.maximum(1.0, np.abs(E1)))
-        # a window without penalties: running-sum change == energy change
-        for _ in range(2):
-            sim.run_batched(1, sub.steps_per_round, sub.n_rungs, 9)
+        # a window without penalties (and without chi swaps, which the
+        # running sum of move dE does not see): running-sum change == energy change
+        sim.run(2 * sub.steps_per_round, 10)
         sim.sync()
         e2 = sim.energies()
         d = (e2[:, :3].sum(1) - E1) - (e2[:, 3] - e1[:, 3])

@@ -83,8 +83,9 @@ def _batched_subset():
     return sub, picked
 
 
-def _oracle_for(w, c, rep):
-    """The oracle system holding replica `rep` of workload `w` (chain `c`)."""
+def _oracle_for(w, c, rep, pos="f32"):
+    """The oracle system holding replica `rep` of workload `w` (chain `c`),
+    with the GPU's FP32 storage arithmetic (pos="f32") or FP64 storage."""
     from chromo_gb300 import workloads as wl
     from chromo_gb300.energetics import dss_parameters, field_prefactors
     from oracle.oracle import OracleSystem
@@ -99,7 +100,7 @@ def _oracle_for(w, c, rep):
                      mu_adjust_factor=1.0, max_binders=-1, field_kind=2, confine_kind=0,
                      nxyz=(w.nbins,) * 3, widths=(width,) * 3, chi=float(w.chi[rep]), vf_limit=0.5,
                      bead_vol=4.0 / 3.0 * np.pi * wl.BEAD_RAD ** 3, pref=np.asarray(pref),
-                     intra=np.asarray(intra), xpref=np.asarray(xpref), pos="f32", fixed_density=1)
+                     intra=np.asarray(intra), xpref=np.asarray(xpref), pos=pos, fixed_density=1)
     o.deposit_all()
     return o
 
@@ -252,4 +253,36 @@ def test_vf_limit_decisions_identical_without_following():
     huge = np.abs(_dE(orecs)) > 1e80
     print(f"vf_limit: {len(log)} moves, {int(huge.sum())} decided by the 1e99 penalty")
     assert huge.any()
+    sim.close()
+
+
+# ------------------------------------------------------------ FP64 storage
+
+def test_small_configuration_fp64_matches_oracle():
+    """The CPU-runnable configuration (1,000 beads, 30^3 grid, one binder,
+    FP64 storage, specific_moves: one attempt of each move kind per MC step,
+    SimpleControl) on the production kernel at the library's launch shape:
+    2,000 MC steps (10,000 moves) move by move against the oracle's FP64
+    replay of the same Philox sub-streams.  FP64 arithmetic on both sides:
+    dE within 1e-9 (the GPU adds a move's bead and voxel terms in another
+    order), decisions identical, final chain, states, grid and controllers
+    bit-identical."""
+    from chromo_gb300 import workloads as wl
+    from oracle.oracle import make_ctl
+    w = wl.make_workload("small")
+    chains = wl.make_chains(w)
+    sim = wl.build_sim(w, chains)
+    assert w.pos_fp64 and sim.pos_fp64
+    o = _oracle_for(w, chains[0], 0, pos="f64")
+    n = int(w.lengths[0])
+    bead, move = wl.amplitude_bounds(n)
+    ctl_o = [make_ctl(m, amp_move=move[m][0], amp_bead=int(bead[m][0]), num_per_cycle=1,
+                      bead_bounds=bead[m], move_bounds=move[m]) for m in MOVE_NAMES]
+    steps = 2000
+    log = sim.run_logged(steps, SEED + 13, steps * 5 + 10)[0]
+    orecs, _, ties = o.mc_sim_philox(ctl_o, steps, SEED + 13, 0, 0, follow=log["accepted"])
+    assert np.all(np.bincount(log["kind"], minlength=5) == steps)
+    worst = compare_records(log, orecs, tol=1e-9, label="small fp64")
+    compare_state(sim, 0, o, sim.get_controllers(0), ctl_o, label="small fp64")
+    print(f"small fp64: {len(log)} moves, worst dE error {worst:.3e}, {ties} tie-band")
     sim.close()

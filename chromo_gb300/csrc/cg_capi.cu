@@ -5,6 +5,7 @@
 // states, int64 fixed-point grid), sizes the per-warp shared-memory region
 // and launches the kernels of cg_mc.cu.
 #include <cuda_runtime.h>
+#include <cstdlib>
 
 #include <algorithm>
 #include <cmath>
@@ -157,6 +158,12 @@ struct cg_sim {
   // pinned host staging for chain uploads / downloads
   void* pinned = nullptr;
   size_t pinned_bytes = 0;
+  // direct host access (cudaDevAttrPageableMemoryAccess): cg_set_chains /
+  // cg_get_chains read and write the caller's arrays from the GPU; the
+  // replica table of host pointers and the upload check flag live here
+  int direct_host = 0;
+  void* hio_tab = nullptr;
+  unsigned* hio_flag = nullptr;
 
   unsigned char* staging(size_t bytes) {
     if (bytes > pinned_bytes) {
@@ -288,6 +295,8 @@ void cg_destroy(cg_sim* s) {
   if (s->pinned) cudaFreeHost(s->pinned);
   if (s->twist) cudaFree(s->twist);
   if (s->steric_work) cudaFree(s->steric_work);
+  if (s->hio_tab) cudaFree(s->hio_tab);
+  if (s->hio_flag) cudaFree(s->hio_flag);
   void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
                   s->bonds32, s->grid, s->access_vol, s->access_sc, s->access_vb, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
                   s->picked, s->d_picked_off, s->eout, s->aout, s->rep_of_rung, s->swaps,
@@ -333,7 +342,10 @@ static int choose_shape(cg_sim* s, int w_req, int g_req) {
   if (ctas_per_sm > reg_ctas) ctas_per_sm = reg_ctas;
   const size_t budget = std::min<size_t>(smem_per_sm / ctas_per_sm - 1024, 220 * 1024);
   const int lhb = 10;
-  const long long sc = G == 32 ? 48 : 32;
+#ifndef CG_STAGE_BEADS
+#define CG_STAGE_BEADS 48
+#endif
+  const long long sc = G == 32 ? CG_STAGE_BEADS : 32;
   // FP32 storage: the position moves of a batch share one pooled voxel table
   // (keys voxel * 32 + slot: grids below 2^26 voxels), as large as fits (up
   // to 4,096 entries); the slots keep 64-entry tables for binding moves
@@ -455,6 +467,17 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   ALLOC(s->nbound, 8 * s->R);
   ALLOC(s->mu_swaps, 8 * s->R);
   ALLOC(s->mu_swap_attempts, 8 * s->R);
+  {
+    // chains move between the caller's arrays and the device in one kernel
+    // pass where the GPU can address pageable host memory (Grace-Blackwell
+    // NVLink-C2C); CHROMO_GB300_STAGED_HOST_IO=1 keeps the staged path
+    int pageable = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+    const char* env = std::getenv("CHROMO_GB300_STAGED_HOST_IO");
+    s->direct_host = pageable == 1 && s->R <= 65535 && !(env && env[0] == '1');
+  }
+  if (s->direct_host) ALLOC(s->hio_tab, 4 * sizeof(void*) * s->R);
+  if (s->direct_host) ALLOC(s->hio_flag, sizeof(unsigned));
 #undef ALLOC
   if (e != cudaSuccess) {
     cg_destroy(s);
@@ -656,9 +679,37 @@ int cg_get_chain(cg_sim* s, int rep, double* r, double* t3, double* t2, int64_t*
   return CG_OK;
 }
 
+// The replica table of host pointers for the direct-access kernels.
+static int put_host_table(cg_sim* s, const double* const* r, const double* const* t3, const double* const* t2,
+                          const int64_t* const* states) {
+  std::vector<const void*> tab(4 * (size_t)s->R, nullptr);
+  for (int rep = 0; rep < s->R; rep++) {
+    tab[4 * rep] = r ? r[rep] : nullptr;
+    tab[4 * rep + 1] = t3 ? t3[rep] : nullptr;
+    tab[4 * rep + 2] = t2 ? t2[rep] : nullptr;
+    tab[4 * rep + 3] = states ? states[rep] : nullptr;
+  }
+  CUDA_TRY(cudaMemcpy(s->hio_tab, tab.data(), tab.size() * sizeof(void*), cudaMemcpyHostToDevice));
+  return CG_OK;
+}
+
 int cg_set_chains(cg_sim* s, const double* const* r, const double* const* t3, const double* const* t2,
                   const int64_t* const* states) {
   if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (s->direct_host) {
+    if (int rc = put_host_table(s, r, t3, t2, states)) return rc;
+    CUDA_TRY(cudaMemset(s->hio_flag, 0, sizeof(unsigned)));
+    cg_launch_host_load(s->args(), s->fp64 != 0, s->hio_tab, s->R, s->max_beads, s->nb, s->hio_flag, 0, 0);
+    CUDA_TRY(cudaGetLastError());
+    unsigned bad = 0;
+    CUDA_TRY(cudaMemcpy(&bad, s->hio_flag, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (bad & 1u) return fail(CG_ERR_NONFINITE, "non-finite position or tangent");
+    if (bad & 2u) return fail(CG_ERR_ARG, "binding states must be in 0..3");
+    cg_launch_host_load(s->args(), s->fp64 != 0, s->hio_tab, s->R, s->max_beads, s->nb, s->hio_flag, 1, 0);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(0));
+    return CG_OK;
+  }
   const long long N = s->total_beads;
   const size_t pb = s->pos_bytes();
   unsigned char* buf = s->staging(pb * N * 3 + 4 * N);
@@ -723,6 +774,15 @@ int cg_set_chains(cg_sim* s, const double* const* r, const double* const* t3, co
 
 int cg_get_chains(cg_sim* s, double* const* r, double* const* t3, double* const* t2, int64_t* const* states) {
   if (!s) return fail(CG_ERR_ARG, "null sim");
+  if (s->direct_host) {
+    if (int rc = put_host_table(s, (const double* const*)r, (const double* const*)t3, (const double* const*)t2,
+                                (const int64_t* const*)states))
+      return rc;
+    cg_launch_host_store(s->args(), s->fp64 != 0, s->hio_tab, s->R, s->max_beads, s->nb, 0);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(0));
+    return CG_OK;
+  }
   const long long N = s->total_beads;
   const size_t pb = s->pos_bytes();
   unsigned char* buf = s->staging(pb * N * 3 + 4 * N);

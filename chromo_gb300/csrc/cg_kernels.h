@@ -182,6 +182,10 @@ constexpr int kAccPerRep = kTerms + kTerms * kTerms + 1;  // running sums of T, 
 void cg_launch_gradient(const cg::KArgs& a, bool fp64, float* out, long long max_beads, cudaStream_t s);
 void cg_launch_gradient64(const cg::KArgs& a, bool fp64, double* out, double* out_t3, long long max_beads,
                           cudaStream_t s);
+void cg_launch_host_load(const cg::KArgs& a, bool fp64, const void* tab, int R, long long max_beads, int nb,
+                         unsigned* flag, int mode, cudaStream_t s);
+void cg_launch_host_store(const cg::KArgs& a, bool fp64, const void* tab, int R, long long max_beads, int nb,
+                          cudaStream_t s);
 void cg_launch_store_chains(const cg::KArgs& a, bool fp64, long long total, const double* r, const double* t3,
                             cudaStream_t s);
 void cg_launch_terms(const cg::KArgs& a, double* terms, double* acc, cudaStream_t s);

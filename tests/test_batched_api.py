@@ -104,3 +104,59 @@ def test_all_replica_transfers_match_per_replica_calls():
         for r, p in enumerate(polys):
             np.testing.assert_array_equal(again[r][0], p.r.astype(np.float32).astype(np.float64))
             np.testing.assert_array_equal(again[r][3], p.states)
+
+
+@pytest.mark.parametrize("fp64", [False, True])
+def test_chain_transfers_direct_and_staged_agree(fp64, monkeypatch):
+    """cg_set_chains / cg_get_chains read and write the caller's arrays from
+    the GPU where it can address pageable host memory, else through a pinned
+    staging buffer (CHROMO_GB300_STAGED_HOST_IO=1 forces that path).  Both
+    give the same resident state and the same arrays back: every replica, a
+    partial upload (None entries keep the resident values), and a rejected
+    upload (a NaN coordinate, or a state outside 0..3), which changes
+    nothing."""
+    from chromo_gb300 import _native as nat
+    from chromo_gb300 import workloads as wl
+    w = wl.make_workload("batched")
+    pick = [0, 5, 77, 200]
+    sub = wl.Workload("transfer", w.lengths[pick], w.nbins, w.n_binders, w.mu[pick], w.chi[pick], w.eps,
+                      w.cross, w.run_length, 2, w.seed)
+    chains = wl.make_chains(w)
+    chains = [chains[i] for i in pick]
+    rng = np.random.default_rng(3)
+    new = [dict(r=c.r + rng.normal(size=c.r.shape), t3=c.t3, t2=c.t2,
+                states=rng.integers(0, 3, size=c.states.shape)) for c in chains]
+    got = {}
+    for mode in ("direct", "staged"):
+        if mode == "staged":
+            monkeypatch.setenv("CHROMO_GB300_STAGED_HOST_IO", "1")
+        sim = wl.build_sim(sub, chains, pos_fp64=fp64)
+        try:
+            sim.set_chains(new)
+            part = [dict(r=new[0]["r"] * 0.5), {}, dict(states=np.zeros_like(new[2]["states"])), {}]
+            sim.set_chains(part)
+            before = sim.get_chains()
+            bad = [dict(r=new[k]["r"].copy()) for k in range(4)]
+            bad[3]["r"][17, 2] = np.nan
+            with pytest.raises(nat.CgError):
+                sim.set_chains(bad)
+            bad_states = [{}, dict(states=np.full_like(new[1]["states"], 7)), {}, {}]
+            with pytest.raises(nat.CgError):
+                sim.set_chains(bad_states)
+            after = sim.get_chains()
+            for x, y in zip(before, after):
+                for a, b in zip(x, y):
+                    np.testing.assert_array_equal(a, b)
+            got[mode] = after
+        finally:
+            sim.close()
+        monkeypatch.delenv("CHROMO_GB300_STAGED_HOST_IO", raising=False)
+    for x, y in zip(got["direct"], got["staged"]):
+        for a, b in zip(x, y):
+            np.testing.assert_array_equal(a, b)
+    # the values are the uploads rounded to the storage type
+    cast = np.float64 if fp64 else np.float32
+    np.testing.assert_array_equal(got["direct"][0][0], (new[0]["r"] * 0.5).astype(cast).astype(np.float64))
+    np.testing.assert_array_equal(got["direct"][1][0], new[1]["r"].astype(cast).astype(np.float64))
+    np.testing.assert_array_equal(got["direct"][2][3], 0)
+    np.testing.assert_array_equal(got["direct"][3][3], new[3]["states"])

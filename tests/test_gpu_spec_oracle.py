@@ -263,10 +263,13 @@ def test_small_configuration_fp64_matches_oracle():
     FP64 storage, specific_moves: one attempt of each move kind per MC step,
     SimpleControl) on the production kernel at the library's launch shape:
     2,000 MC steps (10,000 moves) move by move against the oracle's FP64
-    replay of the same Philox sub-streams.  FP64 arithmetic on both sides:
-    dE within 1e-9 (the GPU adds a move's bead and voxel terms in another
-    order), decisions identical, final chain, states, grid and controllers
-    bit-identical."""
+    replay of the same Philox sub-streams.  FP64 arithmetic on both sides,
+    but not the same library: the rotation angles' sin / cos are CUDA's on
+    the GPU and the C library's in the oracle, which differ in the last bit
+    now and then, so the chains drift apart at the 1e-12 level.  Checked:
+    segments, draws and decisions identical, dE within 1e-9 relative, states
+    and controllers identical, positions within 1e-9, grid cells within 16
+    fixed-point units (of 2^40 per bead)."""
     from chromo_gb300 import workloads as wl
     from oracle.oracle import make_ctl
     w = wl.make_workload("small")
@@ -283,6 +286,13 @@ def test_small_configuration_fp64_matches_oracle():
     orecs, _, ties = o.mc_sim_philox(ctl_o, steps, SEED + 13, 0, 0, follow=log["accepted"])
     assert np.all(np.bincount(log["kind"], minlength=5) == steps)
     worst = compare_records(log, orecs, tol=1e-9, label="small fp64")
-    compare_state(sim, 0, o, sim.get_controllers(0), ctl_o, label="small fp64")
+    r, t3, t2, st = sim.get_chain(0)
+    for a, b in ((r, o.r), (t3, o.t3), (t2, o.t2)):
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-9)
+    np.testing.assert_array_equal(st, o.states)
+    assert np.abs(sim.density(0) - o.density_fx).max() <= 16
+    for cg_, co in zip(sim.get_controllers(0), ctl_o):
+        for f in ("amp_move", "amp_bead", "acc_rate", "num_attempt", "num_success"):
+            assert getattr(cg_, f) == getattr(co, f), (f, getattr(cg_, f), getattr(co, f))
     print(f"small fp64: {len(log)} moves, worst dE error {worst:.3e}, {ties} tie-band")
     sim.close()

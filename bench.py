@@ -330,7 +330,7 @@ def single_chain_bench(args, rank, world):
         spare = other if k == 0 else inp
         inp = out
     n = int(w.lengths[0])
-    io_bytes = n * (3 * (32 if w.pos_fp64 else 16) + 4)
+    io_bytes = n * ((3 * 24 + 8 * w.n_binders) if sim.direct_transfers() else (3 * (32 if w.pos_fp64 else 16) + 4))
     e2e_value = allreduce_sum(attempts, world) / allreduce_max(t_e2e, world)
     launch = sim.launch_shape()
     sim.close()
@@ -671,8 +671,12 @@ def main():
         spare = other if k == 0 else inp  # the start snapshot is never overwritten
         inp = out
     nbeads = int(w.lengths.sum())
-    h2d = nbeads * (3 * pos_b + 4)
-    d2h = nbeads * (3 * pos_b + 4)
+    direct = sim.direct_transfers()
+    # bytes across the host-device link per step: the caller's FP64 arrays and
+    # int64 states read (written) by the GPU itself, or the packed FP32
+    # 4-vectors and 32-bit state words of the staged path
+    h2d = nbeads * ((3 * 24 + 8 * w.n_binders) if direct else (3 * pos_b + 4))
+    d2h = h2d
     e2e_value = allreduce_sum(moves_round * args.steps, world) / allreduce_max(t_e2e, world)
     mark("e2e")
     # ---- plain single chain (one CTA) on the same kernel, settled for the
@@ -750,8 +754,10 @@ def main():
             "e2e": {"value": e2e_value, "unit": "moves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "path": "C ABI, host-driven rounds: cg_set_chains (the previous round's host "
-                            "snapshot, FP64 -> pinned -> HBM, all replicas), cg_deposit, cg_run_batched, "
-                            "cg_get_chains (into reused host arrays)",
+                            "snapshot, all replicas), cg_deposit, cg_run_batched, cg_get_chains (into "
+                            "reused host arrays); transfers: " +
+                            ("the GPU reads and writes the pageable FP64 host arrays over NVLink-C2C"
+                             if direct else "FP64 -> pinned FP32 staging -> HBM and back"),
                     "ms_per_step": dict(zip(("set_chains", "deposit", "round", "get_chains"),
                                             (round(float(x) * 1e3 / args.steps, 3) for x in e2e_parts)))},
             "plain": {"value": plain_value, "unit": "moves/s",

@@ -82,7 +82,7 @@ EXPORTS = [
     "cg_create", "cg_destroy", "cg_last_error", "cg_set_chain", "cg_get_chain", "cg_set_field",
     "cg_set_binding", "cg_set_controllers", "cg_get_controllers", "cg_deposit", "cg_get_density",
     "cg_run", "cg_sync", "cg_run_audit", "cg_energy", "cg_reset_running_energy", "cg_get_tally",
-    "cg_reset_tally", "cg_exchange", "cg_get_chi", "cg_run_batched", "cg_get_launch_info",
+    "cg_reset_tally", "cg_exchange", "cg_get_chi", "cg_run_batched", "cg_get_launch_info", "cg_get_transfer_mode",
     "cg_field_energy_static", "cg_energies", "cg_set_chains", "cg_get_chains", "cg_gradient",
     "cg_sample_terms", "cg_get_samples", "cg_get_launch_shape", "cg_mc_warps_per_sm",
     "cg_set_mu_ladder", "cg_get_mu", "cg_get_swap_counts", "cg_run_logged", "cg_set_round_timing",
@@ -144,6 +144,7 @@ def lib():
             "cg_get_chi": ([P, P], C.c_int),
             "cg_run_batched": ([P, I64, I64, I32, C.c_uint64, P], C.c_int),
             "cg_get_launch_info": ([P, P, P, P], C.c_int),
+            "cg_get_transfer_mode": ([P, P], C.c_int),
             "cg_get_launch_shape": ([P, P, P, P, P], C.c_int),
             "cg_mc_warps_per_sm": ([I32, I32], C.c_int),
             "cg_set_mu_ladder": ([P, I32, I32], C.c_int),
@@ -472,6 +473,13 @@ class Sim:
         w, g, f, hs = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
         check(lib().cg_get_launch_shape(self.h, C.byref(w), C.byref(g), C.byref(f), C.byref(hs)))
         return w.value, g.value, f.value, hs.value
+
+    def direct_transfers(self) -> bool:
+        """Whether set_chains / get_chains read and write the host arrays from
+        the GPU (pageable host memory addressable over NVLink-C2C)."""
+        d = C.c_int32()
+        check(lib().cg_get_transfer_mode(self.h, C.byref(d)))
+        return bool(d.value)
 
     def launch_info(self):
         w, hs, k = C.c_int32(), C.c_int32(), C.c_int64()

@@ -1479,6 +1479,12 @@ int cg_mc_warps_per_sm(int32_t pos_fp64, int32_t lanes) {
   return cg_spec_warps_per_sm(pos_fp64 != 0, lanes);
 }
 
+int cg_get_transfer_mode(cg_sim* s, int32_t* direct) {
+  if (!s || !direct) return fail(CG_ERR_ARG, "null argument");
+  *direct = s->direct_host;
+  return CG_OK;
+}
+
 int cg_get_launch_info(cg_sim* s, int32_t* wpb, int32_t* hash_slots, int64_t* kernels) {
   if (!s) return fail(CG_ERR_ARG, "null sim");
   if (wpb) *wpb = s->spec_w;

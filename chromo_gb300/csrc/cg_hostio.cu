@@ -25,6 +25,11 @@ struct HostRow {  // one replica's host arrays (NULL: not transferred)
   long long* st;
 };
 
+// The host arrays are walked flat (element j of replica rep's [n x 3] or
+// [n x nb] array on thread j), so every warp reads or writes 32 consecutive
+// 8-byte words of host memory: whole 256-byte lines over the link.  The
+// resident side takes the scattered accesses (HBM / L2).
+//
 // mode 0: check only (flag bit 1: non-finite coordinate, bit 2: state out of
 // range); mode 1: write the resident storage.
 template <typename Pos>
@@ -34,29 +39,28 @@ __global__ void host_load_kernel(KArgs a, const HostRow* tab, int nb, unsigned* 
   const long long n = rd.n_beads, off = rd.bead_off;
   const HostRow row = tab[rep];
   const double* src[3] = {row.r, row.t3, row.t2};
-  V4<Pos>* dst[3] = {reinterpret_cast<V4<Pos>*>(a.r4) + off, reinterpret_cast<V4<Pos>*>(a.t34) + off,
-                     reinterpret_cast<V4<Pos>*>(a.t24) + off};
+  Pos* dst[3] = {reinterpret_cast<Pos*>(reinterpret_cast<V4<Pos>*>(a.r4) + off),
+                 reinterpret_cast<Pos*>(reinterpret_cast<V4<Pos>*>(a.t34) + off),
+                 reinterpret_cast<Pos*>(reinterpret_cast<V4<Pos>*>(a.t24) + off)};
+  const long long stride = (long long)gridDim.x * blockDim.x;
   unsigned bad = 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      if (!src[k]) continue;
-      const double x = src[k][3 * i], y = src[k][3 * i + 1], z = src[k][3 * i + 2];
+  for (int k = 0; k < 3; k++) {
+    if (!src[k]) continue;
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < 3 * n; j += stride) {
+      const double x = src[k][j];
       if (mode == 0) {
-        if (!(isfinite(x) && isfinite(y) && isfinite(z))) bad |= 1u;
+        if (!isfinite(x)) bad |= 1u;
       } else {
-        dst[k][i] = V4<Pos>{(Pos)x, (Pos)y, (Pos)z, (Pos)0};
+        dst[k][4 * (j / 3) + j % 3] = (Pos)x;  // the 4-vector's pad stays 0
       }
     }
-    if (row.st) {
-      unsigned w = 0;
-      for (int b = 0; b < nb; b++) {
-        const long long v = row.st[i * nb + b];
-        if (v < 0 || v > CG_MAX_MARK) bad |= 2u;
-        w |= (unsigned)(v & 0xFF) << (8 * b);
-      }
-      if (mode == 1) a.states[off + i] = w;
+  }
+  if (row.st) {
+    unsigned char* sb = reinterpret_cast<unsigned char*>(a.states + off);
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n * nb; j += stride) {
+      const long long v = row.st[j];
+      if (v < 0 || v > CG_MAX_MARK) bad |= 2u;
+      else if (mode == 1) sb[4 * (j / nb) + j % nb] = (unsigned char)v;  // byte b of bead i's word
     }
   }
   if (bad) atomicOr(flag, bad);
@@ -69,30 +73,26 @@ __global__ void host_store_kernel(KArgs a, const HostRow* tab, int nb) {
   const long long n = rd.n_beads, off = rd.bead_off;
   const HostRow row = tab[rep];
   double* dst[3] = {row.r, row.t3, row.t2};
-  const V4<Pos>* src[3] = {reinterpret_cast<const V4<Pos>*>(a.r4) + off,
-                           reinterpret_cast<const V4<Pos>*>(a.t34) + off,
-                           reinterpret_cast<const V4<Pos>*>(a.t24) + off};
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      if (!dst[k]) continue;
-      const V4<Pos> v = src[k][i];
-      dst[k][3 * i] = (double)v.x;
-      dst[k][3 * i + 1] = (double)v.y;
-      dst[k][3 * i + 2] = (double)v.z;
-    }
-    if (row.st) {
-      const unsigned w = a.states[off + i];
-      for (int b = 0; b < nb; b++) row.st[i * nb + b] = (long long)((w >> (8 * b)) & 0xFF);
-    }
+  const Pos* src[3] = {reinterpret_cast<const Pos*>(reinterpret_cast<const V4<Pos>*>(a.r4) + off),
+                       reinterpret_cast<const Pos*>(reinterpret_cast<const V4<Pos>*>(a.t34) + off),
+                       reinterpret_cast<const Pos*>(reinterpret_cast<const V4<Pos>*>(a.t24) + off)};
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (int k = 0; k < 3; k++) {
+    if (!dst[k]) continue;
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < 3 * n; j += stride)
+      dst[k][j] = (double)src[k][4 * (j / 3) + j % 3];
+  }
+  if (row.st) {
+    const unsigned char* sb = reinterpret_cast<const unsigned char*>(a.states + off);
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n * nb; j += stride)
+      row.st[j] = (long long)sb[4 * (j / nb) + j % nb];
   }
 }
 
 }  // namespace cg
 
 static dim3 hostio_grid(int R, long long max_beads) {
-  long long bx = (max_beads + 255) / 256;
+  long long bx = (3 * max_beads + 255) / 256;
   if (bx > 64) bx = 64;
   if (bx < 1) bx = 1;
   return dim3((unsigned)bx, (unsigned)R);

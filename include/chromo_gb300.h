@@ -129,13 +129,22 @@ int cg_get_chain(cg_sim *sim, int32_t rep, double *r, double *t3, double *t2, in
 /* cg_set_chain / cg_get_chain for every replica in one call: r[rep], t3[rep],
  * t2[rep] point to replica rep's [N_rep*3] arrays and states[rep] to its
  * [N_rep*n_binders] array (a NULL array list, or a NULL entry, skips that
- * array or replica).  The host-side conversion runs on several threads and
- * each array crosses the bus in one copy; this is how a batch of chains is
- * moved between the reference's per-polymer numpy arrays and the device. */
+ * array or replica).  Where the GPU can address pageable host memory
+ * (cudaDevAttrPageableMemoryAccess: Grace-Blackwell NVLink-C2C) one kernel
+ * reads or writes the caller's arrays directly (uploads checked in a first
+ * pass, so a rejected one changes nothing); elsewhere, or with the
+ * environment variable CHROMO_GB300_STAGED_HOST_IO=1 at cg_create, the
+ * host-side conversion runs on several threads into a pinned buffer and each
+ * array crosses the bus in one copy.  This is how a batch of chains is moved
+ * between the reference's per-polymer numpy arrays and the device. */
 int cg_set_chains(cg_sim *sim, const double *const *r, const double *const *t3,
                   const double *const *t2, const int64_t *const *states);
 int cg_get_chains(cg_sim *sim, double *const *r, double *const *t3, double *const *t2,
                   int64_t *const *states);
+/* *direct = 1 when cg_set_chains / cg_get_chains access the host arrays from
+ * the GPU, 0 when they stage through pinned memory (no counterpart in the
+ * reference, which has no device). */
+int cg_get_transfer_mode(cg_sim *sim, int32_t *direct);
 
 /* SSTWLC twist for replica rep (chromo/polymers.pyx:1889-2320): per bond
  * i -> i+1 (N - 1 each) the twist modulus eps_twist = lt / bead_length and the

@@ -342,10 +342,7 @@ static int choose_shape(cg_sim* s, int w_req, int g_req) {
   if (ctas_per_sm > reg_ctas) ctas_per_sm = reg_ctas;
   const size_t budget = std::min<size_t>(smem_per_sm / ctas_per_sm - 1024, 220 * 1024);
   const int lhb = 10;
-#ifndef CG_STAGE_BEADS
-#define CG_STAGE_BEADS 48
-#endif
-  const long long sc = G == 32 ? CG_STAGE_BEADS : 32;
+  const long long sc = G == 32 ? 48 : 32;
   // FP32 storage: the position moves of a batch share one pooled voxel table
   // (keys voxel * 32 + slot: grids below 2^26 voxels), as large as fits (up
   // to 4,096 entries); the slots keep 64-entry tables for binding moves

@@ -1123,11 +1123,8 @@ __device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int s, int gl, 
 
 // 168 registers: two CTAs of 6 warps fit one SM's register file (measured
 // faster than 128 registers with 8 warps, which spills).
-#ifndef CG_SPEC_MAXNREG
-#define CG_SPEC_MAXNREG 168
-#endif
 template <typename Pos, int G>
-__global__ void __maxnreg__(CG_SPEC_MAXNREG) spec_kernel(KArgs a) {
+__global__ void __maxnreg__(168) spec_kernel(KArgs a) {
   extern __shared__ __align__(32) unsigned char smem[];
   constexpr int GPW = 32 / G;  // move groups per warp
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;

@@ -74,7 +74,6 @@ class Config(C.Structure):
         ("warps_per_block", C.c_int32), ("n_beads", C.POINTER(C.c_int64)),
         ("grid_dims", C.POINTER(C.c_int32)), ("max_segment", C.c_int64),
         ("max_tangent", C.c_int64), ("nonuniform_access", C.c_int32), ("lanes_per_move", C.c_int32),
-        ("ctas_per_replica", C.c_int32),
     ]
 
 
@@ -191,8 +190,7 @@ class Sim:
     """Owner of one cg_sim handle (R replicas resident on the GPU)."""
 
     def __init__(self, n_beads, grid_dims, n_binders, *, pos_fp64=False, max_segment=152,
-                 max_tangent=1, warps_per_block=0, nonuniform_access=False, lanes_per_move=0,
-                 ctas_per_replica=0):
+                 max_tangent=1, warps_per_block=0, nonuniform_access=False, lanes_per_move=0):
         L = lib()
         self.n_beads = np.ascontiguousarray(n_beads, dtype=np.int64)
         self.grid_dims = np.ascontiguousarray(grid_dims, dtype=np.int32).reshape(-1, 3)
@@ -212,8 +210,6 @@ class Sim:
         cfg.max_tangent = int(max_tangent)
         cfg.nonuniform_access = int(bool(nonuniform_access))
         cfg.lanes_per_move = int(lanes_per_move)
-        cfg.ctas_per_replica = int(ctas_per_replica)
-        self.ctas_per_replica = max(1, int(ctas_per_replica))
         h = C.c_void_p()
         check(L.cg_create(C.byref(cfg), C.byref(h)))
         self.h = h

@@ -16,7 +16,6 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_lib"
 LIB = OUT / "libchromo_gb300.so"
 SOURCES = ["cg_mc.cu", "cg_spec.cu", "cg_spec_f8.cu", "cg_spec_f16.cu", "cg_spec_f32.cu", "cg_spec_d32.cu",
-           "cg_spec_c32.cu",
            "cg_capi.cu", "cg_static.cu", "cg_grad.cu", "cg_guard.cu", "cg_steric.cu", "cg_hostio.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",

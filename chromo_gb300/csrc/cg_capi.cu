@@ -90,7 +90,6 @@ struct cg_sim {
   int logH = 0, warp_smem = 0, off_draws = 0, off_keys = 0, off_used = 0, off_bslot = 0, off_vals = 0, off_stage = 0,
       off_idx = 0;
   int spec_w = 1, spec_g = 32, spec_s = 1, spec_logHB = 11, spec_off_bkeys = 0, spec_off_bmask = 0, spec_off_warps = 0;
-  int spec_c = 1;  // CTAs per replica (a thread-block cluster when > 1)
   int pool_on = 0, pool_logH = 0, off_pkeys = 0, off_pused = 0, off_pvals = 0;
   long long stage_cap = 0;
   size_t spec_bytes = 0;
@@ -196,7 +195,6 @@ struct cg_sim {
     a.off_idx = off_idx; a.off_bslot = off_bslot;
     a.spec_w = spec_w; a.spec_g = spec_g; a.spec_s = spec_s; a.spec_logHB = spec_logHB; a.spec_off_bkeys = spec_off_bkeys;
     a.spec_off_bmask = spec_off_bmask; a.spec_off_warps = spec_off_warps;
-    a.spec_c = spec_c; a.spec_st = spec_c * spec_s;
     a.pool_on = pool_on; a.pool_logH = pool_logH; a.off_pkeys = off_pkeys; a.off_pused = off_pused;
     a.off_pvals = off_pvals;
     a.rep_of_rung = rep_of_rung; a.swaps = swaps; a.swap_attempts = swap_attempts;
@@ -321,9 +319,9 @@ static int default_lanes(const cg_sim* s, int g_req) {
 // resident at once (ceil(R / SMs) CTAs per SM, W warps each, within the
 // register file), and at most 32 moves in flight.
 static int default_warps(const cg_sim* s, int G) {
-  const long long ctas = ((long long)s->R * s->spec_c + s->n_sm - 1) / std::max(1, s->n_sm);
+  const long long ctas = (s->R + s->n_sm - 1) / std::max(1, s->n_sm);
   const long long W = cg_spec_warps_per_sm(s->fp64 != 0, G) / std::max(1LL, ctas);
-  const long long wmax = std::min<long long>(cg::kMaxW, cg::kMaxS / (32 / G) / s->spec_c);
+  const long long wmax = std::min<long long>(cg::kMaxW, cg::kMaxS / (32 / G));
   return (int)std::min<long long>(wmax, std::max<long long>(1, W));
 }
 
@@ -334,18 +332,16 @@ static int choose_shape(cg_sim* s, int w_req, int g_req) {
   // in waves) -- share the SM's shared memory; each move slot gets the
   // largest voxel table that then fits.
   const size_t smem_per_sm = 227 * 1024;
-  long long ctas_per_sm = ((long long)s->R * s->spec_c + s->n_sm - 1) / std::max(1, s->n_sm);
+  long long ctas_per_sm = (s->R + s->n_sm - 1) / std::max(1, s->n_sm);
   if (ctas_per_sm < 1) ctas_per_sm = 1;
   const int G = default_lanes(s, g_req);
   int W = w_req > 0 ? w_req : default_warps(s, G);
   if (W > cg::kMaxW) W = cg::kMaxW;
-  if (W * (32 / G) * s->spec_c > cg::kMaxS) W = cg::kMaxS / (32 / G) / s->spec_c;
+  if (W * (32 / G) > cg::kMaxS) W = cg::kMaxS / (32 / G);
   const long long reg_ctas = std::max(1, cg_spec_warps_per_sm(s->fp64 != 0, G) / W);
   if (ctas_per_sm > reg_ctas) ctas_per_sm = reg_ctas;
   const size_t budget = std::min<size_t>(smem_per_sm / ctas_per_sm - 1024, 220 * 1024);
-  // the batch's voxel table: 1,024 entries, 4,096 for a batch spread over a
-  // cluster (up to 32 moves of ~50 voxels each)
-  const int lhb = s->spec_c > 1 ? 12 : 10;
+  const int lhb = 10;
   const long long sc = G == 32 ? 48 : 32;
   // FP32 storage: the position moves of a batch share one pooled voxel table
   // (keys voxel * 32 + slot: grids below 2^26 voxels), as large as fits (up
@@ -367,7 +363,7 @@ static int choose_shape(cg_sim* s, int w_req, int g_req) {
   s->layout(lh, sc);
   s->spec_bytes = s->cta_layout(lhb, W, G, lhp);
   s->wpb = 1;
-  cudaError_t e = cg_set_spec_smem(s->fp64 != 0, G, (int)s->spec_bytes, s->spec_c > 1);
+  cudaError_t e = cg_set_spec_smem(s->fp64 != 0, G, (int)s->spec_bytes);
   if (e == cudaSuccess) e = cg_set_mc_smem(s->fp64 != 0, (int)(s->spec_off_warps + s->warp_smem));
   if (e != cudaSuccess) return fail(CG_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
   return CG_OK;
@@ -420,31 +416,19 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
     return fail(CG_ERR_ARG, "warps_per_block must be in 0..12");
   }
   {
-    const int C = cfg->ctas_per_replica;
-    if (C != 0 && C != 1 && C != 2 && C != 4) {
-      cg_destroy(s);
-      return fail(CG_ERR_ARG, "ctas_per_replica must be 0, 1, 2 or 4");
-    }
-    if (C > 1 && (s->fp64 || (cfg->lanes_per_move != 0 && cfg->lanes_per_move != 32))) {
-      cg_destroy(s);
-      return fail(CG_ERR_ARG, "a replica on several CTAs needs FP32 storage and 32 lanes per move");
-    }
-    s->spec_c = C > 1 ? C : 1;
-  }
-  {
     const int G = default_lanes(s, cfg->lanes_per_move);
     int W = cfg->warps_per_block > 0 ? cfg->warps_per_block : default_warps(s, G);
-    if (W * (32 / G) * s->spec_c > cg::kMaxS) W = cg::kMaxS / (32 / G) / s->spec_c;
+    if (W * (32 / G) > cg::kMaxS) W = cg::kMaxS / (32 / G);
     s->spec_w = W;
     s->spec_g = G;
     s->spec_s = W * (32 / G);
   }
-  const long long RW = (long long)s->R * s->spec_c * s->spec_s;
-  // tangent-rotation bitmaps: one per (replica, batch slot)
+  const long long RW = (long long)s->R * s->spec_s;
+  // tangent-rotation bitmaps: one per (replica, move slot)
   s->total_picked = 0;
   for (int r = 0; r < s->R; r++) {
     s->picked_off[r] = s->total_picked;
-    s->total_picked += (long long)s->spec_c * s->spec_s * ((s->n_beads[r] + 31) / 32);
+    s->total_picked += (long long)s->spec_s * ((s->n_beads[r] + 31) / 32);
   }
   auto M = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes == 0 ? 16 : bytes); };
   cudaError_t e = cudaSuccess;
@@ -543,10 +527,6 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
   if (e != cudaSuccess) { cg_destroy(s); return fail(CG_ERR_CUDA, cudaGetErrorString(e)); }
   int rc = choose_shape(s, s->spec_w, s->spec_g);
   if (rc) { cg_destroy(s); return rc; }
-  if (s->spec_c > 1 && cg_spec_max_clusters(s->args(), s->spec_bytes) < 1) {
-    cg_destroy(s);
-    return fail(CG_ERR_ARG, "no cluster of this many CTAs with this shared-memory layout fits the GPU");
-  }
   *out = s;
   return CG_OK;
 }
@@ -955,7 +935,7 @@ static int device_errors(cg_sim* s) {
   for (int r = 0; r < s->R; r++) rd[r].err = 0;
   cudaMemcpy(s->reps, rd.data(), sizeof(RepDev) * s->R, cudaMemcpyHostToDevice);
   const long long Hg = 1LL << s->g_logH;
-  const long long RW = (long long)s->R * s->spec_c * s->spec_s;
+  const long long RW = (long long)s->R * s->spec_s;
   cudaMemset(s->g_keys, 0xFF, 4 * Hg * RW);
   cudaMemset(s->g_bslot, 0xFF, 4 * Hg * RW);
   cudaMemset(s->g_vals, 0, 8 * Hg * (s->nb + 1) * RW);
@@ -1486,7 +1466,7 @@ int cg_get_launch_shape(cg_sim* s, int32_t* wpb, int32_t* lanes, int32_t* in_fli
   if (!s) return fail(CG_ERR_ARG, "null sim");
   if (wpb) *wpb = s->spec_w;
   if (lanes) *lanes = s->spec_g;
-  if (in_flight) *in_flight = s->spec_c * s->spec_s;
+  if (in_flight) *in_flight = s->spec_s;
   if (hash_slots) *hash_slots = s->pool_on ? 1 << s->pool_logH : 1 << s->logH;
   return CG_OK;
 }

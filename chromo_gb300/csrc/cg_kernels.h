@@ -115,10 +115,6 @@ struct KArgs {
   // CTA layout: header, block voxel table, then one region per move slot;
   // spec_w warps of 32 / spec_g groups, spec_s = spec_w * 32 / spec_g slots
   int spec_w, spec_g, spec_s, spec_logHB, spec_off_bkeys, spec_off_bmask, spec_off_warps;
-  // CTAs per replica (a thread-block cluster when > 1) and move slots per
-  // replica, spec_st = spec_c * spec_s: the global scratch is per (replica,
-  // batch slot)
-  int spec_c, spec_st;
   // pooled voxel table of the CTA (FP32 storage): 2^pool_logH entries keyed by
   // voxel * 32 + move slot, shared by the position moves of a batch
   int pool_on, pool_logH, off_pkeys, off_pused, off_pvals;
@@ -168,9 +164,7 @@ void cg_launch_steric(const cg::KArgs& a, bool fp64, int rep, long long n_rows, 
                       const double* trial, double e, double V0, double* rows, double* out, cudaStream_t s);
 void cg_launch_mc(const cg::KArgs& a, bool fp64, bool audit, cudaStream_t s);
 void cg_launch_spec(const cg::KArgs& a, bool fp64, size_t smem_bytes, cudaStream_t s);
-cudaError_t cg_set_spec_smem(bool fp64, int lanes_per_move, int bytes, bool cluster = false);
-// clusters of a.spec_c CTAs that can be resident at once (-1: query failed)
-int cg_spec_max_clusters(const cg::KArgs& a, size_t smem_bytes);
+cudaError_t cg_set_spec_smem(bool fp64, int lanes_per_move, int bytes);
 // whether an MC kernel is built for (storage, lanes per move)
 bool cg_spec_shape_ok(bool fp64, int lanes_per_move);
 cudaError_t cg_set_mc_smem(bool fp64, int bytes);

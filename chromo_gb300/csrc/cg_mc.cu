@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(128, 1) mc_kernel(KArgs a) {
   const double* bonds = a.bonds + rd.bead_off * 6;
   const float* bonds32 = a.bonds32 + rd.bead_off * 8;
   // per-replica global scratch (used when a move is too large for shared memory)
-  const long long gi = (long long)rep * a.spec_st;  // the replica's first move-slot region
+  const long long gi = (long long)rep * a.spec_s;  // the replica's first move-slot region
   int* g_keys = a.g_keys + gi * (1 << a.g_logH);
   int* g_used = a.g_used + gi * (1 << a.g_logH);
   long long* g_vals = a.g_vals + gi * (1 << a.g_logH) * ncol;

@@ -10,9 +10,6 @@ void cg_launch_spec_f8(const cg::KArgs& a, size_t smem, cudaStream_t s);
 void cg_launch_spec_f16(const cg::KArgs& a, size_t smem, cudaStream_t s);
 void cg_launch_spec_f32(const cg::KArgs& a, size_t smem, cudaStream_t s);
 void cg_launch_spec_d32(const cg::KArgs& a, size_t smem, cudaStream_t s);
-cudaError_t cg_launch_spec_c32(const cg::KArgs& a, size_t smem, cudaStream_t s);
-cudaError_t cg_spec_smem_c32(int bytes);
-int cg_spec_max_clusters_c32(const cg::KArgs& a, size_t smem);
 cudaError_t cg_spec_smem_f8(int bytes);
 cudaError_t cg_spec_smem_f16(int bytes);
 cudaError_t cg_spec_smem_f32(int bytes);
@@ -25,11 +22,7 @@ int cg_spec_regs_d32();
 bool cg_spec_shape_ok(bool fp64, int g) { return fp64 ? g == 32 : (g == 8 || g == 16 || g == 32); }
 
 void cg_launch_spec(const cg::KArgs& a, bool fp64, size_t smem_bytes, cudaStream_t s) {
-  // the cluster form exists for FP32 storage with 32 lanes per move (the
-  // library refuses other cluster shapes); a launch error is left for the
-  // caller's cudaGetLastError
-  if (a.spec_c > 1) (void)cg_launch_spec_c32(a, smem_bytes, s);
-  else if (fp64) cg_launch_spec_d32(a, smem_bytes, s);
+  if (fp64) cg_launch_spec_d32(a, smem_bytes, s);
   else if (a.spec_g == 8) cg_launch_spec_f8(a, smem_bytes, s);
   else if (a.spec_g == 16) cg_launch_spec_f16(a, smem_bytes, s);
   else cg_launch_spec_f32(a, smem_bytes, s);
@@ -42,19 +35,18 @@ void cg_launch_spec(const cg::KArgs& a, bool fp64, size_t smem_bytes, cudaStream
 namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_smem_mu;
-int g_spec_smem[kMaxDevices][5];
+int g_spec_smem[kMaxDevices][4];
 }  // namespace
 
-cudaError_t cg_set_spec_smem(bool fp64, int g, int bytes, bool cluster) {
-  const int k = cluster ? 4 : fp64 ? 3 : g == 8 ? 0 : g == 16 ? 1 : 2;
+cudaError_t cg_set_spec_smem(bool fp64, int g, int bytes) {
+  const int k = fp64 ? 3 : g == 8 ? 0 : g == 16 ? 1 : 2;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lock(g_smem_mu);
   int* cur = dev >= 0 && dev < kMaxDevices ? &g_spec_smem[dev][k] : nullptr;
   if (cur && bytes <= *cur) return cudaSuccess;
-  if (cluster) e = cg_spec_smem_c32(bytes);
-  else if (fp64) e = cg_spec_smem_d32(bytes);
+  if (fp64) e = cg_spec_smem_d32(bytes);
   else if (g == 8) e = cg_spec_smem_f8(bytes);
   else if (g == 16) e = cg_spec_smem_f16(bytes);
   else e = cg_spec_smem_f32(bytes);
@@ -68,8 +60,4 @@ int cg_spec_warps_per_sm(bool fp64, int g) {
   if (regs <= 0) return cg::kMaxW;
   const int per_warp = (regs * 32 + 255) / 256 * 256;  // allocation unit: 256 registers
   return 65536 / per_warp;
-}
-
-int cg_spec_max_clusters(const cg::KArgs& a, size_t smem_bytes) {
-  return a.spec_c > 1 ? cg_spec_max_clusters_c32(a, smem_bytes) : -1;
 }

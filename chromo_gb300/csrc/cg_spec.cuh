@@ -34,7 +34,6 @@
 // executed by the whole warp with per-group masks, so groups may diverge only
 // in code without collectives.
 #pragma once
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "cg_device.cuh"
@@ -42,38 +41,6 @@
 #include "cg_move.cuh"
 
 namespace cg {
-
-// A replica on a thread-block cluster of spec_c CTAs (one SM each), for
-// workloads with fewer replicas than SMs: the batch then holds spec_c *
-// spec_s moves, batch slot g = rank * spec_s + s in the CTA of that rank.
-// Each CTA proposes, deposits and evaluates its own moves in its own shared
-// memory; the moves' plans and the batch's voxel -> move-bitmask table (in the
-// rank-0 CTA) are shared through distributed shared memory, and every CTA
-// resolves the batch and keeps the books from all plans, so all ranks take
-// the same decisions and the result is still the one-move-at-a-time one.
-template <bool CL>
-__device__ __forceinline__ int cta_rank() {
-  if constexpr (CL) return (int)cooperative_groups::this_cluster().block_rank();
-  else return 0;
-}
-template <bool CL, typename T>
-__device__ __forceinline__ T* in_rank(T* p, int rank) {
-  if constexpr (CL) return cooperative_groups::this_cluster().map_shared_rank(p, (unsigned)rank);
-  else return p;
-}
-// The batch-wide barrier: the cluster's (release / acquire at cluster scope,
-// so global-memory commits of one rank are seen by the others) or the CTA's.
-template <bool CL>
-__device__ __forceinline__ void batch_sync() {
-  if constexpr (CL) cooperative_groups::this_cluster().sync();
-  else __syncthreads();
-}
-// The plan of batch slot g (S move slots per CTA).
-template <bool CL>
-__device__ __forceinline__ MovePlan& plan_at(SpecShared& sh, int g, int S) {
-  if constexpr (CL) return *in_rank<CL>(&sh.plan[g % S], g / S);
-  else return sh.plan[g];
-}
 
 // Draw j (>= kDrawCache) of a move's sub-stream: word j & 3 of Philox block
 // j >> 2.  Out of line: few moves draw this many numbers, and inlined at every
@@ -312,7 +279,7 @@ template <> __device__ __forceinline__ double load_acc<double>(long long, double
 // error bits go to the move's plan.  A move whose optimistic table overflows
 // (E_OVF: a pool or a table past 3/4 load) is skipped from then on; its
 // group deposits it again in its global table.  Called by every thread.
-template <typename Pos, bool CL>
+template <typename Pos>
 __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, int kind) {
   using Acc = typename AccOf<Pos>::type;
   unsigned char* smem = reinterpret_cast<unsigned char*>(&sh);
@@ -355,8 +322,7 @@ __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, in
       for (int i = 0; i < 3; i++)
         for (int j = 0; j < 4; j++) M[i][j] = Mp[4 * i + j];
       V4<Pos>* stage = P.gstage ? reinterpret_cast<V4<Pos>*>(a.g_stage) +
-                                      ((long long)rep * a.spec_st + cta_rank<CL>() * a.spec_s + s) *
-                                          a.g_stage_cap * 3
+                                      ((long long)rep * a.spec_s + s) * a.g_stage_cap * 3
                                 : reinterpret_cast<V4<Pos>*>(wb + a.off_stage);
       bool left, right;
       Acc pterm;
@@ -405,9 +371,8 @@ __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, in
 // per warp and move), so the sum does not depend on which thread took which
 // voxel.  Entries of moves that overflowed the pool are skipped (their
 // groups redo them in their global tables).  Called by every thread.
-template <bool CL>
 static __device__ void block_field_pool(const KArgs& a, SpecShared& sh, unsigned char* smem, int* bkeys,
-                                        unsigned* bmask) {
+                                 unsigned* bmask) {
   const WarpShared& ws = sh.ws;
   const RepDev& rd = ws.rd;
   const int* pkeys = reinterpret_cast<const int*>(smem + a.off_pkeys);
@@ -416,7 +381,6 @@ static __device__ void block_field_pool(const KArgs& a, SpecShared& sh, unsigned
   const long long* grid = a.grid + rd.vox_off * a.ncol;
   const int n = sh.npool;
   const int lane = (int)(threadIdx.x & 31u);
-  const int gbase = cta_rank<CL>() * a.spec_s;  // batch slot of this CTA's move slot 0
   for (int e0 = (int)(threadIdx.x & ~31u); e0 < n; e0 += (int)blockDim.x) {
     const int e = e0 + lane;
     int s = -1;
@@ -436,12 +400,11 @@ static __device__ void block_field_pool(const KArgs& a, SpecShared& sh, unsigned
         if (b < 0) {
           atomicOr(&P.freg, 1);
         } else {
-          const int gs = gbase + s;
-          const unsigned prior = atomicOr(&bmask[b], 1u << gs);
-          const unsigned below = (1u << gs) - 1u, above = ~((2u << gs) - 1u);
+          const unsigned prior = atomicOr(&bmask[b], 1u << s);
+          const unsigned below = (1u << s) - 1u, above = ~((2u << s) - 1u);
           if (prior & below) atomicOr(&P.cmask, prior & below);
           for (unsigned later = prior & above; later; later &= later - 1)
-            atomicOr(&plan_at<CL>(sh, __ffs((int)later) - 1, a.spec_s).cmask, 1u << gs);
+            atomicOr(&sh.plan[__ffs((int)later) - 1].cmask, 1u << s);
         }
         if (!is_zero64(part.hard)) atomicAdd(&P.fh, part.hard);
         if (hp) atomicAdd(reinterpret_cast<unsigned long long*>(&P.fH), (unsigned long long)hp);
@@ -473,22 +436,20 @@ static __device__ void block_field_pool(const KArgs& a, SpecShared& sh, unsigned
 // the post-move rows of the standing accepted moves (the first `cut`, bits of
 // `acc`) go to the grid with 16-byte stores; every entry is cleared, and so
 // is the block voxel table.
-template <bool CL>
 static __device__ void block_commit_pool(const KArgs& a, SpecShared& sh, unsigned char* smem, int cut, unsigned acc,
-                                         int* bkeys, unsigned* bmask) {
+                                  int* bkeys, unsigned* bmask) {
   const RepDev& rd = sh.ws.rd;
   int* pkeys = reinterpret_cast<int*>(smem + a.off_pkeys);
   const int* pused = reinterpret_cast<const int*>(smem + a.off_pused);
   long long* pvals = reinterpret_cast<long long*>(smem + a.off_pvals);
   long long* grid = a.grid + rd.vox_off * a.ncol;
   const int n = sh.npool, hcol = a.hcol, ncol = a.ncol;
-  const int gbase = cta_rank<CL>() * a.spec_s;
   for (int e = (int)threadIdx.x; e < n; e += (int)blockDim.x) {
     const int slot = pused[e];
     const int key = pkeys[slot];
-    const int s = key & 31, gs = gbase + s;
+    const int s = key & 31;
     long long* src = pvals + (long long)slot * hcol;
-    if (gs < cut && ((acc >> gs) & 1u) && !(sh.plan[s].derr & E_OVF)) {
+    if (s < cut && ((acc >> s) & 1u) && !(sh.plan[s].derr & E_OVF)) {
       longlong2* dst = reinterpret_cast<longlong2*>(grid + (long long)(key >> 5) * ncol);
       dst[0] = make_longlong2(src[0], src[1]);
       if (ncol == 4) dst[1] = make_longlong2(hcol > 2 ? src[2] : 0, hcol > 3 ? src[3] : 0);
@@ -543,13 +504,11 @@ __device__ __forceinline__ void add_pool_terms(double& s, const MovePlan& P) {
 // a move, which run the collectives and block barriers with empty work.
 // Every thread of the CTA calls it (position moves hold two block barriers
 // around the block-wide deposit); B is the batch's number of moves.
-// Move slot s of this CTA (batch slot gs = rank * spec_s + s of the batch's
-// Bt moves; B of them in this CTA).  bkeys / bmask: the batch's voxel table.
-template <typename Pos, int G, bool CL>
+template <typename Pos, int G>
 __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, int gl, bool live, int kind,
                               const cg_move_ctl& c, unsigned long long t, unsigned* draws,
                               const SlotScratch& sm, const SlotScratch& gm, int* bkeys, unsigned* bmask,
-                              int logHB, int B, int Bt) {
+                              int logHB, int B) {
   using Real = Pos;
   using Acc = typename AccOf<Real>::type;
   const RepDev& rd = sh.ws.rd;
@@ -565,7 +524,6 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
   const double* bonds = a.bonds + rd.bead_off * 6;
   const float* bonds32 = a.bonds32 + rd.bead_off * 8;
   MovePlan& P = sh.plan[s];
-  const int gs = cta_rank<CL>() * a.spec_s + s;
   MoveRng g;
   if (__any_sync(kFull, live)) g.init<G>(a.seed, rep, t, draws, gl);
   unsigned err = 0;
@@ -685,22 +643,22 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       for (int i = 0; i < 3; i++)
         for (int j = 0; j < 4; j++) Mp[4 * i + j] = M[i][j];
     }
-    batch_sync<CL>();  // every plan of the batch written
-    block_deposit<Pos, CL>(a, sh, rep, B, kind);
+    __syncthreads();
+    block_deposit<Pos>(a, sh, rep, B, kind);
     // earlier moves u of the batch whose written beads [ind0, indf) meet the
     // beads this move reads (its segment and both neighbours); a move with no
     // beads (failed or empty) is never accepted, so it needs no exclusion
-    for (int u0 = 0; u0 < Bt; u0 += G) {
+    for (int u0 = 0; u0 < B; u0 += G) {
       const int u = u0 + gl;
       bool hit = false;
-      if (m > 0 && u < gs) {
-        const MovePlan& U = plan_at<CL>(sh, u, a.spec_s);
+      if (m > 0 && u < s) {
+        const MovePlan& U = sh.plan[u];
         hit = U.m > 0 && (long long)U.ind0 <= indf && ind0 - 1 <= (long long)U.indf - 1;
       }
       cmb |= gballot<G>(hit) << u0;
     }
     __syncthreads();
-    if (pool && density) block_field_pool<CL>(a, sh, reinterpret_cast<unsigned char*>(&sh), bkeys, bmask);
+    if (pool && density) block_field_pool(a, sh, reinterpret_cast<unsigned char*>(&sh), bkeys, bmask);
     Acc part = acc_zero<Acc>();
     int oob = 0;
     bool ovf = false;
@@ -977,7 +935,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
   int regfail = 0;
   if (density && check_field) {
     const int nu = (live && !err && !empty) ? *nused : 0;
-    const unsigned below = (1u << gs) - 1u, above = ~((2u << gs) - 1u);
+    const unsigned below = (1u << s) - 1u, above = ~((2u << s) - 1u);
     for (int i = gl; i < nu; i += G) {
       int v = S.keys[S.used[i]];
       int b = block_insert(bkeys, logHB, v);
@@ -985,11 +943,11 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       if (b < 0) {
         regfail = 1;
       } else {
-        const unsigned prior = atomicOr(&bmask[b], 1u << gs);
+        const unsigned prior = atomicOr(&bmask[b], 1u << s);
         if (kind <= CG_SLIDE) {
           cmb |= prior & below;
           for (unsigned later = prior & above; later; later &= later - 1)
-            atomicOr(&plan_at<CL>(sh, __ffs((int)later) - 1, a.spec_s).cmask, 1u << gs);
+            atomicOr(&sh.plan[__ffs((int)later) - 1].cmask, 1u << s);
         }
       }
     }
@@ -1018,14 +976,12 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
   }
 }
 
-// Bits of earlier moves of the batch (u < gs, of Bt) whose footprint meets
-// the footprint of this CTA's move slot s (batch slot gs).
-template <int G, bool CL>
+// Bits of earlier moves of the batch (u < s) whose footprint meets move s's.
+template <int G>
 __device__ void conflict_mask(const KArgs& a, SpecShared& sh, unsigned char* smem, int rep, int s, int gl,
-                              bool live, int kind, int Bt, const SlotScratch& sm, const SlotScratch& gm,
+                              bool live, int kind, int B, const SlotScratch& sm, const SlotScratch& gm,
                               const unsigned* bmask) {
   MovePlan& P = sh.plan[s];
-  const int S = a.spec_s, gs = cta_rank<CL>() * S + s;
   const RepDev& rd = sh.ws.rd;
   const bool act = live && !P.err && !P.empty;
   unsigned cm = 0;
@@ -1038,19 +994,17 @@ __device__ void conflict_mask(const KArgs& a, SpecShared& sh, unsigned char* sme
     }
     cm = gor<G>(cm);
   }
-  cm &= (1u << gs) - 1u;
+  cm &= (1u << s) - 1u;
   if (kind == CG_TANGENT_ROTATION) {
     // rotated beads of u against those of s and their neighbours
     const int* lw = P.gstage ? gm.idx : sm.idx;
-    for (int u = 0; u < Bt; u++) {
-      const MovePlan& U = plan_at<CL>(sh, u, S);
+    for (int u = 0; u < B; u++) {
+      const MovePlan& U = sh.plan[u];
       int hit = 0;
-      if (act && u < gs && !U.err && !U.empty) {
-        const int* lu = U.gstage ? a.g_idx + ((long long)rep * a.spec_st + u) * a.g_stage_cap
-                                 : in_rank<CL>(reinterpret_cast<const int*>(smem + a.spec_off_warps +
-                                                                            (size_t)(u % S) * a.warp_smem +
-                                                                            a.off_idx),
-                                               u / S);
+      if (act && u < s && !U.err && !U.empty) {
+        const int* lu = U.gstage ? a.g_idx + ((long long)rep * a.spec_s + u) * a.g_stage_cap
+                                 : reinterpret_cast<const int*>(smem + a.spec_off_warps +
+                                                                (size_t)u * a.warp_smem + a.off_idx);
         for (int k = gl; k < P.m && !hit; k += G) {
           int j = lw[k];
           for (int q = 0; q < U.m; q++) {
@@ -1065,11 +1019,11 @@ __device__ void conflict_mask(const KArgs& a, SpecShared& sh, unsigned char* sme
     // lane gl takes the earlier moves u = u0 + gl: beads written by u,
     // [ind0, indf), against the beads read by s -- the segment and, for
     // position moves, its two neighbours
-    for (int u0 = 0; u0 < Bt; u0 += G) {
+    for (int u0 = 0; u0 < B; u0 += G) {
       const int u = u0 + gl;
       bool hit = false;
-      if (act && u < gs) {
-        const MovePlan& U = plan_at<CL>(sh, u, S);
+      if (act && u < s) {
+        const MovePlan& U = sh.plan[u];
         if (!U.err && !U.empty) {
           const long long wlo = U.ind0, whi = (long long)U.indf - 1;
           const long long rlo = P.kind == CG_CHANGE_BINDING_STATE ? P.ind0 : (long long)P.ind0 - 1;
@@ -1169,7 +1123,7 @@ __device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int s, int gl, 
 
 // 168 registers: two CTAs of 6 warps fit one SM's register file (measured
 // faster than 128 registers with 8 warps, which spills).
-template <typename Pos, int G, bool CL = false>
+template <typename Pos, int G>
 __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
   extern __shared__ __align__(32) unsigned char smem[];
   constexpr int GPW = 32 / G;  // move groups per warp
@@ -1177,18 +1131,11 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
   const int gl = lane & (G - 1);
   const int slot = warp * GPW + lane / G;
   const int Sn = a.spec_s;
-  // a cluster of spec_c CTAs per replica (consecutive blocks), else one
-  const int crank = cta_rank<CL>();
-  const int Sc = CL ? a.spec_c * Sn : Sn;  // moves of a full batch
-  const int gslot = crank * Sn + slot;     // this group's batch slot
-  const int rep = CL ? (int)(blockIdx.x / (unsigned)a.spec_c) : (int)blockIdx.x;
-  if (rep >= a.n_reps) return;  // whole clusters: every rank of a cluster has the same rep
+  const int rep = blockIdx.x;
+  if (rep >= a.n_reps) return;
   SpecShared& sh = *reinterpret_cast<SpecShared*>(smem);
   int* bkeys = reinterpret_cast<int*>(smem + a.spec_off_bkeys);
   unsigned* bmask = reinterpret_cast<unsigned*>(smem + a.spec_off_bmask);
-  // the batch's voxel -> move-bitmask table: the rank-0 CTA's
-  int* cbkeys = in_rank<CL>(bkeys, 0);
-  unsigned* cbmask = in_rank<CL>(bmask, 0);
   const int HB = 1 << a.spec_logHB;
   const int hcol = a.hcol;
   unsigned char* wb = smem + a.spec_off_warps + (size_t)slot * a.warp_smem;
@@ -1201,7 +1148,7 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
   sm.logH = a.logH;
   sm.stage = wb + a.off_stage;
   sm.idx = reinterpret_cast<int*>(wb + a.off_idx);
-  const long long gi = (long long)rep * a.spec_st + gslot;
+  const long long gi = (long long)rep * Sn + slot;
   const long long Hg = 1LL << a.g_logH;
   gm.keys = a.g_keys + gi * Hg;
   gm.used = a.g_used + gi * Hg;
@@ -1240,11 +1187,9 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
     sh.cut = 0;
     sh.npool = 0;
   }
-  // every rank of a cluster running, and the rank-0 batch table clear, before
-  // any rank registers voxels there
-  batch_sync<CL>();
+  __syncthreads();
   const long long words = (sh.ws.rd.n_beads + 31) / 32;
-  sm.picked = gm.picked = a.picked + a.picked_off[rep] + gslot * words;
+  sm.picked = gm.picked = a.picked + a.picked_off[rep] + slot * words;
 
   for (long long step = 0; step < a.n_steps; step++) {
     for (int ci = 0; ci < a.n_ctl; ci++) {
@@ -1261,31 +1206,28 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
             __syncthreads();
             break;
           }
-          // Bt moves in the batch, B of them in this CTA (slots crank * Sn ...)
-          const int Bt = (int)(c.num_per_cycle - done < Sc ? c.num_per_cycle - done : Sc);
-          const int Bl = Bt - crank * Sn;
-          const int B = Bl < 0 ? 0 : (Bl > Sn ? Sn : Bl);
+          const int B = (int)(c.num_per_cycle - done < Sn ? c.num_per_cycle - done : Sn);
           const bool wlive = warp * GPW < B;  // the warp has a move of this batch
           const bool live = slot < B;
-          evaluate_move<Pos, G, CL>(a, sh, rep, slot, gl, live, kind, c, sh.t0 + (unsigned long long)gslot, draws,
-                                    sm, gm, cbkeys, cbmask, a.spec_logHB, B, Bt);
-          batch_sync<CL>();
+          evaluate_move<Pos, G>(a, sh, rep, slot, gl, live, kind, c, sh.t0 + (unsigned long long)slot, draws,
+                                sm, gm, bkeys, bmask, a.spec_logHB, B);
+          __syncthreads();
           if (kind > CG_SLIDE) {  // position moves set their masks while evaluating
-            if (wlive) conflict_mask<G, CL>(a, sh, smem, rep, slot, gl, live, kind, Bt, sm, gm, cbmask);
-            batch_sync<CL>();
+            if (wlive) conflict_mask<G>(a, sh, smem, rep, slot, gl, live, kind, B, sm, gm, bmask);
+            __syncthreads();
           }
           // Resolve, computed by every warp from the plans (lane u reads move u):
           // the batch stands up to the first move that failed or meets an
           // earlier accepted move (everything before it stands, so "earlier
           // accepted" is the accepted moves below it), or up to and including
           // the first move whose voxels could not be registered.
-          const bool valid = lane < Bt;
-          const MovePlan& Pl = plan_at<CL>(sh, valid ? lane : 0, Sn);
+          const bool valid = lane < B;
+          const MovePlan& Pl = sh.plan[valid ? lane : 0];
           const bool p_err = valid && Pl.err != 0;
           const unsigned D = __ballot_sync(kFull, valid && !Pl.empty && Pl.dec);
           const unsigned F = __ballot_sync(kFull, p_err || (valid && (Pl.cmask & D & ((1u << lane) - 1u))));
           const unsigned RF = __ballot_sync(kFull, valid && Pl.regfail);
-          const int first_fail = F ? __ffs((int)F) - 1 : Bt;
+          const int first_fail = F ? __ffs((int)F) - 1 : B;
           int cut = first_fail;
           if (RF && __ffs((int)RF) < cut) cut = __ffs((int)RF);
           const unsigned acc = cut >= 32 ? D : (D & ((1u << cut) - 1u));
@@ -1313,8 +1255,8 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
               double run = sh.run_dE, rate = c.acc_rate;
               const double alpha = c.alpha, beta = 1 - c.alpha;
               for (int w = 0; w < cut; w++) {
-                const MovePlan& P = plan_at<CL>(sh, w, Sn);
-                if (a.mlog && crank == 0) log_move(a, rep, sh.t0 + (unsigned long long)w - sh.tlog, P);
+                const MovePlan& P = sh.plan[w];
+                if (a.mlog) log_move(a, rep, sh.t0 + (unsigned long long)w - sh.tlog, P);
                 if (P.empty) continue;
                 if (P.dec && soft_dE(P.dE)) run += P.dE;
                 rate = (P.dec ? alpha : 0.0) + beta * rate;
@@ -1322,18 +1264,16 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
               sh.run_dE = run;
               c.acc_rate = rate;
               sh.t0 += (unsigned long long)cut;
-              if (cut == first_fail && first_fail < Bt && plan_at<CL>(sh, first_fail, Sn).err)
-                sh.stop = plan_at<CL>(sh, first_fail, Sn).err;
+              if (cut == first_fail && first_fail < B && sh.plan[first_fail].err) sh.stop = sh.plan[first_fail].err;
             }
           }
           if (wlive && live)
-            commit_and_clear<Pos, G>(a, sh, slot, gl, gslot < cut && ((acc >> gslot) & 1u), sm, gm, cbkeys,
-                                     cbmask);
+            commit_and_clear<Pos, G>(a, sh, slot, gl, slot < cut && ((acc >> slot) & 1u), sm, gm, bkeys, bmask);
           __syncwarp();
           if (live && gl == 0) sh.nused[slot] = 0;
           if (kind <= CG_SLIDE && a.pool_on && sh.ws.rd.field_kind == 2)
-            block_commit_pool<CL>(a, sh, smem, cut, acc, bkeys, bmask);
-          batch_sync<CL>();  // commits seen by every rank; the batch table is clear
+            block_commit_pool(a, sh, smem, cut, acc, bkeys, bmask);
+          __syncthreads();
           done += cut;
           if (sh.stop) break;
         }
@@ -1344,10 +1284,7 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
     }
     if (sh.stop) break;
   }
-  // no rank leaves while another may still read its shared memory; every rank
-  // holds the same books, rank 0 writes them
-  batch_sync<CL>();
-  if (crank != 0) return;
+  __syncthreads();
   {
     unsigned* cd = reinterpret_cast<unsigned*>(a.ctl + (long long)rep * 5);
     const unsigned* cs = reinterpret_cast<const unsigned*>(sh.ws.ctl);
@@ -1366,45 +1303,6 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
 }  // namespace cg
 
 // Launch, shared-memory opt-in and register count of one instantiation.
-// CG_SPEC_INSTANTIATE_CLUSTER: the cluster form (a.spec_c CTAs per replica,
-// consecutive blocks, one thread-block cluster each).
-#define CG_SPEC_INSTANTIATE_CLUSTER(Pos, G, NAME)                                                  \
-  cudaError_t cg_launch_spec_##NAME(const cg::KArgs& a, size_t smem, cudaStream_t s) {             \
-    cudaLaunchConfig_t cfg = {};                                                                   \
-    cfg.gridDim = dim3((unsigned)(a.n_reps * a.spec_c));                                           \
-    cfg.blockDim = dim3((unsigned)(32 * a.spec_w));                                                \
-    cfg.dynamicSmemBytes = smem;                                                                   \
-    cfg.stream = s;                                                                                \
-    cudaLaunchAttribute at[1];                                                                     \
-    at[0].id = cudaLaunchAttributeClusterDimension;                                                \
-    at[0].val.clusterDim.x = (unsigned)a.spec_c;                                                   \
-    at[0].val.clusterDim.y = 1;                                                                    \
-    at[0].val.clusterDim.z = 1;                                                                    \
-    cfg.attrs = at;                                                                                \
-    cfg.numAttrs = 1;                                                                              \
-    return cudaLaunchKernelEx(&cfg, cg::spec_kernel<Pos, G, true>, a);                             \
-  }                                                                                                \
-  cudaError_t cg_spec_smem_##NAME(int bytes) {                                                     \
-    return cudaFuncSetAttribute(cg::spec_kernel<Pos, G, true>,                                     \
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);               \
-  }                                                                                                \
-  int cg_spec_max_clusters_##NAME(const cg::KArgs& a, size_t smem) {                               \
-    cudaLaunchConfig_t cfg = {};                                                                   \
-    cfg.gridDim = dim3((unsigned)(a.n_reps * a.spec_c));                                           \
-    cfg.blockDim = dim3((unsigned)(32 * a.spec_w));                                                \
-    cfg.dynamicSmemBytes = smem;                                                                   \
-    cudaLaunchAttribute at[1];                                                                     \
-    at[0].id = cudaLaunchAttributeClusterDimension;                                                \
-    at[0].val.clusterDim.x = (unsigned)a.spec_c;                                                   \
-    at[0].val.clusterDim.y = 1;                                                                    \
-    at[0].val.clusterDim.z = 1;                                                                    \
-    cfg.attrs = at;                                                                                \
-    cfg.numAttrs = 1;                                                                              \
-    int n = 0;                                                                                     \
-    return cudaOccupancyMaxActiveClusters(&n, cg::spec_kernel<Pos, G, true>, &cfg) == cudaSuccess  \
-               ? n : -1;                                                                           \
-  }
-
 #define CG_SPEC_INSTANTIATE(Pos, G, NAME)                                                          \
   void cg_launch_spec_##NAME(const cg::KArgs& a, size_t smem, cudaStream_t s) {                    \
     cg::spec_kernel<Pos, G><<<a.n_reps, 32 * a.spec_w, smem, s>>>(a);                              \

@@ -191,16 +191,14 @@ def binder_names(nb):
     return ["HP1", "PRC1", "B3"][:nb]
 
 
-def build_sim(w: Workload, chains=None, pos_fp64=None, warps_per_block=0, lanes_per_move=0,
-              ctas_per_replica=0) -> nat.Sim:
+def build_sim(w: Workload, chains=None, pos_fp64=None, warps_per_block=0, lanes_per_move=0) -> nat.Sim:
     chains = chains if chains is not None else make_chains(w)
     pos_fp64 = w.pos_fp64 if pos_fp64 is None else pos_fp64
     R, nb = w.replicas, w.n_binders
     confined = w.sphere_radius > 0
     sim = nat.Sim(w.lengths, [[w.nbins] * 3] * R, nb, pos_fp64=pos_fp64, max_segment=152,
                   max_tangent=int(max(w.lengths)), warps_per_block=warps_per_block,
-                  lanes_per_move=lanes_per_move, nonuniform_access=confined,
-                  ctas_per_replica=ctas_per_replica)
+                  lanes_per_move=lanes_per_move, nonuniform_access=confined)
     width = w.nbins * VOXEL
     access = _sphere_volumes(w.nbins, w.sphere_radius) if confined else None
     vint = 4.0 / 3.0 * np.pi * R_INT ** 3

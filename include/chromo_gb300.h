@@ -110,10 +110,6 @@ typedef struct {
     int32_t nonuniform_access; /* 1: per-voxel accessible volumes are uploaded */
     int32_t lanes_per_move;    /* lanes evaluating one move: 8, 16 or 32 (FP64 storage: 32);
                                   0: chosen by the library */
-    int32_t ctas_per_replica;  /* 0 or 1: one CTA per replica; 2 or 4: each replica on a
-                                  thread-block cluster of that many CTAs (one SM each), its
-                                  batch of moves in flight spread over them (FP32 storage,
-                                  32 lanes per move; for fewer replicas than SMs) */
 } cg_config;
 
 /* Allocate device state for R replicas.  Replaces constructing the reference's

@@ -62,49 +62,6 @@ def test_moves_in_flight_equal_sequential(fp64):
         np.testing.assert_array_equal(base[3], tal_w)
 
 
-CLUSTER_SHAPES = [(6, 2), (12, 2), (4, 4), (8, 4)]  # (warps per CTA, CTAs per replica)
-
-
-def test_cluster_batches_equal_sequential():
-    """A replica spread over a thread-block cluster of 2 or 4 CTAs (up to 32
-    moves in flight, plans and the batch's voxel table shared through
-    distributed shared memory) gives the one-move-at-a-time result bit for
-    bit: chains, grids, controllers and tallies, over every move kind."""
-    w = _small()
-    chains = wl.make_chains(w)
-    runs = {}
-    for W, C in [(1, 1)] + CLUSTER_SHAPES:
-        sim = wl.build_sim(w, chains, warps_per_block=W, lanes_per_move=32, ctas_per_replica=C)
-        assert sim.launch_shape()[:3] == (W, 32, W * C)
-        sim.run(6, 99)
-        sim.sync()
-        runs[(W, C)] = ([sim.get_chain(r) for r in range(w.replicas)],
-                        [sim.density(r) for r in range(w.replicas)],
-                        [[(c.amp_move, c.amp_bead, c.num_attempt, c.num_success, c.acc_rate)
-                          for c in sim.get_controllers(r)] for r in range(w.replicas)],
-                        np.stack([sim.tally(r) for r in range(w.replicas)]))
-        sim.close()
-    base = runs[(1, 1)]
-    for shape in CLUSTER_SHAPES:
-        chains_c, dens_c, ctl_c, tal_c = runs[shape]
-        for r in range(w.replicas):
-            for a, b in zip(base[0][r], chains_c[r]):
-                np.testing.assert_array_equal(a, b, err_msg=str(shape))
-            np.testing.assert_array_equal(base[1][r], dens_c[r], err_msg=str(shape))
-            assert base[2][r] == ctl_c[r], shape
-        np.testing.assert_array_equal(base[3], tal_c, err_msg=str(shape))
-
-
-def test_cluster_shape_checks():
-    """Clusters need FP32 storage and 32 lanes per move, and 2 or 4 CTAs."""
-    from chromo_gb300 import _native as nat
-    w = _small(nrep=2)
-    for kw in (dict(pos_fp64=True, ctas_per_replica=2), dict(lanes_per_move=16, ctas_per_replica=2),
-               dict(ctas_per_replica=3)):
-        with pytest.raises(nat.CgError):
-            wl.build_sim(w, **kw)
-
-
 @pytest.mark.parametrize("lanes", [8, 16, 32])
 def test_grid_consistent_after_parallel_run(lanes):
     w = _small(nrep=4, n=3000, nbins=16)

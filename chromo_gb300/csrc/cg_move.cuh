@@ -408,6 +408,18 @@ template <typename Real>
 __device__ __forceinline__ int out_of_bounds(const RepDev& rd, const Real q[3], bool trial) {
   return out_of_bounds3(rd, (double)q[0], (double)q[1], (double)q[2], trial);
 }
+// FP32 positions in a sphere: |q|^2 in FP32 (relative error below 2e-7)
+// decides every position further than 1e-5 |q|^2 from the boundary, as the
+// FP64 test would; the rest take the FP64 test.
+__device__ __forceinline__ int out_of_bounds(const RepDev& rd, const float q[3], bool trial) {
+  if (rd.confine_kind == 1) {
+    const float s = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+    const float l2 = (float)(rd.confine_length * rd.confine_length);
+    if (s < l2 * 0.99999f) return 0;
+    if (s > l2 * 1.00001f) return 1;
+  }
+  return out_of_bounds3(rd, (double)q[0], (double)q[1], (double)q[2], trial);
+}
 
 __device__ __forceinline__ double bind_f(const RepDev& rd, int b, int nm, int s) {
   return rd.bind_f[(b * (CG_MAX_MARK + 1) + nm) * (CG_MAX_MARK + 1) + s];

@@ -4,10 +4,14 @@ The fixtures ``tests/golden/stats/eq_<case>.npz`` (written by
 ``tests/golden/make_equilibrium.py`` from the reference's own ``mc_sim``)
 hold the per-run time averages of independent reference runs from one seeded
 start: a 100-bead chain in a periodic 6^3-voxel box with one binder
-(one_binder) or with two binders and cross talk (two_binders).  Here 64
+(one_binder) or with two binders and cross talk (two_binders), or confined to
+a 100 nm sphere in an 8^3-voxel box with the accessible volumes of the voxels
+the sphere cuts (sphere_confined; bead counts per voxel are density times
+accessible volume on both sides).  Here 64
 replicas of the same start run on the GPU (FP32 storage, independent Philox
-streams) for the same burn-in and sampling schedule -- the two-binder case at
-the launch shape of the batched benchmark, 6 warps x 32 lanes per replica --
+streams) for the same burn-in and sampling schedule -- the two-binder and
+confined cases at the launch shape of the batched benchmark, 6 warps x 32
+lanes per replica --
 and every observable (squared end-to-end distance and radius of gyration,
 each binder's occupancy, the histogram of bead counts per voxel and its
 second moment) must agree with the reference's mean within 3 combined
@@ -43,14 +47,17 @@ def _replicas(g, R, shape=(0, 0)):
     nb = len(g["sites"])
     ctl0 = g["ctl0"]
     max_seg = int(max(max(row[1], row[5]) for k, row in enumerate(ctl0) if k != 3)) + 2
+    confined = "access_vol" in g and int(g["confine_kind"]) != 0
     sim = nat.Sim([n] * R, [list(g["nxyz"])] * R, nb, max_segment=max_seg,
                   max_tangent=int(max(ctl0[3][1], ctl0[3][5])), warps_per_block=shape[0],
-                  lanes_per_move=shape[1])
+                  lanes_per_move=shape[1], nonuniform_access=confined)
     bonds = bonds_array(g["eps_bend"], g["gamma"], g["eps_par"], g["eps_perp"], g["eta"])
     fp = field_params(field_kind=2, nxyz=g["nxyz"], widths=g["widths"], n_binders=nb,
                       chi=float(g["chi"]), vf_limit=float(g["vf_limit"]),
                       bead_vol=4.0 / 3.0 * np.pi * float(g["bead_rad"]) ** 3, pref=g["pref"],
-                      intra=g["intra"], xpref=g["xpref"])
+                      intra=g["intra"], xpref=g["xpref"],
+                      confine_kind=int(g["confine_kind"]) if confined else 0,
+                      confine_length=float(g["confine_length"]) if confined else 0.0)
     bp = binding_params(sites=g["sites"], e_mod=g["e_mod"], e_nomod=g["e_nomod"], mu=g["mu"],
                         mu_adjust_factor=1.0)
     ctls = [move_ctl(MOVE_NAMES[k], amp_move=row[0], amp_bead=int(row[1]), num_per_cycle=int(row[2]),
@@ -59,14 +66,15 @@ def _replicas(g, R, shape=(0, 0)):
     for rep in range(R):
         sim.set_chain(rep, r=g["r0"], t3=g["t30"], t2=g["t20"], states=g["states0"], marks=g["marks"],
                       bonds=bonds)
-        sim.set_field(rep, fp)
+        sim.set_field(rep, fp, access_vol=g["access_vol"] if confined else None)
         sim.set_binding(rep, bp)
         sim.set_controllers(rep, ctls)
     sim.deposit(-1)
     return sim
 
 
-@pytest.mark.parametrize("case,shape", [("one_binder", (0, 0)), ("two_binders", (6, 32))])
+@pytest.mark.parametrize("case,shape", [("one_binder", (0, 0)), ("two_binders", (6, 32)),
+                                        ("sphere_confined", (6, 32))])
 def test_equilibrium_statistics_match_reference(case, shape):
     fixture = STATS / f"eq_{case}.npz"
     if not fixture.exists():

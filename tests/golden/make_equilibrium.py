@@ -15,7 +15,8 @@ eps = -3), chi = 1.5.  sphere_confined: a 100-bead chain (HP1 as in
 one_binder, chi = 1) confined to a sphere of radius 100 nm (Spherical
 confinement) centred in a 320 nm box of 8^3 voxels, with the accessible
 volumes of the voxels the sphere cuts (assume_fully_accessible=0), started
-from a seeded walk inside the sphere.  Each system is run RUNS times
+from a seeded walk inside the sphere.  twist: the one_binder system as an
+SSTWLC chain (twist persistence length 100 nm).  Each system is run RUNS times
 from the same seeded start with independent random streams (libc ``srand``
 and numpy seeds per run; ``mc_sim`` reseeds numpy on every call, so every call
 gets its own seed).  After BURN MC steps, SAMPLES snapshots are taken every
@@ -53,6 +54,8 @@ CASES = {
                         chi=1.5, moves="all", seed=22, run=20),
     "sphere_confined": dict(n=100, nbins=8, vox=40.0, binders=[("HP1", -0.4, -4.0, {})], chi=1.0,
                             confine=("Spherical", 100.0), access=True, moves="all", seed=23, run=20),
+    "twist": dict(n=100, nbins=6, vox=40.0, binders=[("HP1", -0.4, -4.0, {})], chi=1.0, lt=100.0,
+                  moves="all", seed=24, run=20),
 }
 RUNS, BURN, SAMPLES, EVERY = 16, 1500, 300, 20
 BINS = np.array([-np.inf, 0.05, 0.25, 0.5, 1.0, np.inf])
@@ -157,7 +160,9 @@ def main(name):
         ctl0=np.array(ctl0, dtype=np.float64),
         confine_kind={"": 0, "Spherical": 1, "Cubical": 2}[field.confine_type],
         confine_length=float(field.confine_length),
-        access_vol=np.array([field.access_vols[i] for i in range(field.nx * field.ny * field.nz)]))
+        access_vol=np.array([field.access_vols[i] for i in range(field.nx * field.ny * field.nz)]),
+        **({"eps_twist": np.asarray(p.eps_twist).copy(),
+            "omega0": np.asarray(p.bead_length) * (2 * np.pi / 10.5) / 0.332} if cfg.get("lt") else {}))
     m, se = runs.mean(axis=0), runs.std(axis=0, ddof=1) / np.sqrt(RUNS)
     for nm, a, b_ in zip(obs_names(names), m, se):
         print(f"{nm:>20}: {a:.6g} +- {b_:.3g}")

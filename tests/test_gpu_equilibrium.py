@@ -7,11 +7,11 @@ start: a 100-bead chain in a periodic 6^3-voxel box with one binder
 (one_binder) or with two binders and cross talk (two_binders), or confined to
 a 100 nm sphere in an 8^3-voxel box with the accessible volumes of the voxels
 the sphere cuts (sphere_confined; bead counts per voxel are density times
-accessible volume on both sides).  Here 64
+accessible volume on both sides), or the one-binder system as a twistable
+SSTWLC chain (twist).  Here 64
 replicas of the same start run on the GPU (FP32 storage, independent Philox
-streams) for the same burn-in and sampling schedule -- the two-binder and
-confined cases at the launch shape of the batched benchmark, 6 warps x 32
-lanes per replica --
+streams) for the same burn-in and sampling schedule -- all but the first at
+the launch shape of the batched benchmark, 6 warps x 32 lanes per replica --
 and every observable (squared end-to-end distance and radius of gyration,
 each binder's occupancy, the histogram of bead counts per voxel and its
 second moment) must agree with the reference's mean within 3 combined
@@ -67,6 +67,8 @@ def _replicas(g, R, shape=(0, 0)):
         sim.set_chain(rep, r=g["r0"], t3=g["t30"], t2=g["t20"], states=g["states0"], marks=g["marks"],
                       bonds=bonds)
         sim.set_field(rep, fp, access_vol=g["access_vol"] if confined else None)
+        if "eps_twist" in g:  # SSTWLC
+            sim.set_twist(rep, g["eps_twist"], g["omega0"])
         sim.set_binding(rep, bp)
         sim.set_controllers(rep, ctls)
     sim.deposit(-1)
@@ -74,7 +76,7 @@ def _replicas(g, R, shape=(0, 0)):
 
 
 @pytest.mark.parametrize("case,shape", [("one_binder", (0, 0)), ("two_binders", (6, 32)),
-                                        ("sphere_confined", (6, 32))])
+                                        ("sphere_confined", (6, 32)), ("twist", (6, 32))])
 def test_equilibrium_statistics_match_reference(case, shape):
     fixture = STATS / f"eq_{case}.npz"
     if not fixture.exists():

@@ -54,8 +54,10 @@ CASES = {
                         chi=1.5, moves="all", seed=22, run=20),
     "sphere_confined": dict(n=100, nbins=8, vox=40.0, binders=[("HP1", -0.4, -4.0, {})], chi=1.0,
                             confine=("Spherical", 100.0), access=True, moves="all", seed=23, run=20),
+    # the twisted chain's extension relaxes slowly and its per-run averages
+    # scatter widely: four times the runs
     "twist": dict(n=100, nbins=6, vox=40.0, binders=[("HP1", -0.4, -4.0, {})], chi=1.0, lt=100.0,
-                  moves="all", seed=24, run=20),
+                  moves="all", seed=24, run=20, runs=64),
 }
 RUNS, BURN, SAMPLES, EVERY = 16, 1500, 300, 20
 BINS = np.array([-np.inf, 0.05, 0.25, 0.5, 1.0, np.inf])
@@ -139,8 +141,9 @@ def main(name):
     rows = field.binder_dict
     objs = [mg.cb.get_by_name(b[0]) for b in cfg["binders"]]
     names = [b[0] for b in cfg["binders"]]
-    with mp.get_context("spawn").Pool(min(RUNS, mp.cpu_count())) as pool:
-        runs = np.array(pool.map(one_run, [(name, k) for k in range(RUNS)]))
+    n_runs = cfg.get("runs", RUNS)
+    with mp.get_context("spawn").Pool(min(n_runs, mp.cpu_count())) as pool:
+        runs = np.array(pool.map(one_run, [(name, k) for k in range(n_runs)]))
     out.parent.mkdir(exist_ok=True)
     np.savez_compressed(
         out, obs_names=np.array(obs_names(names)), runs=runs, burn=BURN, samples=SAMPLES, every=EVERY,
@@ -163,7 +166,7 @@ def main(name):
         access_vol=np.array([field.access_vols[i] for i in range(field.nx * field.ny * field.nz)]),
         **({"eps_twist": np.asarray(p.eps_twist).copy(),
             "omega0": np.asarray(p.bead_length) * (2 * np.pi / 10.5) / 0.332} if cfg.get("lt") else {}))
-    m, se = runs.mean(axis=0), runs.std(axis=0, ddof=1) / np.sqrt(RUNS)
+    m, se = runs.mean(axis=0), runs.std(axis=0, ddof=1) / np.sqrt(n_runs)
     for nm, a, b_ in zip(obs_names(names), m, se):
         print(f"{nm:>20}: {a:.6g} +- {b_:.3g}")
 

@@ -183,6 +183,45 @@ def mc_sim(polymers, readerproteins, num_mc_steps, mc_move_controllers, field,
         sim.close()
 
 
+class ResidentChain:
+    """One polymer kept on the device across successive runs.
+
+    ``polymer_in_field`` (chromo/mc/__init__.py:36-161) calls ``mc_sim`` once
+    per snapshot, and each call would upload the chain, its field and its
+    controllers and read them back.  Here the device state stays resident
+    between runs: ``run`` continues the same simulation (its move counter keeps
+    counting, so every run draws fresh random streams whatever its seed), then
+    refreshes the polymer, the field's density and the controllers on the host
+    as ``mc_sim`` does.  A changed ``mu_adjust_factor`` is uploaded before the
+    run it applies to."""
+
+    def __init__(self, polymers, field, mc_move_controllers):
+        self.poly = _check(polymers, field)
+        self.field = field
+        self.ctrls = list(mc_move_controllers)
+        self.maf = float(getattr(self.poly, "mu_adjust_factor", 1.0))
+        self.sim = _device(self.poly, field, self.ctrls) if self.ctrls else None
+
+    def run(self, num_mc_steps, mu_adjust_factor, random_seed):
+        num_mc_steps = int(num_mc_steps)
+        if num_mc_steps < 0:
+            raise ValueError("num_mc_steps must be non-negative")
+        self.poly.mu_adjust_factor = float(mu_adjust_factor)
+        if self.sim is None or num_mc_steps == 0:
+            return
+        if self.poly.mu_adjust_factor != self.maf:
+            self.sim.set_binding(0, _binding_struct(self.poly))
+            self.maf = self.poly.mu_adjust_factor
+        self.sim.run(num_mc_steps, int(random_seed))
+        self.sim.sync()
+        _pull(self.sim, self.poly, self.field, self.ctrls)
+
+    def close(self):
+        if self.sim is not None:
+            self.sim.close()
+            self.sim = None
+
+
 _STEP_SEEDS = itertools.count(0x5EED000000000000)
 
 

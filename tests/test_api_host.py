@@ -160,7 +160,7 @@ def test_mc_step_runs_one_move_at_current_amplitudes(monkeypatch):
 def test_continue_polymer_in_field_from_latest_snapshot(monkeypatch, tmp_path):
     """continue_polymer_in_field_simulation (chromo/mc/__init__.py:167-227)
     reads each polymer's latest <name>-<i>.csv, puts it in the field, and
-    continues the snapshot numbering (the MC steps are mc_sim's, faked here)."""
+    continues the snapshot numbering (the device runs are faked here)."""
     import chromo_gb300.mc as mc
     binders = cb.make_binder_collection([cb.get_by_name("HP1")])
     p = Chromatin.straight_line_in_x("chr", np.full(49, 16.5), binder_names=np.array(["HP1"]))
@@ -172,12 +172,20 @@ def test_continue_polymer_in_field_from_latest_snapshot(monkeypatch, tmp_path):
     field = UniformDensityField([p], binders, 400, 10, 400, 10, 400, 10)
     seen = []
 
-    def fake_mc_sim(polymers, readerproteins, n_steps, ctrls, fld, maf, seed):
-        (q,) = polymers
-        seen.append((q.r.copy(), q.states.copy(), fld is field and q in fld, n_steps))
-        q.r[:, 2] += 1.0
+    class FakeChain:  # the device steps, faked: each run shifts the chain by 1 in z
+        def __init__(self, polymers, fld, ctrls):
+            (self.q,) = polymers
+            self.fld = fld
 
-    monkeypatch.setattr(mc, "mc_sim", fake_mc_sim)
+        def run(self, n_steps, maf, seed):
+            q = self.q
+            seen.append((q.r.copy(), q.states.copy(), self.fld is field and q in self.fld, n_steps))
+            q.r[:, 2] += 1.0
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(mc, "ResidentChain", FakeChain)
     assert {k: v[0] for k, v in mc.latest_snapshots(tmp_path).items()} == {"chr": 1}
     snaps = mc.continue_polymer_in_field_simulation(Chromatin, binders, field, str(tmp_path), 5, 2)
     assert len(snaps) == 2 and len(seen) == 2
@@ -208,3 +216,73 @@ def test_confined_workload_chains_and_volumes():
                             confine_length=w.sphere_radius, assume_fully_accessible=0)
     np.testing.assert_array_equal(wl._sphere_volumes(w.nbins, w.sphere_radius), f.access_vols)
     assert f.access_vols.min() > 0
+
+
+def _fake_chain_class(log, fail_at=None):
+    class FakeChain:
+        """Stands in for the resident device chain: run k moves every bead by k + 1 in x."""
+        def __init__(self, polymers, fld, ctrls):
+            (self.q,) = polymers
+            self.k = 0
+            log.append("init")
+
+        def run(self, n_steps, maf, seed):
+            self.k += 1
+            self.q.r[:, 0] += self.k
+            self.q.states[:, 0] = self.k % 2
+            log.append(("run", n_steps, maf, seed))
+
+        def close(self):
+            log.append("close")
+    return FakeChain
+
+
+def test_polymer_in_field_writes_snapshots_in_the_background(monkeypatch, tmp_path):
+    """polymer_in_field keeps one resident chain for all segments and writes each
+    snapshot's CSV on a background thread from a frozen copy: the files hold
+    the snapshots even though the polymer moves on before they are written;
+    the segments get the mu_schedule factor and seeds drawn from random_seed."""
+    import chromo_gb300.mc as mc
+    from chromo_gb300.mc.moves import Bounds
+    log = []
+    monkeypatch.setattr(mc, "ResidentChain", _fake_chain_class(log))
+    p = Chromatin.straight_line_in_x("chr", np.full(30, 16.5), binder_names=np.array(["HP1"]))
+    binders = cb.make_binder_collection([cb.get_by_name("HP1")])
+    field = UniformDensityField([p], binders, 400, 10, 400, 10, 400, 10)
+    x0 = p.r[:, 0].copy()
+
+    class Sched:
+        @staticmethod
+        def function(i, n):
+            return 1.0 - 0.25 * i
+
+    b = Bounds("b", {})
+    snaps = mc.polymer_in_field([p], binders, field, 7, 3, b, b, mc_move_controllers=[object()],
+                                random_seed=11, mu_schedule=Sched, output_dir=tmp_path, start_index=4)
+    assert log[0] == "init" and log[-1] == "close" and len(log) == 5
+    np.random.seed(11)
+    seeds = [np.random.randint(0, 1E9) for _ in range(3)]
+    assert [e[1:] for e in log[1:4]] == [(7, 1.0, seeds[0]), (7, 0.75, seeds[1]), (7, 0.5, seeds[2])]
+    for i in range(3):
+        q = Chromatin.from_file(str(tmp_path / f"chr-{4 + i}.csv"), "chr")
+        np.testing.assert_array_equal(q.r, snaps[i][0]["r"])
+        np.testing.assert_array_equal(q.states, snaps[i][0]["states"])
+        np.testing.assert_allclose(q.r[:, 0], x0 + sum(range(1, i + 2)))
+    np.testing.assert_array_equal(p.r, snaps[-1][0]["r"])
+
+
+def test_polymer_in_field_reports_a_failed_snapshot_write(monkeypatch, tmp_path):
+    """A snapshot that cannot be written raises from polymer_in_field (after the
+    resident chain is closed)."""
+    import chromo_gb300.mc as mc
+    from chromo_gb300.mc.moves import Bounds
+    log = []
+    monkeypatch.setattr(mc, "ResidentChain", _fake_chain_class(log))
+    p = Chromatin.straight_line_in_x("chr", np.full(10, 16.5), binder_names=np.array(["HP1"]))
+    binders = cb.make_binder_collection([cb.get_by_name("HP1")])
+    field = UniformDensityField([p], binders, 400, 10, 400, 10, 400, 10)
+    b = Bounds("b", {})
+    with pytest.raises(OSError):
+        mc.polymer_in_field([p], binders, field, 2, 2, b, b, mc_move_controllers=[object()],
+                            output_dir=tmp_path / "missing" / "dir")
+    assert log[-1] == "close"

@@ -79,3 +79,49 @@ def test_polymer_in_field_writes_csv_snapshots(tmp_path):
         np.testing.assert_array_equal(q.r, snaps[i][0]["r"])
         np.testing.assert_array_equal(q.states, snaps[i][0]["states"])
     np.testing.assert_array_equal(q.r, p.r)
+
+
+@pytest.mark.gpu
+def test_polymer_in_field_segments_continue_one_resident_simulation(tmp_path):
+    """polymer_in_field runs its segments on one resident simulation: segment i
+    is num_save_mc steps with the i-th seed drawn from random_seed and the
+    i-th mu_schedule factor, continuing the device state (chains, grid,
+    controllers, move counter) of segment i - 1.  The snapshots (and their
+    CSV files, written in the background) equal those of the same runs made
+    by hand on one Sim."""
+    from chromo_gb300.mc import get_amplitude_bounds, polymer_in_field
+    from chromo_gb300.mc.mc_sim import _binding_struct, _device
+    from golden_cases import load
+    from test_gpu_api import _setup
+
+    class Sched:
+        @staticmethod
+        def function(i, n):
+            return 1.0 - 0.2 * i
+
+    g = load("two_binders")
+    p, binders, f, ctrls = _setup(g)
+    bab, mab = get_amplitude_bounds([p])
+    snaps = polymer_in_field([p], binders, f, 4, 3, bab, mab, ctrls, random_seed=9,
+                             mu_schedule=Sched, output_dir=tmp_path)
+    q, _, f2, ctrls2 = _setup(load("two_binders"))  # fresh arrays: the run above moved p's
+    np.random.seed(9)
+    sim = _device(q, f2, ctrls2)
+    try:
+        for i in range(3):
+            seed = np.random.randint(0, 1E9)
+            q.mu_adjust_factor = Sched.function(i, 3)
+            sim.set_binding(0, _binding_struct(q))
+            sim.run(4, seed)
+            sim.sync()
+            r, t3, t2, st = sim.get_chain(0)
+            np.testing.assert_array_equal(snaps[i][0]["r"], r)
+            np.testing.assert_array_equal(snaps[i][0]["t3"], t3)
+            np.testing.assert_array_equal(snaps[i][0]["states"], st)
+            c = type(p).from_file(str(tmp_path / f"{p.name}-{i}.csv"))
+            np.testing.assert_array_equal(c.r, r)
+        dev = sim.get_controllers(0, len(ctrls))
+        for ctrl, d in zip(ctrls, dev):
+            assert ctrl.move.amp_bead == int(d.amp_bead) and ctrl.move.num_attempt == int(d.num_attempt)
+    finally:
+        sim.close()

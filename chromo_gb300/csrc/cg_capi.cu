@@ -164,6 +164,30 @@ struct cg_sim {
   int direct_host = 0;
   void* hio_tab = nullptr;
   unsigned* hio_flag = nullptr;
+  // device staging arrays of a direct upload (resident layout; allocated on
+  // the first upload, hio_stage_failed when there was no room)
+  void *hio_r4 = nullptr, *hio_t34 = nullptr, *hio_t24 = nullptr;
+  unsigned* hio_states = nullptr;
+  int hio_stage_failed = 0;
+  bool upload_stage() {
+    if (hio_r4) return true;
+    if (hio_stage_failed) return false;
+    const size_t pb = pos_bytes() * (size_t)total_beads;
+    void* p[4] = {nullptr, nullptr, nullptr, nullptr};
+    const size_t bytes[4] = {pb, pb, pb, 4 * (size_t)total_beads};
+    bool ok = true;
+    for (int k = 0; k < 4 && ok; k++) ok = cudaMalloc(&p[k], bytes[k] == 0 ? 16 : bytes[k]) == cudaSuccess;
+    for (int k = 0; k < 4 && ok; k++) ok = cudaMemset(p[k], 0, bytes[k] == 0 ? 16 : bytes[k]) == cudaSuccess;
+    if (!ok) {
+      for (void* q : p)
+        if (q) cudaFree(q);
+      cudaGetLastError();  // the failed allocation is not an error of a later call
+      hio_stage_failed = 1;
+      return false;
+    }
+    hio_r4 = p[0]; hio_t34 = p[1]; hio_t24 = p[2]; hio_states = static_cast<unsigned*>(p[3]);
+    return true;
+  }
 
   unsigned char* staging(size_t bytes) {
     if (bytes > pinned_bytes) {
@@ -297,6 +321,11 @@ void cg_destroy(cg_sim* s) {
   if (s->steric_work) cudaFree(s->steric_work);
   if (s->hio_tab) cudaFree(s->hio_tab);
   if (s->hio_flag) cudaFree(s->hio_flag);
+  {
+    void* stage[] = {s->hio_r4, s->hio_t34, s->hio_t24, s->hio_states};
+    for (void* p : stage)
+      if (p) cudaFree(p);
+  }
   void* ptrs[] = {s->reps, s->ctl, s->tally, s->r4, s->t34, s->t24, s->states, s->marks, s->bonds,
                   s->bonds32, s->grid, s->access_vol, s->access_sc, s->access_vb, s->g_keys, s->g_used, s->g_bslot, s->g_vals, s->g_stage, s->g_idx,
                   s->picked, s->d_picked_off, s->eout, s->aout, s->rep_of_rung, s->swaps,
@@ -696,6 +725,23 @@ int cg_set_chains(cg_sim* s, const double* const* r, const double* const* t3, co
   if (s->direct_host) {
     if (int rc = put_host_table(s, r, t3, t2, states)) return rc;
     CUDA_TRY(cudaMemset(s->hio_flag, 0, sizeof(unsigned)));
+    if (s->upload_stage()) {
+      // one pass over the host arrays into the staging arrays, checked; then
+      // the given arrays are copied into the resident state on the device
+      KArgs st = s->args();
+      st.r4 = s->hio_r4; st.t34 = s->hio_t34; st.t24 = s->hio_t24; st.states = s->hio_states;
+      cg_launch_host_load(st, s->fp64 != 0, s->hio_tab, s->R, s->max_beads, s->nb, s->hio_flag, 2, 0);
+      CUDA_TRY(cudaGetLastError());
+      unsigned bad = 0;
+      CUDA_TRY(cudaMemcpy(&bad, s->hio_flag, sizeof(unsigned), cudaMemcpyDeviceToHost));
+      if (bad & 1u) return fail(CG_ERR_NONFINITE, "non-finite position or tangent");
+      if (bad & 2u) return fail(CG_ERR_ARG, "binding states must be in 0..3");
+      cg_launch_stage_commit(s->args(), s->fp64 != 0, s->hio_tab, s->R, s->max_beads, s->hio_r4, s->hio_t34,
+                             s->hio_t24, s->hio_states, 0);
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaStreamSynchronize(0));
+      return CG_OK;
+    }
     cg_launch_host_load(s->args(), s->fp64 != 0, s->hio_tab, s->R, s->max_beads, s->nb, s->hio_flag, 0, 0);
     CUDA_TRY(cudaGetLastError());
     unsigned bad = 0;

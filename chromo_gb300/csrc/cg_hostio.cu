@@ -8,10 +8,13 @@
 // caller's numpy arrays where they lie and writes the resident 4-vectors (or
 // the reverse), with no host-side conversion into a pinned buffer and no
 // separate DMA.  The replica table (one host pointer per array and replica,
-// NULL to skip) is copied to the device first.  Uploads are checked in a
-// first pass (non-finite coordinates, states outside 0..3) and written in a
-// second, so a rejected upload leaves the resident state unchanged, as the
-// staged path does.
+// NULL to skip) is copied to the device first.  An upload is read once from
+// the host, checked (non-finite coordinates, states outside 0..3) and written
+// into device staging arrays of the resident layout; only an upload that
+// passed is then copied into the resident state (device to device), so a
+// rejected upload leaves the resident state unchanged, as the host-staged
+// path does.  Without room for the device staging arrays, the upload is
+// checked in a first pass over the host arrays and written in a second.
 #include <cuda_runtime.h>
 
 #include "cg_kernels.h"
@@ -31,7 +34,7 @@ struct HostRow {  // one replica's host arrays (NULL: not transferred)
 // resident side takes the scattered accesses (HBM / L2).
 //
 // mode 0: check only (flag bit 1: non-finite coordinate, bit 2: state out of
-// range); mode 1: write the resident storage.
+// range); mode 1: write a's storage; mode 2: check and write.
 template <typename Pos>
 __global__ void host_load_kernel(KArgs a, const HostRow* tab, int nb, unsigned* flag, int mode) {
   const int rep = blockIdx.y;
@@ -48,11 +51,8 @@ __global__ void host_load_kernel(KArgs a, const HostRow* tab, int nb, unsigned* 
     if (!src[k]) continue;
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < 3 * n; j += stride) {
       const double x = src[k][j];
-      if (mode == 0) {
-        if (!isfinite(x)) bad |= 1u;
-      } else {
-        dst[k][4 * (j / 3) + j % 3] = (Pos)x;  // the 4-vector's pad stays 0
-      }
+      if (mode != 1 && !isfinite(x)) bad |= 1u;
+      if (mode != 0) dst[k][4 * (j / 3) + j % 3] = (Pos)x;  // the 4-vector's pad stays 0
     }
   }
   if (row.st) {
@@ -60,10 +60,33 @@ __global__ void host_load_kernel(KArgs a, const HostRow* tab, int nb, unsigned* 
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n * nb; j += stride) {
       const long long v = row.st[j];
       if (v < 0 || v > CG_MAX_MARK) bad |= 2u;
-      else if (mode == 1) sb[4 * (j / nb) + j % nb] = (unsigned char)v;  // byte b of bead i's word
+      else if (mode != 0) sb[4 * (j / nb) + j % nb] = (unsigned char)v;  // byte b of bead i's word
     }
   }
   if (bad) atomicOr(flag, bad);
+}
+
+// Copy the arrays an upload gave (the table's non-NULL entries) from the
+// staging arrays (same layout) into the resident state.
+template <typename Pos>
+__global__ void stage_commit_kernel(KArgs a, const HostRow* tab, const V4<Pos>* s_r, const V4<Pos>* s_t3,
+                                    const V4<Pos>* s_t2, const unsigned* s_st) {
+  const int rep = blockIdx.y;
+  const RepDev& rd = a.reps[rep];
+  const long long n = rd.n_beads, off = rd.bead_off;
+  const HostRow row = tab[rep];
+  const bool give[3] = {row.r != nullptr, row.t3 != nullptr, row.t2 != nullptr};
+  const V4<Pos>* src[3] = {s_r + off, s_t3 + off, s_t2 + off};
+  V4<Pos>* dst[3] = {reinterpret_cast<V4<Pos>*>(a.r4) + off, reinterpret_cast<V4<Pos>*>(a.t34) + off,
+                     reinterpret_cast<V4<Pos>*>(a.t24) + off};
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (int k = 0; k < 3; k++) {
+    if (!give[k]) continue;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) dst[k][i] = src[k][i];
+  }
+  if (row.st)
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride)
+      a.states[off + i] = s_st[off + i];
 }
 
 template <typename Pos>
@@ -103,6 +126,21 @@ void cg_launch_host_load(const cg::KArgs& a, bool fp64, const void* tab, int R, 
   const auto* t = static_cast<const cg::HostRow*>(tab);
   if (fp64) cg::host_load_kernel<double><<<hostio_grid(R, max_beads), 256, 0, s>>>(a, t, nb, flag, mode);
   else cg::host_load_kernel<float><<<hostio_grid(R, max_beads), 256, 0, s>>>(a, t, nb, flag, mode);
+}
+
+void cg_launch_stage_commit(const cg::KArgs& a, bool fp64, const void* tab, int R, long long max_beads,
+                            const void* s_r, const void* s_t3, const void* s_t2, const unsigned* s_st,
+                            cudaStream_t s) {
+  const auto* t = static_cast<const cg::HostRow*>(tab);
+  const dim3 grid = hostio_grid(R, (max_beads + 2) / 3);  // one thread per bead
+  if (fp64)
+    cg::stage_commit_kernel<double><<<grid, 256, 0, s>>>(a, t, static_cast<const cg::V4<double>*>(s_r),
+                                                         static_cast<const cg::V4<double>*>(s_t3),
+                                                         static_cast<const cg::V4<double>*>(s_t2), s_st);
+  else
+    cg::stage_commit_kernel<float><<<grid, 256, 0, s>>>(a, t, static_cast<const cg::V4<float>*>(s_r),
+                                                        static_cast<const cg::V4<float>*>(s_t3),
+                                                        static_cast<const cg::V4<float>*>(s_t2), s_st);
 }
 
 void cg_launch_host_store(const cg::KArgs& a, bool fp64, const void* tab, int R, long long max_beads, int nb,

@@ -186,6 +186,9 @@ void cg_launch_host_load(const cg::KArgs& a, bool fp64, const void* tab, int R, 
                          unsigned* flag, int mode, cudaStream_t s);
 void cg_launch_host_store(const cg::KArgs& a, bool fp64, const void* tab, int R, long long max_beads, int nb,
                           cudaStream_t s);
+void cg_launch_stage_commit(const cg::KArgs& a, bool fp64, const void* tab, int R, long long max_beads,
+                            const void* s_r, const void* s_t3, const void* s_t2, const unsigned* s_st,
+                            cudaStream_t s);
 void cg_launch_store_chains(const cg::KArgs& a, bool fp64, long long total, const double* r, const double* t3,
                             cudaStream_t s);
 void cg_launch_terms(const cg::KArgs& a, double* terms, double* acc, cudaStream_t s);

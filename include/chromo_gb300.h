@@ -131,8 +131,9 @@ int cg_get_chain(cg_sim *sim, int32_t rep, double *r, double *t3, double *t2, in
  * [N_rep*n_binders] array (a NULL array list, or a NULL entry, skips that
  * array or replica).  Where the GPU can address pageable host memory
  * (cudaDevAttrPageableMemoryAccess: Grace-Blackwell NVLink-C2C) one kernel
- * reads or writes the caller's arrays directly (uploads checked in a first
- * pass, so a rejected one changes nothing); elsewhere, or with the
+ * reads or writes the caller's arrays directly (an upload is read once into
+ * device staging arrays, checked, and copied into the resident state only if
+ * it passed, so a rejected one changes nothing); elsewhere, or with the
  * environment variable CHROMO_GB300_STAGED_HOST_IO=1 at cg_create, the
  * host-side conversion runs on several threads into a pinned buffer and each
  * array crosses the bus in one copy.  This is how a batch of chains is moved

@@ -164,6 +164,18 @@ struct cg_sim {
   int direct_host = 0;
   void* hio_tab = nullptr;
   unsigned* hio_flag = nullptr;
+  // replicas using SSTWLC twist or confinement (the MC kernel's full form);
+  // with none, launches take its lean form
+  std::vector<unsigned char> full_of;
+  long long n_full = 0;
+  void note_features(int rep, const RepDev& d) {
+    const unsigned char f = d.twist != 0 || d.confine_kind != 0;
+    if (f == full_of[rep]) return;
+    const bool was_lean = n_full == 0;
+    n_full += f ? 1 : -1;
+    full_of[rep] = f;
+    if (was_lean != (n_full == 0)) drop_graph();  // the captured launches' form changes
+  }
   // device staging arrays of a direct upload (resident layout; allocated on
   // the first upload, hio_stage_failed when there was no room)
   void *hio_r4 = nullptr, *hio_t34 = nullptr, *hio_t24 = nullptr;
@@ -225,6 +237,7 @@ struct cg_sim {
     a.xround = xround;
     a.mu_rungs = mu_rungs; a.mu_binder = mu_binder; a.nbound = nbound;
     a.mu_swaps = mu_swaps; a.mu_swap_attempts = mu_swap_attempts;
+    a.lean = n_full == 0 ? 1 : 0;
     return a;
   }
 
@@ -405,6 +418,7 @@ int cg_create(const cg_config* cfg, cg_sim** out) {
     return fail(CG_ERR_ARG, "n_binders must be in 1..3");
   cg_sim* s = new cg_sim();
   s->R = cfg->n_replicas;
+  s->full_of.assign(s->R, 0);
   s->nb = cfg->n_binders;
   s->ncol = cfg->n_binders + 1 <= 2 ? 2 : 4;
   s->fp64 = cfg->pos_fp64 ? 1 : 0;
@@ -572,6 +586,7 @@ static int get_rep(cg_sim* s, int rep, RepDev* d) {
 }
 static int put_rep(cg_sim* s, int rep, const RepDev* d) {
   CUDA_TRY(cudaMemcpy(s->reps + rep, d, sizeof(RepDev), cudaMemcpyHostToDevice));
+  s->note_features(rep, *d);
   return CG_OK;
 }
 
@@ -1027,6 +1042,7 @@ int cg_run_logged(cg_sim* s, int64_t n_steps, uint64_t seed, cg_move_record* rec
     a.seed = seed;
     a.mlog = d_log;
     a.mlog_cap = max_records;
+    a.lean = 0;  // the move log is in the full form only
     cg_launch_spec(a, s->fp64, s->spec_bytes, 0);
     s->kernels++;
     e = cudaGetLastError();
@@ -1477,6 +1493,11 @@ int cg_load_state(cg_sim* s, const void* buf, int64_t bytes) {
     off += p.bytes;
   }
   if (s->guard_every) CUDA_TRY(cudaMemset(s->guard_init, 0, sizeof(int) * s->R));  // new reference energies
+  {  // the restored replicas' twist and confinement choose the MC kernel's form
+    std::vector<RepDev> rd(s->R);
+    CUDA_TRY(cudaMemcpy(rd.data(), s->reps, sizeof(RepDev) * s->R, cudaMemcpyDeviceToHost));
+    for (int r = 0; r < s->R; r++) s->note_features(r, rd[r]);
+  }
   return CG_OK;
 }
 

@@ -137,12 +137,13 @@ struct ChainView {
   const double* bonds;
   const float* bonds32;
   const double* twist;  // (eps_twist, omega0) per bond, SSTWLC replicas only
-  __device__ ChainView(const KArgs& a, const RepDev& rd)
+  // lean: the caller's instantiation has no SSTWLC replica (twist stays null)
+  __device__ ChainView(const KArgs& a, const RepDev& rd, bool lean)
       : r4(reinterpret_cast<const V4<Pos>*>(a.r4) + rd.bead_off),
         t34(reinterpret_cast<const V4<Pos>*>(a.t34) + rd.bead_off),
         t24(reinterpret_cast<const V4<Pos>*>(a.t24) + rd.bead_off),
         st(a.states + rd.bead_off), bonds(a.bonds + rd.bead_off * 6), bonds32(a.bonds32 + rd.bead_off * 8),
-        twist(rd.twist ? a.twist + rd.bead_off * 2 : nullptr) {}
+        twist(!lean && rd.twist ? a.twist + rd.bead_off * 2 : nullptr) {}
 };
 
 // Lanes per bead of the position-move deposit; each lane takes 8 / kLanesPerBead
@@ -279,15 +280,15 @@ template <> __device__ __forceinline__ double load_acc<double>(long long, double
 // error bits go to the move's plan.  A move whose optimistic table overflows
 // (E_OVF: a pool or a table past 3/4 load) is skipped from then on; its
 // group deposits it again in its global table.  Called by every thread.
-template <typename Pos>
+template <typename Pos, bool LEAN>
 __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, int kind) {
   using Acc = typename AccOf<Pos>::type;
   unsigned char* smem = reinterpret_cast<unsigned char*>(&sh);
   const RepDev& rd = sh.ws.rd;
   const GridF& gf = sh.ws.gf;
-  const ChainView<Pos> cv(a, rd);
+  const ChainView<Pos> cv(a, rd, LEAN);
   const long long N = rd.n_beads;
-  const bool conf = rd.field_kind != 0 && rd.confine_kind;
+  const bool conf = !LEAN && rd.field_kind != 0 && rd.confine_kind;
   const int Hs = 1 << a.logH, hcol = a.hcol;
   const bool pool = a.pool_on != 0;
   // lane j of every warp holds the end of move j's tasks in the batch's
@@ -504,7 +505,7 @@ __device__ __forceinline__ void add_pool_terms(double& s, const MovePlan& P) {
 // a move, which run the collectives and block barriers with empty work.
 // Every thread of the CTA calls it (position moves hold two block barriers
 // around the block-wide deposit); B is the batch's number of moves.
-template <typename Pos, int G>
+template <typename Pos, int G, bool LEAN>
 __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, int gl, bool live, int kind,
                               const cg_move_ctl& c, unsigned long long t, unsigned* draws,
                               const SlotScratch& sm, const SlotScratch& gm, int* bkeys, unsigned* bmask,
@@ -547,7 +548,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
   if (threadIdx.x == 0) sh.npool = 0;  // every reader of the last batch's pool passed a barrier since
 
   if (kind <= CG_SLIDE) {
-    const ChainView<Pos> cv(a, rd);
+    const ChainView<Pos> cv(a, rd, LEAN);
     Real M[3][4];
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 4; j++) M[i][j] = i == j ? (Real)1 : (Real)0;
@@ -644,7 +645,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
         for (int j = 0; j < 4; j++) Mp[4 * i + j] = M[i][j];
     }
     __syncthreads();
-    block_deposit<Pos>(a, sh, rep, B, kind);
+    block_deposit<Pos, LEAN>(a, sh, rep, B, kind);
     // earlier moves u of the batch whose written beads [ind0, indf) meet the
     // beads this move reads (its segment and both neighbours); a move with no
     // beads (failed or empty) is never accepted, so it needs no exclusion
@@ -708,7 +709,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
           Acc pterm;
           int ob;
           bead_task<Pos, Acc>(rd, gf, cv, kind, M, N, ind0, indf, m, k, cl, stage, density,
-                              check_field && rd.confine_kind, vq, q, sw, e, left, right, pterm, ob);
+                              !LEAN && check_field && rd.confine_kind, vq, q, sw, e, left, right, pterm, ob);
           if (left || right) acc_add(part, pterm);
           oob += ob;
         }
@@ -732,7 +733,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     }
     err = gor<G>(err);
     dEp = gsum<G>(part);
-    if (check_field && rd.confine_kind) {
+    if (!LEAN && check_field && rd.confine_kind) {
       int oo = gsum<G>(oob);
       dEH += ((long long)(oo >> 16) - (long long)(oo & 0xFFFF)) << 40;
     }
@@ -827,7 +828,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
       Acc de = acc_zero<Acc>();
       if (hl) acc_add(de, pair_dE_fwd(bl, r0, r, r, t30, t3, tt3));
       if (hr) acc_add(de, pair_dE_rev(br, r, r, r1, t3, tt3, t31));
-      if (rd.twist) {  // SSTWLC: twist terms of both bonds
+      if (!LEAN && rd.twist) {  // SSTWLC: twist terms of both bonds
         const double* tw = a.twist + rd.bead_off * 2;
         const Frame cur = frame_of(t2, t3), nw = frame_of(tt2, tt3);
         double dt = 0;
@@ -972,7 +973,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     P.kind = kind; P.m = (int)m; P.ind0 = (int)ind0; P.indf = (int)indf;
     P.empty = empty ? 1 : 0; P.err = (int)err; P.regfail = regfail; P.dec = dec ? 1 : 0;
     P.nvox = (int)nvox; P.gtab = gtab; P.gstage = gstage;
-    if (a.mlog) log_terms(P, dEp, g.pos);
+    if (!LEAN && a.mlog) log_terms(P, dEp, g.pos);
   }
 }
 
@@ -1122,8 +1123,11 @@ __device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int s, int gl, 
 }
 
 // 168 registers: two CTAs of 6 warps fit one SM's register file (measured
-// faster than 128 registers with 8 warps, which spills).
-template <typename Pos, int G>
+// faster than 128 registers with 8 warps, which spills).  LEAN: the
+// instantiation for launches with no SSTWLC replica, no confinement and no
+// move log, whose code for those is left out (it holds the batch loop's
+// state in registers without spills; the host picks it per launch, a.lean).
+template <typename Pos, int G, bool LEAN>
 __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
   extern __shared__ __align__(32) unsigned char smem[];
   constexpr int GPW = 32 / G;  // move groups per warp
@@ -1209,7 +1213,7 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
           const int B = (int)(c.num_per_cycle - done < Sn ? c.num_per_cycle - done : Sn);
           const bool wlive = warp * GPW < B;  // the warp has a move of this batch
           const bool live = slot < B;
-          evaluate_move<Pos, G>(a, sh, rep, slot, gl, live, kind, c, sh.t0 + (unsigned long long)slot, draws,
+          evaluate_move<Pos, G, LEAN>(a, sh, rep, slot, gl, live, kind, c, sh.t0 + (unsigned long long)slot, draws,
                                 sm, gm, bkeys, bmask, a.spec_logHB, B);
           __syncthreads();
           if (kind > CG_SLIDE) {  // position moves set their masks while evaluating
@@ -1256,7 +1260,7 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
               const double alpha = c.alpha, beta = 1 - c.alpha;
               for (int w = 0; w < cut; w++) {
                 const MovePlan& P = sh.plan[w];
-                if (a.mlog) log_move(a, rep, sh.t0 + (unsigned long long)w - sh.tlog, P);
+                if (!LEAN && a.mlog) log_move(a, rep, sh.t0 + (unsigned long long)w - sh.tlog, P);
                 if (P.empty) continue;
                 if (P.dec && soft_dE(P.dE)) run += P.dE;
                 rate = (P.dec ? alpha : 0.0) + beta * rate;
@@ -1302,16 +1306,25 @@ __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
 
 }  // namespace cg
 
-// Launch, shared-memory opt-in and register count of one instantiation.
+// Launch, shared-memory opt-in and register count of one storage / lanes
+// pair (both its lean and full forms).
 #define CG_SPEC_INSTANTIATE(Pos, G, NAME)                                                          \
   void cg_launch_spec_##NAME(const cg::KArgs& a, size_t smem, cudaStream_t s) {                    \
-    cg::spec_kernel<Pos, G><<<a.n_reps, 32 * a.spec_w, smem, s>>>(a);                              \
+    if (a.lean)                                                                                    \
+      cg::spec_kernel<Pos, G, true><<<a.n_reps, 32 * a.spec_w, smem, s>>>(a);                      \
+    else                                                                                           \
+      cg::spec_kernel<Pos, G, false><<<a.n_reps, 32 * a.spec_w, smem, s>>>(a);                     \
   }                                                                                                \
   cudaError_t cg_spec_smem_##NAME(int bytes) {                                                     \
-    return cudaFuncSetAttribute(cg::spec_kernel<Pos, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+    cudaError_t e = cudaFuncSetAttribute(cg::spec_kernel<Pos, G, false>,                           \
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);      \
+    if (e != cudaSuccess) return e;                                                                \
+    return cudaFuncSetAttribute(cg::spec_kernel<Pos, G, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                 bytes);                                                            \
   }                                                                                                \
   int cg_spec_regs_##NAME() {                                                                      \
-    cudaFuncAttributes at;                                                                         \
-    return cudaFuncGetAttributes(&at, cg::spec_kernel<Pos, G>) == cudaSuccess ? at.numRegs : 0;    \
+    cudaFuncAttributes at, bt;                                                                     \
+    if (cudaFuncGetAttributes(&at, cg::spec_kernel<Pos, G, false>) != cudaSuccess) return 0;       \
+    if (cudaFuncGetAttributes(&bt, cg::spec_kernel<Pos, G, true>) != cudaSuccess) return 0;        \
+    return at.numRegs > bt.numRegs ? at.numRegs : bt.numRegs;                                      \
   }

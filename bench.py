@@ -746,9 +746,8 @@ def main():
             "move_stats": wl.move_stats(tal),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
-                         # the lean form serves launches without confinement or twist
-                         "kernel": "spec_kernel<float,%d,%s>" % (sim.launch_shape()[1],
-                                                                 "false" if w.sphere_radius > 0 else "true"),
+                         # the lean form serves launches without SSTWLC twist
+                         "kernel": "spec_kernel<float,%d,true>" % sim.launch_shape()[1],
                          "peak_source": peak_kind, "bytes_per_launch": bytes_per_launch,
                          "avg_launch_ms": avg_launch_s * 1e3, "moves_per_launch": attempts / args.steps,
                          "timing": "the MC kernel of the K timed rounds: CUDA event-record nodes "

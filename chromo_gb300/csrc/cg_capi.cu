@@ -164,12 +164,12 @@ struct cg_sim {
   int direct_host = 0;
   void* hio_tab = nullptr;
   unsigned* hio_flag = nullptr;
-  // replicas using SSTWLC twist or confinement (the MC kernel's full form);
-  // with none, launches take its lean form
+  // replicas using SSTWLC twist (the MC kernel's full form); with none,
+  // launches take its lean form
   std::vector<unsigned char> full_of;
   long long n_full = 0;
   void note_features(int rep, const RepDev& d) {
-    const unsigned char f = d.twist != 0 || d.confine_kind != 0;
+    const unsigned char f = d.twist != 0;
     if (f == full_of[rep]) return;
     const bool was_lean = n_full == 0;
     n_full += f ? 1 : -1;
@@ -1493,7 +1493,7 @@ int cg_load_state(cg_sim* s, const void* buf, int64_t bytes) {
     off += p.bytes;
   }
   if (s->guard_every) CUDA_TRY(cudaMemset(s->guard_init, 0, sizeof(int) * s->R));  // new reference energies
-  {  // the restored replicas' twist and confinement choose the MC kernel's form
+  {  // the restored replicas' twist chooses the MC kernel's form
     std::vector<RepDev> rd(s->R);
     CUDA_TRY(cudaMemcpy(rd.data(), s->reps, sizeof(RepDev) * s->R, cudaMemcpyDeviceToHost));
     for (int r = 0; r < s->R; r++) s->note_features(r, rd[r]);

@@ -119,8 +119,8 @@ struct KArgs {
   // voxel * 32 + move slot, shared by the position moves of a batch
   int pool_on, pool_logH, off_pkeys, off_pused, off_pvals;
   unsigned long long seed;
-  // the MC kernel's lean form: no replica uses SSTWLC twist or confinement
-  // and the move log is off
+  // the MC kernel's lean form: no replica uses SSTWLC twist and the move log
+  // is off
   int lean;
   // audit mode
   int audit_rep;

@@ -288,7 +288,7 @@ __device__ void block_deposit(const KArgs& a, SpecShared& sh, int rep, int B, in
   const GridF& gf = sh.ws.gf;
   const ChainView<Pos> cv(a, rd, LEAN);
   const long long N = rd.n_beads;
-  const bool conf = !LEAN && rd.field_kind != 0 && rd.confine_kind;
+  const bool conf = rd.field_kind != 0 && rd.confine_kind;
   const int Hs = 1 << a.logH, hcol = a.hcol;
   const bool pool = a.pool_on != 0;
   // lane j of every warp holds the end of move j's tasks in the batch's
@@ -709,7 +709,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
           Acc pterm;
           int ob;
           bead_task<Pos, Acc>(rd, gf, cv, kind, M, N, ind0, indf, m, k, cl, stage, density,
-                              !LEAN && check_field && rd.confine_kind, vq, q, sw, e, left, right, pterm, ob);
+                              check_field && rd.confine_kind, vq, q, sw, e, left, right, pterm, ob);
           if (left || right) acc_add(part, pterm);
           oob += ob;
         }
@@ -733,7 +733,7 @@ __device__ void evaluate_move(const KArgs& a, SpecShared& sh, int rep, int s, in
     }
     err = gor<G>(err);
     dEp = gsum<G>(part);
-    if (!LEAN && check_field && rd.confine_kind) {
+    if (check_field && rd.confine_kind) {
       int oo = gsum<G>(oob);
       dEH += ((long long)(oo >> 16) - (long long)(oo & 0xFFFF)) << 40;
     }
@@ -1124,9 +1124,9 @@ __device__ void commit_and_clear(const KArgs& a, SpecShared& sh, int s, int gl, 
 
 // 168 registers: two CTAs of 6 warps fit one SM's register file (measured
 // faster than 128 registers with 8 warps, which spills).  LEAN: the
-// instantiation for launches with no SSTWLC replica, no confinement and no
-// move log, whose code for those is left out (it holds the batch loop's
-// state in registers without spills; the host picks it per launch, a.lean).
+// instantiation for launches with no SSTWLC replica and no move log, whose
+// code for those is left out (it holds the batch loop's state in registers
+// without spills; the host picks it per launch, a.lean).
 template <typename Pos, int G, bool LEAN>
 __global__ void __maxnreg__(168) spec_kernel(KArgs a) {
   extern __shared__ __align__(32) unsigned char smem[];
